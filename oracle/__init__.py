@@ -1,0 +1,277 @@
+"""CPU oracle for the VortonSim velocity-from-vorticity step.
+
+TEST INFRASTRUCTURE ONLY.  Only ``tests/``, ``__graft_entry__.smoke()`` and
+``bench.py``'s CPU-baseline leg (``cpu_baseline`` and ``--impl reference``)
+may import this package, and only as the checker or the timed CPU baseline.
+The product package ``vortegrid_gb300`` never imports it.
+
+Two libraries are wrapped:
+  * ``liboracle`` -- ``vg_oracle.c``, a plain-C restatement of the reference's
+    algorithms (each function cites the reference file:line it follows) plus
+    the strict FP64 direct-sum oracle.  Built by ``build()`` below.
+  * ``libvgref_{serial,mt}`` -- the reference's own C++ (staged by
+    ``ref_build/prepare.py`` and built by ``ref_build/Makefile``), used to pin
+    the restatement and as the CPU baseline.  Optional: absent when neither the
+    reference tree nor a staged copy of it is available.
+"""
+import ctypes
+import os
+import subprocess
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+BUILD = os.path.join(HERE, "_build")
+LIB = os.path.join(BUILD, "liboracle.so")
+REF_DIR = os.path.join(HERE, "_ref")
+REF_TREE = "/root/reference/Samples/MjgIntelFluidDemo_Part20"
+
+
+def build(quiet=True):
+    """Compile vg_oracle.c (and, when reference sources are staged, the
+    reference harness) for this host."""
+    os.makedirs(BUILD, exist_ok=True)
+    src = os.path.join(HERE, "vg_oracle.c")
+    if not os.path.exists(LIB) or os.path.getmtime(LIB) < max(
+            os.path.getmtime(src), os.path.getmtime(os.path.join(HERE, "vg_oracle.h"))):
+        subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off",
+                               "-o", LIB, src, "-lm"])
+    staged = os.path.join(REF_DIR, "src", ".staged")
+    if not os.path.exists(staged) and os.path.isdir(REF_TREE):
+        subprocess.check_call(["python3", os.path.join(HERE, "ref_build", "prepare.py"), REF_TREE],
+                              stdout=subprocess.DEVNULL if quiet else None)
+    if os.path.exists(staged):
+        subprocess.check_call(["make", "-s", "-C", os.path.join(HERE, "ref_build"), "-j8"],
+                              stdout=subprocess.DEVNULL if quiet else None,
+                              stderr=subprocess.DEVNULL if quiet else None)
+
+
+class Geom(ctypes.Structure):
+    """vgo_geom: UniformGridGeometry fields."""
+    _fields_ = [("mn", ctypes.c_float * 3), ("ext", ctypes.c_float * 3), ("cell", ctypes.c_float * 3),
+                ("cpe", ctypes.c_float * 3), ("np", ctypes.c_uint * 3)]
+
+    @property
+    def points(self):
+        return tuple(int(v) for v in self.np)
+
+    @property
+    def capacity(self):
+        return int(self.np[0]) * int(self.np[1]) * int(self.np[2])
+
+    def as12(self):
+        return np.array(list(self.mn) + list(self.ext) + list(self.cell) + list(self.cpe), dtype=np.float32)
+
+    @staticmethod
+    def from12(g12, np3):
+        g = Geom()
+        for a in range(3):
+            g.mn[a] = float(g12[a]); g.ext[a] = float(g12[3 + a])
+            g.cell[a] = float(g12[6 + a]); g.cpe[a] = float(g12[9 + a]); g.np[a] = int(np3[a])
+        return g
+
+
+_lib = None
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB):
+            build()
+        _lib = ctypes.CDLL(LIB)
+        _lib.vgo_finvsqrtf.restype = ctypes.c_float
+        _lib.vgo_finvsqrtf.argtypes = [ctypes.c_float]
+        _lib.vgo_influence_tree.restype = ctypes.c_size_t
+        _lib.vgo_offset_of_position.restype = ctypes.c_uint
+        _lib.vgo_nested_shape.restype = ctypes.c_int
+        _lib.vgo_relres_f64.restype = ctypes.c_double
+        _lib.vgo_relres_f64d.restype = ctypes.c_double
+    return _lib
+
+
+def _p(a):
+    return a.ctypes.data_as(ctypes.c_void_p) if a is not None else None
+
+
+def f32(a):
+    return np.ascontiguousarray(a, dtype=np.float32)
+
+
+def define_shape(n, vmin, vmax, pow2=True):
+    g = Geom()
+    lib().vgo_define_shape(ctypes.c_size_t(n), _p(f32(vmin)), _p(f32(vmax)), ctypes.c_int(int(pow2)), ctypes.byref(g))
+    return g
+
+
+def step_geometry(pos, radius, extra_min=None, extra_max=None):
+    g = Geom()
+    pos = f32(pos)
+    lib().vgo_step_geometry(_p(pos), ctypes.c_size_t(len(pos)), ctypes.c_float(radius),
+                            _p(f32(extra_min)) if extra_min is not None else None,
+                            _p(f32(extra_max)) if extra_max is not None else None, ctypes.byref(g))
+    return g
+
+
+def indices_of_position(g, pos):
+    pos = f32(pos)
+    idx = np.zeros((len(pos), 3), np.uint32)
+    off = np.zeros(len(pos), np.uint32)
+    lib().vgo_indices_batch(ctypes.byref(g), _p(pos), ctypes.c_size_t(len(pos)), _p(idx), _p(off))
+    return idx, off
+
+
+def nested_shape(g):
+    layers = (Geom * 32)()
+    dec = np.zeros(96, np.uint32)
+    depth = lib().vgo_nested_shape(ctypes.byref(g), layers, _p(dec))
+    return [layers[i] for i in range(depth)], dec[:3 * depth].reshape(depth, 3)
+
+
+def direct(kind, pos, angvel, size, q, spread_range=1.0, spread_circ=1.0, f64=False):
+    pos, angvel, size, q = f32(pos), f32(angvel), f32(size), f32(q)
+    out = np.zeros((len(q), 3), np.float64 if f64 else np.float32)
+    fn = lib().vgo_direct_f64 if f64 else lib().vgo_direct
+    fn(ctypes.c_int(kind), _p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), _p(q), ctypes.c_size_t(len(q)),
+       ctypes.c_float(spread_range), ctypes.c_float(spread_circ), _p(out))
+    return out
+
+
+def influence_tree(pos, angvel, size, g):
+    pos, angvel, size = f32(pos), f32(angvel), f32(size)
+    total = lib().vgo_influence_tree(_p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g), None)
+    out = np.zeros((total, 7), np.float32)
+    lib().vgo_influence_tree(_p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g), _p(out))
+    return out
+
+
+def tree(kind, pos, angvel, size, g, q, spread_range=1.0, spread_circ=1.0):
+    pos, angvel, size, q = f32(pos), f32(angvel), f32(size), f32(q)
+    out = np.zeros((len(q), 3), np.float32)
+    lib().vgo_tree(ctypes.c_int(kind), _p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g),
+                   _p(q), ctypes.c_size_t(len(q)), ctypes.c_float(spread_range), ctypes.c_float(spread_circ), _p(out))
+    return out
+
+
+def splat(pos, angvel, size, g, scale=-1.0):
+    pos, angvel, size = f32(pos), f32(angvel), f32(size)
+    out = np.zeros((g.capacity, 3), np.float32)
+    lib().vgo_splat(_p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g), ctypes.c_float(scale),
+                    _p(out))
+    return out
+
+
+def boundary_vecpot(pos, angvel, size, g, boundaries_only=True, copy_odd_x=True):
+    pos, angvel, size = f32(pos), f32(angvel), f32(size)
+    out = np.zeros((g.capacity, 3), np.float32)
+    lib().vgo_boundary_vecpot(_p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g),
+                              ctypes.c_int(int(boundaries_only)), ctypes.c_int(int(copy_odd_x)), _p(out))
+    return out
+
+
+def sor(g, soln, lap, steps):
+    s = f32(soln).copy()
+    lib().vgo_sor(ctypes.byref(g), _p(s), _p(f32(lap)), ctypes.c_int(steps))
+    return s
+
+
+def downsample(fine, fv, coarse, inject=True):
+    out = np.zeros((coarse.capacity, 3), np.float32)
+    lib().vgo_downsample(ctypes.byref(fine), _p(f32(fv)), ctypes.c_int(int(inject)), ctypes.byref(coarse), _p(out))
+    return out
+
+
+def upsample(coarse, cv, fine, fine_init, interior_only=True):
+    out = f32(fine_init).copy()
+    lib().vgo_upsample(ctypes.byref(coarse), _p(f32(cv)), ctypes.byref(fine), ctypes.c_int(int(interior_only)),
+                       _p(out))
+    return out
+
+
+def cascade(g, soln, rhs, steps=16):
+    s = f32(soln).copy()
+    lib().vgo_cascade(ctypes.byref(g), _p(s), _p(f32(rhs)), ctypes.c_int(steps))
+    return s
+
+
+def jacobian(g, vec):
+    out = np.zeros((g.capacity, 9), np.float32)
+    lib().vgo_jacobian(ctypes.byref(g), _p(f32(vec)), _p(out))
+    return out
+
+
+def curl_from_jacobian(jac):
+    jac = f32(jac)
+    out = np.zeros((len(jac), 3), np.float32)
+    lib().vgo_curl_from_jacobian(ctypes.c_size_t(len(jac)), _p(jac), _p(out))
+    return out
+
+
+def stretch(pos, angvel, g, jac9, dt):
+    w = f32(angvel).copy()
+    pos = f32(pos)
+    lib().vgo_stretch(_p(pos), _p(w), ctypes.c_size_t(len(pos)), ctypes.byref(g), _p(f32(jac9)), ctypes.c_float(dt))
+    return w
+
+
+def pse(pos, angvel, size, g, viscosity, dt, symmetric=False):
+    w = f32(angvel).copy()
+    pos, size = f32(pos), f32(size)
+    fn = lib().vgo_pse_symmetric if symmetric else lib().vgo_pse_sequential
+    fn(_p(pos), _p(w), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g), ctypes.c_float(viscosity),
+       ctypes.c_float(dt))
+    return w
+
+
+def gather(g, velgrid, pos):
+    pos = f32(pos)
+    out = np.zeros((len(pos), 3), np.float32)
+    lib().vgo_gather(ctypes.byref(g), _p(f32(velgrid)), _p(pos), ctypes.c_size_t(len(pos)), _p(out))
+    return out
+
+
+def evolve(pos, vel, dt):
+    p = f32(pos).copy()
+    lib().vgo_evolve(_p(p), _p(f32(vel)), ctypes.c_size_t(len(p)), ctypes.c_float(dt))
+    return p
+
+
+def relres(g, a, b):
+    if a.dtype == np.float64:
+        return lib().vgo_relres_f64d(ctypes.byref(g), _p(np.ascontiguousarray(a)), _p(f32(b)))
+    return lib().vgo_relres_f64(ctypes.byref(g), _p(f32(a)), _p(f32(b)))
+
+
+def step_fields(pos, vel, angvel, size, g, dt, viscosity, pse_mode=0):
+    pos, size = f32(pos), f32(size)
+    v = f32(vel).copy()
+    w = f32(angvel).copy()
+    vg = np.zeros((g.capacity, 3), np.float32)
+    ap = np.zeros((g.capacity, 3), np.float32)
+    nv = np.zeros((g.capacity, 3), np.float32)
+    lib().vgo_step_fields(_p(pos), _p(v), _p(w), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g),
+                          ctypes.c_float(dt), ctypes.c_float(viscosity), ctypes.c_int(pse_mode), _p(vg), _p(ap), _p(nv))
+    return v, w, vg, ap, nv
+
+
+# ---------------------------------------------------------------- reference
+
+def ref_available(kind="serial"):
+    return os.path.exists(os.path.join(REF_DIR, f"libvgref_{kind}.so"))
+
+
+_ref = {}
+
+
+def ref(kind="serial"):
+    """The reference's own code (serial: USE_TBB=0; mt: USE_TBB=1 on a
+    std::thread TBB stand-in using NUMBER_OF_PROCESSORS threads)."""
+    if kind not in _ref:
+        path = os.path.join(REF_DIR, f"libvgref_{kind}.so")
+        L = ctypes.CDLL(path)
+        L.vgref_sizeof_particle.restype = ctypes.c_size_t
+        L.vgref_influence_tree.restype = ctypes.c_size_t
+        L.vgref_nested_grid_shape.restype = ctypes.c_int
+        L.vgref_step.restype = ctypes.c_int
+        _ref[kind] = L
+    return _ref[kind]

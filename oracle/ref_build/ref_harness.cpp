@@ -1,0 +1,470 @@
+/* C-ABI harness over the reference's own VortonSim code (built from the staged
+ * reference sources by oracle/ref_build/Makefile).
+ *
+ * TEST INFRASTRUCTURE ONLY.  Tests, smoke() and bench.py's CPU-baseline leg
+ * call this library to (a) generate golden vectors that pin the C oracle and
+ * (b) time the reference's own CPU path.  The product never links it.
+ *
+ * Every entry point calls the reference's functions in the order the
+ * reference's VortonSim step calls them (VortonFluid/vortonSim.cpp,
+ * Core/SpatialPartition/uniformGrid.h, uniformGridMath.cpp,
+ * Particles/Operation/pclOpAdvect.cpp, pclOpEvolve.cpp); this file is glue
+ * that moves flat float arrays in and out of the reference's containers.
+ *
+ * Vortons cross this boundary as the reference's own Particle records
+ * (sizeof(Particle) bytes each, see vgref_sizeof_particle).
+ */
+#define private public
+#define protected public
+#include "VortonFluid/vortonSim.h"
+#include "VortonFluid/pclOpVortonSim.h"
+#include "Particles/Operation/pclOpFindBoundingBox.h"
+#include "Core/SpatialPartition/uniformGridMath.h"
+#undef private
+#undef protected
+#include <cstring>
+#include <vector>
+#include "tbb/vg_tbb.h"  /* blocked_range for the serial build too */
+
+#if ! USE_TBB
+unsigned gNumberOfProcessors = 1;
+#endif
+
+extern void AssignVelocityFromField(VECTOR<Particle>& particles, const UniformGrid<Vec3>* velocityGrid, const float gain);
+
+namespace {
+
+struct Geom {
+  float mn[3], ext[3], cell[3], cpe[3];
+  unsigned np[3];
+};
+
+void load_geom(UniformGridGeometry& g, const float* geom12, const unsigned* np) {
+  g.mMinCorner = Vec3(geom12[0], geom12[1], geom12[2]);
+  g.mGridExtent = Vec3(geom12[3], geom12[4], geom12[5]);
+  g.mNumPoints[0] = np[0];
+  g.mNumPoints[1] = np[1];
+  g.mNumPoints[2] = np[2];
+  g.PrecomputeSpacing();
+}
+
+void store_geom(const UniformGridGeometry& g, float* geom12, unsigned* np) {
+  const Vec3& a = g.GetMinCorner();
+  const Vec3& b = g.GetExtent();
+  const Vec3& c = g.GetCellSpacing();
+  const Vec3& d = g.GetCellsPerExtent();
+  const float v[12] = {a.x, a.y, a.z, b.x, b.y, b.z, c.x, c.y, c.z, d.x, d.y, d.z};
+  std::memcpy(geom12, v, sizeof(v));
+  np[0] = g.GetNumPoints(0);
+  np[1] = g.GetNumPoints(1);
+  np[2] = g.GetNumPoints(2);
+}
+
+void load_vortons(VECTOR<Vorton>& v, const float* pos, const float* angvel, const float* size, size_t n) {
+  v.Clear();
+  v.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Vorton w;
+    w.mPosition = Vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    w.mAngularVelocity = Vec3(angvel[3 * i], angvel[3 * i + 1], angvel[3 * i + 2]);
+    w.mSize = size[i];
+    v.PushBack(w);
+  }
+}
+
+void grid_to_floats(const UniformGrid<Vec3>& g, float* out) {
+  const size_t n = g.GetGridCapacity();
+  for (size_t i = 0; i < n; ++i) {
+    out[3 * i] = g[i].x;
+    out[3 * i + 1] = g[i].y;
+    out[3 * i + 2] = g[i].z;
+  }
+}
+
+void floats_to_grid(UniformGrid<Vec3>& g, const float* in) {
+  const size_t n = g.GetGridCapacity();
+  for (size_t i = 0; i < n; ++i) g[i] = Vec3(in[3 * i], in[3 * i + 1], in[3 * i + 2]);
+}
+
+/* A VortonSim whose grid template is set directly (geom) instead of derived
+ * from the bounding box, so each stage can be exercised on a given grid. */
+struct Sim {
+  VECTOR<Vorton> vortons;
+  VortonSim sim;
+  Sim(const float* pos, const float* angvel, const float* size, size_t n, const float* geom12, const unsigned* np,
+      float viscosity)
+      : sim(viscosity, 1.0f) {
+    load_vortons(vortons, pos, angvel, size, n);
+    sim.SetVortons(&vortons);
+    sim.SetFluidSimulationTechnique(VortonSim::FLUID_SIM_VORTEX_PARTICLE_METHOD);
+    load_geom(sim.mGridTemplate, geom12, np);
+  }
+};
+
+/* Run body over [0, m): TBB-parallel in the USE_TBB build, else serial. */
+template <class Body>
+void run_range(size_t m, const Body& body) {
+#if USE_TBB
+  tbb::parallel_for(tbb::blocked_range<size_t>(0, m, Max2(size_t(1), m / gNumberOfProcessors)), body);
+#else
+  body(tbb::blocked_range<size_t>(0, m));
+#endif
+}
+
+}  // namespace
+
+extern "C" {
+
+int vgref_uses_tbb(void) { return USE_TBB; }
+size_t vgref_sizeof_particle(void) { return sizeof(Particle); }
+
+void vgref_set_threads(unsigned n) { gNumberOfProcessors = n ? n : 1; }
+
+/* UniformGridGeometry::DefineShape (uniformGrid.h:259-322). */
+void vgref_define_shape(size_t n, const float vmin[3], const float vmax[3], int pow2, float geom12[12], unsigned np[3]) {
+  UniformGridGeometry g;
+  g.DefineShape(n, Vec3(vmin[0], vmin[1], vmin[2]), Vec3(vmax[0], vmax[1], vmax[2]), pow2 != 0);
+  store_geom(g, geom12, np);
+}
+
+/* UniformGridGeometry::IndicesOfPosition / OffsetOfPosition (uniformGrid.h:536-574, 645-651). */
+void vgref_indices_of_position(const float geom12[12], const unsigned np[3], const float* pos, size_t n,
+                               unsigned* idx3, unsigned* offset) {
+  UniformGridGeometry g;
+  load_geom(g, geom12, np);
+  for (size_t i = 0; i < n; ++i) {
+    unsigned ind[4];
+    const Vec3 p(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    g.IndicesOfPosition(ind, p);
+    idx3[3 * i] = ind[0];
+    idx3[3 * i + 1] = ind[1];
+    idx3[3 * i + 2] = ind[2];
+    offset[i] = g.OffsetOfPosition(p);
+  }
+}
+
+/* NestedGrid::Initialize shape (nestedGrid.h:69-85, 312-391): returns depth. */
+int vgref_nested_grid_shape(const float geom12[12], const unsigned np[3], unsigned* layer_np, unsigned* decim, int max_layers) {
+  UniformGridGeometry g;
+  load_geom(g, geom12, np);
+  NestedGrid<Vec3> ng(g);
+  const int depth = (int)ng.GetDepth();
+  for (int l = 0; l < depth && l < max_layers; ++l) {
+    layer_np[3 * l] = ng[l].GetNumPoints(0);
+    layer_np[3 * l + 1] = ng[l].GetNumPoints(1);
+    layer_np[3 * l + 2] = ng[l].GetNumPoints(2);
+    if (l > 0) {
+      const unsigned* d = ng.GetDecimations(l);
+      decim[3 * l] = d[0];
+      decim[3 * l + 1] = d[1];
+      decim[3 * l + 2] = d[2];
+    } else {
+      decim[0] = decim[1] = decim[2] = 0;
+    }
+  }
+  return depth;
+}
+
+/* CreateInfluenceTree (vortonSim.cpp:1605-1624): every layer's supervortons as
+ * 7 floats per point (pos xyz, angvel xyz, size), layers concatenated leaf first.
+ * Returns the number of points written (or needed, if cap is too small). */
+size_t vgref_influence_tree(const float* pos, const float* angvel, const float* size, size_t n, const float geom12[12],
+                            const unsigned np[3], float* out7, size_t cap_points) {
+  Sim s(pos, angvel, size, n, geom12, np, 0.0f);
+  NestedGrid<Vorton> tree;
+  s.sim.CreateInfluenceTree(tree);
+  size_t total = 0;
+  for (size_t l = 0; l < tree.GetDepth(); ++l) total += tree[l].GetGridCapacity();
+  if (total > cap_points) return total;
+  size_t k = 0;
+  for (size_t l = 0; l < tree.GetDepth(); ++l) {
+    for (size_t i = 0; i < tree[l].GetGridCapacity(); ++i, ++k) {
+      const Vorton& v = tree[l][i];
+      float* o = out7 + 7 * k;
+      o[0] = v.mPosition.x; o[1] = v.mPosition.y; o[2] = v.mPosition.z;
+      o[3] = v.mAngularVelocity.x; o[4] = v.mAngularVelocity.y; o[5] = v.mAngularVelocity.z;
+      o[6] = v.mSize;
+    }
+  }
+  return total;
+}
+
+/* ComputeVelocity_Direct / ComputeVectorPotential_Direct (vortonSim.cpp:1113-1158)
+ * at arbitrary query points; kind 0 = velocity, 1 = vector potential. */
+void vgref_direct(int kind, const float* pos, const float* angvel, const float* size, size_t n, const float* q, size_t m,
+                  float spread_range, float spread_circ, float* out) {
+  VECTOR<Vorton> v;
+  load_vortons(v, pos, angvel, size, n);
+  VortonSim sim(0.0f, 1.0f);
+  sim.SetVortons(&v);
+  sim.mSpreadingRangeFactor = spread_range;
+  sim.mSpreadingCirculationFactor = spread_circ;
+  struct Body {
+    VortonSim* sim; int kind; const float* q; float* out;
+    void operator()(const tbb::blocked_range<size_t>& r) const {
+      for (size_t i = r.begin(); i < r.end(); ++i) {
+        const Vec3 p(q[3 * i], q[3 * i + 1], q[3 * i + 2]);
+        const Vec3 u = kind == 0 ? sim->ComputeVelocity_Direct(p) : sim->ComputeVectorPotential_Direct(p);
+        out[3 * i] = u.x; out[3 * i + 1] = u.y; out[3 * i + 2] = u.z;
+      }
+    }
+  } body = {&sim, kind, q, out};
+  run_range(m, body);
+}
+
+/* ComputeVelocity_Tree / ComputeVectorPotential_Tree (vortonSim.cpp:1650-1905)
+ * from the root, as ComputeVelocityAtGridpoints_Slice calls them
+ * (vortonSim.cpp:2264-2267), at arbitrary query points. */
+void vgref_tree(int kind, const float* pos, const float* angvel, const float* size, size_t n, const float geom12[12],
+                const unsigned np[3], const float* q, size_t m, float spread_range, float spread_circ, float* out) {
+  Sim s(pos, angvel, size, n, geom12, np, 0.0f);
+  NestedGrid<Vorton> tree;
+  s.sim.CreateInfluenceTree(tree);
+  s.sim.mSpreadingRangeFactor = spread_range;
+  s.sim.mSpreadingCirculationFactor = spread_circ;
+  UniformGrid<VECTOR<unsigned> > dummy;
+  struct Body {
+    VortonSim* sim; NestedGrid<Vorton>* tree; UniformGrid<VECTOR<unsigned> >* idx; int kind; const float* q; float* out;
+    void operator()(const tbb::blocked_range<size_t>& r) const {
+      static const unsigned zeros[3] = {0, 0, 0};
+      const size_t numLayers = tree->GetDepth();
+      for (size_t i = r.begin(); i < r.end(); ++i) {
+        const Vec3 p(q[3 * i], q[3 * i + 1], q[3 * i + 2]);
+        Vec3 u;
+        if (numLayers > 1)
+          u = kind == 0 ? sim->ComputeVelocity_Tree(p, zeros, numLayers - 1, *idx, *tree)
+                        : sim->ComputeVectorPotential_Tree(p, zeros, numLayers - 1, *idx, *tree);
+        else
+          u = kind == 0 ? sim->ComputeVelocity_Direct(p) : sim->ComputeVectorPotential_Direct(p);
+        out[3 * i] = u.x; out[3 * i + 1] = u.y; out[3 * i + 2] = u.z;
+      }
+    }
+  } body = {&s.sim, &tree, &dummy, kind, q, out};
+  run_range(m, body);
+}
+
+/* PopulateVorticityGridFromVortons(grid, scale) (vortonSim.cpp:2372-2436). */
+void vgref_splat(const float* pos, const float* angvel, const float* size, size_t n, const float geom12[12],
+                 const unsigned np[3], float scale, float* grid_out) {
+  Sim s(pos, angvel, size, n, geom12, np, 0.0f);
+  UniformGrid<Vec3> g;
+  s.sim.PopulateVorticityGridFromVortons(g, scale);
+  grid_to_floats(g, grid_out);
+}
+
+/* ComputeVectorPotentialFromVorticity_Integral(boundariesOnly) on a zeroed grid
+ * (vortonSim.cpp:2055-2138, 2154-2204). */
+void vgref_boundary_vecpot(const float* pos, const float* angvel, const float* size, size_t n, const float geom12[12],
+                           const unsigned np[3], int boundaries_only, float* grid_out) {
+  Sim s(pos, angvel, size, n, geom12, np, 0.0f);
+  NestedGrid<Vorton> tree;
+  s.sim.CreateInfluenceTree(tree);
+  s.sim.mVelGrid.CopyShape(s.sim.mGridTemplate);
+  s.sim.mVelGrid.Init();
+  s.sim.mVectorPotentialMultiGrid.Initialize(s.sim.mGridTemplate);
+  s.sim.mVectorPotentialMultiGrid[0].Init(Vec3(0.0f, 0.0f, 0.0f));
+  UniformGrid<VECTOR<unsigned> > dummy;
+  s.sim.ComputeVectorPotentialFromVorticity_Integral(boundaries_only != 0, dummy, tree);
+  grid_to_floats(s.sim.mVectorPotentialMultiGrid[0], grid_out);
+}
+
+/* SolveVectorPoisson(soln, lap, steps, Dirichlet) (uniformGridMath.cpp:1369-1405). */
+void vgref_sor(const float geom12[12], const unsigned np[3], float* soln_inout, const float* lap, int steps) {
+  UniformGrid<Vec3> soln, rhs;
+  load_geom(soln, geom12, np);
+  load_geom(rhs, geom12, np);
+  soln.Init();
+  rhs.Init();
+  floats_to_grid(soln, soln_inout);
+  floats_to_grid(rhs, lap);
+  Stats_Float stats;
+  SolveVectorPoisson(soln, rhs, (size_t)steps, BC_DIRICHLET, stats);
+  grid_to_floats(soln, soln_inout);
+}
+
+/* DownSampleInto(1, mode) then UpSampleFrom(1, region) on a 2-layer NestedGrid
+ * (nestedGrid.h:253-293, uniformGrid.h:1453-1700).  fine_in: the fine layer;
+ * coarse_out: the restricted coarse layer; fine_out: fine layer after
+ * up-sampling coarse_out back into it (region 0 entire, 1 interior only). */
+void vgref_down_up(const float geom12[12], const unsigned np[3], const float* fine_in, int accuracy, int region,
+                   float* coarse_out, unsigned coarse_np[3], float* fine_out) {
+  UniformGridGeometry g;
+  load_geom(g, geom12, np);
+  NestedGrid<Vec3> ng(g);
+  ng[0].Init();
+  floats_to_grid(ng[0], fine_in);
+  ng[1].Init();
+  ng.DownSampleInto(1, accuracy ? UniformGridGeometry::FASTER_LESS_ACCURATE : UniformGridGeometry::SLOWER_MORE_ACCURATE);
+  grid_to_floats(ng[1], coarse_out);
+  coarse_np[0] = ng[1].GetNumPoints(0);
+  coarse_np[1] = ng[1].GetNumPoints(1);
+  coarse_np[2] = ng[1].GetNumPoints(2);
+  ng.UpSampleFrom(1, region ? UniformGridGeometry::INTERIOR_ONLY : UniformGridGeometry::ENTIRE_DOMAIN);
+  grid_to_floats(ng[0], fine_out);
+}
+
+/* The multigrid cascade of VortonSim::ComputeVectorPotential
+ * (vortonSim.cpp:2539-2571): soln_inout holds the boundary values (interior
+ * zero) on entry and the cascade's result on exit; rhs is -vorticity. */
+void vgref_cascade(const float geom12[12], const unsigned np[3], float* soln_inout, const float* rhs, int steps) {
+  UniformGridGeometry g;
+  load_geom(g, geom12, np);
+  NestedGrid<Vec3> a(g), b(g);
+  for (size_t l = 0; l < a.GetDepth(); ++l) { a[l].Init(); b[l].Init(); }
+  floats_to_grid(a[0], soln_inout);
+  floats_to_grid(b[0], rhs);
+  Stats_Float stats;
+  const size_t numSolverSteps = (size_t)steps;
+  SolveVectorPoisson(a[0], b[0], numSolverSteps, BC_DIRICHLET, stats);
+  unsigned maxValidDepth = 0;
+  for (unsigned iLayer = 1; iLayer < b.GetDepth(); ++iLayer) {
+    const unsigned minDim = MIN3(b[iLayer].GetNumPoints(0), b[iLayer].GetNumPoints(1), b[iLayer].GetNumPoints(2));
+    if (minDim > 2) {
+      b.DownSampleInto(iLayer, UniformGridGeometry::FASTER_LESS_ACCURATE);
+      a.DownSampleInto(iLayer, UniformGridGeometry::FASTER_LESS_ACCURATE);
+      SolveVectorPoisson(a[iLayer], b[iLayer], numSolverSteps, BC_DIRICHLET, stats);
+    } else {
+      maxValidDepth = iLayer - 1;
+      break;
+    }
+  }
+  for (unsigned iLayer = maxValidDepth; iLayer >= 1; --iLayer) {
+    a.UpSampleFrom(iLayer, UniformGridGeometry::INTERIOR_ONLY);
+    SolveVectorPoisson(a[iLayer - 1], b[iLayer - 1], numSolverSteps, BC_DIRICHLET, stats);
+  }
+  grid_to_floats(a[0], soln_inout);
+}
+
+/* ComputeJacobian + ComputeCurlFromJacobian (uniformGridMath.cpp:207-451). */
+void vgref_jacobian_curl(const float geom12[12], const unsigned np[3], const float* vec, float* jac9_out, float* curl_out) {
+  UniformGrid<Vec3> v, c;
+  UniformGrid<Mat33> j;
+  load_geom(v, geom12, np);
+  load_geom(c, geom12, np);
+  load_geom(j, geom12, np);
+  v.Init(); c.Init(); j.Init();
+  floats_to_grid(v, vec);
+  ComputeJacobian(j, v);
+  ComputeCurlFromJacobian(c, j);
+  const size_t n = j.GetGridCapacity();
+  for (size_t i = 0; i < n; ++i) {
+    const Mat33& m = j[i];
+    float* o = jac9_out + 9 * i;
+    o[0] = m.x.x; o[1] = m.x.y; o[2] = m.x.z;
+    o[3] = m.y.x; o[4] = m.y.y; o[5] = m.y.z;
+    o[6] = m.z.x; o[7] = m.z.y; o[8] = m.z.z;
+  }
+  grid_to_floats(c, curl_out);
+}
+
+/* StretchAndTiltVortons (vortonSim.cpp:2748-2820) with mVelGrid = velgrid. */
+void vgref_stretch(float* pos, float* angvel_inout, const float* size, size_t n, const float geom12[12], const unsigned np[3],
+                   const float* velgrid, float dt) {
+  Sim s(pos, angvel_inout, size, n, geom12, np, 0.0f);
+  s.sim.mVelGrid.CopyShape(s.sim.mGridTemplate);
+  s.sim.mVelGrid.Init();
+  floats_to_grid(s.sim.mVelGrid, velgrid);
+  s.sim.StretchAndTiltVortons(dt, 0);
+  for (size_t i = 0; i < n; ++i) {
+    angvel_inout[3 * i] = s.vortons[i].mAngularVelocity.x;
+    angvel_inout[3 * i + 1] = s.vortons[i].mAngularVelocity.y;
+    angvel_inout[3 * i + 2] = s.vortons[i].mAngularVelocity.z;
+  }
+}
+
+/* PartitionVortons + DiffuseAndDissipateVorticityPSE (vortonSim.cpp:3578-3879). */
+void vgref_pse(const float* pos, float* angvel_inout, const float* size, size_t n, const float geom12[12], const unsigned np[3],
+               float viscosity, float dt) {
+  Sim s(pos, angvel_inout, size, n, geom12, np, viscosity);
+  s.sim.PartitionVortons(dt, 0, s.sim.mVortonIndicesGrid);
+  s.sim.DiffuseAndDissipateVorticityPSE(dt, 0, s.sim.mVortonIndicesGrid);
+  for (size_t i = 0; i < n; ++i) {
+    angvel_inout[3 * i] = s.vortons[i].mAngularVelocity.x;
+    angvel_inout[3 * i + 1] = s.vortons[i].mAngularVelocity.y;
+    angvel_inout[3 * i + 2] = s.vortons[i].mAngularVelocity.z;
+  }
+}
+
+/* AssignVelocityFromField(gain 1) then Evolve (pclOpAdvect.cpp:42-152,
+ * pclOpEvolve.cpp:36-58) on particles given by position; vel_out receives the
+ * gathered velocity, pos_inout the advected position. */
+void vgref_advect(float* pos_inout, float* vel_out, size_t n, const float geom12[12], const unsigned np[3],
+                  const float* velgrid, float dt) {
+  UniformGrid<Vec3> g;
+  load_geom(g, geom12, np);
+  g.Init();
+  floats_to_grid(g, velgrid);
+  VECTOR<Particle> p;
+  p.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle q;
+    q.mPosition = Vec3(pos_inout[3 * i], pos_inout[3 * i + 1], pos_inout[3 * i + 2]);
+    p.PushBack(q);
+  }
+  AssignVelocityFromField(p, &g, 1.0f);
+  for (size_t i = 0; i < n; ++i) {
+    vel_out[3 * i] = p[i].mVelocity.x; vel_out[3 * i + 1] = p[i].mVelocity.y; vel_out[3 * i + 2] = p[i].mVelocity.z;
+    Particle& pc = p[i];
+    pc.mPosition += pc.mVelocity * dt;  /* EvolveParticlesSlice body (pclOpEvolve.cpp:51) */
+    pos_inout[3 * i] = pc.mPosition.x; pos_inout[3 * i + 1] = pc.mPosition.y; pos_inout[3 * i + 2] = pc.mPosition.z;
+  }
+}
+
+/* Find the AABB the way PclOpFindBoundingBox does (pclOpFindBoundingBox.cpp:102-140). */
+void vgref_find_bbox(const float* pos, size_t n, float mn[3], float mx[3]) {
+  VECTOR<Particle> p;
+  p.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle q;
+    q.mPosition = Vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    p.PushBack(q);
+  }
+  Vec3 a(FLT_MAX, FLT_MAX, FLT_MAX), b(-FLT_MAX, -FLT_MAX, -FLT_MAX);
+  PclOpFindBoundingBox::FindBoundingBox(p, a, b);
+  mn[0] = a.x; mn[1] = a.y; mn[2] = a.z;
+  mx[0] = b.x; mx[1] = b.y; mx[2] = b.z;
+}
+
+/* One PclOpVortonSim::Operate (pclOpVortonSim.cpp:51-71) on Particle records
+ * (sizeof(Particle) stride), with an optional extra box (the tracers' AABB).
+ * The reference's grids outlive the call in a static op so that
+ * vgref_last_grids can read them. */
+static PclOpVortonSim* g_op = 0;
+
+int vgref_step(void* particles, size_t n, const float* extra_min, const float* extra_max, float dt, unsigned frame,
+               float viscosity, float geom12_out[12], unsigned np_out[3]) {
+  if (!g_op) g_op = new PclOpVortonSim;
+  g_op->mVortonSim.mViscosity = viscosity;
+  g_op->mVortonSim.SetFluidSimulationTechnique(VortonSim::FLUID_SIM_VORTEX_PARTICLE_METHOD);
+  VECTOR<Particle> v;
+  v.Reserve(n);
+  const Particle* src = static_cast<const Particle*>(particles);
+  for (size_t i = 0; i < n; ++i) v.PushBack(src[i]);
+  static Vec3 emin, emax;
+  if (extra_min && extra_max) {
+    emin = Vec3(extra_min[0], extra_min[1], extra_min[2]);
+    emax = Vec3(extra_max[0], extra_max[1], extra_max[2]);
+    g_op->mMinCorner = &emin;
+    g_op->mMaxCorner = &emax;
+  } else {
+    g_op->mMinCorner = 0;
+    g_op->mMaxCorner = 0;
+  }
+  g_op->Operate(v, dt, frame);
+  Particle* dst = static_cast<Particle*>(particles);
+  for (size_t i = 0; i < n; ++i) dst[i] = v[i];
+  g_op->mVortonSim.SetVortons(0);
+  store_geom(g_op->mVortonSim.mGridTemplate, geom12_out, np_out);
+  return 0;
+}
+
+/* Velocity grid and finest vector-potential / negative-vorticity layers of the
+ * last vgref_step (sizes from its np_out). */
+void vgref_last_grids(float* vel_out, float* vecpot_out, float* negvort_out) {
+  if (!g_op) return;
+  if (vel_out) grid_to_floats(g_op->mVortonSim.mVelGrid, vel_out);
+  if (vecpot_out) grid_to_floats(g_op->mVortonSim.mVectorPotentialMultiGrid[0], vecpot_out);
+  if (negvort_out) grid_to_floats(g_op->mVortonSim.mNegativeVorticityMultiGrid[0], negvort_out);
+}
+
+}  // extern "C"

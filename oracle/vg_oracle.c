@@ -1,0 +1,958 @@
+/* CPU oracle for the VortonSim velocity-from-vorticity step.
+ *
+ * TEST INFRASTRUCTURE ONLY (see vg_oracle.h).  A plain-C restatement of the
+ * reference's algorithms, following the float operation order of the
+ * reference's C++ (which the compiler would otherwise be free to fuse), so
+ * results are bit-identical to the reference built with -ffp-contract=off.
+ * Reference paths are relative to Samples/MjgIntelFluidDemo_Part20.
+ */
+#include "vg_oracle.h"
+
+#include <float.h>
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+
+#define PI_F 3.1415926535897932384626433832795f
+
+static float maxf_(float a, float b) { return a > b ? a : b; } /* Max2 (Core/Utility/macros.h:64) */
+static float minf_(float a, float b) { return a < b ? a : b; } /* Min2 (Core/Utility/macros.h:61) */
+static float clampf_(float x, float lo, float hi) { return minf_(maxf_(x, lo), hi); }
+
+/* finvsqrtf (Core/Math/math.h:206-216): Lomont's magic-constant estimate
+ * 0x5f3759df - (i >> 1) refined by one Newton step. */
+float vgo_finvsqrtf(float v) {
+  int32_t i;
+  memcpy(&i, &v, 4);
+  i = 0x5f3759df - (i >> 1);
+  float y;
+  memcpy(&y, &i, 4);
+  const float f = 1.5f;
+  const float x = v * 0.5f;
+  y = y * (f - (x * y * y));
+  return y;
+}
+
+/* ------------------------------------------------------------------ geometry */
+
+/* PrecomputeSpacing (uniformGrid.h:794-809). */
+void vgo_precompute_spacing(vgo_geom* g) {
+  for (int a = 0; a < 3; ++a) g->cell[a] = g->ext[a] / (float)(g->np[a] - 1);
+  g->cpe[0] = (float)(g->np[0] - 1) / g->ext[0];
+  g->cpe[1] = (float)(g->np[1] - 1) / g->ext[1];
+  g->cpe[2] = (0.0f == g->ext[2]) ? 1.0f / FLT_MIN : (float)(g->np[2] - 1) / g->ext[2];
+}
+
+/* NearestPowerOfTwo (Core/Math/math.h:149-175). */
+static size_t nearest_pow2(size_t v) {
+  if (v == 0) return 1;
+  --v;
+  unsigned shift = 0;
+  while ((v >> shift) != 0) ++shift;
+  return (size_t)(1U << shift);
+}
+
+/* DefineShape (uniformGrid.h:259-322). */
+void vgo_define_shape(size_t n, const float vmin[3], const float vmax[3], int pow2, vgo_geom* g) {
+  memset(g, 0, sizeof(*g));
+  if (n == 0) return;
+  const float nudge = 1.0f + FLT_EPSILON;
+  float eff[3];
+  int dims = 3;
+  for (int a = 0; a < 3; ++a) {
+    g->mn[a] = vmin[a];
+    g->ext[a] = (vmax[a] - vmin[a]) * nudge;
+    eff[a] = g->ext[a];
+  }
+  for (int a = 0; a < 3; ++a) {
+    if (0.0f == eff[a]) {
+      eff[a] = 1.0f;
+      g->ext[a] = 0.0f;
+      --dims;
+    }
+  }
+  const float volume = eff[0] * eff[1] * eff[2];
+  const float inv_cell = powf(volume / (float)n, -1.0f / (float)dims);
+  size_t nc[3];
+  for (int a = 0; a < 3; ++a) {
+    size_t c = (size_t)(g->ext[a] * inv_cell + 0.5f);
+    nc[a] = c > 1 ? c : 1;
+  }
+  if (pow2)
+    for (int a = 0; a < 3; ++a) nc[a] = nearest_pow2(nc[a]);
+  while (nc[0] * nc[1] * nc[2] >= n * 8)
+    for (int a = 0; a < 3; ++a) nc[a] = nc[a] / 2 > 1 ? nc[a] / 2 : 1;
+  for (int a = 0; a < 3; ++a) g->np[a] = (unsigned)(nc[a] + 1);
+  vgo_precompute_spacing(g);
+}
+
+/* Decimate (uniformGrid.h:398-412). */
+void vgo_decimate(const vgo_geom* src, unsigned dec, vgo_geom* dst) {
+  vgo_geom d = *src;
+  for (int a = 0; a < 3; ++a) {
+    d.np[a] = (src->np[a] - 1) / dec + 1;
+    if (dec > 1 && d.np[a] < 2) d.np[a] = 2;
+  }
+  vgo_precompute_spacing(&d);
+  *dst = d;
+}
+
+/* IndicesOfPosition (uniformGrid.h:536-574): FP32 (p - min) * cellsPerExtent,
+ * truncated toward zero (x87 fistp under a truncating control word). */
+void vgo_indices_of_position(const vgo_geom* g, const float p[3], unsigned idx[3]) {
+  for (int a = 0; a < 3; ++a) {
+    const float rel = p[a] - g->mn[a];
+    const float v = rel * g->cpe[a];
+    idx[a] = (unsigned)(int)v;
+  }
+}
+
+/* OffsetOfPosition (uniformGrid.h:645-651). */
+unsigned vgo_offset_of_position(const vgo_geom* g, const float p[3]) {
+  unsigned i[3];
+  vgo_indices_of_position(g, p, i);
+  return i[0] + g->np[0] * (i[1] + g->np[1] * i[2]);
+}
+
+void vgo_indices_batch(const vgo_geom* g, const float* pos, size_t n, unsigned* idx3, unsigned* offset) {
+  for (size_t k = 0; k < n; ++k) {
+    vgo_indices_of_position(g, pos + 3 * k, idx3 + 3 * k);
+    offset[k] = vgo_offset_of_position(g, pos + 3 * k);
+  }
+}
+
+static size_t capacity(const vgo_geom* g) { return (size_t)g->np[0] * g->np[1] * g->np[2]; }
+
+/* NestedGrid::Initialize + PrecomputeDecimations (nestedGrid.h:69-85, 355-391):
+ * layer 0 copies g; each parent decimates its child by 2 until the child has
+ * at most 8 points.  decim3[3l..3l+2] = child cells / parent cells (l >= 1). */
+int vgo_nested_shape(const vgo_geom* g, vgo_geom* layers, unsigned* decim3) {
+  int depth = 0;
+  vgo_decimate(g, 1, &layers[depth++]);
+  while (capacity(&layers[depth - 1]) > 8 && depth < VGO_MAX_LAYERS) {
+    vgo_decimate(&layers[depth - 1], 2, &layers[depth]);
+    ++depth;
+  }
+  decim3[0] = decim3[1] = decim3[2] = 0;
+  for (int l = 1; l < depth; ++l)
+    for (int a = 0; a < 3; ++a) decim3[3 * l + a] = (layers[l - 1].np[a] - 1) / (layers[l].np[a] - 1);
+  return depth;
+}
+
+/* PclOpFindBoundingBox::FindBoundingBox serial form (pclOpFindBoundingBox.cpp:115-136). */
+void vgo_bbox(const float* pos, size_t n, float mn[3], float mx[3]) {
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = FLT_MAX;
+    mx[a] = -FLT_MAX;
+  }
+  for (size_t k = 0; k < n; ++k)
+    for (int a = 0; a < 3; ++a) {
+      mn[a] = minf_(mn[a], pos[3 * k + a]);
+      mx[a] = maxf_(mx[a], pos[3 * k + a]);
+    }
+}
+
+/* PclOpVortonSim::Operate's box -> VortonSim::UpdateBoundingBox(final)
+ * (pclOpVortonSim.cpp:51-71, vortonSim.cpp:1027-1096): vorton AABB, joined
+ * with the extra box (or the first vorton), padded by 3 radii, then
+ * DefineShape(n, ..., pow2). */
+void vgo_step_geometry(const float* pos, size_t n, float radius, const float* extra_min, const float* extra_max,
+                       vgo_geom* g) {
+  float mn[3], mx[3];
+  vgo_bbox(pos, n, mn, mx);
+  const float* emin = (extra_min && extra_max) ? extra_min : pos;
+  const float* emax = (extra_min && extra_max) ? extra_max : pos;
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = minf_(mn[a], emin[a]);
+    mx[a] = maxf_(mx[a], emax[a]);
+  }
+  const float margin = (1.0f + 2.0f) * radius;
+  for (int a = 0; a < 3; ++a) {
+    const float d = mx[a] - mn[a];
+    mn[a] -= 0.0f * d; /* expansionFactor 0 (vortonSim.cpp:1068-1074) */
+    mx[a] += 0.0f * d;
+    mn[a] -= margin * 1.0f;
+    mx[a] += margin * 1.0f;
+  }
+  vgo_define_shape(n, mn, mx, 1, g);
+}
+
+/* ------------------------------------------------------------- vorton laws */
+
+static const float kTwoThirds = 2.0f / 3.0f; /* vorton.h:92 */
+
+/* VORTON_ACCUMULATE_VELOCITY_private (vorton.h:161-179). */
+static void accum_velocity(float acc[3], const float q[3], const float p[3], const float w[3], float size, float sr,
+                           float sc) {
+  const float d0 = q[0] - p[0], d1 = q[1] - p[1], d2 = q[2] - p[2];
+  const float radius = size * 0.5f * sr;
+  const float r2 = radius * radius;
+  const float dist2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const float law = (dist2 < r2) ? (1.0f / (r2 * radius)) : (vgo_finvsqrtf(dist2) / dist2);
+  const float s = kTwoThirds * r2 * radius;
+  const float a0 = w[0] * s, a1 = w[1] * s, a2 = w[2] * s;
+  const float b0 = d0 * law, b1 = d1 * law, b2 = d2 * law;
+  const float c0 = a1 * b2 - a2 * b1, c1 = a2 * b0 - a0 * b2, c2 = a0 * b1 - a1 * b0;
+  acc[0] += c0 * sc;
+  acc[1] += c1 * sc;
+  acc[2] += c2 * sc;
+}
+
+/* VORTON_ACCUMULATE_VECTOR_POTENTIAL_private (vorton.h:118-136). */
+static void accum_vecpot(float acc[3], const float q[3], const float p[3], const float w[3], float size, float sr,
+                         float sc) {
+  const float d0 = q[0] - p[0], d1 = q[1] - p[1], d2 = q[2] - p[2];
+  const float radius = size * 0.5f * sr;
+  const float r2 = radius * radius;
+  const float dist2 = d0 * d0 + d1 * d1 + d2 * d2;
+  const float law = (dist2 < r2) ? (dist2 / (r2 * radius)) : vgo_finvsqrtf(dist2);
+  const float s = kTwoThirds * r2 * radius;
+  acc[0] += ((w[0] * s) * law) * sc;
+  acc[1] += ((w[1] * s) * law) * sc;
+  acc[2] += ((w[2] * s) * law) * sc;
+}
+
+static void accum(int kind, float acc[3], const float q[3], const float p[3], const float w[3], float size, float sr,
+                  float sc) {
+  if (kind == 0)
+    accum_velocity(acc, q, p, w, size, sr, sc);
+  else
+    accum_vecpot(acc, q, p, w, size, sr, sc);
+}
+
+void vgo_direct(int kind, const float* pos, const float* angvel, const float* size, size_t n, const float* q,
+                size_t m, float sr, float sc, float* out) {
+  for (size_t j = 0; j < m; ++j) {
+    float acc[3] = {0.0f, 0.0f, 0.0f};
+    for (size_t i = 0; i < n; ++i) accum(kind, acc, q + 3 * j, pos + 3 * i, angvel + 3 * i, size[i], sr, sc);
+    memcpy(out + 3 * j, acc, sizeof(acc));
+  }
+}
+
+/* The same mollified laws in FP64 with an exact 1/sqrt: the strict oracle. */
+void vgo_direct_f64(int kind, const float* pos, const float* angvel, const float* size, size_t n, const float* q,
+                    size_t m, float sr, float sc, double* out) {
+  for (size_t j = 0; j < m; ++j) {
+    double acc[3] = {0, 0, 0};
+    for (size_t i = 0; i < n; ++i) {
+      const double d0 = (double)q[3 * j] - pos[3 * i], d1 = (double)q[3 * j + 1] - pos[3 * i + 1],
+                   d2 = (double)q[3 * j + 2] - pos[3 * i + 2];
+      const double radius = (double)size[i] * 0.5 * sr;
+      const double r2 = radius * radius;
+      const double dist2 = d0 * d0 + d1 * d1 + d2 * d2;
+      const double s = (2.0 / 3.0) * r2 * radius * sc;
+      const double w0 = angvel[3 * i] * s, w1 = angvel[3 * i + 1] * s, w2 = angvel[3 * i + 2] * s;
+      if (kind == 0) {
+        const double law = dist2 < r2 ? 1.0 / (r2 * radius) : 1.0 / (sqrt(dist2) * dist2);
+        acc[0] += (w1 * d2 - w2 * d1) * law;
+        acc[1] += (w2 * d0 - w0 * d2) * law;
+        acc[2] += (w0 * d1 - w1 * d0) * law;
+      } else {
+        const double law = dist2 < r2 ? dist2 / (r2 * radius) : 1.0 / sqrt(dist2);
+        acc[0] += w0 * law;
+        acc[1] += w1 * law;
+        acc[2] += w2 * law;
+      }
+    }
+    out[3 * j] = acc[0];
+    out[3 * j + 1] = acc[1];
+    out[3 * j + 2] = acc[2];
+  }
+}
+
+/* ------------------------------------------------------------ influence tree */
+
+typedef struct {
+  int depth;
+  vgo_geom layer[VGO_MAX_LAYERS];
+  unsigned decim[3 * VGO_MAX_LAYERS];
+  size_t base[VGO_MAX_LAYERS]; /* first point of each layer in sv */
+  float* sv;                   /* 7 floats per point: pos, angvel, size */
+} tree_t;
+
+static float vort_mag(const float w[3]) {
+  /* GetVorticity().Magnitude(): sqrtf(Mag2(angvel * 2)) (vorton.h:316-320, vec3.h:415-418) */
+  const float a = w[0] * 2.0f, b = w[1] * 2.0f, c = w[2] * 2.0f;
+  return sqrtf(a * a + b * b + c * c);
+}
+
+static void tree_build(tree_t* t, const float* pos, const float* angvel, const float* size, size_t n,
+                       const vgo_geom* g) {
+  t->depth = vgo_nested_shape(g, t->layer, t->decim);
+  size_t total = 0;
+  for (int l = 0; l < t->depth; ++l) {
+    t->base[l] = total;
+    total += capacity(&t->layer[l]);
+  }
+  t->sv = (float*)calloc(total * 7, sizeof(float));
+  /* MakeBaseVortonGrid (vortonSim.cpp:1192-1321). */
+  const vgo_geom* leaf = &t->layer[0];
+  const size_t nleaf = capacity(leaf);
+  float* aux = (float*)malloc(nleaf * sizeof(float));
+  for (size_t k = 0; k < nleaf; ++k) aux[k] = FLT_MIN; /* VortonClusterAux (vortonClusterAux.h:71) */
+  for (size_t i = 0; i < n; ++i) {
+    const unsigned off = vgo_offset_of_position(leaf, pos + 3 * i);
+    float* c = t->sv + 7 * (t->base[0] + off);
+    const float mag = vort_mag(angvel + 3 * i);
+    c[0] += pos[3 * i] * mag;
+    c[1] += pos[3 * i + 1] * mag;
+    c[2] += pos[3 * i + 2] * mag;
+    c[3] += angvel[3 * i];
+    c[4] += angvel[3 * i + 1];
+    c[5] += angvel[3 * i + 2];
+    c[6] = size[i];
+    aux[off] += mag;
+  }
+  for (size_t k = 0; k < nleaf; ++k) {
+    if (aux[k] != FLT_MIN) {
+      float* c = t->sv + 7 * (t->base[0] + k);
+      const float r = 1.0f / aux[k];
+      c[0] *= r;
+      c[1] *= r;
+      c[2] *= r;
+    }
+  }
+  free(aux);
+  /* AggregateClusters (vortonSim.cpp:1337-1569). */
+  for (int l = 1; l < t->depth; ++l) {
+    const vgo_geom* P = &t->layer[l];
+    const vgo_geom* C = &t->layer[l - 1];
+    const unsigned* d = t->decim + 3 * l;
+    for (unsigned pz = 0; pz < P->np[2] - 1; ++pz)
+      for (unsigned py = 0; py < P->np[1] - 1; ++py)
+        for (unsigned px = 0; px < P->np[0] - 1; ++px) {
+          float* p = t->sv + 7 * (t->base[l] + px + P->np[0] * (py + P->np[1] * pz));
+          float a = FLT_MIN;
+          for (unsigned iz = 0; iz < d[2]; ++iz)
+            for (unsigned iy = 0; iy < d[1]; ++iy)
+              for (unsigned ix = 0; ix < d[0]; ++ix) {
+                const unsigned cx = px * d[0] + ix, cy = py * d[1] + iy, cz = pz * d[2] + iz;
+                const float* c = t->sv + 7 * (t->base[l - 1] + cx + C->np[0] * (cy + C->np[1] * cz));
+                const float mag = vort_mag(c + 3);
+                p[0] += c[0] * mag;
+                p[1] += c[1] * mag;
+                p[2] += c[2] * mag;
+                p[3] += c[3];
+                p[4] += c[4];
+                p[5] += c[5];
+                a += mag;
+                if (c[6] != 0.0f) p[6] = c[6];
+              }
+          const float r = 1.0f / a;
+          p[0] *= r;
+          p[1] *= r;
+          p[2] *= r;
+        }
+  }
+}
+
+size_t vgo_influence_tree(const float* pos, const float* angvel, const float* size, size_t n, const vgo_geom* g,
+                          float* out7) {
+  tree_t t;
+  if (!out7) {
+    vgo_geom layers[VGO_MAX_LAYERS];
+    unsigned dec[3 * VGO_MAX_LAYERS];
+    const int depth = vgo_nested_shape(g, layers, dec);
+    size_t total = 0;
+    for (int l = 0; l < depth; ++l) total += capacity(&layers[l]);
+    return total;
+  }
+  tree_build(&t, pos, angvel, size, n, g);
+  const size_t total = t.base[t.depth - 1] + capacity(&t.layer[t.depth - 1]);
+  memcpy(out7, t.sv, total * 7 * sizeof(float));
+  free(t.sv);
+  return total;
+}
+
+/* ComputeVelocity_Tree / ComputeVectorPotential_Tree (vortonSim.cpp:1650-1905):
+ * open the child cell containing q (within 1e-4 cell spacings) while the
+ * layer is above the leaf's parent; otherwise add the child supervorton. */
+static void tree_eval(const tree_t* t, int kind, const float q[3], const unsigned idx[3], int layer, float sr,
+                      float sc, float acc_out[3]) {
+  const vgo_geom* C = &t->layer[layer - 1];
+  const unsigned* d = t->decim + 3 * layer;
+  const unsigned cmin[3] = {idx[0] * d[0], idx[1] * d[1], idx[2] * d[2]};
+  const float margin_factor = 0.0001f;
+  float margin[3] = {margin_factor * C->cell[0], margin_factor * C->cell[1], margin_factor * C->cell[2]};
+  margin[0] = margin[0] + 0.0f;
+  margin[1] = margin[1] + 0.0f;
+  margin[2] = margin[2] + (0.0f == C->cell[2] ? FLT_MIN : 0.0f);
+  float acc[3] = {0.0f, 0.0f, 0.0f};
+  for (unsigned iz = 0; iz < d[2]; ++iz) {
+    unsigned ch[3];
+    ch[2] = cmin[2] + iz;
+    const float mnz = C->mn[2] + (float)ch[2] * C->cell[2];
+    const float mxz = C->mn[2] + (float)(ch[2] + 1) * C->cell[2];
+    for (unsigned iy = 0; iy < d[1]; ++iy) {
+      ch[1] = cmin[1] + iy;
+      const float mny = C->mn[1] + (float)ch[1] * C->cell[1];
+      const float mxy = C->mn[1] + (float)(ch[1] + 1) * C->cell[1];
+      for (unsigned ix = 0; ix < d[0]; ++ix) {
+        ch[0] = cmin[0] + ix;
+        const float mnx = C->mn[0] + (float)ch[0] * C->cell[0];
+        const float mxx = C->mn[0] + (float)(ch[0] + 1) * C->cell[0];
+        if (layer > 1 && q[0] >= mnx - margin[0] && q[1] >= mny - margin[1] && q[2] >= mnz - margin[2] &&
+            q[0] < mxx + margin[0] && q[1] < mxy + margin[1] && q[2] < mxz + margin[2]) {
+          float sub[3];
+          tree_eval(t, kind, q, ch, layer - 1, sr, sc, sub);
+          acc[0] += sub[0];
+          acc[1] += sub[1];
+          acc[2] += sub[2];
+        } else {
+          const float* s = t->sv + 7 * (t->base[layer - 1] + ch[0] + C->np[0] * (ch[1] + C->np[1] * ch[2]));
+          accum(kind, acc, q, s, s + 3, s[6], sr, sc);
+        }
+      }
+    }
+  }
+  memcpy(acc_out, acc, sizeof(acc));
+}
+
+static void tree_query(const tree_t* t, int kind, const float* pos, const float* angvel, const float* size, size_t n,
+                       const float q[3], float sr, float sc, float out[3]) {
+  static const unsigned zeros[3] = {0, 0, 0};
+  if (t->depth > 1) {
+    tree_eval(t, kind, q, zeros, t->depth - 1, sr, sc, out);
+  } else {
+    float acc[3] = {0, 0, 0};
+    for (size_t i = 0; i < n; ++i) accum(kind, acc, q, pos + 3 * i, angvel + 3 * i, size[i], sr, sc);
+    memcpy(out, acc, sizeof(acc));
+  }
+}
+
+void vgo_tree(int kind, const float* pos, const float* angvel, const float* size, size_t n, const vgo_geom* g,
+              const float* q, size_t m, float sr, float sc, float* out) {
+  tree_t t;
+  tree_build(&t, pos, angvel, size, n, g);
+  for (size_t j = 0; j < m; ++j) tree_query(&t, kind, pos, angvel, size, n, q + 3 * j, sr, sc, out + 3 * j);
+  free(t.sv);
+}
+
+/* -------------------------------------------------------------- grid fields */
+
+/* PopulateVorticityGridFromVortons (vortonSim.cpp:2372-2436) with
+ * UniformGrid::Accumulate (uniformGrid.h:1278-1342). */
+void vgo_splat(const float* pos, const float* angvel, const float* size, size_t n, const vgo_geom* g, float scale,
+               float* grid) {
+  memset(grid, 0, capacity(g) * 3 * sizeof(float));
+  if (n == 0) return;
+  const float radius = size[0] * 0.5f;
+  const float cell_volume = g->cell[0] * g->cell[1] * g->cell[2];
+  const float four_pi_over3 = (4.0f * PI_F) / 3.0f;
+  const float vorton_volume = four_pi_over3 * (radius * radius * radius);
+  const float corr = scale * vorton_volume / cell_volume;
+  const unsigned nx = g->np[0], nxy = g->np[0] * g->np[1];
+  for (size_t i = 0; i < n; ++i) {
+    const float* p = pos + 3 * i;
+    const float item[3] = {(angvel[3 * i] * 2.0f) * corr, (angvel[3 * i + 1] * 2.0f) * corr,
+                           (angvel[3 * i + 2] * 2.0f) * corr};
+    unsigned idx[3];
+    vgo_indices_of_position(g, p, idx);
+    float tw[3], om[3];
+    for (int a = 0; a < 3; ++a) {
+      const float cmin = g->mn[a] + (float)idx[a] * g->cell[a];
+      const float diff = p[a] - cmin;
+      tw[a] = clampf_(diff * g->cpe[a], 0.0f, 1.0f);
+      om[a] = 1.0f - tw[a];
+    }
+    const size_t o = idx[0] + (size_t)nx * (idx[1] + (size_t)g->np[1] * idx[2]);
+    const size_t offs[8] = {o, o + 1, o + nx, o + nx + 1, o + nxy, o + nxy + 1, o + nxy + nx, o + nxy + nx + 1};
+    const float w[8] = {om[0] * om[1] * om[2], tw[0] * om[1] * om[2], om[0] * tw[1] * om[2], tw[0] * tw[1] * om[2],
+                        om[0] * om[1] * tw[2], tw[0] * om[1] * tw[2], om[0] * tw[1] * tw[2], tw[0] * tw[1] * tw[2]};
+    for (int c = 0; c < 8; ++c)
+      for (int a = 0; a < 3; ++a) grid[3 * offs[c] + a] += w[c] * item[a];
+  }
+}
+
+/* ComputeVectorPotentialAtGridpoints_Slice (vortonSim.cpp:2055-2138) over all
+ * z; copy_odd_x reproduces the reference's reuse of the preceding even-x value
+ * on odd-x points. */
+void vgo_boundary_vecpot(const float* pos, const float* angvel, const float* size, size_t n, const vgo_geom* g,
+                         int boundaries_only, int copy_odd_x, float* grid) {
+  tree_t t;
+  tree_build(&t, pos, angvel, size, n, g);
+  const float nudge = 1.0f - 2.0f * FLT_EPSILON;
+  const float sp[3] = {g->cell[0] * nudge, g->cell[1] * nudge, g->cell[2] * nudge};
+  const unsigned* dims = g->np;
+  const unsigned nxy = dims[0] * dims[1];
+  const unsigned inc_interior = boundaries_only ? (dims[0] - 1) : 1;
+  for (unsigned z = 0; z < dims[2]; ++z) {
+    float p[3];
+    p[2] = g->mn[2] + (float)z * sp[2];
+    const int tb = (0 == z) || (dims[2] - 1 == z);
+    for (unsigned y = 0; y < dims[1]; ++y) {
+      p[1] = g->mn[1] + (float)y * sp[1];
+      const int fb = (0 == y) || (dims[1] - 1 == y);
+      const unsigned incx = (tb || fb) ? 1 : inc_interior;
+      for (unsigned x = 0; x < dims[0]; x += incx) {
+        p[0] = g->mn[0] + (float)x * sp[0];
+        const unsigned off = x + y * dims[0] + z * nxy;
+        if (!copy_odd_x || 0 == (x & 1))
+          tree_query(&t, 1, pos, angvel, size, n, p, 1.0f, 1.0f, grid + 3 * off);
+        else
+          memcpy(grid + 3 * off, grid + 3 * (off - 1), 3 * sizeof(float));
+      }
+    }
+  }
+  free(t.sv);
+}
+
+/* StepTowardVectorPoissonSolution, red then black, Dirichlet
+ * (uniformGridMath.cpp:1116-1339, 1369-1405): SOR with relaxation 1.72 over
+ * x-rows whose (y + z) parity matches the colour, each row swept in +x. */
+void vgo_sor(const vgo_geom* g, float* s, const float* lap, int steps) {
+  const float* sp = g->cell;
+  const float rs[3] = {1.0f / sp[0], 1.0f / sp[1], sp[2] > FLT_EPSILON ? 1.0f / sp[2] : 0.0f};
+  const float rs2[3] = {rs[0] * rs[0], rs[1] * rs[1], rs[2] * rs[2]};
+  const float H = 0.5f / (rs2[0] + rs2[1] + rs2[2]);
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  const float relax = 1.72f;
+  const float omr = 1.0f - relax;
+  for (int it = 0; it < steps; ++it) {
+    for (unsigned color = 0; color < 2; ++color) {
+      for (size_t z = 1; z + 1 < nz; ++z) {
+        const size_t yshift = (z % 2 == color) ? 1 : 0;
+        for (size_t y = 1 + yshift; y + 1 < ny; y += 2) {
+          for (size_t x = 1; x + 1 < nx; ++x) {
+            const size_t c = x + nx * y + nxy * z;
+            for (int a = 0; a < 3; ++a) {
+              const float v = ((s[3 * (c + 1) + a] + s[3 * (c - 1) + a]) * rs2[0] +
+                               (s[3 * (c + nx) + a] + s[3 * (c - nx) + a]) * rs2[1] +
+                               (s[3 * (c + nxy) + a] + s[3 * (c - nxy) + a]) * rs2[2] - lap[3 * c + a]) *
+                              H;
+              s[3 * c + a] = omr * s[3 * c + a] + relax * v;
+            }
+          }
+        }
+      }
+    }
+  }
+}
+
+/* DownSampleSlice (uniformGrid.h:1453-1585): inject = FASTER_LESS_ACCURATE
+ * (copy the cluster's min-corner point); else SLOWER_MORE_ACCURATE (27-point
+ * full weighting around it, out-of-range points omitted). */
+void vgo_downsample(const vgo_geom* fine, const float* fv, int inject, const vgo_geom* coarse, float* cv) {
+  const unsigned cd[3] = {(fine->np[0] - 1) / (coarse->np[0] - 1), (fine->np[1] - 1) / (coarse->np[1] - 1),
+                          (fine->np[2] - 1) / (coarse->np[2] - 1)};
+  const unsigned fnx = fine->np[0], fnxy = fine->np[0] * fine->np[1];
+  for (unsigned z = 0; z < coarse->np[2]; ++z)
+    for (unsigned y = 0; y < coarse->np[1]; ++y)
+      for (unsigned x = 0; x < coarse->np[0]; ++x) {
+        float* o = cv + 3 * (x + coarse->np[0] * (y + coarse->np[1] * z));
+        const unsigned mx = x * cd[0], my = y * cd[1], mz = z * cd[2];
+        if (inject) {
+          const float* f = fv + 3 * (mx + my * fnx + mz * fnxy);
+          o[0] = f[0];
+          o[1] = f[1];
+          o[2] = f[2];
+        } else {
+          /* USE_ALL_NEIGHBORS (uniformGrid.h:43): 27-point full weighting,
+             8/4/2/1 by Manhattan distance, normalised by 64 */
+          static const float table[4] = {8.0f, 4.0f, 2.0f, 1.0f};
+          const unsigned sh[3] = {cd[0] / 2, cd[1] / 2, cd[2] / 2};
+          float acc[3] = {0, 0, 0};
+          for (unsigned iz = 0; iz < cd[2] + sh[2]; ++iz) {
+            const int s2 = (int)iz - (int)sh[2];
+            const unsigned hz = mz + (unsigned)s2;
+            if (hz >= fine->np[2]) continue;
+            for (unsigned iy = 0; iy < cd[1] + sh[1]; ++iy) {
+              const int s1 = (int)iy - (int)sh[1];
+              const unsigned hy = my + (unsigned)s1;
+              if (hy >= fine->np[1]) continue;
+              for (unsigned ix = 0; ix < cd[0] + sh[0]; ++ix) {
+                const int s0 = (int)ix - (int)sh[0];
+                const unsigned hx = mx + (unsigned)s0;
+                if (hx >= fine->np[0]) continue;
+                const unsigned md = (unsigned)(abs(s0) + abs(s1) + abs(s2));
+                const float* f = fv + 3 * (hx + hy * fnx + hz * fnxy);
+                acc[0] += table[md] * f[0];
+                acc[1] += table[md] * f[1];
+                acc[2] += table[md] * f[2];
+              }
+            }
+          }
+          const float r = 1.0f / 64.0f;
+          o[0] = acc[0] * r;
+          o[1] = acc[1] * r;
+          o[2] = acc[2] * r;
+        }
+      }
+}
+
+/* UniformGrid::Interpolate (uniformGrid.h:1117-1148) for a 3-vector field. */
+void vgo_interpolate3(const vgo_geom* g, const float* f, const float p[3], float out[3]) {
+  unsigned idx[3];
+  vgo_indices_of_position(g, p, idx);
+  float tw[3], om[3];
+  for (int a = 0; a < 3; ++a) {
+    const float cmin = g->mn[a] + (float)idx[a] * g->cell[a];
+    tw[a] = (p[a] - cmin) * g->cpe[a];
+    om[a] = 1.0f - tw[a];
+  }
+  const size_t nx = g->np[0], nxy = (size_t)g->np[0] * g->np[1];
+  const size_t o = idx[0] + nx * (idx[1] + (size_t)g->np[1] * idx[2]);
+  for (int a = 0; a < 3; ++a) {
+    const float v000 = f[3 * o + a], v100 = f[3 * (o + 1) + a], v010 = f[3 * (o + nx) + a],
+                v110 = f[3 * (o + nx + 1) + a], v001 = f[3 * (o + nxy) + a], v101 = f[3 * (o + nxy + 1) + a],
+                v011 = f[3 * (o + nxy + nx) + a], v111 = f[3 * (o + nxy + nx + 1) + a];
+    out[a] = ((om[0] * v000 + tw[0] * v100) * om[1] + (om[0] * v010 + tw[0] * v110) * tw[1]) * om[2] +
+             ((om[0] * v001 + tw[0] * v101) * om[1] + (om[0] * v011 + tw[0] * v111) * tw[1]) * tw[2];
+  }
+}
+
+/* Interpolate for a field of k floats per point (Mat33: k = 9). */
+static void interpolate_k(const vgo_geom* g, const float* f, int k, const float p[3], float* out) {
+  unsigned idx[3];
+  vgo_indices_of_position(g, p, idx);
+  float tw[3], om[3];
+  for (int a = 0; a < 3; ++a) {
+    const float cmin = g->mn[a] + (float)idx[a] * g->cell[a];
+    tw[a] = (p[a] - cmin) * g->cpe[a];
+    om[a] = 1.0f - tw[a];
+  }
+  const size_t nx = g->np[0], nxy = (size_t)g->np[0] * g->np[1];
+  const size_t o = idx[0] + nx * (idx[1] + (size_t)g->np[1] * idx[2]);
+  for (int a = 0; a < k; ++a) {
+    const float v000 = f[k * o + a], v100 = f[k * (o + 1) + a], v010 = f[k * (o + nx) + a],
+                v110 = f[k * (o + nx + 1) + a], v001 = f[k * (o + nxy) + a], v101 = f[k * (o + nxy + 1) + a],
+                v011 = f[k * (o + nxy + nx) + a], v111 = f[k * (o + nxy + nx + 1) + a];
+    out[a] = ((om[0] * v000 + tw[0] * v100) * om[1] + (om[0] * v010 + tw[0] * v110) * tw[1]) * om[2] +
+             ((om[0] * v001 + tw[0] * v101) * om[1] + (om[0] * v011 + tw[0] * v111) * tw[1]) * tw[2];
+  }
+}
+
+/* UpSampleSlice (uniformGrid.h:1637-1700): sample the coarse grid at fine
+ * points nudged inward by 2 eps |min| and spacing * (1 - 4 eps). */
+void vgo_upsample(const vgo_geom* coarse, const float* cv, const vgo_geom* fine, int interior_only, float* fv) {
+  const float pmin[3] = {fine->mn[0] + fabsf(fine->mn[0]) * 2.0f * FLT_EPSILON,
+                         fine->mn[1] + fabsf(fine->mn[1]) * 2.0f * FLT_EPSILON,
+                         fine->mn[2] + fabsf(fine->mn[2]) * 2.0f * FLT_EPSILON};
+  const float shrink = 1.0f - 4.0f * FLT_EPSILON;
+  const float sp[3] = {fine->cell[0] * shrink, fine->cell[1] * shrink, fine->cell[2] * shrink};
+  unsigned lo[3] = {0, 0, 0}, hi[3] = {fine->np[0], fine->np[1], fine->np[2]};
+  if (interior_only) {
+    for (int a = 0; a < 3; ++a) {
+      lo[a] = 1;
+      hi[a] = (fine->np[a] > 1 ? fine->np[a] : 1) - 1;
+    }
+  }
+  for (unsigned z = lo[2]; z < hi[2]; ++z) {
+    float p[3];
+    p[2] = pmin[2] + (float)z * sp[2];
+    for (unsigned y = lo[1]; y < hi[1]; ++y) {
+      p[1] = pmin[1] + (float)y * sp[1];
+      for (unsigned x = lo[0]; x < hi[0]; ++x) {
+        p[0] = pmin[0] + (float)x * sp[0];
+        vgo_interpolate3(coarse, cv, p, fv + 3 * (x + fine->np[0] * (y + fine->np[1] * z)));
+      }
+    }
+  }
+}
+
+/* The cascade in VortonSim::ComputeVectorPotential (vortonSim.cpp:2539-2571). */
+void vgo_cascade(const vgo_geom* g, float* soln, const float* rhs, int steps) {
+  vgo_geom L[VGO_MAX_LAYERS];
+  unsigned dec[3 * VGO_MAX_LAYERS];
+  const int depth = vgo_nested_shape(g, L, dec);
+  float* a[VGO_MAX_LAYERS];
+  float* b[VGO_MAX_LAYERS];
+  for (int l = 0; l < depth; ++l) {
+    a[l] = (float*)calloc(capacity(&L[l]) * 3, sizeof(float));
+    b[l] = (float*)calloc(capacity(&L[l]) * 3, sizeof(float));
+  }
+  memcpy(a[0], soln, capacity(g) * 3 * sizeof(float));
+  memcpy(b[0], rhs, capacity(g) * 3 * sizeof(float));
+  vgo_sor(&L[0], a[0], b[0], steps);
+  int max_valid = 0;
+  for (int l = 1; l < depth; ++l) {
+    unsigned mind = L[l].np[0] < L[l].np[1] ? L[l].np[0] : L[l].np[1];
+    if (L[l].np[2] < mind) mind = L[l].np[2];
+    if (mind > 2) {
+      vgo_downsample(&L[l - 1], b[l - 1], 1, &L[l], b[l]);
+      vgo_downsample(&L[l - 1], a[l - 1], 1, &L[l], a[l]);
+      vgo_sor(&L[l], a[l], b[l], steps);
+    } else {
+      max_valid = l - 1;
+      break;
+    }
+  }
+  for (int l = max_valid; l >= 1; --l) {
+    vgo_upsample(&L[l], a[l], &L[l - 1], 1, a[l - 1]);
+    vgo_sor(&L[l - 1], a[l - 1], b[l - 1], steps);
+  }
+  memcpy(soln, a[0], capacity(g) * 3 * sizeof(float));
+  for (int l = 0; l < depth; ++l) {
+    free(a[l]);
+    free(b[l]);
+  }
+}
+
+/* ComputeJacobian (uniformGridMath.cpp:304-451): j[3*a + b] = d v_b / d a;
+ * central differences inside, one-sided on each boundary face. */
+void vgo_jacobian(const vgo_geom* g, const float* v, float* jac) {
+  const float* sp = g->cell;
+  const float rs[3] = {1.0f / sp[0], 1.0f / sp[1], sp[2] > FLT_EPSILON ? 1.0f / sp[2] : 0.0f};
+  const float hrs[3] = {0.5f * rs[0], 0.5f * rs[1], 0.5f * rs[2]};
+  const size_t n[3] = {g->np[0], g->np[1], g->np[2]};
+  const size_t stride[3] = {1, n[0], n[0] * n[1]};
+  for (size_t z = 0; z < n[2]; ++z)
+    for (size_t y = 0; y < n[1]; ++y)
+      for (size_t x = 0; x < n[0]; ++x) {
+        const size_t c = x + stride[1] * y + stride[2] * z;
+        const size_t idx[3] = {x, y, z};
+        for (int a = 0; a < 3; ++a) {
+          size_t hi = c, lo = c;
+          float f;
+          if (idx[a] == 0) {
+            hi = c + stride[a];
+            f = rs[a];
+          } else if (idx[a] == n[a] - 1) {
+            lo = c - stride[a];
+            f = rs[a];
+          } else {
+            hi = c + stride[a];
+            lo = c - stride[a];
+            f = hrs[a];
+          }
+          for (int b = 0; b < 3; ++b) jac[9 * c + 3 * a + b] = (v[3 * hi + b] - v[3 * lo + b]) * f;
+        }
+      }
+}
+
+/* ComputeCurlFromJacobian (uniformGridMath.cpp:207-232). */
+void vgo_curl_from_jacobian(size_t points, const float* j, float* curl) {
+  for (size_t c = 0; c < points; ++c) {
+    const float* m = j + 9 * c;
+    curl[3 * c] = m[5] - m[7];     /* j.y.z - j.z.y */
+    curl[3 * c + 1] = m[6] - m[2]; /* j.z.x - j.x.z */
+    curl[3 * c + 2] = m[1] - m[3]; /* j.x.y - j.y.x */
+  }
+}
+
+/* StretchAndTiltVortons (vortonSim.cpp:2748-2820): interpolate the velocity
+ * Jacobian at each vorton, stretchTilt = angvel * J (transpose form),
+ * angvel += 0.5 * stretchTilt * dt. */
+void vgo_stretch(const float* pos, float* w, size_t n, const vgo_geom* g, const float* jac9, float dt) {
+  if (0.0f == g->ext[0] || 0.0f == g->ext[1] || 0.0f == g->ext[2]) return;
+  for (size_t i = 0; i < n; ++i) {
+    float J[9];
+    interpolate_k(g, jac9, 9, pos + 3 * i, J);
+    float* a = w + 3 * i;
+    const float st[3] = {J[0] * a[0] + J[1] * a[1] + J[2] * a[2], J[3] * a[0] + J[4] * a[1] + J[5] * a[2],
+                         J[6] * a[0] + J[7] * a[1] + J[8] * a[2]};
+    a[0] += (0.5f * st[0]) * dt;
+    a[1] += (0.5f * st[1]) * dt;
+    a[2] += (0.5f * st[2]) * dt;
+  }
+}
+
+/* ---------------------------------------------------------------- PSE */
+
+typedef struct {
+  unsigned* start; /* per cell, points layout of g */
+  unsigned* count;
+  unsigned* items; /* vorton indices, ascending within each cell */
+} cells_t;
+
+/* PartitionParticles (particle.cpp:398-437): each vorton's index appended to
+ * the list of the cell OffsetOfPosition names, in index order. */
+static void cells_build(cells_t* c, const float* pos, size_t n, const vgo_geom* g) {
+  const size_t cap = capacity(g);
+  c->start = (unsigned*)calloc(cap + 1, sizeof(unsigned));
+  c->count = (unsigned*)calloc(cap, sizeof(unsigned));
+  c->items = (unsigned*)malloc((n ? n : 1) * sizeof(unsigned));
+  unsigned* off = (unsigned*)malloc((n ? n : 1) * sizeof(unsigned));
+  for (size_t i = 0; i < n; ++i) {
+    off[i] = vgo_offset_of_position(g, pos + 3 * i);
+    c->count[off[i]]++;
+  }
+  for (size_t k = 0; k < cap; ++k) c->start[k + 1] = c->start[k] + c->count[k];
+  unsigned* fill = (unsigned*)calloc(cap, sizeof(unsigned));
+  for (size_t i = 0; i < n; ++i) c->items[c->start[off[i]] + fill[off[i]]++] = (unsigned)i;
+  free(fill);
+  free(off);
+}
+
+static void cells_free(cells_t* c) {
+  free(c->start);
+  free(c->count);
+  free(c->items);
+}
+
+/* ExchangeVorticityOrMergeVortons without merging (vortonSim.cpp:3616-3669). */
+static void exchange(const float* pos, float* w, const float* size, unsigned h, unsigned t, float viscosity,
+                     float dt) {
+  const float range = 4.0f * size[h];
+  const float range2 = range * range;
+  const float s0 = pos[3 * h] - pos[3 * t], s1 = pos[3 * h + 1] - pos[3 * t + 1], s2 = pos[3 * h + 2] - pos[3 * t + 2];
+  const float dist2 = s0 * s0 + s1 * s1 + s2 * s2;
+  const float law = expf(-dist2 / range2);
+  const float d[3] = {w[3 * h] - w[3 * t], w[3 * h + 1] - w[3 * t + 1], w[3 * h + 2] - w[3 * t + 2]};
+  const float frac = clampf_(2.0f * viscosity * dt * law, -0.5f, 0.5f);
+  for (int a = 0; a < 3; ++a) {
+    const float e = frac * d[a];
+    w[3 * h + a] -= e;
+    w[3 * t + a] += e;
+  }
+}
+
+/* The 7 forward neighbour cells (vortonSim.cpp:3712-3727). */
+static void forward_offsets(const vgo_geom* g, size_t off[7]) {
+  const size_t nx = g->np[0], nxy = (size_t)g->np[0] * g->np[1];
+  off[0] = 1;
+  off[1] = nx;
+  off[2] = 1 + nx;
+  off[3] = nxy;
+  off[4] = 1 + nxy;
+  off[5] = nx + nxy;
+  off[6] = 1 + nx + nxy;
+}
+
+/* DiffuseAndDissipateVorticityPSESlice, serial PHASE_BOTH
+ * (vortonSim.cpp:3678-3800): in-place pairwise exchange in cell order. */
+void vgo_pse_sequential(const float* pos, float* w, const float* size, size_t n, const vgo_geom* g, float viscosity,
+                        float dt) {
+  cells_t c;
+  cells_build(&c, pos, n, g);
+  size_t fo[7];
+  forward_offsets(g, fo);
+  const float diss = viscosity * dt;
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  for (size_t z = 0; z + 1 < nz; ++z)
+    for (size_t y = 0; y + 1 < ny; ++y)
+      for (size_t x = 0; x + 1 < nx; ++x) {
+        const size_t cell = x + y * nx + z * nxy;
+        for (unsigned ih = 0; ih < c.count[cell]; ++ih) {
+          const unsigned h = c.items[c.start[cell] + ih];
+          for (unsigned it = ih + 1; it < c.count[cell]; ++it)
+            exchange(pos, w, size, h, c.items[c.start[cell] + it], viscosity, dt);
+          for (int k = 0; k < 7; ++k) {
+            const size_t nb = cell + fo[k];
+            for (unsigned it = 0; it < c.count[nb]; ++it) exchange(pos, w, size, h, c.items[c.start[nb] + it], viscosity, dt);
+          }
+          for (int a = 0; a < 3; ++a) w[3 * h + a] -= diss * w[3 * h + a];
+        }
+      }
+  cells_free(&c);
+}
+
+/* Order-independent form of the same exchange, used by the GPU: every pair
+ * the reference visits (same cell, or cells offset by {0,1}^3 in either
+ * direction, the "here" cell strictly inside the point range) exchanges
+ * using the values from before the step; each vorton whose cell is a "here"
+ * cell then dissipates.  Differs from the reference's in-place order by
+ * O((2 nu dt)^2) of the vorticity differences. */
+void vgo_pse_symmetric(const float* pos, float* w, const float* size, size_t n, const vgo_geom* g, float viscosity,
+                       float dt) {
+  cells_t c;
+  cells_build(&c, pos, n, g);
+  float* w0 = (float*)malloc((n ? n : 1) * 3 * sizeof(float));
+  memcpy(w0, w, n * 3 * sizeof(float));
+  const float diss = viscosity * dt;
+  const int nx = (int)g->np[0], ny = (int)g->np[1], nz = (int)g->np[2];
+  for (size_t i = 0; i < n; ++i) {
+    unsigned id[3];
+    vgo_indices_of_position(g, pos + 3 * i, id);
+    const int ci[3] = {(int)id[0], (int)id[1], (int)id[2]};
+    const int here_ok = ci[0] < nx - 1 && ci[1] < ny - 1 && ci[2] < nz - 1;
+    double acc[3] = {0, 0, 0};
+    for (int s = -1; s <= 1; s += 2) {
+      for (int k = 0; k < 8; ++k) {
+        const int d[3] = {s * (k & 1), s * ((k >> 1) & 1), s * ((k >> 2) & 1)};
+        if (k == 0 && s == 1) continue; /* same cell handled with s == -1 */
+        const int nc[3] = {ci[0] + d[0], ci[1] + d[1], ci[2] + d[2]};
+        if (nc[0] < 0 || nc[1] < 0 || nc[2] < 0 || nc[0] >= nx || nc[1] >= ny || nc[2] >= nz) continue;
+        /* the pair is visited from the lower cell, which must be a "here" cell */
+        const int* lower = (s == 1) ? ci : nc;
+        if (!(lower[0] < nx - 1 && lower[1] < ny - 1 && lower[2] < nz - 1)) continue;
+        const size_t cell = (size_t)nc[0] + (size_t)nx * ((size_t)nc[1] + (size_t)ny * nc[2]);
+        for (unsigned it = 0; it < c.count[cell]; ++it) {
+          const unsigned j = c.items[c.start[cell] + it];
+          if (j == i) continue;
+          /* the range uses the size of the pair's "here" vorton: the one in
+             the lower cell, or the lower index within one cell */
+          const size_t here = (k == 0) ? (i < j ? i : j) : (s == 1 ? i : j);
+          const float range = 4.0f * size[here];
+          const float range2 = range * range;
+          const float s0 = pos[3 * i] - pos[3 * j], s1 = pos[3 * i + 1] - pos[3 * j + 1], s2 = pos[3 * i + 2] - pos[3 * j + 2];
+          const float dist2 = s0 * s0 + s1 * s1 + s2 * s2;
+          const float law = expf(-dist2 / range2);
+          const float frac = clampf_(2.0f * viscosity * dt * law, -0.5f, 0.5f);
+          for (int a = 0; a < 3; ++a) acc[a] += (double)frac * ((double)w0[3 * j + a] - w0[3 * i + a]);
+        }
+      }
+    }
+    for (int a = 0; a < 3; ++a) {
+      float v = (float)((double)w0[3 * i + a] + acc[a]);
+      if (here_ok) v -= diss * v;
+      w[3 * i + a] = v;
+    }
+  }
+  free(w0);
+  cells_free(&c);
+}
+
+/* AssignParticleVelocityFromField_Slice, gain 1 (pclOpAdvect.cpp:42-81). */
+void vgo_gather(const vgo_geom* g, const float* velgrid, const float* pos, size_t n, float* vel) {
+  for (size_t i = 0; i < n; ++i) vgo_interpolate3(g, velgrid, pos + 3 * i, vel + 3 * i);
+}
+
+/* EvolveParticlesSlice (pclOpEvolve.cpp:36-58): pos += vel * dt. */
+void vgo_evolve(float* pos, const float* vel, size_t n, float dt) {
+  for (size_t i = 0; i < 3 * n; ++i) pos[i] += vel[i] * dt;
+}
+
+/* ----------------------------------------------------------- residual norms */
+
+static double relres_impl(const vgo_geom* g, const float* af, const double* ad, const float* b) {
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  const double h2[3] = {1.0 / ((double)g->cell[0] * g->cell[0]), 1.0 / ((double)g->cell[1] * g->cell[1]),
+                        1.0 / ((double)g->cell[2] * g->cell[2])};
+  double rr = 0, bb = 0;
+#define A_(i) (af ? (double)af[i] : ad[i])
+  for (size_t z = 1; z + 1 < nz; ++z)
+    for (size_t y = 1; y + 1 < ny; ++y)
+      for (size_t x = 1; x + 1 < nx; ++x) {
+        const size_t c = x + nx * y + nxy * z;
+        for (int a = 0; a < 3; ++a) {
+          const double ac = A_(3 * c + a);
+          const double lap = (A_(3 * (c + 1) + a) + A_(3 * (c - 1) + a) - 2 * ac) * h2[0] +
+                             (A_(3 * (c + nx) + a) + A_(3 * (c - nx) + a) - 2 * ac) * h2[1] +
+                             (A_(3 * (c + nxy) + a) + A_(3 * (c - nxy) + a) - 2 * ac) * h2[2];
+          const double r = (double)b[3 * c + a] - lap;
+          rr += r * r;
+          bb += (double)b[3 * c + a] * b[3 * c + a];
+        }
+      }
+#undef A_
+  return bb > 0 ? sqrt(rr / bb) : sqrt(rr);
+}
+
+double vgo_relres_f64(const vgo_geom* g, const float* a, const float* b) { return relres_impl(g, a, NULL, b); }
+double vgo_relres_f64d(const vgo_geom* g, const double* a, const float* b) { return relres_impl(g, NULL, a, b); }
+
+/* ------------------------------------------------------------- full step */
+
+/* VortonSim::UpdateVortexParticleMethod with the shipped switches
+ * (vortonSim.cpp:4117-4256): splat -vorticity, treecode boundary A,
+ * cascade, Jacobian -> curl velocity grid, stretch/tilt, PSE, gather. */
+void vgo_step_fields(const float* pos, float* vel, float* w, const float* size, size_t n, const vgo_geom* g, float dt,
+                     float viscosity, int pse_mode, float* velgrid, float* vecpot, float* negvort) {
+  const size_t cap = capacity(g);
+  vgo_splat(pos, w, size, n, g, -1.0f, negvort);
+  memset(vecpot, 0, cap * 3 * sizeof(float));
+  vgo_boundary_vecpot(pos, w, size, n, g, 1, 1, vecpot);
+  vgo_cascade(g, vecpot, negvort, 16);
+  float* jac = (float*)malloc(cap * 9 * sizeof(float));
+  vgo_jacobian(g, vecpot, jac);
+  vgo_curl_from_jacobian(cap, jac, velgrid);
+  vgo_jacobian(g, velgrid, jac);
+  vgo_stretch(pos, w, n, g, jac, dt);
+  free(jac);
+  if (pse_mode == 0)
+    vgo_pse_sequential(pos, w, size, n, g, viscosity, dt);
+  else
+    vgo_pse_symmetric(pos, w, size, n, g, viscosity, dt);
+  vgo_gather(g, velgrid, pos, n, vel);
+}

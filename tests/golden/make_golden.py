@@ -1,0 +1,193 @@
+#!/usr/bin/env python3
+"""Generate the golden vectors in tests/golden/ from the reference's own code.
+
+Runs the reference's VortonSim functions (built from the reference sources by
+oracle/ref_build, serial USE_TBB=0 build) on small seeded inputs and stores
+inputs and outputs in reference.npz.  The inputs are stored too, so the tests
+never depend on the random generator of the machine they run on.
+
+Usage (needs the reference tree or a staged copy; run in this container):
+    python tests/golden/make_golden.py
+"""
+import ctypes
+import os
+import sys
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+import oracle  # noqa: E402
+from vortegrid_gb300 import workloads  # noqa: E402
+
+OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference.npz")
+
+
+def P(a):
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+def main():
+    oracle.build()
+    R = oracle.ref("serial")
+    g = {}
+    # --- a7 DefineShape: ring box, degenerate z, one element, a long box
+    shapes = [(1500, [-1.4, -1.4, -0.4], [1.4, 1.4, 0.4]), (4096, [-1.5, -1.5, -1.5], [1.5, 1.5, 1.5]),
+              (1024, [0, 0, 0], [2, 3, 5]), (100, [-1, -1, 0.25], [1, 1, 0.25]), (1, [0, 0, 0], [1, 1, 1]),
+              (262144, [-2.05, -2.05, -2.05], [2.05, 2.05, 2.05]), (77, [-3, 0.1, 2], [5, 0.3, 9])]
+    g12s, nps = [], []
+    for n, a, b in shapes:
+        g12 = np.zeros(12, np.float32)
+        np3 = np.zeros(3, np.uint32)
+        R.vgref_define_shape(ctypes.c_size_t(n), P(np.array(a, np.float32)), P(np.array(b, np.float32)), 1, P(g12),
+                             P(np3))
+        g12s.append(g12)
+        nps.append(np3)
+    g["shape_n"] = np.array([s[0] for s in shapes], np.uint64)
+    g["shape_min"] = np.array([s[1] for s in shapes], np.float32)
+    g["shape_max"] = np.array([s[2] for s in shapes], np.float32)
+    g["shape_geom"] = np.array(g12s)
+    g["shape_np"] = np.array(nps)
+
+    # --- a9 NestedGrid shape for every geometry above
+    depth, layers, decims = [], [], []
+    for g12, np3 in zip(g12s, nps):
+        ln = np.zeros(96, np.uint32)
+        dc = np.zeros(96, np.uint32)
+        d = R.vgref_nested_grid_shape(P(g12), P(np3), P(ln), P(dc), 32)
+        depth.append(d)
+        layers.append(ln)
+        decims.append(dc)
+    g["nested_depth"] = np.array(depth, np.int32)
+    g["nested_np"] = np.array(layers)
+    g["nested_decim"] = np.array(decims)
+
+    # --- vortons: a small ring, tilted, plus tracers
+    pos, w, s = workloads.ring(1500, seed=11, axis=(0.3, 0.2, 1.0))
+    n = len(pos)
+    mn = pos.min(0) - 0.15
+    mx = pos.max(0) + 0.15
+    g12 = np.zeros(12, np.float32)
+    np3 = np.zeros(3, np.uint32)
+    R.vgref_define_shape(ctypes.c_size_t(n), P(mn.astype(np.float32)), P(mx.astype(np.float32)), 1, P(g12), P(np3))
+    cap = int(np3.prod())
+    g.update(pos=pos, angvel=w, size=s, geom=g12, np=np3)
+
+    # --- a8 binning incl. points nudged to cell corners
+    rng = np.random.default_rng(5)
+    cell = g12[6:9]
+    corner = (g12[0:3] + rng.integers(0, np3 - 1, (200, 3)).astype(np.float32) * cell).astype(np.float32)
+    nudged = np.concatenate([corner, np.nextafter(corner, np.float32(-10)), np.nextafter(corner, np.float32(10)),
+                             pos]).astype(np.float32)
+    idx = np.zeros((len(nudged), 3), np.uint32)
+    off = np.zeros(len(nudged), np.uint32)
+    R.vgref_indices_of_position(P(g12), P(np3), P(nudged), ctypes.c_size_t(len(nudged)), P(idx), P(off))
+    g.update(bin_pos=nudged, bin_idx=idx, bin_off=off)
+
+    # --- a10/a11 influence tree
+    tot = R.vgref_influence_tree(P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), None, ctypes.c_size_t(0))
+    tree = np.zeros((tot, 7), np.float32)
+    R.vgref_influence_tree(P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), P(tree), ctypes.c_size_t(tot))
+    g["tree"] = tree
+
+    # --- a2/a3/a5 direct and a12 treecode at queries (incl. one at a vorton, inside the core)
+    q = np.concatenate([workloads.tracers(400, seed=6, lo=-1.3, hi=1.3), pos[:50] + 0.01]).astype(np.float32)
+    g["q"] = q
+    sr = np.float32(1.5)
+    sc = np.float32(1.0) / (sr * sr * sr)
+    g["spread"] = np.array([sr, sc], np.float32)
+    for kind, name in ((0, "vel"), (1, "vecpot")):
+        o = np.zeros((len(q), 3), np.float32)
+        R.vgref_direct(kind, P(pos), P(w), P(s), ctypes.c_size_t(n), P(q), ctypes.c_size_t(len(q)), ctypes.c_float(1),
+                       ctypes.c_float(1), P(o))
+        g[f"direct_{name}"] = o
+        o = np.zeros((len(q), 3), np.float32)
+        R.vgref_tree(kind, P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), P(q), ctypes.c_size_t(len(q)),
+                     ctypes.c_float(1), ctypes.c_float(1), P(o))
+        g[f"tree_{name}"] = o
+        o = np.zeros((len(q), 3), np.float32)
+        R.vgref_tree(kind, P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), P(q), ctypes.c_size_t(len(q)),
+                     ctypes.c_float(sr), ctypes.c_float(sc), P(o))
+        g[f"tree_{name}_spread"] = o
+
+    # --- a14 splat (scale -1)
+    negvort = np.zeros((cap, 3), np.float32)
+    R.vgref_splat(P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), ctypes.c_float(-1.0), P(negvort))
+    g["negvort"] = negvort
+    # --- a13 boundary A
+    bvp = np.zeros((cap, 3), np.float32)
+    R.vgref_boundary_vecpot(P(pos), P(w), P(s), ctypes.c_size_t(n), P(g12), P(np3), 1, P(bvp))
+    g["boundary_vecpot"] = bvp
+    # --- a16 SOR (5 sweeps) and a15 cascade
+    a = bvp.copy()
+    R.vgref_sor(P(g12), P(np3), P(a), P(negvort), 5)
+    g["sor5"] = a
+    a = bvp.copy()
+    R.vgref_cascade(P(g12), P(np3), P(a), P(negvort), 16)
+    g["cascade"] = a
+    # --- a17/a18 restriction (injection and averaging) and prolongation
+    for acc, name in ((1, "inject"), (0, "average")):
+        for reg, rname in ((1, "interior"), (0, "entire")):
+            co = np.zeros((cap, 3), np.float32)
+            cn = np.zeros(3, np.uint32)
+            fo = np.zeros((cap, 3), np.float32)
+            R.vgref_down_up(P(g12), P(np3), P(a), acc, reg, P(co), P(cn), P(fo))
+            ccap = int(cn.prod())
+            g[f"down_{name}"] = co[:ccap].copy()
+            g["coarse_np"] = cn
+            g[f"up_{name}_{rname}"] = fo
+    # --- a19 Jacobian + curl of the cascade result
+    jac = np.zeros((cap, 9), np.float32)
+    curl = np.zeros((cap, 3), np.float32)
+    R.vgref_jacobian_curl(P(g12), P(np3), P(a), P(jac), P(curl))
+    g["jacobian"] = jac
+    g["curl"] = curl
+    # --- a20 stretch with that velocity grid
+    ww = w.copy()
+    dt = np.float32(1.0 / 30.0)
+    R.vgref_stretch(P(pos), P(ww), P(s), ctypes.c_size_t(n), P(g12), P(np3), P(curl), ctypes.c_float(dt))
+    g["stretched"] = ww
+    # --- a22 PSE (serial, reference order)
+    ww = w.copy()
+    R.vgref_pse(P(pos), P(ww), P(s), ctypes.c_size_t(n), P(g12), P(np3), ctypes.c_float(0.01), ctypes.c_float(dt))
+    g["pse"] = ww
+    # --- a23/a24 gather + Euler of tracers inside the grid
+    tr = (g12[0:3] + (g12[3:6] * 0.999) * np.random.default_rng(8).uniform(0, 1, (700, 3))).astype(np.float32)
+    pp = tr.copy()
+    vv = np.zeros_like(pp)
+    R.vgref_advect(P(pp), P(vv), ctypes.c_size_t(len(pp)), P(g12), P(np3), P(curl), ctypes.c_float(dt))
+    g.update(tracers=tr, tracer_vel=vv, tracer_pos1=pp)
+    # --- a25 AABB
+    bmn = np.zeros(3, np.float32)
+    bmx = np.zeros(3, np.float32)
+    R.vgref_find_bbox(P(pos), ctypes.c_size_t(n), P(bmn), P(bmx))
+    g.update(bbox_min=bmn, bbox_max=bmx)
+
+    # --- a26 full PclOpVortonSim::Operate on Particle records with a tracer box
+    rec = np.zeros((n, 24), np.float32)  # 96-byte Particle records
+    rec[:, 0:3] = pos
+    rec[:, 9:12] = w
+    rec[:, 12] = 1.0  # density
+    rec[:, 13] = s
+    rec_in = rec.copy()
+    emin = np.array([-1.5, -1.5, -0.5], np.float32)
+    emax = np.array([1.5, 1.5, 0.5], np.float32)
+    sg = np.zeros(12, np.float32)
+    sn = np.zeros(3, np.uint32)
+    assert R.vgref_sizeof_particle() == 96
+    R.vgref_step(P(rec), ctypes.c_size_t(n), P(emin), P(emax), ctypes.c_float(dt), ctypes.c_uint(0),
+                 ctypes.c_float(0.01), P(sg), P(sn))
+    scap = int(sn.prod())
+    vel = np.zeros((scap, 3), np.float32)
+    vp = np.zeros((scap, 3), np.float32)
+    nv = np.zeros((scap, 3), np.float32)
+    R.vgref_last_grids(P(vel), P(vp), P(nv))
+    g.update(step_in=rec_in, step_out=rec, step_extra_min=emin, step_extra_max=emax, step_geom=sg, step_np=sn,
+             step_velgrid=vel, step_vecpot=vp, step_negvort=nv)
+
+    np.savez_compressed(OUT, **g)
+    print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e6:.2f} MB, {len(g)} arrays)")
+
+
+if __name__ == "__main__":
+    main()
