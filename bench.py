@@ -1,0 +1,447 @@
+#!/usr/bin/env python3
+"""Benchmark of the GB300 VortonSim step.
+
+Headline (one JSON line on rank 0): direct mollified Biot-Savart throughput in
+G interactions/s on the direct-sum workload -- a seeded vortex ring of 4,096
+vortons (major radius 1, tube radius 0.25, Gaussian core sigma 0.1, peak
+vorticity 10, vorton radius 0.05); velocity by direct summation at every
+vorton and at the 33^3 points of a 32^3-cell grid on [-1.5, 1.5]^3; vortons
+advected by Euler at dt = 1/30; 65,536 tracers (uniform in [-1.5, 1.5)^3)
+advected through the velocity grid.  A step is that whole pass; interactions
+per step = 4,096 x (4,096 + 35,937).
+
+Keys beyond the base contract:
+  * "e2e": the same metric through the host-buffer C ABI (vg_step on the
+    reference's 96-byte Particle records + vg_advect on tracer records, from
+    pinned host memory, copies included);
+  * "roofline": the direct-sum kernel against the FP32 pipe (2 flops x 128
+    lanes x 152 SMs x the SM clock sampled during the run), 26 algorithmic
+    flops per interaction;
+  * "cpu_baseline": the reference's own direct sum (built from its sources,
+    std::thread TBB stand-in, all host threads) on the same workload;
+  * "poisson": the vector-potential solve to 1e-6 relative residual on the
+    multigrid workload (262,144 puff vortons, 129^3 grid, dx = 1/32): plain
+    multigrid ms per solve, cycles and residuals.
+
+--impl reference times the reference's own CPU code for the same step
+(oracle/_ref, or the C oracle when the reference was not built) on all host
+threads; under torchrun only rank 0 runs it.
+"""
+import argparse
+import ctypes
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+N_VORTONS = 4096
+GRID_POINTS = 33
+N_TRACERS = 65536
+DT = np.float32(1.0 / 30.0)
+FLOPS_PER_INTERACTION = 26
+METRIC = "Poisson ms @1e-6 resid: NN warm-start vs plain MG; direct Biot-Savart Gint/s"
+WORKLOAD = ("direct-sum step: vortex ring, 4096 vortons, velocity at vortons + 33^3 gridpoints on [-1.5,1.5]^3, "
+            "Euler advection of vortons and 65536 tracers, dt=1/30")
+
+
+def interactions():
+    return N_VORTONS * (N_VORTONS + GRID_POINTS ** 3)
+
+
+def make_inputs():
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(N_VORTONS, seed=1)
+    tr = workloads.tracers(N_TRACERS, seed=4, lo=-1.5, hi=1.5)
+    return pos, w, s, tr
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled every 200 ms."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.proc = None
+        self.rows = []
+
+    def __enter__(self):
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", f"--id={self.index}", f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([x.strip() for x in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.rows:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm = [float(r[1]) for r in self.rows if len(r) > 8 and r[1].replace(".", "").isdigit()]
+        mx = [float(r[2]) for r in self.rows if len(r) > 8 and r[2].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = set()
+        for r in self.rows:
+            if len(r) > 8:
+                for k, nm in enumerate(names):
+                    if r[5 + k].lower().startswith("active"):
+                        reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": sorted(reasons), "samples": len(self.rows)}
+
+
+def dist_setup():
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl")
+    return world, rank, local
+
+
+def max_over_ranks(x, world):
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+# ---------------------------------------------------------------- CPU legs
+
+def reference_lib():
+    """The reference's own code (multithreaded build) if it was built, else None."""
+    import oracle
+    os.environ.setdefault("NUMBER_OF_PROCESSORS", str(os.cpu_count() or 1))
+    try:
+        oracle.build()
+    except Exception:
+        pass
+    if oracle.ref_available("mt"):
+        L = oracle.ref("mt")
+        L.vgref_set_threads(int(os.environ["NUMBER_OF_PROCESSORS"]))
+        return L
+    return None
+
+
+def cpu_direct_rate(pos, w, s, q, budget_s=3.0):
+    """Reference direct sum (vortonSim.cpp:1144-1158) on all host threads:
+    returns (Gint/s, kind, cores, sample description)."""
+    import oracle
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    L = reference_lib()
+    out = np.zeros((len(q), 3), np.float32)
+    reps, t0 = 0, time.perf_counter()
+    if L is not None:
+        cores = int(os.environ["NUMBER_OF_PROCESSORS"])
+        kind = "reference"
+        while True:
+            L.vgref_direct(0, P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(q), ctypes.c_size_t(len(q)),
+                           ctypes.c_float(1.0), ctypes.c_float(1.0), P(out))
+            reps += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+    else:
+        cores, kind = 1, "port"
+        qs = q[:2048]
+        while True:
+            oracle.direct(0, pos, w, s, qs)
+            reps += 1
+            if time.perf_counter() - t0 > budget_s:
+                break
+        q = qs
+    dt = time.perf_counter() - t0
+    rate = reps * len(pos) * len(q) / dt / 1e9
+    return rate, kind, cores, f"{reps} x direct velocity, {len(pos)} sources x {len(q)} targets"
+
+
+def run_reference_arm(args, world, rank):
+    if rank != 0:
+        return
+    import oracle
+    pos, w, s, tr = make_inputs()
+    from vortegrid_gb300 import workloads
+    q = np.concatenate([workloads.grid_points([-1.5] * 3, [3.0 / 32] * 3, [GRID_POINTS] * 3), pos]).astype(np.float32)
+    L = reference_lib()
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    cores = int(os.environ.get("NUMBER_OF_PROCESSORS", "1")) if L is not None else 1
+    kind = "reference" if L is not None else "port"
+    g12 = np.array([-1.5, -1.5, -1.5, 3.0, 3.0, 3.0, 3.0 / 32, 3.0 / 32, 3.0 / 32, 32 / 3.0, 32 / 3.0, 32 / 3.0],
+                   np.float32)
+    np3 = np.array([GRID_POINTS] * 3, np.uint32)
+
+    def step():
+        vel = np.zeros((len(q), 3), np.float32)
+        if L is not None:
+            L.vgref_direct(0, P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(q), ctypes.c_size_t(len(q)),
+                           ctypes.c_float(1.0), ctypes.c_float(1.0), P(vel))
+            grid = np.ascontiguousarray(vel[: GRID_POINTS ** 3])
+            p = pos + vel[GRID_POINTS ** 3:] * DT
+            t = tr.copy()
+            tv = np.zeros_like(t)
+            L.vgref_advect(P(t), P(tv), ctypes.c_size_t(len(t)), P(g12), P(np3), P(grid), ctypes.c_float(DT))
+        else:  # C oracle port, single thread, on a bounded sample of targets
+            vel = oracle.direct(0, pos, w, s, q[:: max(1, len(q) // 4096)])
+            p = pos
+        return p
+
+    for _ in range(args.warmup):
+        step()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        step()
+    el = time.perf_counter() - t0
+    ms = el / args.steps * 1e3
+    inter = interactions() if L is not None else N_VORTONS * len(q[:: max(1, len(q) // 4096)])
+    value = inter / (ms * 1e-3) / 1e9
+    sample = ("full step: direct velocity at 4096 vortons + 35937 gridpoints, tracer gather + Euler"
+              if L is not None else "direct velocity on a 4096-target sample (C oracle, 1 thread)")
+    line = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+            "config": {"workload": WORKLOAD, "l2": "n/a (CPU)"}, "impl": "reference",
+            "cpu_baseline": {"value": value, "unit": "Gint/s", "cores": cores, "kind": kind, "sample": sample},
+            "e2e": {"value": value, "unit": "Gint/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------- GPU arm
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    import vortegrid_gb300 as vg
+
+    torch.cuda.set_device(local)
+    stream = torch.cuda.Stream()
+    pos, w, s, tr = make_inputs()
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [GRID_POINTS] * 3)
+    cfg = vg.default_config(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid, enable_stretch=0,
+                            enable_diffusion=0, device=local)
+    cfg.stream = stream.cuda_stream
+    ctx = vg.VortonSim(cfg=cfg)
+
+    def f4(a, wv=None):
+        o = np.zeros((len(a), 4), np.float32)
+        o[:, :3] = a
+        if wv is not None:
+            o[:, 3] = wv
+        return torch.from_numpy(o).cuda()
+
+    ps0, w0, tr0 = f4(pos, s), f4(w), f4(tr)
+    ps, ww, vel = ps0.clone(), w0.clone(), torch.zeros_like(ps0)
+    trp, trv = tr0.clone(), torch.zeros_like(tr0)
+    flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")  # > 129 MB L2
+
+    def step():
+        ps.copy_(ps0, non_blocking=True)
+        ww.copy_(w0, non_blocking=True)
+        trp.copy_(tr0, non_blocking=True)
+        ctx.UpdateDevice(ps, ww, vel, float(DT))
+        ctx.EvolveDevice(ps, vel, float(DT))
+        ctx.AdvectDevice(trp, trv, float(DT))
+
+    with torch.cuda.stream(stream):
+        for _ in range(args.warmup):
+            step()
+        ctx.synchronize()
+        stats = ctx.stats()
+        launches_per_step = stats.kernels_launched + 2
+        barrier(world)
+        torch.cuda.synchronize()
+        ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]
+        with ClockSampler(local) as clk:
+            for k in range(args.steps):
+                flush.zero_()
+                ev[k][0].record(stream)
+                step()
+                ev[k][1].record(stream)
+            ctx.synchronize()
+            torch.cuda.synchronize()
+        barrier(world)
+        ms_steps = [a.elapsed_time(b) for a, b in ev]
+    ms_total = max_over_ranks(sum(ms_steps), world)
+    ms_per_step = ms_total / args.steps
+    value = world * interactions() / (ms_per_step * 1e-3) / 1e9
+
+    # correctness gate on the measured configuration: FP64 oracle on a sample
+    import oracle
+    v = vel.cpu().numpy()[:, :3]
+    samp = slice(0, N_VORTONS, 16)
+    ref64 = oracle.direct(0, pos, w, s, pos[samp], f64=True)
+    rel_err = float(np.linalg.norm(v[samp] - ref64) / np.linalg.norm(ref64))
+
+    result = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": world, "steps": args.steps,
+              "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
+              "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded)",
+              "config": {"workload": WORKLOAD, "parallelism": "replicas" if world > 1 else "single GPU",
+                         "l2": "flushed between timed steps (256 MB write, outside the per-step events)",
+                         "numerics": "fast", "rel_l2_vs_fp64": rel_err},
+              "gpu_launches": launches_per_step * args.steps}
+    if rank != 0:
+        return
+    result["clocks"] = clk.summary()
+
+    # ---- roofline of the direct-sum kernel (events on the context stream)
+    q = torch.cat([vg_grid_points(grid), ps0[:, :4]]).contiguous()
+    out = torch.zeros_like(q)
+    lib = vg.lib()
+    with torch.cuda.stream(stream):
+        for _ in range(3):
+            lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), N_VORTONS, vg._ptr(q), q.shape[0], 1.0, 1.0,
+                                 vg._ptr(out))
+        reps = 20
+        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        for _ in range(reps):
+            lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), N_VORTONS, vg._ptr(q), q.shape[0], 1.0, 1.0,
+                                 vg._ptr(out))
+        b.record(stream)
+        torch.cuda.synchronize()
+    kms = a.elapsed_time(b) / reps
+    achieved = FLOPS_PER_INTERACTION * interactions() / (kms * 1e-3) / 1e12
+    clk_mhz = result["clocks"].get("sm_mhz") or 2070.0
+    peak = 2 * 128 * 152 * clk_mhz * 1e6 / 1e12
+    result["roofline"] = {"bound": "fp32", "kernel": "k_direct_fast (+prep, +partial reduce)",
+                          "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                          "traffic": None, "ms_per_launch": kms,
+                          "peak_basis": f"2 flops x 128 FP32 lanes x 152 SMs x {clk_mhz:.0f} MHz (sampled median)",
+                          "flops_per_interaction": FLOPS_PER_INTERACTION,
+                          "gint_per_s_kernel": interactions() / (kms * 1e-3) / 1e9}
+
+    # ---- e2e through the host-buffer ABI from pinned memory
+    recs_t = torch.empty(N_VORTONS * 96, dtype=torch.uint8, pin_memory=True)
+    recs = recs_t.numpy().view(vg.PARTICLE_DTYPE)
+    recs0 = vg.make_particles(pos, w, s)
+    trr_t = torch.empty(N_TRACERS * 96, dtype=torch.uint8, pin_memory=True)
+    trr = trr_t.numpy().view(vg.PARTICLE_DTYPE)
+    trr0 = vg.make_particles(tr)
+    host = vg.VortonSim(cfg=cfg)
+    e2e_ms = []
+    for k in range(args.warmup + args.steps):
+        recs[...] = recs0
+        trr[...] = trr0
+        t0 = time.perf_counter()
+        host.Update(recs, float(DT), k)
+        recs["position"] += recs["velocity"] * DT  # PclOpEvolve on the host records (vortons)
+        host.Advect(trr, float(DT))
+        t1 = time.perf_counter()
+        if k >= args.warmup:
+            e2e_ms.append((t1 - t0) * 1e3)
+    e2e_step = statistics.mean(e2e_ms)
+    result["e2e"] = {"value": interactions() / (e2e_step * 1e-3) / 1e9, "unit": "Gint/s",
+                     "h2d_bytes_per_step": N_VORTONS * 56 + N_TRACERS * 12,
+                     "d2h_bytes_per_step": N_VORTONS * 36 + N_TRACERS * 24, "ms_per_step": e2e_step,
+                     "path": "vg_step (Particle records) + host Evolve + vg_advect (tracer records), pinned"}
+
+    # ---- CPU baseline (reference code, all host threads)
+    from vortegrid_gb300 import workloads
+    qc = np.concatenate([workloads.grid_points([-1.5] * 3, [3.0 / 32] * 3, [GRID_POINTS] * 3), pos]).astype(np.float32)
+    rate, kind, cores, sample = cpu_direct_rate(pos, w, s, qc, budget_s=args.cpu_seconds)
+    result["cpu_baseline"] = {"value": rate, "unit": "Gint/s", "cores": cores, "kind": kind, "sample": sample}
+
+    # ---- Poisson solve to 1e-6 on the multigrid workload
+    if not args.skip_poisson:
+        result["poisson"] = poisson_section(vg, torch, stream, local)
+    print(json.dumps(result), flush=True)
+
+
+def vg_grid_points(grid):
+    import torch
+    from vortegrid_gb300 import workloads
+    p = workloads.grid_points(list(grid.min_corner), list(grid.cell_spacing), grid.points)
+    o = np.zeros((len(p), 4), np.float32)
+    o[:, :3] = p
+    return torch.from_numpy(o).cuda()
+
+
+def poisson_section(vg, torch, stream, local, steps=3):
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.puff(262144, seed=3)
+    grid = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [129] * 3)
+    cfg = vg.default_config(fixed_grid=grid, device=local)
+    cfg.stream = stream.cuda_stream
+    ctx = vg.VortonSim(cfg=cfg)
+    o = np.zeros((len(pos), 4), np.float32)
+    o[:, :3] = pos
+    o[:, 3] = s
+    ps0 = torch.from_numpy(o).cuda()
+    o2 = np.zeros((len(pos), 4), np.float32)
+    o2[:, :3] = w
+    w0 = torch.from_numpy(o2).cuda()
+    ps, ww, vel = ps0.clone(), w0.clone(), torch.zeros_like(ps0)
+    res = []
+    with torch.cuda.stream(stream):
+        for k in range(steps + 1):
+            ps.copy_(ps0)
+            ww.copy_(w0)
+            ctx.UpdateDevice(ps, ww, vel, float(DT))
+            st = ctx.stats()
+            if k > 0:
+                res.append((st.ms_poisson, st.ms_total, st.poisson_cycles, st.poisson_relres0, st.poisson_relres))
+    ms_p = statistics.median(r[0] for r in res)
+    return {"workload": "puff: 262144 vortons N(0,0.5^2), vorticity N(0,2^2), 129^3 grid on [-2,2]^3 (dx=1/32), "
+                        "treecode boundary, FP32 V(2,2)-cycles in FP64 iterative refinement",
+            "plain_mg_ms": ms_p, "step_ms": statistics.median(r[1] for r in res), "cycles": res[-1][2],
+            "relres0": res[-1][3], "relres": res[-1][4], "tolerance": 1e-6, "nn_warm_start_ms": None,
+            "nn_note": "learned warm start not built yet"}
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--cpu-seconds", type=float, default=3.0)
+    ap.add_argument("--skip-poisson", action="store_true")
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
+    world, rank, local = dist_setup() if args.impl == "ours" else (int(os.environ.get("WORLD_SIZE", "1")),
+                                                                  int(os.environ.get("RANK", "0")), 0)
+    if args.impl == "reference":
+        run_reference_arm(args, world, rank)
+        return
+    run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

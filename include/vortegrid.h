@@ -1,0 +1,255 @@
+/* vortegrid.h -- C ABI of the GB300 (sm_103a) VortonSim velocity-from-vorticity step.
+ *
+ * This library is a drop-in for the reference's VortonSim step behind its
+ * particle-operation plugin API (mijagourlay/VorteGrid,
+ * Samples/MjgIntelFluidDemo_Part20).  Every entry point below names the
+ * reference interface it replaces (file:line, paths relative to that sample).
+ *
+ * Conventions
+ *  - Vortons and tracers cross the host boundary as the reference's own
+ *    Particle records (Particles/particle.h:425-431): position float[3] at
+ *    byte 0, velocity float[3] at 12, angular velocity (= vorticity / 2)
+ *    float[3] at 36, size (= diameter) float at 52.  The record stride is a
+ *    parameter (96 bytes for the reference's LP64 build).
+ *  - *_device entry points take device pointers (CUDA global memory of the
+ *    context's device) and run on the context's stream without
+ *    synchronising; all others take host pointers and return after the
+ *    results are in host memory.
+ *  - Grid fields are float[3] per point, x fastest, num_points[0] *
+ *    num_points[1] * num_points[2] points; points = cells + 1 per axis.
+ *  - Every call returns a vg_status; nothing traps or asserts on the device.
+ *    Errors found by device stages (a sample outside the grid, a non-finite
+ *    position) set a device flag that the next synchronising call reports.
+ *    vg_last_error() gives a one-line explanation of the last failure.
+ *  - A context is used by one host thread at a time (the reference's
+ *    VortonSim is not re-entrant either, vortonSim.cpp:2668-2670).
+ */
+#ifndef VORTEGRID_H
+#define VORTEGRID_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define VG_ABI_VERSION 1
+
+typedef enum vg_status {
+  VG_OK = 0,
+  VG_EMPTY = 1,         /* no vortons: nothing computed (vortonSim.cpp:4123) */
+  VG_OUT_OF_GRID = 2,   /* a query lies outside the grid it samples */
+  VG_NONFINITE = 3,     /* NaN or Inf in inputs or results */
+  VG_OOM = 4,           /* device allocation failed */
+  VG_TIMEOUT = 5,       /* a bounded device wait gave up */
+  VG_INVALID = 6,       /* bad argument */
+  VG_CUDA_ERROR = 7,    /* CUDA runtime error (see vg_last_error) */
+  VG_NOT_CONVERGED = 8, /* Poisson solve hit its cycle limit above tolerance */
+  VG_TOO_LARGE = 9      /* a size exceeds a fixed capacity of this entry point */
+} vg_status;
+
+/* Velocity-from-vorticity techniques (VortonFluid/vorton.h:39-47). */
+typedef enum vg_velocity_technique {
+  VG_VELOCITY_POISSON = 0, /* treecode boundary A + Poisson solve + curl (the shipped default) */
+  VG_VELOCITY_TREE = 1,    /* treecode at gridpoints */
+  VG_VELOCITY_DIRECT = 2   /* direct O(N^2) sum at gridpoints */
+} vg_velocity_technique;
+
+/* Arithmetic of the vorton kernels and grid stages. */
+typedef enum vg_numerics {
+  VG_NUMERICS_FAST = 0,     /* hardware rsqrt, fused multiply-add, reassociated sums */
+  VG_NUMERICS_REFERENCE = 1 /* the reference's operation order and magic-constant rsqrt
+                               (Core/Math/math.h:206-216): bit-identical FP32 results */
+} vg_numerics;
+
+typedef enum vg_poisson_solver {
+  VG_POISSON_MULTIGRID = 0,        /* FP32 V-cycles in FP64 iterative refinement, to a tolerance */
+  VG_POISSON_REFERENCE_CASCADE = 1 /* the reference's fixed-work cascade (vortonSim.cpp:2539-2571) */
+} vg_poisson_solver;
+
+typedef enum vg_warm_start {
+  VG_WARM_ZERO = 0,     /* interior starts at zero (the reference's choice, vortonSim.cpp:2532) */
+  VG_WARM_PREVIOUS = 1, /* previous step's solution, when the grid shape is unchanged */
+  VG_WARM_NETWORK = 2   /* the learned 3D U-Net guess (vg_load_network) */
+} vg_warm_start;
+
+/* UniformGridGeometry (Core/SpatialPartition/uniformGrid.h:144-860). */
+typedef struct vg_grid_geom {
+  float min_corner[3];
+  float extent[3];
+  float cell_spacing[3];
+  float cells_per_extent[3];
+  unsigned num_points[3];
+} vg_grid_geom;
+
+typedef struct vg_config {
+  unsigned abi_version;      /* VG_ABI_VERSION */
+  int device;                /* CUDA device ordinal */
+  void* stream;              /* cudaStream_t to run on; NULL = the context creates one */
+  int velocity_technique;    /* vg_velocity_technique */
+  int numerics;              /* vg_numerics */
+  int poisson_solver;        /* vg_poisson_solver */
+  int warm_start;            /* vg_warm_start */
+  float viscosity;           /* VortonSim(viscosity) (vortonSim.cpp:373) */
+  double poisson_tolerance;  /* relative residual ||b - L a|| / ||b|| target (multigrid) */
+  int poisson_max_cycles;    /* cap on V-cycles (multigrid) */
+  int cascade_steps;         /* SOR sweeps per level (cascade), reference 16 (vortonSim.cpp:2541) */
+  int enable_stretch;        /* StretchAndTiltVortons (vortonSim.cpp:4209-4216) */
+  int enable_diffusion;      /* DiffuseAndDissipateVorticityPSE (vortonSim.cpp:4238-4241) */
+  int boundary_copy_odd_x;   /* reuse even-x boundary values on odd x (vortonSim.cpp:2110-2129) */
+  int use_fixed_grid;        /* 1: use fixed_grid instead of the bounding-box rule */
+  vg_grid_geom fixed_grid;
+} vg_config;
+
+/* Per-step statistics (the reference's Poisson stats, vortonSim.h:318-319, as
+ * true residuals). */
+typedef struct vg_step_stats {
+  vg_grid_geom grid;
+  int tree_depth;
+  int poisson_cycles;
+  double poisson_relres;     /* FP64 relative residual after the solve */
+  double poisson_relres0;    /* before the first cycle (warm start quality) */
+  float ms_total;            /* device time of the last step (CUDA events) */
+  float ms_poisson;          /* device time of the Poisson solve */
+  unsigned kernels_launched; /* this library's kernels in the last step */
+} vg_step_stats;
+
+typedef struct vg_ctx vg_ctx;
+
+const char* vg_status_string(vg_status s);
+const char* vg_last_error(const vg_ctx* ctx);
+unsigned vg_abi_version(void);
+
+/* Fill a config with the reference's shipped settings: Poisson technique,
+ * FAST numerics, multigrid to 1e-6, viscosity 0.01, stretch and diffusion on. */
+vg_status vg_config_default(vg_config* cfg);
+
+/* Replaces constructing VortonSim / PclOpVortonSim (vortonSim.cpp:373-420,
+ * VortonFluid/pclOpVortonSim.h:46-71). */
+vg_status vg_create(const vg_config* cfg, vg_ctx** out);
+vg_status vg_destroy(vg_ctx* ctx);
+vg_status vg_set_config(vg_ctx* ctx, const vg_config* cfg);
+
+/* Replaces PclOpVortonSim::Operate (VortonFluid/pclOpVortonSim.cpp:51-71):
+ * FindBoundingBox, UpdateBoundingBox(extra box or first vorton, final),
+ * VortonSim::Update (vortonSim.cpp:4279-4344).  Reads positions, angular
+ * velocities and sizes of n Particle records; writes back each record's
+ * velocity (vortonSim.cpp:4251-4255) and angular velocity (stretch, PSE).
+ * extra_min / extra_max: the tracers' box (PclOpVortonSim::mMinCorner /
+ * mMaxCorner) or NULL. */
+vg_status vg_step(vg_ctx* ctx, void* particles, size_t n, size_t stride, const float* extra_min,
+                  const float* extra_max, float dt, unsigned frame);
+
+/* Device-resident form of vg_step.  pos_size: float4 per vorton (x, y, z,
+ * size); angvel: float4 (x, y, z, unused), updated in place; vel: float4
+ * written.  extra_minmax: 6 host floats (min xyz, max xyz) or NULL. */
+vg_status vg_step_device(vg_ctx* ctx, const float* pos_size, float* angvel, float* vel, size_t n,
+                         const float* extra_minmax, float dt, unsigned frame);
+
+/* Replaces VortonSim::GetVelocityGrid (vortonSim.h:334-335).  Copies the last
+ * step's velocity grid (float[3] per point) into host memory when xyz is not
+ * NULL and cap_points is large enough; always fills geom. */
+vg_status vg_get_velocity_grid(vg_ctx* ctx, float* xyz, size_t cap_points, vg_grid_geom* geom);
+/* Device pointer to the velocity grid (float[3] per point). */
+vg_status vg_get_velocity_grid_device(vg_ctx* ctx, const float** dev_xyz, vg_grid_geom* geom);
+/* Replaces VortonSim::GetVectorPotentialMultiGrid()[0] (vortonSim.h:342-343). */
+vg_status vg_get_vector_potential(vg_ctx* ctx, float* xyz, size_t cap_points, vg_grid_geom* geom);
+/* Statistics of the last step (waits for that step to finish). */
+vg_status vg_get_stats(vg_ctx* ctx, vg_step_stats* stats);
+/* Wait for the context's stream and report any error a device stage flagged
+ * since the last synchronising call (VG_OUT_OF_GRID, VG_NONFINITE).  The
+ * *_device entry points do not synchronise; host-buffer calls do this
+ * themselves. */
+vg_status vg_synchronize(vg_ctx* ctx);
+
+/* Replaces PclOpAssignVelocityFromField (gain 1) followed by PclOpEvolve
+ * (Particles/Operation/pclOpAdvect.cpp:42-152, pclOpEvolve.cpp:36-58) for
+ * tracers: velocity gathered trilinearly from the last step's velocity grid,
+ * then position += velocity * dt.  Particles must lie inside the grid. */
+vg_status vg_advect(vg_ctx* ctx, void* particles, size_t m, size_t stride, float dt);
+/* Device form: pos float4 (xyz, w untouched) updated in place, vel float4
+ * written (may be NULL). */
+vg_status vg_advect_device(vg_ctx* ctx, float* pos, float* vel, size_t m, float dt);
+
+/* Replaces PclOpEvolve (Particles/Operation/pclOpEvolve.cpp:36-58) on device
+ * records: pos4[i].xyz += vel4[i].xyz * dt (w untouched). */
+vg_status vg_evolve_device(vg_ctx* ctx, float* pos4, const float* vel4, size_t m, float dt);
+
+/* ---- Stage entry points on device memory (run on the context's stream).
+ * Each replaces one reference function and is what the step composes; they
+ * exist so that callers holding their own buffers can run one stage, and so
+ * that each stage can be checked against the oracle. */
+
+/* UniformGridGeometry::DefineShape (uniformGrid.h:259-322), host-side. */
+vg_status vg_define_shape(size_t n, const float vmin[3], const float vmax[3], int pow2, vg_grid_geom* out);
+
+/* IndicesOfPosition / OffsetOfPosition (uniformGrid.h:536-574, 645-651):
+ * idx3 uint32[3 m] and offset uint32[m] for m float4 positions. */
+vg_status vg_bin_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos4, size_t m, unsigned* idx3,
+                        unsigned* offset);
+
+/* ComputeVelocity_Direct / ComputeVectorPotential_Direct
+ * (VortonFluid/vortonSim.cpp:1113-1158) at m query points (float4) from n
+ * vortons; kind 0 velocity, 1 vector potential; out float4 per query. */
+vg_status vg_direct_device(vg_ctx* ctx, int kind, const float* pos_size, const float* angvel, size_t n,
+                           const float* q4, size_t m, float spread_range, float spread_circ, float* out4);
+
+/* CreateInfluenceTree (vortonSim.cpp:1605-1624) on grid g; then
+ * ComputeVelocity_Tree / ComputeVectorPotential_Tree from the root
+ * (vortonSim.cpp:1650-1905) at m query points.  tree_out (optional): 8 floats
+ * per point per layer (pos xyz, size, angvel xyz, unused), leaf first;
+ * tree_points receives the total point count. */
+vg_status vg_tree_device(vg_ctx* ctx, int kind, const vg_grid_geom* g, const float* pos_size,
+                         const float* angvel, size_t n, const float* q4, size_t m, float spread_range,
+                         float spread_circ, float* out4, float* tree_out, size_t tree_cap_points,
+                         size_t* tree_points);
+
+/* PopulateVorticityGridFromVortons(grid, scale) (vortonSim.cpp:2372-2436). */
+vg_status vg_splat_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, const float* angvel, size_t n,
+                          float scale, float* grid3);
+
+/* ComputeVectorPotentialFromVorticity_Integral, boundaries only
+ * (vortonSim.cpp:2055-2204): treecode vector potential on the 6 faces. */
+vg_status vg_boundary_vecpot_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size,
+                                    const float* angvel, size_t n, int copy_odd_x, float* grid3);
+
+/* SolveVectorPoisson, Dirichlet (Core/SpatialPartition/uniformGridMath.cpp:1116-1405). */
+vg_status vg_sor_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* lap3, int steps);
+/* The cascade of VortonSim::ComputeVectorPotential (vortonSim.cpp:2539-2571). */
+vg_status vg_cascade_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* rhs3, int steps);
+/* FP32 V-cycles in FP64 iterative refinement to `tolerance` (new; the
+ * reference's cascade cannot reach a residual target).  soln3 holds the
+ * boundary values and the initial interior guess on entry. */
+vg_status vg_multigrid_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* rhs3,
+                              double tolerance, int max_cycles, int* cycles, double* relres0, double* relres);
+/* DownSampleInto / UpSampleFrom (Core/SpatialPartition/nestedGrid.h:253-293,
+ * uniformGrid.h:1453-1700): inject 1 = FASTER_LESS_ACCURATE, 0 = 27-point;
+ * interior_only 1 = INTERIOR_ONLY. */
+vg_status vg_downsample_device(vg_ctx* ctx, const vg_grid_geom* fine, const float* fine3, const vg_grid_geom* coarse,
+                               int inject, float* coarse3);
+vg_status vg_upsample_device(vg_ctx* ctx, const vg_grid_geom* coarse, const float* coarse3,
+                             const vg_grid_geom* fine, int interior_only, float* fine3);
+
+/* ComputeJacobian + ComputeCurlFromJacobian (uniformGridMath.cpp:207-451):
+ * jac9 (optional) float[9] per point (j[3a+b] = d v_b / d a), curl3 float[3]. */
+vg_status vg_jacobian_curl_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vec3, float* jac9, float* curl3);
+
+/* StretchAndTiltVortons (vortonSim.cpp:2748-2820) with velocity grid vel3. */
+vg_status vg_stretch_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel3, const float* pos_size,
+                            float* angvel, size_t n, float dt);
+
+/* DiffuseAndDissipateVorticityPSE (vortonSim.cpp:3578-3879), order-independent
+ * form: every pair the reference visits exchanges from the pre-step values. */
+vg_status vg_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, float* angvel, size_t n,
+                        float viscosity, float dt);
+
+/* AssignParticleVelocityFromField (gain 1) + EvolveParticlesSlice on float4
+ * positions with grid vel3; vel4 (optional) receives the gathered velocity. */
+vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel3, float* pos4, float* vel4,
+                                  size_t m, float dt);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* VORTEGRID_H */

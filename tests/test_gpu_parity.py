@@ -1,0 +1,318 @@
+"""GPU parity of every stage of the VortonSim step, through the C ABI.
+
+Each test runs one stage of libvortegrid on cuda:0 on the golden inputs and
+compares it with the golden outputs that the reference's own code produced
+(tests/golden/reference.npz) or with the C oracle:
+  * REFERENCE numerics: bit-exact (uint32 view) for every FP32 stage whose
+    summation order the reference fixes;
+  * FAST numerics: stated relative-L2 tolerances against the FP64 oracle;
+  * PSE (order-dependent in the reference): 1e-3 relative L2 on vorticity.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+DT = np.float32(1.0 / 30.0)
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def dev(a):
+    return torch.from_numpy(np.ascontiguousarray(a)).cuda()
+
+
+def f4(xyz, w=None):
+    out = np.zeros((len(xyz), 4), np.float32)
+    out[:, :3] = xyz
+    if w is not None:
+        out[:, 3] = w
+    return out
+
+
+@pytest.fixture(scope="module")
+def vg():
+    import vortegrid_gb300 as vg
+    vg.lib()
+    return vg
+
+
+@pytest.fixture(scope="module")
+def ref_ctx(vg):
+    return vg.Context(numerics=vg.NUMERICS_REFERENCE)
+
+
+@pytest.fixture(scope="module")
+def fast_ctx(vg):
+    return vg.Context(numerics=vg.NUMERICS_FAST)
+
+
+def geom(vg, golden):
+    return vg.GridGeom.from12(golden["geom"], golden["np"])
+
+
+def vortons(golden):
+    return dev(f4(golden["pos"], golden["size"])), dev(f4(golden["angvel"]))
+
+
+def sync():
+    torch.cuda.synchronize()
+
+
+def test_binning_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    p = dev(f4(golden["bin_pos"]))
+    idx = torch.zeros((len(golden["bin_pos"]), 3), dtype=torch.int32, device="cuda")
+    off = torch.zeros(len(golden["bin_pos"]), dtype=torch.int32, device="cuda")
+    ref_ctx.check(vg.lib().vg_bin_device(ref_ctx.h, ctypes.byref(g), vg._ptr(p), len(p), vg._ptr(idx), vg._ptr(off)),
+                  "bin")
+    sync()
+    assert np.array_equal(idx.cpu().numpy().view(np.uint32), golden["bin_idx"])
+    assert np.array_equal(off.cpu().numpy().view(np.uint32), golden["bin_off"])
+
+
+@pytest.mark.parametrize("kind,name", [(0, "vel"), (1, "vecpot")])
+def test_direct_reference_bit_exact(vg, ref_ctx, golden, kind, name):
+    ps, w = vortons(golden)
+    q = dev(f4(golden["q"]))
+    out = torch.zeros((len(q), 4), dtype=torch.float32, device="cuda")
+    ref_ctx.check(vg.lib().vg_direct_device(ref_ctx.h, kind, vg._ptr(ps), vg._ptr(w), len(ps), vg._ptr(q), len(q),
+                                            1.0, 1.0, vg._ptr(out)), "direct")
+    sync()
+    assert np.array_equal(bits(out.cpu().numpy()[:, :3]), bits(golden[f"direct_{name}"]))
+
+
+@pytest.mark.parametrize("kind", [0, 1])
+def test_direct_fast_vs_fp64(vg, fast_ctx, oracle_lib, kind):
+    """FAST direct sum vs the FP64 oracle: rel-L2 <= 1e-5 (FP32 accumulation)."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(4096, seed=1)
+    q = np.concatenate([workloads.grid_points([-1.5] * 3, [3 / 32] * 3, [33] * 3)[::5], pos[::3]])
+    ref = oracle_lib.direct(kind, pos, w, s, q, f64=True)
+    ps, wd, qd = dev(f4(pos, s)), dev(f4(w)), dev(f4(q))
+    out = torch.zeros((len(q), 4), dtype=torch.float32, device="cuda")
+    fast_ctx.check(vg.lib().vg_direct_device(fast_ctx.h, kind, vg._ptr(ps), vg._ptr(wd), len(ps), vg._ptr(qd), len(q),
+                                             1.0, 1.0, vg._ptr(out)), "direct")
+    sync()
+    got = out.cpu().numpy()[:, :3].astype(np.float64)
+    rel = np.linalg.norm(got - ref) / np.linalg.norm(ref)
+    assert rel < 1e-5, rel
+
+
+def test_tree_reference_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    q = dev(f4(golden["q"]))
+    npts = ctypes.c_size_t()
+    lib = vg.lib()
+    ref_ctx.check(lib.vg_tree_device(ref_ctx.h, 0, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps), None, 0, 1.0,
+                                     1.0, None, None, 0, ctypes.byref(npts)), "tree size")
+    tree = torch.zeros((npts.value, 8), dtype=torch.float32, device="cuda")
+    sr, sc = golden["spread"]
+    for kind, name in ((0, "vel"), (1, "vecpot")):
+        for (a, b, suffix) in ((1.0, 1.0, ""), (float(sr), float(sc), "_spread")):
+            out = torch.zeros((len(q), 4), dtype=torch.float32, device="cuda")
+            ref_ctx.check(lib.vg_tree_device(ref_ctx.h, kind, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps),
+                                             vg._ptr(q), len(q), a, b, vg._ptr(out), vg._ptr(tree), npts.value,
+                                             ctypes.byref(npts)), "tree")
+            sync()
+            assert np.array_equal(bits(out.cpu().numpy()[:, :3]), bits(golden[f"tree_{name}{suffix}"])), (name, suffix)
+    t = tree.cpu().numpy()
+    gt = golden["tree"]  # pos xyz, angvel xyz, size
+    mine = np.concatenate([t[:, 0:3], t[:, 4:7], t[:, 3:4]], axis=1)
+    assert np.array_equal(bits(mine), bits(gt))
+
+
+def test_tree_fast_close(vg, fast_ctx, golden):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    q = dev(f4(golden["q"]))
+    out = torch.zeros((len(q), 4), dtype=torch.float32, device="cuda")
+    npts = ctypes.c_size_t()
+    fast_ctx.check(vg.lib().vg_tree_device(fast_ctx.h, 0, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps),
+                                           vg._ptr(q), len(q), 1.0, 1.0, vg._ptr(out), None, 0, ctypes.byref(npts)),
+                   "tree")
+    sync()
+    ref = golden["tree_vel"]
+    got = out.cpu().numpy()[:, :3]
+    # the reference's magic-constant rsqrt carries ~1.8e-3 relative error per pair
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 3e-3
+
+
+def test_splat_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    out = torch.zeros((g.capacity, 3), dtype=torch.float32, device="cuda")
+    ref_ctx.check(vg.lib().vg_splat_device(ref_ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps), -1.0,
+                                           vg._ptr(out)), "splat")
+    sync()
+    assert np.array_equal(bits(out.cpu().numpy()), bits(golden["negvort"]))
+
+
+def test_boundary_vecpot_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    out = torch.zeros((g.capacity, 3), dtype=torch.float32, device="cuda")
+    ref_ctx.check(vg.lib().vg_boundary_vecpot_device(ref_ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps), 1,
+                                                     vg._ptr(out)), "boundary")
+    sync()
+    assert np.array_equal(bits(out.cpu().numpy()), bits(golden["boundary_vecpot"]))
+
+
+def test_sor_and_cascade_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    rhs = dev(golden["negvort"])
+    a = dev(golden["boundary_vecpot"])
+    ref_ctx.check(vg.lib().vg_sor_device(ref_ctx.h, ctypes.byref(g), vg._ptr(a), vg._ptr(rhs), 5), "sor")
+    sync()
+    assert np.array_equal(bits(a.cpu().numpy()), bits(golden["sor5"]))
+    a = dev(golden["boundary_vecpot"])
+    ref_ctx.check(vg.lib().vg_cascade_device(ref_ctx.h, ctypes.byref(g), vg._ptr(a), vg._ptr(rhs), 16), "cascade")
+    sync()
+    assert np.array_equal(bits(a.cpu().numpy()), bits(golden["cascade"]))
+
+
+def test_restrict_prolong_bit_exact(vg, ref_ctx, golden, oracle_lib):
+    g = geom(vg, golden)
+    og = oracle_lib.Geom.from12(golden["geom"], golden["np"])
+    layers, _ = oracle_lib.nested_shape(og)
+    cg = vg.GridGeom.from12(layers[1].as12(), layers[1].points)
+    fine = dev(golden["cascade"])
+    for inject, name in ((1, "inject"), (0, "average")):
+        c = torch.zeros((cg.capacity, 3), dtype=torch.float32, device="cuda")
+        ref_ctx.check(vg.lib().vg_downsample_device(ref_ctx.h, ctypes.byref(g), vg._ptr(fine), ctypes.byref(cg),
+                                                    inject, vg._ptr(c)), "down")
+        sync()
+        assert np.array_equal(bits(c.cpu().numpy()), bits(golden[f"down_{name}"])), name
+        for interior, rname in ((1, "interior"), (0, "entire")):
+            f = dev(golden["cascade"])
+            ref_ctx.check(vg.lib().vg_upsample_device(ref_ctx.h, ctypes.byref(cg), vg._ptr(c), ctypes.byref(g),
+                                                      interior, vg._ptr(f)), "up")
+            sync()
+            assert np.array_equal(bits(f.cpu().numpy()), bits(golden[f"up_{name}_{rname}"])), (name, rname)
+
+
+def test_jacobian_curl_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    a = dev(golden["cascade"])
+    jac = torch.zeros((g.capacity, 9), dtype=torch.float32, device="cuda")
+    curl = torch.zeros((g.capacity, 3), dtype=torch.float32, device="cuda")
+    ref_ctx.check(vg.lib().vg_jacobian_curl_device(ref_ctx.h, ctypes.byref(g), vg._ptr(a), vg._ptr(jac),
+                                                   vg._ptr(curl)), "jac")
+    sync()
+    assert np.array_equal(bits(jac.cpu().numpy()), bits(golden["jacobian"]))
+    assert np.array_equal(bits(curl.cpu().numpy()), bits(golden["curl"]))
+
+
+def test_stretch_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    vel = dev(golden["curl"])
+    ref_ctx.check(vg.lib().vg_stretch_device(ref_ctx.h, ctypes.byref(g), vg._ptr(vel), vg._ptr(ps), vg._ptr(w),
+                                             len(ps), float(DT)), "stretch")
+    sync()
+    assert np.array_equal(bits(w.cpu().numpy()[:, :3]), bits(golden["stretched"]))
+
+
+def test_pse_tolerance(vg, ref_ctx, golden, oracle_lib):
+    g = geom(vg, golden)
+    ps, w = vortons(golden)
+    ref_ctx.check(vg.lib().vg_pse_device(ref_ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(w), len(ps), 0.01,
+                                         float(DT)), "pse")
+    sync()
+    got = w.cpu().numpy()[:, :3]
+    ref = golden["pse"]
+    assert np.linalg.norm(got - ref) / np.linalg.norm(ref) < 1e-3
+    og = oracle_lib.Geom.from12(golden["geom"], golden["np"])
+    sym = oracle_lib.pse(golden["pos"], golden["angvel"], golden["size"], og, 0.01, DT, symmetric=True)
+    assert np.linalg.norm(got - sym) / np.linalg.norm(sym) < 1e-6
+
+
+def test_gather_advect_bit_exact(vg, ref_ctx, golden):
+    g = geom(vg, golden)
+    vel = dev(golden["curl"])
+    p = dev(f4(golden["tracers"]))
+    v = torch.zeros_like(p)
+    ref_ctx.check(vg.lib().vg_gather_advect_device(ref_ctx.h, ctypes.byref(g), vg._ptr(vel), vg._ptr(p), vg._ptr(v),
+                                                   len(p), float(DT)), "advect")
+    sync()
+    assert np.array_equal(bits(v.cpu().numpy()[:, :3]), bits(golden["tracer_vel"]))
+    assert np.array_equal(bits(p.cpu().numpy()[:, :3]), bits(golden["tracer_pos1"]))
+
+
+def test_full_step_reference_numerics(vg, golden):
+    """PclOpVortonSim::Operate on the reference's 96-byte records, REFERENCE
+    numerics + the reference cascade: the velocity grid and vorton velocities
+    are bit-identical to the reference; angular velocity within the PSE bound."""
+    sim = vg.VortonSim(0.01, numerics=vg.NUMERICS_REFERENCE, poisson_solver=vg.POISSON_REFERENCE_CASCADE,
+                       boundary_copy_odd_x=1)
+    recs = np.frombuffer(golden["step_in"].tobytes(), dtype=vg.PARTICLE_DTYPE).copy()
+    sim.Update(recs, DT, 0, golden["step_extra_min"], golden["step_extra_max"])
+    vel, g = sim.GetVelocityGrid()
+    assert np.array_equal(bits(g.as12()), bits(golden["step_geom"]))
+    assert list(g.points) == list(golden["step_np"])
+    assert np.array_equal(bits(vel), bits(golden["step_velgrid"]))
+    ap, _ = sim.GetVectorPotential()
+    assert np.array_equal(bits(ap), bits(golden["step_vecpot"]))
+    out = np.frombuffer(golden["step_out"].tobytes(), dtype=vg.PARTICLE_DTYPE)
+    assert np.array_equal(bits(recs["velocity"]), bits(out["velocity"]))
+    w, wr = recs["angular_velocity"], out["angular_velocity"]
+    assert np.linalg.norm(w - wr) / np.linalg.norm(wr) < 1e-3
+    # untouched fields survive the round trip
+    assert np.array_equal(recs["position"], out["position"])
+    assert np.array_equal(recs["size"], out["size"])
+
+
+def test_multigrid_reaches_tolerance(vg, oracle_lib):
+    """FAST numerics, multigrid to 1e-6: FP64 residual checked on the CPU, and
+    the velocity grid vs the FP64 direct sum."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.puff(20000, seed=5)
+    g = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [65] * 3)
+    sim = vg.VortonSim(0.01, fixed_grid=g, enable_stretch=0, enable_diffusion=0)
+    recs = vg.make_particles(pos, w, s)
+    sim.Update(recs, DT, 0)
+    st = sim.stats()
+    assert st.poisson_relres <= 1e-6 and st.poisson_cycles >= 1, (st.poisson_relres, st.poisson_cycles)
+    a, gg = sim.GetVectorPotential()
+    og = oracle_lib.Geom.from12(gg.as12(), gg.points)
+    b = oracle_lib.splat(pos, w, s, og, -1.0)
+    assert oracle_lib.relres(og, a, b) < 1e-4
+    vel, _ = sim.GetVelocityGrid()
+    # compare the interior velocity with the FP64 direct sum at gridpoints
+    pts = workloads.grid_points(og.mn, og.cell, og.points).reshape(65, 65, 65, 3)[8:-8:4, 8:-8:4, 8:-8:4].reshape(-1, 3)
+    d = oracle_lib.direct(0, pos, w, s, pts, f64=True)
+    v = vel.reshape(65, 65, 65, 3)[8:-8:4, 8:-8:4, 8:-8:4].reshape(-1, 3)
+    rel = np.linalg.norm(v - d) / np.linalg.norm(d)
+    assert rel < 0.15, rel  # discretisation error of the grid method (dx = 1/16)
+
+
+def test_status_paths(vg):
+    sim = vg.VortonSim(0.01)
+    empty = np.zeros(0, vg.PARTICLE_DTYPE)
+    with pytest.raises(vg.VgError) as e:
+        sim.Update(empty, DT, 0)
+    assert e.value.status == vg.EMPTY
+    with pytest.raises(vg.VgError) as e:
+        sim.GetVelocityGrid()
+    assert e.value.status == vg.EMPTY
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(500, seed=3)
+    sim.Update(vg.make_particles(pos, w, s), DT, 0)
+    far = vg.make_particles(np.full((4, 3), 50.0, np.float32))
+    with pytest.raises(vg.VgError) as e:
+        sim.Advect(far, DT)
+    assert e.value.status == vg.OUT_OF_GRID
+    # the context stays usable after a reported error
+    inside = vg.make_particles(pos[:10])
+    sim.Advect(inside, DT)
+    nan = vg.make_particles(np.array([[np.nan, 0, 0]] * 3, np.float32), w[:3], s[:3])
+    with pytest.raises(vg.VgError) as e:
+        sim.Update(nan, DT, 0)
+    assert e.value.status == vg.NONFINITE

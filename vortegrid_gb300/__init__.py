@@ -1,0 +1,347 @@
+"""GB300 (sm_103a) VortonSim velocity-from-vorticity step.
+
+Python host side of ``libvortegrid.so`` (declared in ``include/vortegrid.h``).
+It mirrors the reference's particle-operation interface for this step
+(mijagourlay/VorteGrid, Samples/MjgIntelFluidDemo_Part20):
+
+  * ``PclOpVortonSim.Operate(particles, timeStep, uFrame)`` --
+    VortonFluid/pclOpVortonSim.cpp:51-71, on an array of the reference's
+    96-byte ``Particle`` records (``PARTICLE_DTYPE``);
+  * ``VortonSim`` -- VortonFluid/vortonSim.h:279-455: ``Update``,
+    ``GetVelocityGrid``, ``GetVectorPotential``, settings as in the reference;
+  * ``PclOpAssignVelocityFromFieldAndEvolve`` -- tracer advection
+    (Particles/Operation/pclOpAdvect.cpp:132-152, pclOpEvolve.cpp:36-58).
+
+There is no CPU fallback: every call goes through the CUDA library, and
+importing a function that needs it raises if the library is missing.
+"""
+import ctypes
+import os
+
+import numpy as np
+
+from . import workloads  # noqa: F401
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "_build", "libvortegrid.so")
+
+# vg_status
+OK, EMPTY, OUT_OF_GRID, NONFINITE, OOM, TIMEOUT, INVALID, CUDA_ERROR, NOT_CONVERGED, TOO_LARGE = range(10)
+VELOCITY_POISSON, VELOCITY_TREE, VELOCITY_DIRECT = 0, 1, 2
+NUMERICS_FAST, NUMERICS_REFERENCE = 0, 1
+POISSON_MULTIGRID, POISSON_REFERENCE_CASCADE = 0, 1
+WARM_ZERO, WARM_PREVIOUS, WARM_NETWORK = 0, 1, 2
+
+# The reference's Particle record on LP64 (Particles/particle.h:425-482).
+PARTICLE_DTYPE = np.dtype({
+    "names": ["position", "velocity", "orientation", "angular_velocity", "density", "size", "birth_time",
+              "fuel", "flame", "smoke"],
+    "formats": [(np.float32, 3), (np.float32, 3), (np.float32, 3), (np.float32, 3), np.float32, np.float32,
+                np.int32, np.float32, np.float32, np.float32],
+    "offsets": [0, 12, 24, 36, 48, 52, 56, 60, 64, 68],
+    "itemsize": 96,
+})
+
+
+class VgError(RuntimeError):
+    def __init__(self, status, msg):
+        super().__init__(f"{msg} (status {status})")
+        self.status = status
+
+
+class GridGeom(ctypes.Structure):
+    _fields_ = [("min_corner", ctypes.c_float * 3), ("extent", ctypes.c_float * 3),
+                ("cell_spacing", ctypes.c_float * 3), ("cells_per_extent", ctypes.c_float * 3),
+                ("num_points", ctypes.c_uint * 3)]
+
+    @property
+    def points(self):
+        return tuple(int(v) for v in self.num_points)
+
+    @property
+    def capacity(self):
+        p = self.points
+        return p[0] * p[1] * p[2]
+
+    def as12(self):
+        return np.array(list(self.min_corner) + list(self.extent) + list(self.cell_spacing) +
+                        list(self.cells_per_extent), np.float32)
+
+    @staticmethod
+    def make(min_corner, extent, num_points):
+        """Explicit geometry: spacing and cells-per-extent follow
+        UniformGridGeometry::PrecomputeSpacing (uniformGrid.h:794-809)."""
+        g = GridGeom()
+        for a in range(3):
+            g.min_corner[a] = float(np.float32(min_corner[a]))
+            g.extent[a] = float(np.float32(extent[a]))
+            g.num_points[a] = int(num_points[a])
+            cells = np.float32(int(num_points[a]) - 1)
+            g.cell_spacing[a] = float(np.float32(extent[a]) / cells)
+            g.cells_per_extent[a] = float(cells / np.float32(extent[a]))
+        return g
+
+    @staticmethod
+    def from12(g12, np3):
+        g = GridGeom()
+        for a in range(3):
+            g.min_corner[a] = float(g12[a]); g.extent[a] = float(g12[3 + a])
+            g.cell_spacing[a] = float(g12[6 + a]); g.cells_per_extent[a] = float(g12[9 + a])
+            g.num_points[a] = int(np3[a])
+        return g
+
+
+class Config(ctypes.Structure):
+    _fields_ = [("abi_version", ctypes.c_uint), ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
+                ("velocity_technique", ctypes.c_int), ("numerics", ctypes.c_int), ("poisson_solver", ctypes.c_int),
+                ("warm_start", ctypes.c_int), ("viscosity", ctypes.c_float), ("poisson_tolerance", ctypes.c_double),
+                ("poisson_max_cycles", ctypes.c_int), ("cascade_steps", ctypes.c_int),
+                ("enable_stretch", ctypes.c_int), ("enable_diffusion", ctypes.c_int),
+                ("boundary_copy_odd_x", ctypes.c_int), ("use_fixed_grid", ctypes.c_int),
+                ("fixed_grid", GridGeom)]
+
+
+class StepStats(ctypes.Structure):
+    _fields_ = [("grid", GridGeom), ("tree_depth", ctypes.c_int), ("poisson_cycles", ctypes.c_int),
+                ("poisson_relres", ctypes.c_double), ("poisson_relres0", ctypes.c_double),
+                ("ms_total", ctypes.c_float), ("ms_poisson", ctypes.c_float),
+                ("kernels_launched", ctypes.c_uint)]
+
+
+_lib = None
+
+EXPORTS = [
+    "vg_status_string", "vg_last_error", "vg_abi_version", "vg_config_default", "vg_create", "vg_destroy",
+    "vg_set_config", "vg_step", "vg_step_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
+    "vg_get_vector_potential", "vg_get_stats", "vg_advect", "vg_advect_device", "vg_define_shape",
+    "vg_bin_device", "vg_direct_device", "vg_tree_device", "vg_splat_device", "vg_boundary_vecpot_device",
+    "vg_sor_device", "vg_cascade_device", "vg_multigrid_device", "vg_downsample_device", "vg_upsample_device",
+    "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
+    "vg_evolve_device",
+]
+
+
+def lib():
+    """Load libvortegrid.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError(f"libvortegrid.so not built: run `python -c 'import __graft_entry__ as g; g.build()'` "
+                              f"(expected {LIB_PATH})")
+        L = ctypes.CDLL(LIB_PATH)
+        L.vg_status_string.restype = ctypes.c_char_p
+        L.vg_last_error.restype = ctypes.c_char_p
+        L.vg_last_error.argtypes = [ctypes.c_void_p]
+        L.vg_abi_version.restype = ctypes.c_uint
+        for name in EXPORTS:
+            f = getattr(L, name)
+            if name not in ("vg_status_string", "vg_last_error", "vg_abi_version"):
+                f.restype = ctypes.c_int
+        L.vg_create.argtypes = [ctypes.POINTER(Config), ctypes.POINTER(ctypes.c_void_p)]
+        L.vg_destroy.argtypes = [ctypes.c_void_p]
+        L.vg_set_config.argtypes = [ctypes.c_void_p, ctypes.POINTER(Config)]
+        L.vg_step.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_void_p,
+                              ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
+        L.vg_step_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                     ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
+        L.vg_get_velocity_grid.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GridGeom)]
+        L.vg_get_velocity_grid_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
+                                                  ctypes.POINTER(GridGeom)]
+        L.vg_get_vector_potential.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                              ctypes.POINTER(GridGeom)]
+        L.vg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(StepStats)]
+        L.vg_synchronize.argtypes = [ctypes.c_void_p]
+        L.vg_evolve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_float]
+        L.vg_advect.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_float]
+        L.vg_advect_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                       ctypes.c_float]
+        L.vg_define_shape.argtypes = [ctypes.c_size_t, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_int,
+                                      ctypes.POINTER(GridGeom)]
+        vp, G, sz, fl, i = ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_size_t, ctypes.c_float, ctypes.c_int
+        L.vg_bin_device.argtypes = [vp, G, vp, sz, vp, vp]
+        L.vg_direct_device.argtypes = [vp, i, vp, vp, sz, vp, sz, fl, fl, vp]
+        L.vg_tree_device.argtypes = [vp, i, G, vp, vp, sz, vp, sz, fl, fl, vp, vp, sz, ctypes.POINTER(ctypes.c_size_t)]
+        L.vg_splat_device.argtypes = [vp, G, vp, vp, sz, fl, vp]
+        L.vg_boundary_vecpot_device.argtypes = [vp, G, vp, vp, sz, i, vp]
+        L.vg_sor_device.argtypes = [vp, G, vp, vp, i]
+        L.vg_cascade_device.argtypes = [vp, G, vp, vp, i]
+        L.vg_multigrid_device.argtypes = [vp, G, vp, vp, ctypes.c_double, i, ctypes.POINTER(ctypes.c_int),
+                                          ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_double)]
+        L.vg_downsample_device.argtypes = [vp, G, vp, G, i, vp]
+        L.vg_upsample_device.argtypes = [vp, G, vp, G, i, vp]
+        L.vg_jacobian_curl_device.argtypes = [vp, G, vp, vp, vp]
+        L.vg_stretch_device.argtypes = [vp, G, vp, vp, vp, sz, fl]
+        L.vg_pse_device.argtypes = [vp, G, vp, vp, sz, fl, fl]
+        L.vg_gather_advect_device.argtypes = [vp, G, vp, vp, vp, sz, fl]
+        if L.vg_abi_version() != 1:
+            raise ImportError("libvortegrid ABI version mismatch")
+        _lib = L
+    return _lib
+
+
+def default_config(**kw):
+    cfg = Config()
+    lib().vg_config_default(ctypes.byref(cfg))
+    for k, v in kw.items():
+        if k == "fixed_grid":
+            cfg.fixed_grid = v
+            cfg.use_fixed_grid = 1
+        else:
+            setattr(cfg, k, v)
+    return cfg
+
+
+class Context:
+    """One vg_ctx: a VortonSim instance on one device and stream."""
+
+    def __init__(self, cfg=None, **kw):
+        self.cfg = cfg if cfg is not None else default_config(**kw)
+        h = ctypes.c_void_p()
+        st = lib().vg_create(ctypes.byref(self.cfg), ctypes.byref(h))
+        if st != OK:
+            raise VgError(st, "vg_create: " + lib().vg_last_error(None).decode())
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().vg_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def check(self, st, what):
+        if st != OK:
+            raise VgError(st, f"{what}: {lib().vg_last_error(self.h).decode()}")
+        return st
+
+    def set_config(self, **kw):
+        for k, v in kw.items():
+            if k == "fixed_grid":
+                self.cfg.fixed_grid = v
+                self.cfg.use_fixed_grid = 1
+            else:
+                setattr(self.cfg, k, v)
+        self.check(lib().vg_set_config(self.h, ctypes.byref(self.cfg)), "vg_set_config")
+
+    def synchronize(self):
+        """Wait for the stream; raise for errors flagged by device stages."""
+        self.check(lib().vg_synchronize(self.h), "vg_synchronize")
+
+    def stats(self):
+        s = StepStats()
+        self.check(lib().vg_get_stats(self.h, ctypes.byref(s)), "vg_get_stats")
+        return s
+
+
+def _ptr(a):
+    if a is None:
+        return None
+    if hasattr(a, "data_ptr"):
+        return ctypes.c_void_p(a.data_ptr())
+    return a.ctypes.data_as(ctypes.c_void_p)
+
+
+class VortonSim(Context):
+    """VortonSim (VortonFluid/vortonSim.h:279-455) on the GPU."""
+
+    def __init__(self, viscosity=0.01, cfg=None, **kw):
+        if cfg is not None:
+            super().__init__(cfg)
+        else:
+            super().__init__(viscosity=viscosity, **kw)
+
+    def Update(self, particles, timeStep, uFrame=0, extra_min=None, extra_max=None):
+        """FindBoundingBox + UpdateBoundingBox(final) + Update on host Particle records."""
+        if particles.dtype.itemsize < 56 or not particles.flags.c_contiguous:
+            raise ValueError("particles must be a C-contiguous array of Particle records")
+        emin = np.ascontiguousarray(extra_min, np.float32) if extra_min is not None else None
+        emax = np.ascontiguousarray(extra_max, np.float32) if extra_max is not None else None
+        self.check(lib().vg_step(self.h, _ptr(particles), len(particles), particles.dtype.itemsize, _ptr(emin),
+                                 _ptr(emax), timeStep, uFrame), "vg_step")
+
+    def UpdateDevice(self, pos_size, angvel, vel, timeStep, uFrame=0, extra_minmax=None):
+        e = np.ascontiguousarray(extra_minmax, np.float32) if extra_minmax is not None else None
+        self.check(lib().vg_step_device(self.h, _ptr(pos_size), _ptr(angvel), _ptr(vel), pos_size.shape[0], _ptr(e),
+                                        timeStep, uFrame), "vg_step_device")
+
+    def GetVelocityGrid(self):
+        g = GridGeom()
+        self.check(lib().vg_get_velocity_grid(self.h, None, 0, ctypes.byref(g)), "vg_get_velocity_grid")
+        out = np.zeros((g.capacity, 3), np.float32)
+        self.check(lib().vg_get_velocity_grid(self.h, _ptr(out), g.capacity, ctypes.byref(g)), "vg_get_velocity_grid")
+        return out, g
+
+    def GetVectorPotential(self):
+        g = GridGeom()
+        self.check(lib().vg_get_vector_potential(self.h, None, 0, ctypes.byref(g)), "vg_get_vector_potential")
+        out = np.zeros((g.capacity, 3), np.float32)
+        self.check(lib().vg_get_vector_potential(self.h, _ptr(out), g.capacity, ctypes.byref(g)),
+                   "vg_get_vector_potential")
+        return out, g
+
+    def Advect(self, particles, timeStep):
+        """AssignVelocityFromField (gain 1) + Evolve for tracer records."""
+        self.check(lib().vg_advect(self.h, _ptr(particles), len(particles), particles.dtype.itemsize, timeStep),
+                   "vg_advect")
+
+    def EvolveDevice(self, pos4, vel4, timeStep):
+        """PclOpEvolve on device float4 positions and velocities."""
+        self.check(lib().vg_evolve_device(self.h, _ptr(pos4), _ptr(vel4), pos4.shape[0], timeStep),
+                   "vg_evolve_device")
+
+    def AdvectDevice(self, pos4, vel4, timeStep):
+        self.check(lib().vg_advect_device(self.h, _ptr(pos4), _ptr(vel4), pos4.shape[0], timeStep),
+                   "vg_advect_device")
+
+
+class PclOpVortonSim:
+    """IParticleOperation wrapper (VortonFluid/pclOpVortonSim.h:46-71):
+    Operate(particles, timeStep, uFrame) runs one VortonSim step on the
+    particle group's records; mMinCorner / mMaxCorner (the tracers' box) may be
+    set to extend the grid."""
+
+    def __init__(self, viscosity=0.01, **kw):
+        self.mVortonSim = VortonSim(viscosity, **kw)
+        self.mMinCorner = None
+        self.mMaxCorner = None
+
+    def Operate(self, particles, timeStep, uFrame=0):
+        self.mVortonSim.Update(particles, timeStep, uFrame, self.mMinCorner, self.mMaxCorner)
+
+
+class PclOpAssignVelocityFromFieldAndEvolve:
+    """PclOpAssignVelocityFromField (gain 1) followed by PclOpEvolve for tracers,
+    reading the velocity grid of a VortonSim's last step."""
+
+    def __init__(self, vorton_sim):
+        self.mVortonSim = vorton_sim
+
+    def Operate(self, particles, timeStep, uFrame=0):
+        self.mVortonSim.Advect(particles, timeStep)
+
+
+def make_particles(pos, angvel=None, size=None):
+    """Particle records from positions (and vorton angular velocity = vorticity/2, size = diameter)."""
+    n = len(pos)
+    p = np.zeros(n, PARTICLE_DTYPE)
+    p["position"] = pos
+    if angvel is not None:
+        p["angular_velocity"] = angvel
+    if size is not None:
+        p["size"] = size
+    p["density"] = 1.0
+    return p
+
+
+def define_shape(n, vmin, vmax, pow2=True):
+    g = GridGeom()
+    st = lib().vg_define_shape(n, _ptr(np.ascontiguousarray(vmin, np.float32)),
+                               _ptr(np.ascontiguousarray(vmax, np.float32)), int(pow2), ctypes.byref(g))
+    if st != OK:
+        raise VgError(st, "vg_define_shape")
+    return g

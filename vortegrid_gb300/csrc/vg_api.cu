@@ -1,0 +1,796 @@
+// C ABI of libvortegrid: context, workspace, host-side geometry rules and the
+// VortonSim step (VortonFluid/pclOpVortonSim.cpp:51-71,
+// VortonFluid/vortonSim.cpp:4117-4344) composed from the stage kernels.
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
+#include <algorithm>
+#include <cstdio>
+#include <new>
+
+#include "vg_internal.cuh"
+
+namespace vg {
+
+// ------------------------------------------------------------ host geometry
+// Compiled with -ffp-contract=off so every float operation rounds like the
+// reference's.
+
+void precompute_spacing(Geom& g) {  // uniformGrid.h:794-809
+  for (int a = 0; a < 3; ++a) g.cell[a] = g.ext[a] / (float)(g.np[a] - 1);
+  g.cpe[0] = (float)(g.np[0] - 1) / g.ext[0];
+  g.cpe[1] = (float)(g.np[1] - 1) / g.ext[1];
+  g.cpe[2] = (0.0f == g.ext[2]) ? 1.0f / FLT_MIN : (float)(g.np[2] - 1) / g.ext[2];
+}
+
+static size_t nearest_pow2(size_t v) {  // Core/Math/math.h:149-175
+  if (v == 0) return 1;
+  --v;
+  unsigned shift = 0;
+  while ((v >> shift) != 0) ++shift;
+  return (size_t)(1U << shift);
+}
+
+Geom define_shape(size_t n, const float vmin[3], const float vmax[3], bool pow2) {  // uniformGrid.h:259-322
+  Geom g;
+  memset(&g, 0, sizeof(g));
+  if (n == 0) return g;
+  const float nudge = 1.0f + FLT_EPSILON;
+  float eff[3];
+  int dims = 3;
+  for (int a = 0; a < 3; ++a) {
+    g.mn[a] = vmin[a];
+    g.ext[a] = (vmax[a] - vmin[a]) * nudge;
+    eff[a] = g.ext[a];
+  }
+  for (int a = 0; a < 3; ++a)
+    if (0.0f == eff[a]) {
+      eff[a] = 1.0f;
+      g.ext[a] = 0.0f;
+      --dims;
+    }
+  const float volume = eff[0] * eff[1] * eff[2];
+  const float inv_cell = powf(volume / (float)n, -1.0f / (float)dims);
+  size_t nc[3];
+  for (int a = 0; a < 3; ++a) {
+    const size_t c = (size_t)(g.ext[a] * inv_cell + 0.5f);
+    nc[a] = c > 1 ? c : 1;
+  }
+  if (pow2)
+    for (int a = 0; a < 3; ++a) nc[a] = nearest_pow2(nc[a]);
+  while (nc[0] * nc[1] * nc[2] >= n * 8)
+    for (int a = 0; a < 3; ++a) nc[a] = nc[a] / 2 > 1 ? nc[a] / 2 : 1;
+  for (int a = 0; a < 3; ++a) g.np[a] = (unsigned)(nc[a] + 1);
+  precompute_spacing(g);
+  return g;
+}
+
+Geom decimate(const Geom& src, unsigned dec) {  // uniformGrid.h:398-412
+  Geom d = src;
+  for (int a = 0; a < 3; ++a) {
+    d.np[a] = (src.np[a] - 1) / dec + 1;
+    if (dec > 1 && d.np[a] < 2) d.np[a] = 2;
+  }
+  precompute_spacing(d);
+  return d;
+}
+
+int nested_shape(const Geom& g, Geom* layers, unsigned (*decim)[3]) {  // nestedGrid.h:69-85, 312-391
+  int depth = 0;
+  layers[depth++] = decimate(g, 1);
+  while (layers[depth - 1].points() > 8 && depth < kMaxLayers) {
+    layers[depth] = decimate(layers[depth - 1], 2);
+    ++depth;
+  }
+  decim[0][0] = decim[0][1] = decim[0][2] = 0;
+  for (int l = 1; l < depth; ++l)
+    for (int a = 0; a < 3; ++a) decim[l][a] = (layers[l - 1].np[a] - 1) / (layers[l].np[a] - 1);
+  return depth;
+}
+
+// ------------------------------------------------------------------ context
+
+vg_status fail(Ctx* c, vg_status s, const std::string& msg) {
+  if (c) c->err = msg;
+  return s;
+}
+
+vg_status cuda_check(Ctx* c, cudaError_t e, const char* what) {
+  char buf[512];
+  snprintf(buf, sizeof(buf), "%s: %s", what, cudaGetErrorString(e));
+  return fail(c, e == cudaErrorMemoryAllocation ? VG_OOM : VG_CUDA_ERROR, buf);
+}
+
+vg_status sync_and_check(Ctx* c, const char* what) {
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  int h = 0;
+  VG_CUDA(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (h) {
+    VG_CUDA(c, cudaMemset(c->dflag, 0, sizeof(int)));
+    if (h & DF_NONFINITE) return fail(c, VG_NONFINITE, std::string(what) + ": non-finite vorton position");
+    return fail(c, VG_OUT_OF_GRID, std::string(what) + ": a particle lies outside the grid's cells");
+  }
+  return VG_OK;
+}
+
+void* ws(Ctx* c, int s, size_t bytes, vg_status* st) {
+  Buf& b = c->buf[s];
+  if (b.bytes >= bytes && b.p) return b.p;
+  if (b.p) {
+    cudaStreamSynchronize(c->stream);
+    cudaFree(b.p);
+    b.p = nullptr;
+    b.bytes = 0;
+  }
+  size_t want = bytes + bytes / 8 + 256;
+  cudaError_t e = cudaMalloc(&b.p, want);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    b.p = nullptr;
+    *st = fail(c, VG_OOM, "device allocation of " + std::to_string(want) + " bytes failed");
+    return nullptr;
+  }
+  b.bytes = want;
+  return b.p;
+}
+
+}  // namespace vg
+
+using namespace vg;
+
+struct vg_ctx : public vg::Ctx {};
+
+namespace {
+
+thread_local std::string g_err_noctx;
+
+__global__ void k_unpack_records(const unsigned char* __restrict__ rec, size_t pitch, int n, float4* __restrict__ ps,
+                                 float4* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = (const float*)(rec + (size_t)i * pitch);
+  ps[i] = make_float4(r[0], r[1], r[2], r[13]);  // position @0, size @52
+  w[i] = make_float4(r[9], r[10], r[11], 0.f);   // angular velocity @36
+}
+
+__global__ void k_pack_records(unsigned char* __restrict__ rec, size_t pitch, int n, const float4* __restrict__ v,
+                               const float4* __restrict__ w) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float* r = (float*)(rec + (size_t)i * pitch);  // record bytes [12, 48)
+  r[0] = v[i].x;
+  r[1] = v[i].y;
+  r[2] = v[i].z;
+  r[6] = w[i].x;
+  r[7] = w[i].y;
+  r[8] = w[i].z;
+}
+
+__global__ void k_grid_points(Geom g, float4* __restrict__ q) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= g.points()) return;
+  const unsigned x = (unsigned)(k % g.np[0]), y = (unsigned)((k / g.np[0]) % g.np[1]),
+                 z = (unsigned)(k / ((size_t)g.np[0] * g.np[1]));
+  // gridpoint positions min + i * spacing * (1 - 2 eps) (vortonSim.cpp:2229-2252)
+  const float nudge = 1.0f - 2.0f * FLT_EPSILON;
+  q[k] = make_float4(__fadd_rn(g.mn[0], __fmul_rn((float)x, __fmul_rn(g.cell[0], nudge))),
+                     __fadd_rn(g.mn[1], __fmul_rn((float)y, __fmul_rn(g.cell[1], nudge))),
+                     __fadd_rn(g.mn[2], __fmul_rn((float)z, __fmul_rn(g.cell[2], nudge))), 0.f);
+}
+
+__global__ void k_f4_to_f3(const float4* __restrict__ a, float* __restrict__ b, size_t n) {
+  const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n) {
+    b[3 * i] = a[i].x;
+    b[3 * i + 1] = a[i].y;
+    b[3 * i + 2] = a[i].z;
+  }
+}
+
+__global__ void k_copy_pos3(const unsigned char* __restrict__ rec, size_t pitch, int n, float4* __restrict__ p) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float* r = (const float*)(rec + (size_t)i * pitch);
+  p[i] = make_float4(r[0], r[1], r[2], 0.f);
+}
+
+__global__ void k_store_posvel(unsigned char* __restrict__ rec, size_t pitch, int n, const float4* __restrict__ p,
+                               const float4* __restrict__ v) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float* r = (float*)(rec + (size_t)i * pitch);  // bytes [0, 24): position, velocity
+  r[0] = p[i].x; r[1] = p[i].y; r[2] = p[i].z;
+  r[3] = v[i].x; r[4] = v[i].y; r[5] = v[i].z;
+}
+
+vg_status check_cfg(Ctx* c, const vg_config* cfg) {
+  if (!cfg) return fail(c, VG_INVALID, "config is NULL");
+  if (cfg->abi_version != VG_ABI_VERSION) return fail(c, VG_INVALID, "config abi_version mismatch");
+  if (cfg->velocity_technique < 0 || cfg->velocity_technique > 2) return fail(c, VG_INVALID, "bad velocity_technique");
+  if (cfg->numerics < 0 || cfg->numerics > 1) return fail(c, VG_INVALID, "bad numerics");
+  if (cfg->poisson_solver < 0 || cfg->poisson_solver > 1) return fail(c, VG_INVALID, "bad poisson_solver");
+  if (cfg->warm_start < 0 || cfg->warm_start > 2) return fail(c, VG_INVALID, "bad warm_start");
+  if (cfg->warm_start == VG_WARM_NETWORK) return fail(c, VG_INVALID, "network warm start needs a loaded network");
+  if (!(cfg->viscosity >= 0.0f)) return fail(c, VG_INVALID, "viscosity must be >= 0");
+  if (!(cfg->poisson_tolerance > 0.0)) return fail(c, VG_INVALID, "poisson_tolerance must be > 0");
+  if (cfg->use_fixed_grid) {
+    for (int a = 0; a < 3; ++a)
+      if (cfg->fixed_grid.num_points[a] < 2 || !(cfg->fixed_grid.extent[a] > 0.0f))
+        return fail(c, VG_INVALID, "fixed grid needs >= 2 points and positive extent per axis");
+  }
+  return VG_OK;
+}
+
+bool finite3(const float* v) { return v && std::isfinite(v[0]) && std::isfinite(v[1]) && std::isfinite(v[2]); }
+
+// Geometry of a step: VortonSim::FindBoundingBox + UpdateBoundingBox(final)
+// (vortonSim.cpp:1001-1096): the vortons' AABB joined with the extra box (or
+// the first vorton), padded by 3 vorton radii, DefineShape(n, ..., pow2).
+vg_status step_geometry(Ctx* c, const float4* ps, size_t n, const float* first_pos, float radius,
+                        const float* extra_min, const float* extra_max, Geom* out) {
+  if (c->cfg.use_fixed_grid) {
+    Geom g = to_geom(c->cfg.fixed_grid);
+    precompute_spacing(g);
+    *out = g;
+    return VG_OK;
+  }
+  vg_status st = VG_OK;
+  float* d6 = (float*)ws(c, S_RED, 256, &st);
+  if (st != VG_OK) return st;
+  float* box = d6 + 16;
+  if ((st = launch_bbox(c, ps, n, box)) != VG_OK) return st;
+  float h[6];
+  VG_CUDA(c, cudaMemcpyAsync(h, box, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  if ((st = sync_and_check(c, "bounding box")) != VG_OK) return st;
+  float mn[3] = {h[0], h[1], h[2]}, mx[3] = {h[3], h[4], h[5]};
+  const bool extra = extra_min && extra_max;
+  const float* emin = extra ? extra_min : first_pos;
+  const float* emax = extra ? extra_max : first_pos;
+  for (int a = 0; a < 3; ++a) {
+    mn[a] = mn[a] < emin[a] ? mn[a] : emin[a];
+    mx[a] = mx[a] > emax[a] ? mx[a] : emax[a];
+  }
+  if (!finite3(mn) || !finite3(mx)) return fail(c, VG_NONFINITE, "non-finite vorton position");
+  const float margin = (1.0f + 2.0f) * radius;
+  for (int a = 0; a < 3; ++a) {
+    mn[a] -= margin * 1.0f;
+    mx[a] += margin * 1.0f;
+  }
+  *out = define_shape(n, mn, mx, true);
+  return VG_OK;
+}
+
+// The step on device-resident vortons (ps: pos+size, w: angvel in place, vel out).
+vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const float* first_pos, float radius,
+                   const float* extra_min, const float* extra_max, float dt) {
+  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+  c->launches = 0;
+  VG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+  Geom g;
+  vg_status st = step_geometry(c, ps, n, first_pos, radius, extra_min, extra_max, &g);
+  if (st != VG_OK) return st;
+  const size_t pts = g.points();
+  const bool ref = c->cfg.numerics == VG_NUMERICS_REFERENCE;
+  CellLists cl;
+  if ((st = build_cell_lists(c, g, ps, n, &cl)) != VG_OK) return st;
+  float* velgrid = (float*)ws(c, S_VEL, pts * 3 * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  Tree t;
+  t.depth = 0;
+  c->stats.poisson_cycles = 0;
+  c->stats.poisson_relres = 0.0;
+  c->stats.poisson_relres0 = 0.0;
+  c->stats.ms_poisson = 0.f;
+  const int tech = c->cfg.velocity_technique;
+  if (tech == VG_VELOCITY_POISSON || tech == VG_VELOCITY_TREE) {
+    if ((st = build_tree(c, g, ps, w, n, cl, &t)) != VG_OK) return st;
+  }
+  if (tech == VG_VELOCITY_POISSON) {
+    float* negvort = (float*)ws(c, S_NEGVORT, pts * 3 * sizeof(float), &st);
+    if (st != VG_OK) return st;
+    float* vecpot = (float*)ws(c, S_VECPOT, pts * 3 * sizeof(float), &st);
+    if (st != VG_OK) return st;
+    if ((st = launch_splat(c, g, ps, w, n, cl, -1.0f, radius, negvort)) != VG_OK) return st;
+    const bool warm_prev = c->cfg.warm_start == VG_WARM_PREVIOUS && c->have_prev &&
+                           memcmp(&c->prev_grid, &g, sizeof(Geom)) == 0;
+    if (warm_prev) {
+      float* prev = (float*)c->buf[S_PREV].p;
+      VG_CUDA(c, cudaMemcpyAsync(vecpot, prev, pts * 3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    } else {
+      VG_CUDA(c, cudaMemsetAsync(vecpot, 0, pts * 3 * sizeof(float), c->stream));
+    }
+    if ((st = launch_boundary_vecpot(c, t, g, ps, w, n, c->cfg.boundary_copy_odd_x != 0, ref, vecpot)) != VG_OK)
+      return st;
+    VG_CUDA(c, cudaEventRecord(c->ev2, c->stream));
+    if (c->cfg.poisson_solver == VG_POISSON_REFERENCE_CASCADE) {
+      if ((st = run_cascade(c, g, vecpot, negvort, c->cfg.cascade_steps)) != VG_OK) return st;
+    } else {
+      int cyc = 0;
+      double r0 = 0, r1 = 0;
+      st = run_multigrid(c, g, vecpot, negvort, c->cfg.poisson_tolerance, c->cfg.poisson_max_cycles, &cyc, &r0, &r1);
+      c->stats.poisson_cycles = cyc;
+      c->stats.poisson_relres0 = r0;
+      c->stats.poisson_relres = r1;
+      if (st != VG_OK && st != VG_NOT_CONVERGED) return st;
+    }
+    VG_CUDA(c, cudaEventRecord(c->ev3, c->stream));
+    if (c->cfg.warm_start == VG_WARM_PREVIOUS) {
+      float* prev = (float*)ws(c, S_PREV, pts * 3 * sizeof(float), &st);
+      if (st != VG_OK) return st;
+      VG_CUDA(c, cudaMemcpyAsync(prev, vecpot, pts * 3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+      c->prev_grid = g;
+      c->have_prev = true;
+    }
+    if ((st = launch_curl(c, g, vecpot, velgrid)) != VG_OK) return st;
+  } else {
+    // velocity at gridpoints by treecode (auto mollification, vortonSim.cpp:2458-2477) or direct sum
+    float4* q = (float4*)ws(c, S_JAC, pts * sizeof(float4) * 2, &st);
+    if (st != VG_OK) return st;
+    float4* out4 = q + pts;
+    k_grid_points<<<blocks_for(pts, 256), 256, 0, c->stream>>>(g, q);
+    VG_LAUNCHED(c);
+    float sr = 1.0f, sc = 1.0f;
+    if (tech == VG_VELOCITY_TREE) {
+      volatile float cv = g.cell[0] * g.cell[1];
+      cv = cv * g.cell[2];
+      const float cgl = 1.0f * powf(cv, 1.0f / 3.0f);
+      sr = std::max(cgl / radius, 1.0f);
+      volatile float s3 = sr * sr;
+      s3 = s3 * sr;
+      sc = 1.0f / s3;
+      if ((st = launch_tree_eval(c, 0, ref, t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
+    } else {
+      if ((st = launch_direct(c, 0, ref, ps, w, n, q, pts, 1.0f, 1.0f, out4)) != VG_OK) return st;
+    }
+    k_f4_to_f3<<<blocks_for(pts, 256), 256, 0, c->stream>>>(out4, velgrid, pts);
+    VG_LAUNCHED(c);
+    if (tech == VG_VELOCITY_DIRECT) {
+      // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton
+      if ((st = launch_direct(c, 0, ref, ps, w, n, ps, n, 1.0f, 1.0f, vel)) != VG_OK) return st;
+    }
+  }
+  if (c->cfg.enable_stretch) {
+    float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), pts * 2 * sizeof(float4)), &st);
+    if (st != VG_OK) return st;
+    if ((st = launch_jacobian(c, g, velgrid, jac)) != VG_OK) return st;
+    if ((st = launch_stretch(c, g, jac, ps, w, n, dt)) != VG_OK) return st;
+  }
+  if (c->cfg.enable_diffusion) {
+    if ((st = launch_pse(c, g, cl, ps, w, n, c->cfg.viscosity, dt)) != VG_OK) return st;
+  }
+  if (tech != VG_VELOCITY_DIRECT) {
+    // AssignVelocityFromField(vortons, mVelGrid, 1) (vortonSim.cpp:4251-4255)
+    if ((st = launch_gather_advect(c, g, velgrid, ps, vel, n, 0.0f, false)) != VG_OK) return st;
+  }
+  VG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
+  c->stats_pending = true;
+  c->stats.grid = from_geom(g);
+  c->stats.tree_depth = t.depth;
+  c->stats.kernels_launched = c->launches;
+  c->grid = g;
+  c->have_grid = true;
+  return VG_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+unsigned vg_abi_version(void) { return VG_ABI_VERSION; }
+
+const char* vg_status_string(vg_status s) {
+  switch (s) {
+    case VG_OK: return "ok";
+    case VG_EMPTY: return "empty";
+    case VG_OUT_OF_GRID: return "out of grid";
+    case VG_NONFINITE: return "non-finite value";
+    case VG_OOM: return "out of device memory";
+    case VG_TIMEOUT: return "device wait timed out";
+    case VG_INVALID: return "invalid argument";
+    case VG_CUDA_ERROR: return "CUDA error";
+    case VG_NOT_CONVERGED: return "not converged";
+    case VG_TOO_LARGE: return "too large";
+  }
+  return "unknown status";
+}
+
+const char* vg_last_error(const vg_ctx* ctx) { return ctx ? ctx->err.c_str() : g_err_noctx.c_str(); }
+
+vg_status vg_config_default(vg_config* cfg) {
+  if (!cfg) return VG_INVALID;
+  memset(cfg, 0, sizeof(*cfg));
+  cfg->abi_version = VG_ABI_VERSION;
+  cfg->device = 0;
+  cfg->stream = nullptr;
+  cfg->velocity_technique = VG_VELOCITY_POISSON;
+  cfg->numerics = VG_NUMERICS_FAST;
+  cfg->poisson_solver = VG_POISSON_MULTIGRID;
+  cfg->warm_start = VG_WARM_ZERO;
+  cfg->viscosity = 0.01f;
+  cfg->poisson_tolerance = 1e-6;
+  cfg->poisson_max_cycles = 50;
+  cfg->cascade_steps = 16;
+  cfg->enable_stretch = 1;
+  cfg->enable_diffusion = 1;
+  cfg->boundary_copy_odd_x = 0;
+  cfg->use_fixed_grid = 0;
+  return VG_OK;
+}
+
+vg_status vg_create(const vg_config* cfg, vg_ctx** out) {
+  if (!out) return VG_INVALID;
+  *out = nullptr;
+  vg_ctx* c = new (std::nothrow) vg_ctx();
+  if (!c) return VG_OOM;
+  vg_status st = check_cfg(c, cfg);
+  if (st != VG_OK) {
+    g_err_noctx = c->err;
+    delete c;
+    return st;
+  }
+  c->cfg = *cfg;
+  cudaError_t e = cudaSetDevice(cfg->device);
+  if (e == cudaSuccess && cfg->stream) {
+    c->stream = (cudaStream_t)cfg->stream;
+  } else if (e == cudaSuccess) {
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    c->own_stream = e == cudaSuccess;
+  }
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev0);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev1);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev2);
+  if (e == cudaSuccess) e = cudaEventCreate(&c->ev3);
+  if (e == cudaSuccess) e = cudaMalloc(&c->dflag, 256);
+  if (e == cudaSuccess) e = cudaMemset(c->dflag, 0, 256);
+  if (e != cudaSuccess) {
+    g_err_noctx = std::string("vg_create: ") + cudaGetErrorString(e);
+    cudaGetLastError();
+    vg_destroy(c);
+    return VG_CUDA_ERROR;
+  }
+  memset(&c->stats, 0, sizeof(c->stats));
+  *out = c;
+  return VG_OK;
+}
+
+vg_status vg_destroy(vg_ctx* c) {
+  if (!c) return VG_OK;
+  if (c->stream) cudaStreamSynchronize(c->stream);
+  for (int s = 0; s < S_NUM; ++s)
+    if (c->buf[s].p) cudaFree(c->buf[s].p);
+  if (c->dflag) cudaFree(c->dflag);
+  if (c->ev0) cudaEventDestroy(c->ev0);
+  if (c->ev1) cudaEventDestroy(c->ev1);
+  if (c->ev2) cudaEventDestroy(c->ev2);
+  if (c->ev3) cudaEventDestroy(c->ev3);
+  if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c;
+  return VG_OK;
+}
+
+vg_status vg_set_config(vg_ctx* c, const vg_config* cfg) {
+  if (!c) return VG_INVALID;
+  vg_status st = check_cfg(c, cfg);
+  if (st != VG_OK) return st;
+  void* stream = c->cfg.stream;
+  int dev = c->cfg.device;
+  c->cfg = *cfg;
+  c->cfg.stream = stream;  // stream and device are fixed at creation
+  c->cfg.device = dev;
+  return VG_OK;
+}
+
+vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                  const float* extra_max, float dt, unsigned frame) {
+  (void)frame;
+  if (!c) return VG_INVALID;
+  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+  if (!particles || stride < 56 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 56 / unaligned");
+  if (!std::isfinite(dt)) return fail(c, VG_INVALID, "dt is not finite");
+  vg_status st = VG_OK;
+  unsigned char* stage = (unsigned char*)ws(c, S_HOSTSTAGE, n * 56, &st);
+  if (st != VG_OK) return st;
+  float4* ps = (float4*)ws(c, S_POS, n * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  float4* w = (float4*)ws(c, S_ANGVEL, n * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  float4* vel = (float4*)ws(c, S_VVEL, n * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  // record bytes [0, 56): position, velocity, orientation, angular velocity, density, size
+  VG_CUDA(c, cudaMemcpy2DAsync(stage, 56, particles, stride, 56, n, cudaMemcpyHostToDevice, c->stream));
+  k_unpack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage, 56, (int)n, ps, w);
+  VG_CUDA(c, cudaGetLastError());
+  const float* rec0 = (const float*)particles;
+  const float radius = rec0[13] * 0.5f;  // Particle::GetRadius of the first vorton
+  st = run_step(c, ps, w, vel, n, rec0, radius, extra_min, extra_max, dt);
+  if (st != VG_OK) return st;
+  // write back record bytes [12, 48): velocity, (unchanged) orientation, angular velocity
+  k_pack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage + 12, 56, (int)n, vel, w);
+  VG_CUDA(c, cudaGetLastError());
+  VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + 12, stride, stage + 12, 56, 36, n, cudaMemcpyDeviceToHost,
+                               c->stream));
+  return sync_and_check(c, "vg_step");
+}
+
+vg_status vg_step_device(vg_ctx* c, const float* pos_size, float* angvel, float* vel, size_t n,
+                         const float* extra_minmax, float dt, unsigned frame) {
+  (void)frame;
+  if (!c) return VG_INVALID;
+  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+  if (!pos_size || !angvel || !vel) return fail(c, VG_INVALID, "NULL device pointer");
+  // The first vorton (position for the box rule, radius for the margin and the
+  // treecode's mollification) is only needed on the host when the grid is
+  // derived from the bounding box or the treecode technique is used.
+  float4 p0 = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (!c->cfg.use_fixed_grid || c->cfg.velocity_technique == VG_VELOCITY_TREE) {
+    VG_CUDA(c, cudaMemcpyAsync(&p0, pos_size, sizeof(float4), cudaMemcpyDeviceToHost, c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  const float first[3] = {p0.x, p0.y, p0.z};
+  return run_step(c, (float4*)pos_size, (float4*)angvel, (float4*)vel, n, first, p0.w * 0.5f,
+                  extra_minmax, extra_minmax ? extra_minmax + 3 : nullptr, dt);
+}
+
+vg_status vg_get_velocity_grid(vg_ctx* c, float* xyz, size_t cap_points, vg_grid_geom* geom) {
+  if (!c) return VG_INVALID;
+  if (!c->have_grid) return fail(c, VG_EMPTY, "no step has run");
+  if (geom) *geom = from_geom(c->grid);
+  if (xyz) {
+    if (cap_points < c->grid.points()) return fail(c, VG_TOO_LARGE, "velocity grid buffer too small");
+    VG_CUDA(c, cudaMemcpyAsync(xyz, c->buf[S_VEL].p, c->grid.points() * 3 * sizeof(float), cudaMemcpyDeviceToHost,
+                               c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return VG_OK;
+}
+
+vg_status vg_get_velocity_grid_device(vg_ctx* c, const float** dev, vg_grid_geom* geom) {
+  if (!c || !dev) return VG_INVALID;
+  if (!c->have_grid) return fail(c, VG_EMPTY, "no step has run");
+  *dev = (const float*)c->buf[S_VEL].p;
+  if (geom) *geom = from_geom(c->grid);
+  return VG_OK;
+}
+
+vg_status vg_get_vector_potential(vg_ctx* c, float* xyz, size_t cap_points, vg_grid_geom* geom) {
+  if (!c) return VG_INVALID;
+  if (!c->have_grid || c->cfg.velocity_technique != VG_VELOCITY_POISSON)
+    return fail(c, VG_EMPTY, "no Poisson step has run");
+  if (geom) *geom = from_geom(c->grid);
+  if (xyz) {
+    if (cap_points < c->grid.points()) return fail(c, VG_TOO_LARGE, "vector potential buffer too small");
+    VG_CUDA(c, cudaMemcpyAsync(xyz, c->buf[S_VECPOT].p, c->grid.points() * 3 * sizeof(float),
+                               cudaMemcpyDeviceToHost, c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
+  return VG_OK;
+}
+
+vg_status vg_get_stats(vg_ctx* c, vg_step_stats* s) {
+  if (!c || !s) return VG_INVALID;
+  if (c->stats_pending) {
+    VG_CUDA(c, cudaEventSynchronize(c->ev1));
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+    c->stats.ms_total = ms;
+    if (c->cfg.velocity_technique == VG_VELOCITY_POISSON && cudaEventElapsedTime(&ms, c->ev2, c->ev3) == cudaSuccess)
+      c->stats.ms_poisson = ms;
+    cudaGetLastError();
+    c->stats_pending = false;
+  }
+  *s = c->stats;
+  return VG_OK;
+}
+
+vg_status vg_synchronize(vg_ctx* c) {
+  if (!c) return VG_INVALID;
+  return sync_and_check(c, "device stage");
+}
+
+vg_status vg_advect(vg_ctx* c, void* particles, size_t m, size_t stride, float dt) {
+  if (!c) return VG_INVALID;
+  if (!c->have_grid) return fail(c, VG_EMPTY, "no velocity grid yet: run a step first");
+  if (m == 0) return VG_OK;
+  if (!particles || stride < 24 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 24 / unaligned");
+  if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
+  vg_status st = VG_OK;
+  // staging: records' bytes [0, 24) (position, velocity), then float4 position and velocity
+  const size_t rec_bytes = ((m * 24 + 255) / 256) * 256;
+  unsigned char* stage = (unsigned char*)ws(c, S_TRACERS, rec_bytes + 2 * m * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  float4* p = (float4*)(stage + rec_bytes);
+  float4* v = p + m;
+  VG_CUDA(c, cudaMemcpy2DAsync(stage, 24, particles, stride, 12, m, cudaMemcpyHostToDevice, c->stream));
+  k_copy_pos3<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, 24, (int)m, p);
+  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, p, v, m, dt, true)) != VG_OK) return st;
+  k_store_posvel<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, 24, (int)m, p, v);
+  VG_CUDA(c, cudaGetLastError());
+  VG_CUDA(c, cudaMemcpy2DAsync(particles, stride, stage, 24, 24, m, cudaMemcpyDeviceToHost, c->stream));
+  return sync_and_check(c, "vg_advect");
+}
+
+vg_status vg_advect_device(vg_ctx* c, float* pos, float* vel, size_t m, float dt) {
+  if (!c) return VG_INVALID;
+  if (!c->have_grid) return fail(c, VG_EMPTY, "no velocity grid yet: run a step first");
+  if (!pos) return fail(c, VG_INVALID, "NULL position pointer");
+  return launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, (float4*)pos, (float4*)vel, m, dt, true);
+}
+
+namespace {
+__global__ void k_evolve(float4* __restrict__ pos, const float4* __restrict__ vel, int m, float dt) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float4 p = pos[i];
+  const float4 v = vel[i];
+  p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));  // pcl.mPosition += pcl.mVelocity * timeStep
+  p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+  p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+  pos[i] = p;
+}
+}  // namespace
+
+vg_status vg_evolve_device(vg_ctx* c, float* pos4, const float* vel4, size_t m, float dt) {
+  if (!c || (m && (!pos4 || !vel4))) return VG_INVALID;
+  if (m == 0) return VG_OK;
+  if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
+  k_evolve<<<blocks_for(m, 256), 256, 0, c->stream>>>((float4*)pos4, (const float4*)vel4, (int)m, dt);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+// ------------------------------------------------------------ stage entry points
+
+vg_status vg_define_shape(size_t n, const float vmin[3], const float vmax[3], int pow2, vg_grid_geom* out) {
+  if (!vmin || !vmax || !out) return VG_INVALID;
+  *out = from_geom(define_shape(n, vmin, vmax, pow2 != 0));
+  return VG_OK;
+}
+
+namespace {
+__global__ void k_bin_only(Geom g, const float4* __restrict__ pos, int m, unsigned* __restrict__ idx3,
+                           unsigned* __restrict__ off) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  const float4 p = pos[i];
+  const unsigned ix = bin_axis(p.x, g.mn[0], g.cpe[0]);
+  const unsigned iy = bin_axis(p.y, g.mn[1], g.cpe[1]);
+  const unsigned iz = bin_axis(p.z, g.mn[2], g.cpe[2]);
+  if (idx3) {
+    idx3[3 * i] = ix;
+    idx3[3 * i + 1] = iy;
+    idx3[3 * i + 2] = iz;
+  }
+  if (off) off[i] = ix + g.np[0] * (iy + g.np[1] * iz);
+}
+}  // namespace
+
+vg_status vg_bin_device(vg_ctx* c, const vg_grid_geom* g, const float* pos4, size_t m, unsigned* idx3,
+                        unsigned* offset) {
+  if (!c || !g || (!pos4 && m)) return VG_INVALID;
+  if (m == 0) return VG_OK;
+  k_bin_only<<<blocks_for(m, 256), 256, 0, c->stream>>>(to_geom(*g), (const float4*)pos4, (int)m, idx3, offset);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status vg_direct_device(vg_ctx* c, int kind, const float* pos_size, const float* angvel, size_t n, const float* q4,
+                           size_t m, float sr, float sc, float* out4) {
+  if (!c || (kind != 0 && kind != 1)) return VG_INVALID;
+  return launch_direct(c, kind, c->cfg.numerics == VG_NUMERICS_REFERENCE, (const float4*)pos_size,
+                       (const float4*)angvel, n, (const float4*)q4, m, sr, sc, (float4*)out4);
+}
+
+vg_status vg_tree_device(vg_ctx* c, int kind, const vg_grid_geom* gg, const float* pos_size, const float* angvel,
+                         size_t n, const float* q4, size_t m, float sr, float sc, float* out4, float* tree_out,
+                         size_t tree_cap_points, size_t* tree_points) {
+  if (!c || !gg || (kind != 0 && kind != 1)) return VG_INVALID;
+  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+  Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos_size, n, &cl);
+  if (st != VG_OK) return st;
+  Tree t;
+  if ((st = build_tree(c, g, (const float4*)pos_size, (const float4*)angvel, n, cl, &t)) != VG_OK) return st;
+  if (tree_points) *tree_points = t.total;
+  if (tree_out) {
+    if (tree_cap_points < t.total) return fail(c, VG_TOO_LARGE, "tree buffer too small");
+    VG_CUDA(c, cudaMemcpy2DAsync(tree_out, 32, t.sv_pos, 16, 16, t.total, cudaMemcpyDeviceToDevice, c->stream));
+    VG_CUDA(c, cudaMemcpy2DAsync(tree_out + 4, 32, t.sv_w, 16, 16, t.total, cudaMemcpyDeviceToDevice, c->stream));
+  }
+  if (m && q4 && out4)
+    return launch_tree_eval(c, kind, c->cfg.numerics == VG_NUMERICS_REFERENCE, t, (const float4*)pos_size,
+                            (const float4*)angvel, n, (const float4*)q4, m, sr, sc, (float4*)out4);
+  return VG_OK;
+}
+
+vg_status vg_splat_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, const float* angvel, size_t n,
+                          float scale, float* grid3) {
+  if (!c || !gg || !grid3) return VG_INVALID;
+  Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos_size, n, &cl);
+  if (st != VG_OK) return st;
+  return launch_splat(c, g, (const float4*)pos_size, (const float4*)angvel, n, cl, scale, -1.0f, grid3);
+}
+
+vg_status vg_boundary_vecpot_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, const float* angvel,
+                                    size_t n, int copy_odd_x, float* grid3) {
+  if (!c || !gg || !grid3) return VG_INVALID;
+  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+  Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos_size, n, &cl);
+  if (st != VG_OK) return st;
+  Tree t;
+  if ((st = build_tree(c, g, (const float4*)pos_size, (const float4*)angvel, n, cl, &t)) != VG_OK) return st;
+  return launch_boundary_vecpot(c, t, g, (const float4*)pos_size, (const float4*)angvel, n, copy_odd_x != 0,
+                                c->cfg.numerics == VG_NUMERICS_REFERENCE, grid3);
+}
+
+vg_status vg_sor_device(vg_ctx* c, const vg_grid_geom* g, float* soln3, const float* lap3, int steps) {
+  if (!c || !g || !soln3 || !lap3) return VG_INVALID;
+  return launch_sor(c, to_geom(*g), soln3, lap3, steps);
+}
+
+vg_status vg_cascade_device(vg_ctx* c, const vg_grid_geom* g, float* soln3, const float* rhs3, int steps) {
+  if (!c || !g || !soln3 || !rhs3) return VG_INVALID;
+  return run_cascade(c, to_geom(*g), soln3, rhs3, steps);
+}
+
+vg_status vg_multigrid_device(vg_ctx* c, const vg_grid_geom* g, float* soln3, const float* rhs3, double tol,
+                              int max_cycles, int* cycles, double* relres0, double* relres) {
+  if (!c || !g || !soln3 || !rhs3 || !(tol > 0.0)) return VG_INVALID;
+  return run_multigrid(c, to_geom(*g), soln3, rhs3, tol, max_cycles, cycles, relres0, relres);
+}
+
+vg_status vg_downsample_device(vg_ctx* c, const vg_grid_geom* fine, const float* fine3, const vg_grid_geom* coarse,
+                               int inject, float* coarse3) {
+  if (!c || !fine || !coarse || !fine3 || !coarse3) return VG_INVALID;
+  return launch_downsample(c, to_geom(*fine), fine3, to_geom(*coarse), inject != 0, coarse3);
+}
+
+vg_status vg_upsample_device(vg_ctx* c, const vg_grid_geom* coarse, const float* coarse3, const vg_grid_geom* fine,
+                             int interior_only, float* fine3) {
+  if (!c || !fine || !coarse || !fine3 || !coarse3) return VG_INVALID;
+  return launch_upsample(c, to_geom(*coarse), coarse3, to_geom(*fine), interior_only != 0, fine3);
+}
+
+vg_status vg_jacobian_curl_device(vg_ctx* c, const vg_grid_geom* gg, const float* vec3, float* jac9, float* curl3) {
+  if (!c || !gg || !vec3) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  vg_status st = VG_OK;
+  if (jac9 && (st = launch_jacobian(c, g, vec3, jac9)) != VG_OK) return st;
+  if (curl3 && (st = launch_curl(c, g, vec3, curl3)) != VG_OK) return st;
+  return VG_OK;
+}
+
+vg_status vg_stretch_device(vg_ctx* c, const vg_grid_geom* gg, const float* vel3, const float* pos_size,
+                            float* angvel, size_t n, float dt) {
+  if (!c || !gg || !vel3) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  vg_status st = VG_OK;
+  float* jac = (float*)ws(c, S_JAC, g.points() * 9 * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  if ((st = launch_jacobian(c, g, vel3, jac)) != VG_OK) return st;
+  return launch_stretch(c, g, jac, (const float4*)pos_size, (float4*)angvel, n, dt);
+}
+
+vg_status vg_pse_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, float* angvel, size_t n,
+                        float viscosity, float dt) {
+  if (!c || !gg) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos_size, n, &cl);
+  if (st != VG_OK) return st;
+  return launch_pse(c, g, cl, (const float4*)pos_size, (float4*)angvel, n, viscosity, dt);
+}
+
+vg_status vg_gather_advect_device(vg_ctx* c, const vg_grid_geom* gg, const float* vel3, float* pos4, float* vel4,
+                                  size_t m, float dt) {
+  if (!c || !gg || !vel3 || (!pos4 && m)) return VG_INVALID;
+  return launch_gather_advect(c, to_geom(*gg), vel3, (float4*)pos4, (float4*)vel4, m, dt, true);
+}
+
+}  // extern "C"

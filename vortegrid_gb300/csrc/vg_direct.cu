@@ -1,0 +1,194 @@
+// K1: direct mollified Biot-Savart / vector-potential sums.
+//
+// Replaces ComputeVelocity_Direct / ComputeVectorPotential_Direct
+// (VortonFluid/vortonSim.cpp:1113-1158), the per-pair laws of
+// VortonFluid/vorton.h:118-179.
+//
+// Fast path (FP32-FMA bound):
+//   * a CTA owns TPT * THREADS query points (TPT per thread in registers) and
+//     one of KSPLIT equal chunks of the sources, so that a 40k-target,
+//     4k-source problem still fills 152 SMs;
+//   * sources are staged through shared memory in tiles as two float4 per
+//     vorton -- (position, 1/radius) and (2/3 r^3 * angvel * circulation
+//     factor) -- and read by every warp as broadcasts;
+//   * per pair: law = min(rsqrt(|d|^2), 1/r)^3 (one MUFU.RSQ), 18 FP32 pipe
+//     instructions for the 26 algorithmic flops;
+//   * the KSPLIT partial sums per target go to a scratch buffer and are summed
+//     in a fixed order by a second kernel, so results are run-to-run
+//     deterministic.
+// Reference path: one thread per query, sources in index order, the
+// reference's operation order (bit-identical to the CPU).
+#include "vg_internal.cuh"
+
+namespace vg {
+
+namespace {
+
+constexpr int kThreads = 128;
+constexpr int kTPT = 4;        // targets per thread
+constexpr int kTile = 256;     // sources per shared-memory tile
+
+// Precompute per-source constants for the fast law.
+template <int KIND>
+__global__ void __launch_bounds__(256) k_prep_sources(const float4* __restrict__ ps, const float4* __restrict__ w,
+                                                      int n, float sr, float sc, float4* __restrict__ s0,
+                                                      float4* __restrict__ s1) {
+  int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const float4 p = ps[i];
+  const float4 a = w[i];
+  const float radius = p.w * 0.5f * sr;
+  const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
+  const float invr = 1.0f / radius;
+  s0[i] = make_float4(p.x, p.y, p.z, invr);
+  s1[i] = make_float4(a.x * s, a.y * s, a.z * s, radius * radius);
+}
+
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restrict__ s0, const float4* __restrict__ s1,
+                                                           int n, int chunk, const float4* __restrict__ q, int m,
+                                                           float* __restrict__ partial) {
+  __shared__ float4 sh0[kTile];
+  __shared__ float4 sh1[kTile];
+  const int base = blockIdx.x * (kThreads * kTPT) + threadIdx.x;
+  float qx[kTPT], qy[kTPT], qz[kTPT];
+  float ax[kTPT], ay[kTPT], az[kTPT];
+#pragma unroll
+  for (int t = 0; t < kTPT; ++t) {
+    const int j = base + t * kThreads;
+    const float4 v = (j < m) ? q[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+    qx[t] = v.x; qy[t] = v.y; qz[t] = v.z;
+    ax[t] = 0.f; ay[t] = 0.f; az[t] = 0.f;
+  }
+  const int k0 = blockIdx.y * chunk;
+  const int k1 = min(n, k0 + chunk);
+  for (int tile = k0; tile < k1; tile += kTile) {
+    const int cnt = min(kTile, k1 - tile);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += kThreads) {
+      sh0[i] = s0[tile + i];
+      sh1[i] = s1[tile + i];
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int i = 0; i < cnt; ++i) {
+      const float4 p = sh0[i];
+      const float4 a = sh1[i];
+#pragma unroll
+      for (int t = 0; t < kTPT; ++t) {
+        const float d0 = qx[t] - p.x, d1 = qy[t] - p.y, d2 = qz[t] - p.z;
+        const float dist2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+        if (KIND == 0) {
+          const float inv = fminf(rsqrtf(dist2), p.w);
+          const float law = inv * inv * inv;
+          const float b0 = d0 * law, b1 = d1 * law, b2 = d2 * law;
+          ax[t] = fmaf(a.y, b2, fmaf(-a.z, b1, ax[t]));
+          ay[t] = fmaf(a.z, b0, fmaf(-a.x, b2, ay[t]));
+          az[t] = fmaf(a.x, b1, fmaf(-a.y, b0, az[t]));
+        } else {
+          const float law = (dist2 < a.w) ? dist2 * p.w * p.w * p.w : rsqrtf(dist2);
+          ax[t] = fmaf(a.x, law, ax[t]);
+          ay[t] = fmaf(a.y, law, ay[t]);
+          az[t] = fmaf(a.z, law, az[t]);
+        }
+      }
+    }
+  }
+  float* out = partial + (size_t)blockIdx.y * m * 3;
+#pragma unroll
+  for (int t = 0; t < kTPT; ++t) {
+    const int j = base + t * kThreads;
+    if (j < m) {
+      out[3 * j] = ax[t];
+      out[3 * j + 1] = ay[t];
+      out[3 * j + 2] = az[t];
+    }
+  }
+}
+
+__global__ void k_reduce_partials(const float* __restrict__ partial, int ksplit, int m, float4* __restrict__ out) {
+  int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  float x = 0.f, y = 0.f, z = 0.f;
+  for (int k = 0; k < ksplit; ++k) {
+    const float* p = partial + ((size_t)k * m + j) * 3;
+    x += p[0];
+    y += p[1];
+    z += p[2];
+  }
+  out[j] = make_float4(x, y, z, 0.f);
+}
+
+// Reference order: each thread sums all sources for one query in index order.
+template <int KIND>
+__global__ void __launch_bounds__(kThreads) k_direct_ref(const float4* __restrict__ ps, const float4* __restrict__ w,
+                                                          int n, const float4* __restrict__ q, int m, float sr,
+                                                          float sc, float4* __restrict__ out) {
+  __shared__ float4 sh0[kTile];
+  __shared__ float4 sh1[kTile];
+  const int j = blockIdx.x * kThreads + threadIdx.x;
+  const float4 v = (j < m) ? q[j] : make_float4(0.f, 0.f, 0.f, 0.f);
+  float3 acc = make_float3(0.f, 0.f, 0.f);
+  for (int tile = 0; tile < n; tile += kTile) {
+    const int cnt = min(kTile, n - tile);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += kThreads) {
+      sh0[i] = ps[tile + i];
+      sh1[i] = w[tile + i];
+    }
+    __syncthreads();
+    for (int i = 0; i < cnt; ++i) ref_accum<KIND>(acc, v.x, v.y, v.z, sh0[i], sh1[i], sr, sc);
+  }
+  if (j < m) out[j] = make_float4(acc.x, acc.y, acc.z, 0.f);
+}
+
+}  // namespace
+
+vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
+                        size_t m, float sr, float sc, float4* out) {
+  if (m == 0) return VG_OK;
+  if (n == 0) {
+    VG_CUDA(c, cudaMemsetAsync(out, 0, m * sizeof(float4), c->stream));
+    return VG_OK;
+  }
+  if (n > 0x7fffffff || m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "direct: more than 2^31 sources or targets");
+  if (ref) {
+    dim3 grid(blocks_for(m, kThreads));
+    if (kind == 0)
+      k_direct_ref<0><<<grid, kThreads, 0, c->stream>>>(ps, w, (int)n, q, (int)m, sr, sc, out);
+    else
+      k_direct_ref<1><<<grid, kThreads, 0, c->stream>>>(ps, w, (int)n, q, (int)m, sr, sc, out);
+    VG_LAUNCHED(c);
+    VG_CUDA(c, cudaGetLastError());
+    return VG_OK;
+  }
+  // Split the sources so that the grid covers every SM several times.
+  const unsigned tblocks = blocks_for(m, kThreads * kTPT);
+  unsigned ksplit = 1;
+  while (tblocks * ksplit < 4u * kSMs && (n / (ksplit * 2)) >= (size_t)kTile) ksplit *= 2;
+  const int chunk = (int)((n + ksplit - 1) / ksplit);
+  vg_status st = VG_OK;
+  const size_t srcb = ((n * sizeof(float4) + 255) / 256) * 256;
+  char* scratch = (char*)ws(c, S_DIRECT, 2 * srcb + (size_t)ksplit * m * 3 * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  float4* s0 = (float4*)scratch;
+  float4* s1 = (float4*)(scratch + srcb);
+  float* partial = (float*)(scratch + 2 * srcb);
+  if (kind == 0)
+    k_prep_sources<0><<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, sr, sc, s0, s1);
+  else
+    k_prep_sources<1><<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, sr, sc, s0, s1);
+  VG_LAUNCHED(c);
+  dim3 grid(tblocks, ksplit);
+  if (kind == 0)
+    k_direct_fast<0><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
+  else
+    k_direct_fast<1><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
+  VG_LAUNCHED(c);
+  k_reduce_partials<<<blocks_for(m, 256), 256, 0, c->stream>>>(partial, (int)ksplit, (int)m, out);
+  VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+}  // namespace vg

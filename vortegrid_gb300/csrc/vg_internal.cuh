@@ -1,0 +1,274 @@
+// Internal declarations shared by the sm_103a kernels of libvortegrid.
+//
+// Two arithmetic laws are provided for the vorton kernels:
+//  * ref_*  -- the reference's exact FP32 operation order (VortonFluid/vorton.h:118-179,
+//              Core/Math/math.h:206-216) written with round-to-nearest intrinsics
+//              (__fadd_rn, __fmul_rn, ...), which the compiler never fuses, so the
+//              results are bit-identical to the reference's CPU build;
+//  * fast   -- hardware rsqrt, fused multiply-add and algebraic reassociation.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <string>
+#include <vector>
+
+#include "../../include/vortegrid.h"
+
+namespace vg {
+
+constexpr int kMaxLayers = 24;
+constexpr int kSMs = 152;  // GB300
+
+// Grid geometry on the device: identical fields to vg_grid_geom.
+struct Geom {
+  float mn[3], ext[3], cell[3], cpe[3];
+  unsigned np[3];
+  __host__ __device__ unsigned nx() const { return np[0]; }
+  __host__ __device__ size_t points() const { return (size_t)np[0] * np[1] * np[2]; }
+};
+
+inline Geom to_geom(const vg_grid_geom& g) {
+  Geom d;
+  for (int a = 0; a < 3; ++a) {
+    d.mn[a] = g.min_corner[a];
+    d.ext[a] = g.extent[a];
+    d.cell[a] = g.cell_spacing[a];
+    d.cpe[a] = g.cells_per_extent[a];
+    d.np[a] = g.num_points[a];
+  }
+  return d;
+}
+inline vg_grid_geom from_geom(const Geom& d) {
+  vg_grid_geom g;
+  for (int a = 0; a < 3; ++a) {
+    g.min_corner[a] = d.mn[a];
+    g.extent[a] = d.ext[a];
+    g.cell_spacing[a] = d.cell[a];
+    g.cells_per_extent[a] = d.cpe[a];
+    g.num_points[a] = d.np[a];
+  }
+  return g;
+}
+
+// Host geometry rules (Core/SpatialPartition/uniformGrid.h:259-412).
+void precompute_spacing(Geom& g);
+Geom define_shape(size_t n, const float vmin[3], const float vmax[3], bool pow2);
+Geom decimate(const Geom& src, unsigned dec);
+int nested_shape(const Geom& g, Geom* layers, unsigned (*decim)[3]);
+
+// ------------------------------------------------------------ device helpers
+
+// IndicesOfPosition (uniformGrid.h:536-574): FP32 (p - min) * cellsPerExtent
+// truncated toward zero, each operation rounded separately.
+__device__ __forceinline__ unsigned bin_axis(float p, float mn, float cpe) {
+  return (unsigned)__float2int_rz(__fmul_rn(__fsub_rn(p, mn), cpe));
+}
+
+// finvsqrtf (Core/Math/math.h:206-216): magic-constant estimate + one Newton step.
+__device__ __forceinline__ float ref_finvsqrtf(float v) {
+  int i = __float_as_int(v);
+  i = 0x5f3759df - (i >> 1);
+  float y = __int_as_float(i);
+  const float x = __fmul_rn(v, 0.5f);
+  return __fmul_rn(y, __fsub_rn(1.5f, __fmul_rn(__fmul_rn(x, y), y)));
+}
+
+__device__ __forceinline__ float ref_dot_self(float a, float b, float c) {
+  return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
+}
+
+// 2/3 as the reference's float constant (VortonFluid/vorton.h:92).
+#define VG_TWO_THIRDS (2.0f / 3.0f)
+
+// VORTON_ACCUMULATE_VELOCITY_private (vorton.h:161-179), reference order.
+__device__ __forceinline__ void ref_accum_velocity(float3& acc, float qx, float qy, float qz, float4 ps, float4 w,
+                                                   float sr, float sc) {
+  const float d0 = __fsub_rn(qx, ps.x), d1 = __fsub_rn(qy, ps.y), d2 = __fsub_rn(qz, ps.z);
+  const float radius = __fmul_rn(__fmul_rn(ps.w, 0.5f), sr);
+  const float r2 = __fmul_rn(radius, radius);
+  const float dist2 = ref_dot_self(d0, d1, d2);
+  const float law = (dist2 < r2) ? __fdiv_rn(1.0f, __fmul_rn(r2, radius))
+                                 : __fdiv_rn(ref_finvsqrtf(dist2), dist2);
+  const float s = __fmul_rn(__fmul_rn(VG_TWO_THIRDS, r2), radius);
+  const float a0 = __fmul_rn(w.x, s), a1 = __fmul_rn(w.y, s), a2 = __fmul_rn(w.z, s);
+  const float b0 = __fmul_rn(d0, law), b1 = __fmul_rn(d1, law), b2 = __fmul_rn(d2, law);
+  const float c0 = __fsub_rn(__fmul_rn(a1, b2), __fmul_rn(a2, b1));
+  const float c1 = __fsub_rn(__fmul_rn(a2, b0), __fmul_rn(a0, b2));
+  const float c2 = __fsub_rn(__fmul_rn(a0, b1), __fmul_rn(a1, b0));
+  acc.x = __fadd_rn(acc.x, __fmul_rn(c0, sc));
+  acc.y = __fadd_rn(acc.y, __fmul_rn(c1, sc));
+  acc.z = __fadd_rn(acc.z, __fmul_rn(c2, sc));
+}
+
+// VORTON_ACCUMULATE_VECTOR_POTENTIAL_private (vorton.h:118-136), reference order.
+__device__ __forceinline__ void ref_accum_vecpot(float3& acc, float qx, float qy, float qz, float4 ps, float4 w,
+                                                 float sr, float sc) {
+  const float d0 = __fsub_rn(qx, ps.x), d1 = __fsub_rn(qy, ps.y), d2 = __fsub_rn(qz, ps.z);
+  const float radius = __fmul_rn(__fmul_rn(ps.w, 0.5f), sr);
+  const float r2 = __fmul_rn(radius, radius);
+  const float dist2 = ref_dot_self(d0, d1, d2);
+  const float law = (dist2 < r2) ? __fdiv_rn(dist2, __fmul_rn(r2, radius)) : ref_finvsqrtf(dist2);
+  const float s = __fmul_rn(__fmul_rn(VG_TWO_THIRDS, r2), radius);
+  acc.x = __fadd_rn(acc.x, __fmul_rn(__fmul_rn(__fmul_rn(w.x, s), law), sc));
+  acc.y = __fadd_rn(acc.y, __fmul_rn(__fmul_rn(__fmul_rn(w.y, s), law), sc));
+  acc.z = __fadd_rn(acc.z, __fmul_rn(__fmul_rn(__fmul_rn(w.z, s), law), sc));
+}
+
+template <int KIND>
+__device__ __forceinline__ void ref_accum(float3& acc, float qx, float qy, float qz, float4 ps, float4 w, float sr,
+                                          float sc) {
+  if (KIND == 0)
+    ref_accum_velocity(acc, qx, qy, qz, ps, w, sr, sc);
+  else
+    ref_accum_vecpot(acc, qx, qy, qz, ps, w, sr, sc);
+}
+
+// Fast law, same mathematics: law = min(rsqrt(d2), 1/r)^3 reproduces both the
+// core branch (1/r^3) and the far branch (|d|^-3); vector potential law =
+// |d|^2/r^3 inside, 1/|d| outside.
+template <int KIND>
+__device__ __forceinline__ void fast_accum(float3& acc, float qx, float qy, float qz, float4 ps, float4 w, float sr,
+                                           float sc) {
+  const float d0 = qx - ps.x, d1 = qy - ps.y, d2 = qz - ps.z;
+  const float radius = ps.w * 0.5f * sr;
+  const float invr = 1.0f / radius;
+  const float dist2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+  const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
+  if (KIND == 0) {
+    const float inv = fminf(rsqrtf(dist2), invr);
+    const float law = inv * inv * inv * s;
+    const float b0 = d0 * law, b1 = d1 * law, b2 = d2 * law;
+    acc.x = fmaf(w.y, b2, fmaf(-w.z, b1, acc.x));
+    acc.y = fmaf(w.z, b0, fmaf(-w.x, b2, acc.y));
+    acc.z = fmaf(w.x, b1, fmaf(-w.y, b0, acc.z));
+  } else {
+    const float law = (dist2 < radius * radius) ? dist2 * invr * invr * invr : rsqrtf(dist2);
+    const float f = law * s;
+    acc.x = fmaf(w.x, f, acc.x);
+    acc.y = fmaf(w.y, f, acc.y);
+    acc.z = fmaf(w.z, f, acc.z);
+  }
+}
+
+// ---------------------------------------------------------------- context
+
+struct Ctx;
+
+// Grow-only device workspace slot.
+struct Buf {
+  void* p = nullptr;
+  size_t bytes = 0;
+};
+
+enum Slot {
+  S_BBOX,
+  S_CELL,
+  S_COUNT,
+  S_START,
+  S_FILL,
+  S_ITEMS,
+  S_SCAN,
+  S_TREE,
+  S_NEGVORT,
+  S_VECPOT,
+  S_VEL,
+  S_JAC,
+  S_WOLD,
+  S_MG,
+  S_DIRECT,
+  S_POS,
+  S_ANGVEL,
+  S_VVEL,
+  S_HOSTSTAGE,
+  S_TRACERS,
+  S_RED,
+  S_PREV,
+  S_NUM
+};
+
+struct Ctx {
+  vg_config cfg;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  std::string err;
+  Buf buf[S_NUM];
+  Geom grid;                // last step's grid
+  bool have_grid = false;
+  vg_step_stats stats;
+  cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  unsigned launches = 0;    // kernel launches since the counter was reset
+  Geom prev_grid;           // grid of the stored previous solution
+  bool have_prev = false;
+  int* dflag = nullptr;     // device error word: bit 0 = a sample left the grid
+  bool stats_pending = false;
+};
+
+// Device-side error bits, reported at the next synchronising call.
+enum DevFlag { DF_OUT_OF_GRID = 1, DF_NONFINITE = 2 };
+vg_status sync_and_check(Ctx* c, const char* what);
+
+// Workspace: returns a device buffer of at least `bytes` for slot s.
+void* ws(Ctx* c, int s, size_t bytes, vg_status* st);
+
+vg_status fail(Ctx* c, vg_status s, const std::string& msg);
+vg_status cuda_check(Ctx* c, cudaError_t e, const char* what);
+#define VG_CUDA(ctx, call)                                 \
+  do {                                                     \
+    cudaError_t e_ = (call);                               \
+    if (e_ != cudaSuccess) return cuda_check(ctx, e_, #call); \
+  } while (0)
+#define VG_LAUNCHED(ctx) ((ctx)->launches++)
+
+inline unsigned blocks_for(size_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
+
+// ---------------------------------------------------------- stage launchers
+// (device pointers, context stream; defined in the .cu files)
+
+vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
+                        size_t m, float sr, float sc, float4* out);
+
+// Cell lists: stable counting sort of vortons by leaf cell (OffsetOfPosition).
+struct CellLists {
+  unsigned* cell;   // per vorton: leaf offset
+  unsigned* start;  // per cell (+1): first item
+  unsigned* items;  // vorton indices grouped by cell, ascending within a cell
+};
+vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, CellLists* out);
+
+struct Tree {
+  int depth;
+  Geom layer[kMaxLayers];
+  unsigned decim[kMaxLayers][3];
+  size_t base[kMaxLayers];
+  size_t total;
+  float4* sv_pos;  // per point: pos xyz, size
+  float4* sv_w;    // per point: angvel xyz, 0
+};
+vg_status build_tree(Ctx* c, const Geom& g, const float4* ps, const float4* w, size_t n, const CellLists& cl,
+                     Tree* t);
+vg_status launch_tree_eval(Ctx* c, int kind, bool ref, const Tree& t, const float4* ps, const float4* w, size_t n,
+                           const float4* q, size_t m, float sr, float sc, float4* out);
+vg_status launch_boundary_vecpot(Ctx* c, const Tree& t, const Geom& g, const float4* ps, const float4* w, size_t n,
+                                 bool copy_odd_x, bool ref, float* grid3);
+vg_status launch_splat(Ctx* c, const Geom& g, const float4* ps, const float4* w, size_t n, const CellLists& cl,
+                       float scale, float radius, float* grid3);
+
+vg_status launch_sor(Ctx* c, const Geom& g, float* soln3, const float* lap3, int steps);
+vg_status launch_downsample(Ctx* c, const Geom& fine, const float* f3, const Geom& coarse, bool inject, float* c3);
+vg_status launch_upsample(Ctx* c, const Geom& coarse, const float* c3, const Geom& fine, bool interior, float* f3);
+vg_status run_cascade(Ctx* c, const Geom& g, float* soln3, const float* rhs3, int steps);
+vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, double tol, int max_cycles,
+                        int* cycles, double* relres0, double* relres);
+
+vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9);
+vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);
+vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt);
+vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float4* w, size_t n, float nu,
+                     float dt);
+vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
+                               float dt, bool evolve);
+vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
+
+}  // namespace vg
