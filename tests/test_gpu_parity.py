@@ -269,11 +269,46 @@ def test_full_step_reference_numerics(vg, golden):
     assert np.array_equal(recs["size"], out["size"])
 
 
-def test_multigrid_reaches_tolerance(vg, oracle_lib):
-    """FAST numerics, multigrid to 1e-6: FP64 residual checked on the CPU, and
-    the velocity grid vs the FP64 direct sum."""
+def _exact_discrete_solve(g, b, bc):
+    """Independent FP64 solve of the same discrete Dirichlet problem (scipy CG)."""
+    import scipy.sparse as sp
+    import scipy.sparse.linalg as spl
+    nx, ny, nz = g.points
+    h = [float(g.cell[0]), float(g.cell[1]), float(g.cell[2])]
+
+    def lap1(m, hh):
+        return sp.diags([np.ones(m - 1), -2 * np.ones(m), np.ones(m - 1)], [-1, 0, 1]) / (hh * hh)
+    L = sp.kronsum(sp.kronsum(lap1(nx - 2, h[0]), lap1(ny - 2, h[1])), lap1(nz - 2, h[2])).tocsr()
+    a = bc.copy().reshape(nz, ny, nx, 3).astype(np.float64)
+    B = b.reshape(nz, ny, nx, 3)
+    for c in range(3):
+        rhs = B[1:-1, 1:-1, 1:-1, c].astype(np.float64).copy()
+        A = a[..., c]
+        rhs[:, :, 0] -= A[1:-1, 1:-1, 0] / h[0] ** 2
+        rhs[:, :, -1] -= A[1:-1, 1:-1, -1] / h[0] ** 2
+        rhs[:, 0, :] -= A[1:-1, 0, 1:-1] / h[1] ** 2
+        rhs[:, -1, :] -= A[1:-1, -1, 1:-1] / h[1] ** 2
+        rhs[0, :, :] -= A[0, 1:-1, 1:-1] / h[2] ** 2
+        rhs[-1, :, :] -= A[-1, 1:-1, 1:-1] / h[2] ** 2
+        x, _ = spl.cg(L, rhs.ravel(), rtol=1e-11, maxiter=5000)
+        a[1:-1, 1:-1, 1:-1, c] = x.reshape(nz - 2, ny - 2, nx - 2)
+    return a.reshape(-1, 3)
+
+
+@pytest.mark.parametrize("field", ["ring", "puff"])
+def test_multigrid_reaches_tolerance(vg, oracle_lib, field):
+    """FAST numerics, multigrid to 1e-6 relative residual:
+      * the FP64 residual of the returned field is checked on the CPU;
+      * the vector potential matches an independent FP64 sparse solve of the
+        same discrete problem (so the solver is right);
+      * for the smooth ring, the velocity is within the grid method's
+        discretisation error (dx = 1/16) of the FP64 direct sum.  The
+        white-noise puff's discretisation error is ~35% at this spacing (the
+        exact discrete solution has the same error), so only the solver
+        checks apply to it."""
+    pytest.importorskip("scipy")
     from vortegrid_gb300 import workloads
-    pos, w, s = workloads.puff(20000, seed=5)
+    pos, w, s = workloads.ring(20000, seed=5) if field == "ring" else workloads.puff(20000, seed=5)
     g = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [65] * 3)
     sim = vg.VortonSim(0.01, fixed_grid=g, enable_stretch=0, enable_diffusion=0)
     recs = vg.make_particles(pos, w, s)
@@ -283,14 +318,16 @@ def test_multigrid_reaches_tolerance(vg, oracle_lib):
     a, gg = sim.GetVectorPotential()
     og = oracle_lib.Geom.from12(gg.as12(), gg.points)
     b = oracle_lib.splat(pos, w, s, og, -1.0)
-    assert oracle_lib.relres(og, a, b) < 1e-4
-    vel, _ = sim.GetVelocityGrid()
-    # compare the interior velocity with the FP64 direct sum at gridpoints
-    pts = workloads.grid_points(og.mn, og.cell, og.points).reshape(65, 65, 65, 3)[8:-8:4, 8:-8:4, 8:-8:4].reshape(-1, 3)
-    d = oracle_lib.direct(0, pos, w, s, pts, f64=True)
-    v = vel.reshape(65, 65, 65, 3)[8:-8:4, 8:-8:4, 8:-8:4].reshape(-1, 3)
-    rel = np.linalg.norm(v - d) / np.linalg.norm(d)
-    assert rel < 0.15, rel  # discretisation error of the grid method (dx = 1/16)
+    assert oracle_lib.relres(og, a, b) < 1e-4  # FP32 copy of the FP64 iterate
+    exact = _exact_discrete_solve(og, b, a)  # boundary values: the GPU's own (treecode) boundary
+    assert np.linalg.norm(a - exact) / np.linalg.norm(exact) < 1e-5
+    if field == "ring":
+        vel, _ = sim.GetVelocityGrid()
+        sl = (slice(8, -8, 4),) * 3
+        pts = workloads.grid_points(og.mn, og.cell, og.points).reshape(65, 65, 65, 3)[sl].reshape(-1, 3)
+        d = oracle_lib.direct(0, pos, w, s, pts, f64=True)
+        v = vel.reshape(65, 65, 65, 3)[sl].reshape(-1, 3)
+        assert np.linalg.norm(v - d) / np.linalg.norm(d) < 0.08  # measured 4.2%
 
 
 def test_status_paths(vg):
