@@ -249,6 +249,27 @@ vg_status vg_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_siz
 vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel3, float* pos4, float* vel4,
                                   size_t m, float dt);
 
+/* Allocation-free direct sum.  No counterpart in the reference: it exists for
+ * callers that cannot allocate device memory when they need a velocity -- an
+ * application that gives this library a fixed memory budget up front, a
+ * real-time frame that must not stall on the allocator's implicit device
+ * synchronisation, or an embedding that forbids the CUDA allocator.  Same
+ * arguments and results as vg_direct_device (FAST numerics), but it takes no
+ * context and allocates nothing: its scratch is one fixed 8 MiB device array
+ * inside this library, held by every GPU that loads the library until the
+ * process exits.
+ *  - Limits: n <= 32768 sources and m <= (8 MiB - 32 n) / 12 targets;
+ *    larger calls return VG_TOO_LARGE (use vg_direct_device).
+ *  - The first call on each device looks up that array's device address on
+ *    the current device; make that first call before any stream capture.
+ *  - Every call uses the same array: calls that can overlap on the GPU (on
+ *    different streams, or on one stream from different host threads) race
+ *    and must be ordered by the caller.
+ *  - Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
+ *    returns without synchronising.  Errors: vg_last_error(NULL). */
+vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_size, const float* angvel, size_t n,
+                            const float* q4, size_t m, float spread_range, float spread_circ, float* out4);
+
 #ifdef __cplusplus
 }
 #endif

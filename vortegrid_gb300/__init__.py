@@ -117,7 +117,7 @@ EXPORTS = [
     "vg_bin_device", "vg_direct_device", "vg_tree_device", "vg_splat_device", "vg_boundary_vecpot_device",
     "vg_sor_device", "vg_cascade_device", "vg_multigrid_device", "vg_downsample_device", "vg_upsample_device",
     "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
-    "vg_evolve_device",
+    "vg_evolve_device", "vg_direct_noalloc",
 ]
 
 
@@ -151,6 +151,9 @@ def lib():
                                               ctypes.POINTER(GridGeom)]
         L.vg_get_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(StepStats)]
         L.vg_synchronize.argtypes = [ctypes.c_void_p]
+        L.vg_direct_noalloc.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                                        ctypes.c_size_t, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_float,
+                                        ctypes.c_float, ctypes.c_void_p]
         L.vg_evolve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                        ctypes.c_float]
         L.vg_advect.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t, ctypes.c_float]

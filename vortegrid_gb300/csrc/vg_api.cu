@@ -145,6 +145,15 @@ namespace {
 
 thread_local std::string g_err_noctx;
 
+}  // namespace
+
+vg_status vg::set_noctx_error(vg_status s, const std::string& msg) {
+  g_err_noctx = msg;
+  return s;
+}
+
+namespace {
+
 __global__ void k_unpack_records(const unsigned char* __restrict__ rec, size_t pitch, int n, float4* __restrict__ ps,
                                  float4* __restrict__ w) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;

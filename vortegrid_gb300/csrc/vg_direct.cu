@@ -18,6 +18,8 @@
 //     deterministic.
 // Reference path: one thread per query, sources in index order, the
 // reference's operation order (bit-identical to the CPU).
+#include <mutex>
+
 #include "vg_internal.cuh"
 
 namespace vg {
@@ -192,3 +194,101 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
 }
 
 }  // namespace vg
+
+// ---------------------------------------------------------------------------
+// Allocation-free direct sum (vg_direct_noalloc).
+//
+// Some callers cannot allocate device memory at the moment they need the
+// velocity: a host application that hands this library a fixed memory budget
+// up front, code running inside a real-time frame where an allocation's
+// implicit device synchronisation would stall the frame, or an embedding that
+// forbids the CUDA allocator altogether.  For them the scratch that the
+// split-source direct sum needs (per-source constants and per-target partial
+// sums) lives in one file-scope device array, reserved when the library is
+// loaded and held by every GPU that loads it until the process exits.
+namespace vg {
+namespace {
+
+constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
+constexpr size_t kNoAllocMaxSources = 32768;              // 1 MiB of per-source constants
+static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
+
+std::mutex g_noalloc_mu;
+void* g_noalloc_ptr[64];  // per device: g_noalloc_scratch's device address
+bool g_noalloc_ready[64];
+
+}  // namespace
+
+}  // namespace vg
+
+extern "C" vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_size, const float* angvel, size_t n,
+                                       const float* q4, size_t m, float spread_range, float spread_circ,
+                                       float* out4) {
+  using namespace vg;
+  if (kind != 0 && kind != 1) return set_noctx_error(VG_INVALID, "vg_direct_noalloc: kind must be 0 or 1");
+  if (m == 0) return VG_OK;
+  if (!q4 || !out4 || (n && (!pos_size || !angvel)))
+    return set_noctx_error(VG_INVALID, "vg_direct_noalloc: NULL pointer");
+  if (n > kNoAllocMaxSources)
+    return set_noctx_error(VG_TOO_LARGE, "vg_direct_noalloc: more than 32768 sources (the fixed scratch holds "
+                                         "32768 sources' constants); use vg_direct_device");
+  const size_t src_bytes = ((n * sizeof(float4) + 255) / 256) * 256;
+  const size_t room = kNoAllocScratchBytes - 2 * src_bytes;
+  if (m * 3 * sizeof(float) > room)
+    return set_noctx_error(VG_TOO_LARGE, "vg_direct_noalloc: too many targets for the fixed 8 MiB scratch "
+                                         "(at most (8 MiB - 32 n) / 12 targets); use vg_direct_device");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= 64)
+    return set_noctx_error(VG_CUDA_ERROR, "vg_direct_noalloc: no current CUDA device");
+  void* base = nullptr;
+  {
+    // First call on this device: look up where the loader placed the array
+    // on this device (host code only holds a stand-in for the symbol).
+    std::lock_guard<std::mutex> lock(g_noalloc_mu);
+    if (!g_noalloc_ready[dev]) {
+      void* p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+      if (e != cudaSuccess || !p) {
+        cudaGetLastError();
+        return set_noctx_error(VG_CUDA_ERROR, std::string("vg_direct_noalloc: cudaGetSymbolAddress failed: ") +
+                                                  cudaGetErrorString(e));
+      }
+      g_noalloc_ptr[dev] = p;
+      g_noalloc_ready[dev] = true;
+    }
+    base = g_noalloc_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    e = cudaMemsetAsync(out4, 0, m * sizeof(float4), st);
+    return e == cudaSuccess ? VG_OK : set_noctx_error(VG_CUDA_ERROR, cudaGetErrorString(e));
+  }
+  // Same split as vg_direct_device, capped so the partial sums fit the array.
+  const unsigned tblocks = blocks_for(m, kThreads * kTPT);
+  unsigned ksplit = 1;
+  while (tblocks * ksplit < 4u * kSMs && (n / (ksplit * 2)) >= (size_t)kTile &&
+         (size_t)(ksplit * 2) * m * 3 * sizeof(float) <= room)
+    ksplit *= 2;
+  const int chunk = (int)((n + ksplit - 1) / ksplit);
+  float4* s0 = (float4*)base;
+  float4* s1 = (float4*)((char*)base + src_bytes);
+  float* partial = (float*)((char*)base + 2 * src_bytes);
+  // Every scratch byte read below is written earlier in this call, so nothing
+  // needs clearing between calls.
+  if (kind == 0)
+    k_prep_sources<0><<<blocks_for(n, 256), 256, 0, st>>>((const float4*)pos_size, (const float4*)angvel, (int)n,
+                                                           spread_range, spread_circ, s0, s1);
+  else
+    k_prep_sources<1><<<blocks_for(n, 256), 256, 0, st>>>((const float4*)pos_size, (const float4*)angvel, (int)n,
+                                                           spread_range, spread_circ, s0, s1);
+  dim3 grid(tblocks, ksplit);
+  if (kind == 0)
+    k_direct_fast<0><<<grid, kThreads, 0, st>>>(s0, s1, (int)n, chunk, (const float4*)q4, (int)m, partial);
+  else
+    k_direct_fast<1><<<grid, kThreads, 0, st>>>(s0, s1, (int)n, chunk, (const float4*)q4, (int)m, partial);
+  k_reduce_partials<<<blocks_for(m, 256), 256, 0, st>>>(partial, (int)ksplit, (int)m, (float4*)out4);
+  e = cudaGetLastError();
+  if (e != cudaSuccess) return set_noctx_error(VG_CUDA_ERROR, cudaGetErrorString(e));
+  return VG_OK;
+}

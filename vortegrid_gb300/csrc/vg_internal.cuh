@@ -213,6 +213,8 @@ vg_status sync_and_check(Ctx* c, const char* what);
 void* ws(Ctx* c, int s, size_t bytes, vg_status* st);
 
 vg_status fail(Ctx* c, vg_status s, const std::string& msg);
+// Records an error for calls made without a context (vg_last_error(NULL)).
+vg_status set_noctx_error(vg_status s, const std::string& msg);
 vg_status cuda_check(Ctx* c, cudaError_t e, const char* what);
 #define VG_CUDA(ctx, call)                                 \
   do {                                                     \
