@@ -282,8 +282,13 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
   if (st != VG_OK) return st;
   const size_t pts = g.points();
   const bool ref = c->cfg.numerics == VG_NUMERICS_REFERENCE;
-  CellLists cl;
-  if ((st = build_cell_lists(c, g, ps, n, &cl)) != VG_OK) return st;
+  // Cell lists serve the tree, the splat and PSE; the direct technique
+  // without diffusion needs none.
+  const int tech = c->cfg.velocity_technique;
+  CellLists cl = {nullptr, nullptr, nullptr};
+  if (tech != VG_VELOCITY_DIRECT || c->cfg.enable_diffusion) {
+    if ((st = build_cell_lists(c, g, ps, n, &cl)) != VG_OK) return st;
+  }
   float* velgrid = (float*)ws(c, S_VEL, pts * 3 * sizeof(float), &st);
   if (st != VG_OK) return st;
   Tree t;
@@ -292,7 +297,6 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
   c->stats.poisson_relres = 0.0;
   c->stats.poisson_relres0 = 0.0;
   c->stats.ms_poisson = 0.f;
-  const int tech = c->cfg.velocity_technique;
   if (tech == VG_VELOCITY_POISSON || tech == VG_VELOCITY_TREE) {
     if ((st = build_tree(c, g, ps, w, n, cl, &t)) != VG_OK) return st;
   }
@@ -334,10 +338,12 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
     }
     if ((st = launch_curl(c, g, vecpot, velgrid)) != VG_OK) return st;
   } else {
-    // velocity at gridpoints by treecode (auto mollification, vortonSim.cpp:2458-2477) or direct sum
-    float4* q = (float4*)ws(c, S_JAC, pts * sizeof(float4) * 2, &st);
+    // velocity at gridpoints by treecode (auto mollification, vortonSim.cpp:2458-2477) or direct sum;
+    // the direct technique also evaluates every vorton, in the same launch
+    const size_t nq = pts + (tech == VG_VELOCITY_DIRECT ? n : 0);
+    float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
     if (st != VG_OK) return st;
-    float4* out4 = q + pts;
+    float4* out4 = q + nq;
     k_grid_points<<<blocks_for(pts, 256), 256, 0, c->stream>>>(g, q);
     VG_LAUNCHED(c);
     float sr = 1.0f, sc = 1.0f;
@@ -351,17 +357,16 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
       sc = 1.0f / s3;
       if ((st = launch_tree_eval(c, 0, ref, t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
     } else {
-      if ((st = launch_direct(c, 0, ref, ps, w, n, q, pts, 1.0f, 1.0f, out4)) != VG_OK) return st;
+      // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too
+      VG_CUDA(c, cudaMemcpyAsync(q + pts, ps, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+      if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
+      VG_CUDA(c, cudaMemcpyAsync(vel, out4 + pts, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
     }
     k_f4_to_f3<<<blocks_for(pts, 256), 256, 0, c->stream>>>(out4, velgrid, pts);
     VG_LAUNCHED(c);
-    if (tech == VG_VELOCITY_DIRECT) {
-      // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton
-      if ((st = launch_direct(c, 0, ref, ps, w, n, ps, n, 1.0f, 1.0f, vel)) != VG_OK) return st;
-    }
   }
   if (c->cfg.enable_stretch) {
-    float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), pts * 2 * sizeof(float4)), &st);
+    float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), (pts + n) * 2 * sizeof(float4)), &st);
     if (st != VG_OK) return st;
     if ((st = launch_jacobian(c, g, velgrid, jac)) != VG_OK) return st;
     if ((st = launch_stretch(c, g, jac, ps, w, n, dt)) != VG_OK) return st;
@@ -469,6 +474,8 @@ vg_status vg_destroy(vg_ctx* c) {
   if (c->stream) cudaStreamSynchronize(c->stream);
   for (int s = 0; s < S_NUM; ++s)
     if (c->buf[s].p) cudaFree(c->buf[s].p);
+  for (MgGraphCache& G : c->mg_graph)
+    if (G.exec) cudaGraphExecDestroy(G.exec);
   if (c->dflag) cudaFree(c->dflag);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);

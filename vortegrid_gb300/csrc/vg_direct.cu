@@ -18,6 +18,7 @@
 //     deterministic.
 // Reference path: one thread per query, sources in index order, the
 // reference's operation order (bit-identical to the CPU).
+#include <algorithm>
 #include <mutex>
 
 #include "vg_internal.cuh"
@@ -27,8 +28,16 @@ namespace vg {
 namespace {
 
 constexpr int kThreads = 128;
-constexpr int kTPT = 4;        // targets per thread
+constexpr int kTPT = 8;        // targets per thread
 constexpr int kTile = 256;     // sources per shared-memory tile
+
+// One MUFU.RSQ: approximate reciprocal square root with denormals flushed
+// (rsqrt(0) = +inf, which the min(., 1/r) below turns into the core law).
+__device__ __forceinline__ float rsqrt_ftz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 
 // Precompute per-source constants for the fast law.
 template <int KIND>
@@ -72,7 +81,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restri
       sh1[i] = s1[tile + i];
     }
     __syncthreads();
-#pragma unroll 2
+#pragma unroll 4
     for (int i = 0; i < cnt; ++i) {
       const float4 p = sh0[i];
       const float4 a = sh1[i];
@@ -81,14 +90,14 @@ __global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restri
         const float d0 = qx[t] - p.x, d1 = qy[t] - p.y, d2 = qz[t] - p.z;
         const float dist2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
         if (KIND == 0) {
-          const float inv = fminf(rsqrtf(dist2), p.w);
+          const float inv = fminf(rsqrt_ftz(dist2), p.w);
           const float law = inv * inv * inv;
           const float b0 = d0 * law, b1 = d1 * law, b2 = d2 * law;
           ax[t] = fmaf(a.y, b2, fmaf(-a.z, b1, ax[t]));
           ay[t] = fmaf(a.z, b0, fmaf(-a.x, b2, ay[t]));
           az[t] = fmaf(a.x, b1, fmaf(-a.y, b0, az[t]));
         } else {
-          const float law = (dist2 < a.w) ? dist2 * p.w * p.w * p.w : rsqrtf(dist2);
+          const float law = (dist2 < a.w) ? dist2 * p.w * p.w * p.w : rsqrt_ftz(dist2);
           ax[t] = fmaf(a.x, law, ax[t]);
           ay[t] = fmaf(a.y, law, ay[t]);
           az[t] = fmaf(a.z, law, az[t]);
@@ -144,6 +153,23 @@ __global__ void __launch_bounds__(kThreads) k_direct_ref(const float4* __restric
   if (j < m) out[j] = make_float4(acc.x, acc.y, acc.z, 0.f);
 }
 
+// Resident CTAs of k_direct_fast across the device (SMs x occupancy), queried once.
+unsigned direct_slots(int kind) {
+  static unsigned cached[2] = {0, 0};
+  if (!cached[kind]) {
+    int dev = 0, sms = kSMs, per_sm = 1;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    if (kind == 0)
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_fast<0>, kThreads, 0);
+    else
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_fast<1>, kThreads, 0);
+    cudaGetLastError();
+    cached[kind] = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per_sm);
+  }
+  return cached[kind];
+}
+
 }  // namespace
 
 vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
@@ -164,11 +190,16 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
     VG_CUDA(c, cudaGetLastError());
     return VG_OK;
   }
-  // Split the sources so that the grid covers every SM several times.
+  // Split the sources into `ksplit` chunks so that target blocks x chunks
+  // fills the resident CTA slots of the GPU (SMs x CTAs per SM) once, with no
+  // partial second wave; every CTA then does the same amount of work.
   const unsigned tblocks = blocks_for(m, kThreads * kTPT);
-  unsigned ksplit = 1;
-  while (tblocks * ksplit < 4u * kSMs && (n / (ksplit * 2)) >= (size_t)kTile) ksplit *= 2;
+  const unsigned slots = direct_slots(kind);
+  unsigned ksplit = std::max(1u, slots / tblocks);
+  const size_t min_chunk = 64;  // keep each CTA's source loop long enough to amortise its set-up
+  if (n / ksplit < min_chunk) ksplit = (unsigned)std::max<size_t>(1, n / min_chunk);
   const int chunk = (int)((n + ksplit - 1) / ksplit);
+  ksplit = (unsigned)((n + chunk - 1) / chunk);
   vg_status st = VG_OK;
   const size_t srcb = ((n * sizeof(float4) + 255) / 256) * 256;
   char* scratch = (char*)ws(c, S_DIRECT, 2 * srcb + (size_t)ksplit * m * 3 * sizeof(float), &st);

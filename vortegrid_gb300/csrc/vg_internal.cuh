@@ -188,8 +188,17 @@ enum Slot {
   S_NUM
 };
 
+// A captured multigrid cycle, replayed while the grid and buffers are unchanged.
+struct MgGraphCache {
+  cudaGraphExec_t exec = nullptr;
+  Geom g;
+  const void* key[4] = {nullptr, nullptr, nullptr, nullptr};
+  unsigned launches = 0;
+};
+
 struct Ctx {
   vg_config cfg;
+  MgGraphCache mg_graph[2];  // phase-1 and phase-2 cycle graphs
   cudaStream_t stream = nullptr;
   bool own_stream = false;
   std::string err;

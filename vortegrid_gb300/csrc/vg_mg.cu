@@ -4,16 +4,24 @@
 // The reference solves the same equation with a fixed-work cascade
 // (VortonFluid/vortonSim.cpp:2539-2571) that never targets a residual; this
 // is a correction-scheme multigrid in iterative refinement:
-//   outer loop (FP64): r = b - L a64 computed in FP64 from the FP64 iterate,
-//                      stored as FP32; ||r|| and ||b|| as FP64 sums reduced in
-//                      a fixed order (deterministic);
-//   inner solve (FP32): one V(pre, post)-cycle on the correction e with
-//                      point red-black Gauss-Seidel (colour = (x+y+z) parity),
-//                      27-point full-weighting restriction of the residual
-//                      (the reference's SLOWER_MORE_ACCURATE weights,
-//                      uniformGrid.h:1453-1585) and trilinear prolongation;
-//   coarsest grid (FP64): red-black Gauss-Seidel run to convergence in one CTA;
-//   a64 += e.
+//   * each cycle: r = b - L a (the residual of the current iterate, norms
+//     accumulated in FP64 and reduced in a fixed order), then one FP32
+//     V(2,2)-cycle on L e = r -- point red-black Gauss-Seidel (colour = parity
+//     of x+y+z), 27-point full-weighting restriction fused with the residual
+//     (the reference's SLOWER_MORE_ACCURATE weights, uniformGrid.h:1453-1585),
+//     trilinear prolongation, FP64 Gauss-Seidel on the coarsest grid -- and
+//     a += e;
+//   * phase 1 iterates on the FP32 field with an FP32 residual while FP32 can
+//     still represent it (relative residual above 1e-4);
+//   * phase 2 (iterative refinement) keeps the iterate in FP64, evaluates
+//     r = b - L a in FP64 arithmetic, solves the correction L e = r with FP32
+//     cycles (the correction's residual is small, so FP32 tracks it well),
+//     adds e in FP64 and checks with another FP64 residual -- reaching
+//     residuals far below FP32's cancellation floor (~1e-4 at 128^3) with two
+//     FP64 residual evaluations per solve.
+// FP64 is used only for that residual, the coarsest-grid solve and the norms.
+// The levels of at most 17^3 points run inside one CTA with their fields in
+// shared memory; each cycle is captured once as a CUDA graph and replayed.
 // Grids are float[3] per point (x fastest); the three components are three
 // independent scalar problems solved together.
 #include <float.h>
@@ -35,70 +43,110 @@ struct Lev {
   size_t base;             // offset (points) into level arrays
 };
 
+// Grids here have fewer than 2^32 points, so index math stays in 32 bits
+// (64-bit integer division costs tens of instructions on the GPU).
 __device__ __forceinline__ void unflat(size_t k, const Geom& g, unsigned& x, unsigned& y, unsigned& z) {
-  x = (unsigned)(k % g.np[0]);
-  y = (unsigned)((k / g.np[0]) % g.np[1]);
-  z = (unsigned)(k / ((size_t)g.np[0] * g.np[1]));
+  const unsigned k32 = (unsigned)k, nx = g.np[0], ny = g.np[1];
+  const unsigned q = k32 / nx;
+  x = k32 - q * nx;
+  z = q / ny;
+  y = q - z * ny;
 }
 
 __device__ __forceinline__ bool interior(const Geom& g, unsigned x, unsigned y, unsigned z) {
   return x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2];
 }
 
-// FP64 residual of the FP64 iterate; writes FP32 r (0 on the boundary) and
-// per-block partial sums of r^2 and b^2.
-__global__ void __launch_bounds__(kRedThreads) k_residual64(Geom g, double r2x, double r2y, double r2z,
-                                                            const double* __restrict__ a, const float* __restrict__ b,
-                                                            float* __restrict__ r, double* __restrict__ part) {
+// Block reduction of two sums into part[2 * blockIdx.x + {0, 1}]: 32-term
+// warp sums in FP32 (relative error ~1e-6, irrelevant for a norm), then FP64
+// across warps, blocks and the grid.
+__device__ __forceinline__ void block_sum2(float a32, float b32, double* __restrict__ part) {
+  __shared__ double s_a[kRedThreads / 32], s_b[kRedThreads / 32];
+  for (int o = 16; o > 0; o >>= 1) {
+    a32 += __shfl_xor_sync(0xffffffffu, a32, o);
+    b32 += __shfl_xor_sync(0xffffffffu, b32, o);
+  }
+  if ((threadIdx.x & 31) == 0) {
+    s_a[threadIdx.x >> 5] = (double)a32;
+    s_b[threadIdx.x >> 5] = (double)b32;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double t1 = 0.0, t2 = 0.0;
+    for (int w = 0; w < kRedThreads / 32; ++w) {
+      t1 += s_a[w];
+      t2 += s_b[w];
+    }
+    part[2 * blockIdx.x] = t1;
+    part[2 * blockIdx.x + 1] = t2;
+  }
+}
+
+// Phase 1 residual: r = b - L a in FP32 from the FP32 iterate; per-block FP64
+// partial sums of r^2 and b^2.
+__global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, float r2y, float r2z,
+                                                             const float* __restrict__ a, const float* __restrict__ b,
+                                                             float* __restrict__ r, double* __restrict__ part) {
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  double rr = 0.0, bb = 0.0;
+  float rr = 0.f, bb = 0.f;
   if (k < g.points()) {
     unsigned x, y, z;
     unflat(k, g, x, y, z);
     if (interior(g, x, y, z)) {
-      const size_t nx = g.np[0], nxy = (size_t)g.np[0] * g.np[1];
+      const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const double ac = a[3 * k + c];
-        const double lap = (a[3 * (k + 1) + c] + a[3 * (k - 1) + c] - 2.0 * ac) * r2x +
-                           (a[3 * (k + nx) + c] + a[3 * (k - nx) + c] - 2.0 * ac) * r2y +
-                           (a[3 * (k + nxy) + c] + a[3 * (k - nxy) + c] - 2.0 * ac) * r2z;
-        const double bv = (double)b[3 * k + c];
-        const double rv = bv - lap;
-        r[3 * k + c] = (float)rv;
-        rr += rv * rv;
-        bb += bv * bv;
+        const float ac = a[3 * k + c];
+        const float lap = (a[3 * (k + 1) + c] + a[3 * (k - 1) + c] - 2.f * ac) * r2x +
+                          (a[3 * (k + sy) + c] + a[3 * (k - sy) + c] - 2.f * ac) * r2y +
+                          (a[3 * (k + sz) + c] + a[3 * (k - sz) + c] - 2.f * ac) * r2z;
+        const float bv = b[3 * k + c];
+        const float rv = bv - lap;
+        r[3 * k + c] = rv;
+        rr = fmaf(rv, rv, rr);
+        bb = fmaf(bv, bv, bb);
       }
     } else {
-      r[3 * k] = 0.f;
-      r[3 * k + 1] = 0.f;
-      r[3 * k + 2] = 0.f;
+      r[3 * k] = r[3 * k + 1] = r[3 * k + 2] = 0.f;
     }
   }
-  __shared__ double s_rr[kRedThreads / 32], s_bb[kRedThreads / 32];
-  for (int o = 16; o > 0; o >>= 1) {
-    rr += __shfl_xor_sync(0xffffffffu, rr, o);
-    bb += __shfl_xor_sync(0xffffffffu, bb, o);
-  }
-  if ((threadIdx.x & 31) == 0) {
-    s_rr[threadIdx.x >> 5] = rr;
-    s_bb[threadIdx.x >> 5] = bb;
-  }
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    double a1 = 0.0, a2 = 0.0;
-    for (int w = 0; w < kRedThreads / 32; ++w) {
-      a1 += s_rr[w];
-      a2 += s_bb[w];
-    }
-    part[2 * blockIdx.x] = a1;
-    part[2 * blockIdx.x + 1] = a2;
-  }
+  block_sum2(rr, bb, part);
 }
 
-// Sum the per-block partials in a fixed order (one block).
+// Phase 2 residual: r = b - L a in FP64 arithmetic from the FP64 iterate,
+// stored as FP32; per-block FP64 partial sums of r^2 (b^2 slot unused).
+__global__ void __launch_bounds__(kRedThreads) k_residual64(Geom g, double r2x, double r2y, double r2z,
+                                                            const double* __restrict__ a, const float* __restrict__ b,
+                                                            float* __restrict__ r, double* __restrict__ part) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  float rr = 0.f;
+  if (k < g.points()) {
+    unsigned x, y, z;
+    unflat(k, g, x, y, z);
+    if (interior(g, x, y, z)) {
+      const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
+      const double d = -2.0 * (r2x + r2y + r2z);
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        const double lap = fma(a[3 * k + c], d,
+                               fma(a[3 * (k + 1) + c] + a[3 * (k - 1) + c], r2x,
+                                   fma(a[3 * (k + sy) + c] + a[3 * (k - sy) + c], r2y,
+                                       (a[3 * (k + sz) + c] + a[3 * (k - sz) + c]) * r2z)));
+        const float rv = (float)((double)b[3 * k + c] - lap);
+        r[3 * k + c] = rv;
+        rr = fmaf(rv, rv, rr);
+      }
+    } else {
+      r[3 * k] = r[3 * k + 1] = r[3 * k + 2] = 0.f;
+    }
+  }
+  block_sum2(rr, 0.f, part);
+}
+
+// Sum the per-block partials in a fixed order (one block); with keep_b the
+// ||b||^2 slot is left as phase 1's first residual wrote it.
 __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict__ part, int nb,
-                                                       double* __restrict__ out2) {
+                                                       double* __restrict__ out2, int keep_b) {
   __shared__ double s1[1024], s2[1024];
   double a1 = 0.0, a2 = 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -117,29 +165,14 @@ __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict_
   }
   if (threadIdx.x == 0) {
     out2[0] = s1[0];
-    out2[1] = s2[0];
+    if (!keep_b) out2[1] = s2[0];
   }
 }
 
-// Point red-black Gauss-Seidel on L e = r (FP32).  One thread per x-pair:
-// updates the point of `color` among (2j, 2j+1).  zero_first: e is zero
-// before this sweep (first pre-smoothing sweep), so neighbours read as 0.
-__global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, float r2z, float H,
-                                              float* __restrict__ e, const float* __restrict__ r, unsigned color,
-                                              int zero_first) {
-  const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
-  const unsigned half = (nx + 1) / 2;
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  const size_t rows = (size_t)ny * nz;
-  if (t >= rows * half) return;
-  const unsigned j = (unsigned)(t % half);
-  const size_t row = t / half;
-  const unsigned y = (unsigned)(row % ny), z = (unsigned)(row / ny);
-  if (y == 0 || z == 0 || y + 1 >= ny || z + 1 >= nz) return;
-  unsigned x = 2 * j + ((y + z + color) & 1u);
-  if (x == 0 || x + 1 >= nx) return;
-  const size_t k = x + (size_t)nx * (y + (size_t)ny * z);
-  const size_t sy = nx, sz = (size_t)nx * ny;
+__device__ __forceinline__ void rbgs_point(const Geom& g, float r2x, float r2y, float r2z, float H,
+                                           float* __restrict__ e, const float* __restrict__ r, size_t k,
+                                           bool zero_first) {
+  const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
 #pragma unroll
   for (int c = 0; c < 3; ++c) {
     float v;
@@ -155,44 +188,42 @@ __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, floa
   }
 }
 
-// FP32 residual res = r - L e on interior points (0 on the boundary).
-__global__ void __launch_bounds__(256) k_residual32(Geom g, float r2x, float r2y, float r2z,
-                                                    const float* __restrict__ e, const float* __restrict__ r,
-                                                    float* __restrict__ res) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.points()) return;
-  unsigned x, y, z;
-  unflat(k, g, x, y, z);
-  if (!interior(g, x, y, z)) {
-    res[3 * k] = res[3 * k + 1] = res[3 * k + 2] = 0.f;
-    return;
-  }
-  const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
-#pragma unroll
-  for (int c = 0; c < 3; ++c) {
-    const float ec = e[3 * k + c];
-    const float lap = (e[3 * (k + 1) + c] + e[3 * (k - 1) + c] - 2.f * ec) * r2x +
-                      (e[3 * (k + sy) + c] + e[3 * (k - sy) + c] - 2.f * ec) * r2y +
-                      (e[3 * (k + sz) + c] + e[3 * (k - sz) + c] - 2.f * ec) * r2z;
-    res[3 * k + c] = r[3 * k + c] - lap;
-  }
+// Point red-black Gauss-Seidel on L e = r (FP32).  One thread per x-pair:
+// updates the point of `color` among (2j, 2j+1).  zero_first: e is zero
+// before this sweep, so the red points take -r H directly.
+__global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, float r2z, float H,
+                                              float* __restrict__ e, const float* __restrict__ r, unsigned color,
+                                              int zero_first) {
+  const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
+  const unsigned half = (nx + 1) / 2;
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= ny * nz * half) return;
+  const unsigned row = t / half;
+  const unsigned j = t - row * half;
+  const unsigned z = row / ny, y = row - z * ny;
+  if (y == 0 || z == 0 || y + 1 >= ny || z + 1 >= nz) return;
+  const unsigned x = 2 * j + ((y + z + color) & 1u);
+  if (x == 0 || x + 1 >= nx) return;
+  rbgs_point(g, r2x, r2y, r2z, H, e, r, x + (size_t)nx * (y + (size_t)ny * z), zero_first != 0);
 }
 
-// Full-weighting restriction of the fine residual to coarse interior points.
-__global__ void __launch_bounds__(256) k_restrict(Geom F, Geom C, const float* __restrict__ res,
-                                                  float* __restrict__ rc) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= C.points()) return;
+// Fused FP32 residual + full-weighting restriction: coarse interior point
+// (x, y, z) sums the fine residuals r - L e at the 27 fine points around
+// (2x, 2y, 2z) with weights 8/4/2/1 / 64, recomputing them instead of
+// writing the fine residual field.
+__device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geom& C, float r2x, float r2y,
+                                                        float r2z, const float* __restrict__ e,
+                                                        const float* __restrict__ r, size_t k,
+                                                        float* __restrict__ rc) {
   unsigned x, y, z;
   unflat(k, C, x, y, z);
   if (!interior(C, x, y, z)) {
     rc[3 * k] = rc[3 * k + 1] = rc[3 * k + 2] = 0.f;
     return;
   }
-  const size_t fx = 2 * x, fy = 2 * y, fz = 2 * z;
-  const size_t sy = F.np[0], sz = (size_t)F.np[0] * F.np[1];
-  const size_t f0 = fx + sy * fy + sz * fz;
-  float a0 = 0.f, a1 = 0.f, a2 = 0.f;
+  const ptrdiff_t sy = F.np[0], sz = (ptrdiff_t)F.np[0] * F.np[1];
+  const size_t f0 = (size_t)(2 * x) + sy * (2 * y) + sz * (2 * z);
+  float acc[3] = {0.f, 0.f, 0.f};
 #pragma unroll
   for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
@@ -200,29 +231,40 @@ __global__ void __launch_bounds__(256) k_restrict(Geom F, Geom C, const float* _
 #pragma unroll
       for (int dx = -1; dx <= 1; ++dx) {
         const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
-        const size_t o = f0 + dx + (ptrdiff_t)sy * dy + (ptrdiff_t)sz * dz;
-        a0 = fmaf(wt, res[3 * o], a0);
-        a1 = fmaf(wt, res[3 * o + 1], a1);
-        a2 = fmaf(wt, res[3 * o + 2], a2);
+        const size_t o = f0 + dx + sy * dy + sz * dz;
+        // fine points on the boundary carry no residual (Dirichlet)
+        if (!interior(F, 2 * x + dx, 2 * y + dy, 2 * z + dz)) continue;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float ec = e[3 * o + c];
+          const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
+                            (e[3 * (o + sy) + c] + e[3 * (o - sy) + c] - 2.f * ec) * r2y +
+                            (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
+          acc[c] = fmaf(wt, r[3 * o + c] - lap, acc[c]);
+        }
       }
   const float s = 1.0f / 64.0f;
-  rc[3 * k] = a0 * s;
-  rc[3 * k + 1] = a1 * s;
-  rc[3 * k + 2] = a2 * s;
+  rc[3 * k] = acc[0] * s;
+  rc[3 * k + 1] = acc[1] * s;
+  rc[3 * k + 2] = acc[2] * s;
+}
+
+__global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float r2x, float r2y, float r2z,
+                                                           const float* __restrict__ e, const float* __restrict__ r,
+                                                           float* __restrict__ rc) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < C.points()) residual_restrict_point(F, C, r2x, r2y, r2z, e, r, k, rc);
 }
 
 // e_fine += trilinear(e_coarse) on fine interior points.
-__global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
-                                                     float* __restrict__ ef) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= F.points()) return;
+__device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, const float* __restrict__ ec,
+                                              float* __restrict__ ef, size_t k) {
   unsigned x, y, z;
   unflat(k, F, x, y, z);
   if (!interior(F, x, y, z)) return;
-  const unsigned cx = x >> 1, cy = y >> 1, cz = z >> 1;
   const unsigned ox = x & 1, oy = y & 1, oz = z & 1;
   const size_t sy = C.np[0], sz = (size_t)C.np[0] * C.np[1];
-  const size_t c0 = cx + sy * cy + sz * cz;
+  const size_t c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
   const float wt = 1.0f / (float)(1u << (ox + oy + oz));
   for (unsigned iz = 0; iz <= oz; ++iz)
@@ -238,32 +280,113 @@ __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float
   ef[3 * k + 2] += a2 * wt;
 }
 
-// Coarsest grid: FP64 red-black Gauss-Seidel to convergence, one CTA.
-__global__ void __launch_bounds__(1024) k_coarse_solve(Geom g, double r2x, double r2y, double r2z,
-                                                       const float* __restrict__ r, float* __restrict__ e,
-                                                       double* __restrict__ work, int sweeps) {
+__global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
+                                                     float* __restrict__ ef) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < F.points()) prolong_point(F, C, ec, ef, k);
+}
+
+// The small levels of a V-cycle in one CTA, their e and r in shared memory:
+// pre-smoothing and fused residual-restriction down to the coarsest grid, an
+// FP64 Gauss-Seidel solve there, then prolongation and post-smoothing back up.
+// The first small level reads its r from global memory and writes its e back.
+constexpr int kSmallMax = 8;
+constexpr size_t kSmallLevelPoints = 17 * 17 * 17;
+struct SmallLevels {
+  int n;  // levels handled here
+  Geom g[kSmallMax];
+  float r2x[kSmallMax], r2y[kSmallMax], r2z[kSmallMax], H[kSmallMax];
+  unsigned off[kSmallMax];  // float offsets of e (r follows e) in shared memory
+  const float* r_in;        // first small level's r (global)
+  float* e_out;             // first small level's e (global)
+  int pre, post, coarse_sweeps;
+};
+
+__device__ __forceinline__ float* sm_e(float* sm, const SmallLevels& S, int l) { return sm + S.off[l]; }
+__device__ __forceinline__ float* sm_r(float* sm, const SmallLevels& S, int l) {
+  return sm + S.off[l] + 3 * S.g[l].points();
+}
+
+__device__ void block_rb_sweep(float* sm, const SmallLevels& S, int l, unsigned color, bool zero_first) {
+  const Geom& g = S.g[l];
   const size_t n = g.points();
-  const double H = 0.5 / (r2x + r2y + r2z);
-  for (size_t k = threadIdx.x; k < 3 * n; k += blockDim.x) work[k] = 0.0;
+  float* e = sm_e(sm, S, l);
+  const float* r = sm_r(sm, S, l);
+  for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+    unsigned x, y, z;
+    unflat(k, g, x, y, z);
+    if (!interior(g, x, y, z) || ((x + y + z) & 1u) != color) continue;
+    rbgs_point(g, S.r2x[l], S.r2y[l], S.r2z[l], S.H[l], e, r, k, zero_first);
+  }
   __syncthreads();
-  const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
-  for (int it = 0; it < sweeps; ++it) {
-    for (unsigned color = 0; color < 2; ++color) {
-      for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
-        unsigned x, y, z;
-        unflat(k, g, x, y, z);
-        if (!interior(g, x, y, z) || ((x + y + z) & 1u) != color) continue;
-        for (int c = 0; c < 3; ++c) {
-          const double s = (work[3 * (k + 1) + c] + work[3 * (k - 1) + c]) * r2x +
-                           (work[3 * (k + sy) + c] + work[3 * (k - sy) + c]) * r2y +
-                           (work[3 * (k + sz) + c] + work[3 * (k - sz) + c]) * r2z;
-          work[3 * k + c] = (s - (double)r[3 * k + c]) * H;
+}
+
+__global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ SmallLevels S,
+                                                       double* __restrict__ work) {
+  extern __shared__ float sm[];
+  {  // e = 0 everywhere (boundaries stay 0), r of the first level from global
+    const size_t total = S.off[S.n - 1] + 6 * S.g[S.n - 1].points();
+    for (size_t k = threadIdx.x; k < total; k += blockDim.x) sm[k] = 0.f;
+    __syncthreads();
+    const size_t n0 = 3 * S.g[0].points();
+    float* r0 = sm_r(sm, S, 0);
+    for (size_t k = threadIdx.x; k < n0; k += blockDim.x) r0[k] = S.r_in[k];
+    __syncthreads();
+  }
+  for (int l = 0; l < S.n - 1; ++l) {
+    for (int s = 0; s < S.pre; ++s) {
+      block_rb_sweep(sm, S, l, 0, s == 0);
+      block_rb_sweep(sm, S, l, 1, false);
+    }
+    const Geom& C = S.g[l + 1];
+    for (size_t k = threadIdx.x; k < C.points(); k += blockDim.x)
+      residual_restrict_point(S.g[l], C, S.r2x[l], S.r2y[l], S.r2z[l], sm_e(sm, S, l), sm_r(sm, S, l), k,
+                              sm_r(sm, S, l + 1));
+    __syncthreads();
+  }
+  {  // coarsest grid: FP64 red-black Gauss-Seidel from zero
+    const int l = S.n - 1;
+    const Geom& g = S.g[l];
+    const size_t n = g.points();
+    const double cx = 1.0 / ((double)g.cell[0] * g.cell[0]), cy = 1.0 / ((double)g.cell[1] * g.cell[1]),
+                 cz = 1.0 / ((double)g.cell[2] * g.cell[2]);
+    const double H = 0.5 / (cx + cy + cz);
+    const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
+    const float* r = sm_r(sm, S, l);
+    for (size_t k = threadIdx.x; k < 3 * n; k += blockDim.x) work[k] = 0.0;
+    __syncthreads();
+    for (int it = 0; it < S.coarse_sweeps; ++it)
+      for (unsigned color = 0; color < 2; ++color) {
+        for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
+          unsigned x, y, z;
+          unflat(k, g, x, y, z);
+          if (!interior(g, x, y, z) || ((x + y + z) & 1u) != color) continue;
+          for (int c = 0; c < 3; ++c) {
+            const double sv = (work[3 * (k + 1) + c] + work[3 * (k - 1) + c]) * cx +
+                              (work[3 * (k + sy) + c] + work[3 * (k - sy) + c]) * cy +
+                              (work[3 * (k + sz) + c] + work[3 * (k - sz) + c]) * cz;
+            work[3 * k + c] = (sv - (double)r[3 * k + c]) * H;
+          }
         }
+        __syncthreads();
       }
-      __syncthreads();
+    float* e = sm_e(sm, S, l);
+    for (size_t k = threadIdx.x; k < 3 * n; k += blockDim.x) e[k] = (float)work[k];
+    __syncthreads();
+  }
+  for (int l = S.n - 2; l >= 0; --l) {
+    const Geom& F = S.g[l];
+    for (size_t k = threadIdx.x; k < F.points(); k += blockDim.x)
+      prolong_point(F, S.g[l + 1], sm_e(sm, S, l + 1), sm_e(sm, S, l), k);
+    __syncthreads();
+    for (int s = 0; s < S.post; ++s) {
+      block_rb_sweep(sm, S, l, 0, false);
+      block_rb_sweep(sm, S, l, 1, false);
     }
   }
-  for (size_t k = threadIdx.x; k < 3 * n; k += blockDim.x) e[k] = (float)work[k];
+  const size_t n0 = 3 * S.g[0].points();
+  const float* e0 = sm_e(sm, S, 0);
+  for (size_t k = threadIdx.x; k < n0; k += blockDim.x) S.e_out[k] = e0[k];
 }
 
 __global__ void k_to_f64(const float* __restrict__ a, double* __restrict__ b, size_t n) {
@@ -274,6 +397,11 @@ __global__ void k_to_f64(const float* __restrict__ a, double* __restrict__ b, si
 __global__ void k_add_f64(double* __restrict__ a, const float* __restrict__ e, size_t n) {
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) a[k] += (double)e[k];
+}
+
+__global__ void k_add_f32(float* __restrict__ a, const float* __restrict__ e, size_t n) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n) a[k] += e[k];
 }
 
 __global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
@@ -287,6 +415,8 @@ struct MgPlan {
   int nlev;
   Lev lev[kMaxLayers];
   size_t total;
+  int first_small;    // first level run by k_vcycle_small
+  size_t small_smem;  // its dynamic shared memory (bytes)
 };
 
 static MgPlan plan_levels(const Geom& g) {
@@ -312,100 +442,235 @@ static MgPlan plan_levels(const Geom& g) {
     cur = decimate(cur, 2);
   }
   P.total = total;
+  int fs = P.nlev - 1;  // the coarsest level always runs in the CTA kernel
+  while (fs > 1 && P.lev[fs - 1].g.points() <= kSmallLevelPoints && P.nlev - (fs - 1) <= kSmallMax) --fs;
+  if (P.nlev == 1) fs = 0;
+  P.first_small = fs;
+  size_t floats = 0;
+  for (int l = fs; l < P.nlev; ++l) floats += 6 * P.lev[l].g.points();
+  P.small_smem = floats * sizeof(float);
   return P;
+}
+
+struct MgBufs {
+  float* E;
+  float* R;
+  double* a64;
+  double* part;
+  double* sums;
+  double* cwork;
+  unsigned nb0;
+};
+
+// One V(pre, post)-cycle on L e = R[level 0] (level 0's e starts from zero).
+static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsigned* nl) {
+  const int pre = 2, post = 2;
+  const int fs = P.first_small;
+  for (int l = 0; l < fs; ++l) {
+    const Lev& L = P.lev[l];
+    float* e = B.E + 3 * L.base;
+    float* r = B.R + 3 * L.base;
+    const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
+    for (int s = 0; s < pre; ++s)
+      for (unsigned col = 0; col < 2; ++col) {
+        k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
+                                                              (s == 0 && col == 0) ? 1 : 0);
+        ++*nl;
+      }
+    const Lev& Cn = P.lev[l + 1];
+    k_residual_restrict<<<blocks_for(Cn.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e,
+                                                                               r, B.R + 3 * Cn.base);
+    ++*nl;
+  }
+  {
+    SmallLevels S;
+    S.n = P.nlev - fs;
+    unsigned off = 0;
+    for (int i = 0; i < S.n; ++i) {
+      const Lev& L = P.lev[fs + i];
+      S.g[i] = L.g;
+      S.r2x[i] = L.r2x;
+      S.r2y[i] = L.r2y;
+      S.r2z[i] = L.r2z;
+      S.H[i] = L.H;
+      S.off[i] = off;
+      off += (unsigned)(6 * L.g.points());
+    }
+    S.r_in = B.R + 3 * P.lev[fs].base;
+    S.e_out = B.E + 3 * P.lev[fs].base;
+    S.pre = pre;
+    S.post = post;
+    const Geom& cg = P.lev[P.nlev - 1].g;
+    // Gauss-Seidel on m interior points per axis contracts by about
+    // cos^2(pi / (m + 1)) per sweep; 3 (m + 1)^2 sweeps reach ~1e-13.
+    const unsigned m = std::max(cg.np[0], std::max(cg.np[1], cg.np[2])) - 1;
+    S.coarse_sweeps = (int)std::min(3u * m * m + 2u, 4000u);
+    k_vcycle_small<<<1, 1024, P.small_smem, c->stream>>>(S, B.cwork);
+    ++*nl;
+  }
+  for (int l = fs - 1; l >= 0; --l) {
+    const Lev& L = P.lev[l];
+    const Lev& Cn = P.lev[l + 1];
+    float* e = B.E + 3 * L.base;
+    float* r = B.R + 3 * L.base;
+    const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
+    k_prolong_add<<<blocks_for(L.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    ++*nl;
+    for (int s = 0; s < post; ++s)
+      for (unsigned col = 0; col < 2; ++col) {
+        k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+        ++*nl;
+      }
+  }
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+// One cycle on L x = rhs: V-cycle on the current residual R, x += e, then
+// R = rhs - L x in FP32 with its FP64-accumulated norm.
+static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
+                               unsigned* nl) {
+  vg_status st = enqueue_vcycle(c, P, B, nl);
+  if (st != VG_OK) return st;
+  const size_t n3 = 3 * g.points();
+  const Lev& L0 = P.lev[0];
+  k_add_f32<<<blocks_for(n3, 256), 256, 0, c->stream>>>(x, B.E, n3);
+  k_residual32n<<<B.nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, x, rhs, B.R, B.part);
+  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
+  *nl += 3;
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+// Capture (or reuse) the cycle graph for (x, rhs) in cache slot `slot`.
+static void cycle_graph(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
+                        int slot) {
+  MgGraphCache& G = c->mg_graph[slot];
+  const void* key[4] = {B.E, B.R, rhs, x};
+  if (G.exec && memcmp(&G.g, &g, sizeof(Geom)) == 0 && memcmp(G.key, key, sizeof(key)) == 0) return;
+  if (G.exec) {
+    cudaGraphExecDestroy(G.exec);
+    G.exec = nullptr;
+  }
+  cudaGraph_t graph = nullptr;
+  unsigned nl = 0;
+  if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    const vg_status cst = enqueue_cycle(c, P, g, B, x, rhs, &nl);
+    const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+    if (cst == VG_OK && ce == cudaSuccess && graph && cudaGraphInstantiate(&G.exec, graph, 0) == cudaSuccess) {
+      G.g = g;
+      memcpy(G.key, key, sizeof(key));
+      G.launches = nl;
+    } else {
+      G.exec = nullptr;
+    }
+    if (graph) cudaGraphDestroy(graph);
+  }
+  cudaGetLastError();  // capture unavailable (e.g. the legacy stream): launch directly instead
+}
+
+static vg_status run_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
+                           int slot) {
+  cycle_graph(c, P, g, B, x, rhs, slot);
+  MgGraphCache& G = c->mg_graph[slot];
+  if (G.exec) {
+    VG_CUDA(c, cudaGraphLaunch(G.exec, c->stream));
+    c->launches += G.launches;
+    return VG_OK;
+  }
+  unsigned nl = 0;
+  const vg_status st = enqueue_cycle(c, P, g, B, x, rhs, &nl);
+  c->launches += nl;
+  return st;
+}
+
+static vg_status read_norm(Ctx* c, const MgBufs& B, double* rr, double* bb) {
+  double h[2];
+  VG_CUDA(c, cudaMemcpyAsync(h, B.sums, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  *rr = h[0];
+  if (bb) *bb = h[1];
+  if (!(h[0] == h[0])) return fail(c, VG_NONFINITE, "multigrid: non-finite residual");
+  return VG_OK;
 }
 
 vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, double tol, int max_cycles,
                         int* cycles_out, double* relres0_out, double* relres_out) {
   const MgPlan P = plan_levels(g);
   const size_t n0 = g.points();
-  const int pre = 2, post = 2;
-  // workspace: e, r, res for every level (FP32), a64 (FP64), partials, coarse work
   const unsigned nb0 = blocks_for(n0, kRedThreads);
   const size_t coarse_pts = P.lev[P.nlev - 1].g.points();
-  const size_t bytes = 3 * P.total * 3 * sizeof(float) + n0 * 3 * sizeof(double) + (size_t)nb0 * 2 * sizeof(double) +
-                       4 * sizeof(double) + coarse_pts * 3 * sizeof(double) + 1024;
+  const size_t bytes = 2 * P.total * 3 * sizeof(float) + n0 * 3 * sizeof(double) + (size_t)nb0 * 2 * sizeof(double) +
+                       4 * sizeof(double) + coarse_pts * 3 * sizeof(double) + 2 * n0 * 3 * sizeof(float) + 4096;
+  if (P.small_smem > 200 * 1024) return fail(c, VG_TOO_LARGE, "multigrid: coarse levels exceed shared memory");
   vg_status st = VG_OK;
   char* mem = (char*)ws(c, S_MG, bytes, &st);
   if (st != VG_OK) return st;
-  float* E = (float*)mem;
-  float* R = E + 3 * P.total;
-  float* RES = R + 3 * P.total;
-  double* a64 = (double*)(((uintptr_t)(RES + 3 * P.total) + 255) & ~(uintptr_t)255);
-  double* part = a64 + 3 * n0;
-  double* sums = part + 2 * (size_t)nb0;
-  double* cwork = sums + 4;
-  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]);
-  const double r2y = 1.0 / ((double)g.cell[1] * g.cell[1]);
-  const double r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
-  k_to_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, a64, 3 * n0);
-  VG_LAUNCHED(c);
-  double relres = 0.0, relres0 = -1.0;
-  int cyc = 0;
-  for (;;) {
-    k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, a64, rhs3, R, part);
-    k_sum_partials<<<1, 1024, 0, c->stream>>>(part, (int)nb0, sums);
-    c->launches += 2;
-    double h[2];
-    VG_CUDA(c, cudaMemcpyAsync(h, sums, sizeof(h), cudaMemcpyDeviceToHost, c->stream));
-    VG_CUDA(c, cudaStreamSynchronize(c->stream));
-    relres = h[1] > 0.0 ? std::sqrt(h[0] / h[1]) : std::sqrt(h[0]);
-    if (relres0 < 0.0) relres0 = relres;
-    if (!(relres == relres)) return fail(c, VG_NONFINITE, "multigrid: non-finite residual");
-    if (relres <= tol || cyc >= max_cycles) break;
-    // one V-cycle on the correction
-    for (int l = 0; l < P.nlev; ++l) {
-      const Lev& L = P.lev[l];
-      float* e = E + 3 * L.base;
-      float* r = R + 3 * L.base;
-      float* res = RES + 3 * L.base;
-      const size_t npts = L.g.points();
-      const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
-      if (l == P.nlev - 1) {
-        // Gauss-Seidel on m interior points per axis contracts by about
-        // cos^2(pi / (m + 1)) per sweep: 3 (m + 1)^2 sweeps reduce the error
-        // by ~1e-13, far below what the V-cycle around it needs.
-        unsigned m = std::max(L.g.np[0], std::max(L.g.np[1], L.g.np[2])) - 1;
-        int sweeps = (int)std::min(3u * m * m + 2u, 4000u);
-        const double cx = 1.0 / ((double)L.g.cell[0] * L.g.cell[0]), cy = 1.0 / ((double)L.g.cell[1] * L.g.cell[1]),
-                     cz = 1.0 / ((double)L.g.cell[2] * L.g.cell[2]);
-        k_coarse_solve<<<1, 1024, 0, c->stream>>>(L.g, cx, cy, cz, r, e, cwork, sweeps);
-        VG_LAUNCHED(c);
-        break;
-      }
-      for (int s = 0; s < pre; ++s)
-        for (unsigned col = 0; col < 2; ++col) {
-          k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
-                                                                (s == 0 && col == 0) ? 1 : 0);
-          VG_LAUNCHED(c);
-        }
-      // zero_first only covers the red points; black points read red values
-      // and r, so e needs no clearing as long as the red sweep writes every
-      // red interior point and the black sweep every black one.
-      k_residual32<<<blocks_for(npts, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, e, r, res);
-      const Lev& Cn = P.lev[l + 1];
-      k_restrict<<<blocks_for(Cn.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, res, R + 3 * Cn.base);
-      c->launches += 2;
-    }
-    for (int l = P.nlev - 2; l >= 0; --l) {
-      const Lev& L = P.lev[l];
-      const Lev& Cn = P.lev[l + 1];
-      float* e = E + 3 * L.base;
-      float* r = R + 3 * L.base;
-      const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
-      k_prolong_add<<<blocks_for(L.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, E + 3 * Cn.base, e);
-      VG_LAUNCHED(c);
-      for (int s = 0; s < post; ++s)
-        for (unsigned col = 0; col < 2; ++col) {
-          k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
-          VG_LAUNCHED(c);
-        }
-    }
-    k_add_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(a64, E, 3 * n0);
-    VG_LAUNCHED(c);
-    ++cyc;
+  MgBufs B;
+  B.E = (float*)mem;
+  B.R = B.E + 3 * P.total;
+  B.a64 = (double*)(((uintptr_t)(B.R + 3 * P.total) + 255) & ~(uintptr_t)255);
+  B.part = B.a64 + 3 * n0;
+  B.sums = B.part + 2 * (size_t)nb0;
+  B.cwork = B.sums + 4;
+  B.nb0 = nb0;
+  float* etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
+  float* rir = etot + 3 * n0;                                                                 // IR right-hand side
+  static bool smem_set = false;
+  if (!smem_set) {
+    cudaFuncSetAttribute(k_vcycle_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    smem_set = true;
   }
-  k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(a64, soln3, 3 * n0);
+  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
+               r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
+  // e must be zero on every level's boundary (Dirichlet correction); the
+  // kernels only ever write interior points.
+  VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
+  const Lev& L0 = P.lev[0];
+  k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
+  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
+  c->launches += 2;
+  double rr = 0.0, bnorm2 = 0.0;
+  if ((st = read_norm(c, B, &rr, &bnorm2)) != VG_OK) return st;
+  const double bn = bnorm2 > 0.0 ? std::sqrt(bnorm2) : 1.0;
+  double relres = std::sqrt(rr) / bn;
+  const double relres0 = relres;
+  int cyc = 0;
+  // Phase 1: FP32 cycles on the field itself while FP32 can represent the
+  // residual (relative residual above 1e-4).
+  const double switch_tol = std::max(tol, 1e-4);
+  while (relres > switch_tol && cyc < max_cycles) {
+    if ((st = run_cycle(c, P, g, B, soln3, rhs3, 0)) != VG_OK) return st;
+    ++cyc;
+    if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
+    relres = std::sqrt(rr) / bn;
+  }
+  // Phase 2: iterative refinement.  FP64 residual of the FP64 iterate, FP32
+  // cycles on the correction equation L e = r (its residual updated in FP32,
+  // accurate because r is already small), a64 += e, and an FP64 check.
+  k_to_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.a64, 3 * n0);
+  VG_LAUNCHED(c);
+  for (;;) {
+    k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+    c->launches += 2;
+    if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
+    relres = std::sqrt(rr) / bn;
+    if (relres <= tol || cyc >= max_cycles) break;
+    const double inner_tol = std::max(0.05 * tol, 1e-4 * relres);
+    VG_CUDA(c, cudaMemsetAsync(etot, 0, 3 * n0 * sizeof(float), c->stream));
+    VG_CUDA(c, cudaMemcpyAsync(B.R, rir, 3 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    double inner = relres;
+    while (inner > inner_tol && cyc < max_cycles) {
+      if ((st = run_cycle(c, P, g, B, etot, rir, 1)) != VG_OK) return st;
+      ++cyc;
+      if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
+      inner = std::sqrt(rr) / bn;
+    }
+    k_add_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, etot, 3 * n0);
+    VG_LAUNCHED(c);
+  }
+  k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, soln3, 3 * n0);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   if (cycles_out) *cycles_out = cyc;
