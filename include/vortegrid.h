@@ -34,7 +34,7 @@
 extern "C" {
 #endif
 
-#define VG_ABI_VERSION 1
+#define VG_ABI_VERSION 2
 
 typedef enum vg_status {
   VG_OK = 0,
@@ -71,7 +71,7 @@ typedef enum vg_poisson_solver {
 typedef enum vg_warm_start {
   VG_WARM_ZERO = 0,     /* interior starts at zero (the reference's choice, vortonSim.cpp:2532) */
   VG_WARM_PREVIOUS = 1, /* previous step's solution, when the grid shape is unchanged */
-  VG_WARM_NETWORK = 2   /* the learned 3D U-Net guess (vg_load_network) */
+  VG_WARM_NETWORK = 2   /* the learned 3D U-Net guess (vg_set_network) */
 } vg_warm_start;
 
 /* UniformGridGeometry (Core/SpatialPartition/uniformGrid.h:144-860). */
@@ -113,6 +113,7 @@ typedef struct vg_step_stats {
   float ms_total;            /* device time of the last step (CUDA events) */
   float ms_poisson;          /* device time of the Poisson solve */
   unsigned kernels_launched; /* this library's kernels in the last step */
+  int warm_start_used;       /* vg_warm_start the last Poisson solve started from */
 } vg_step_stats;
 
 typedef struct vg_ctx vg_ctx;
@@ -269,6 +270,65 @@ vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const floa
  *    returns without synchronising.  Errors: vg_last_error(NULL). */
 vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_size, const float* angvel, size_t n,
                             const float* q4, size_t m, float spread_range, float spread_circ, float* out4);
+
+/* ------------------------------------------------------------------------
+ * Learned warm start (no counterpart in the reference).  A 3D U-Net (4 levels,
+ * 16/32/64/128 channels, 3x3x3 convolutions, BF16 weights and activations,
+ * FP32 accumulation) maps the Poisson right-hand side and the Dirichlet
+ * boundary values of an (edge+1)^3 grid to an initial vector potential;
+ * multigrid then finishes the solve to its tolerance.  The network is trained
+ * on this library's own forward and backward kernels.
+ *
+ * A network object owns its device buffers and a stream (the caller's, or one
+ * it creates).  Attached to a context with vg_set_network, it runs on the
+ * context's stream inside vg_step; calls on the network itself must not
+ * overlap a step of that context unless both use the same stream.
+ * Errors: vg_net_last_error(net), or vg_last_error(NULL) from vg_net_create. */
+typedef struct vg_net vg_net;
+
+/* edge: network grid edge = grid points per axis - 1; 32 or a multiple of 64 up to 1024. */
+vg_status vg_net_create(int device, void* stream, unsigned edge, vg_net** out);
+vg_status vg_net_destroy(vg_net* net);
+const char* vg_net_last_error(const vg_net* net);
+/* Number of FP32 parameters: per layer W[27][Co][Ci] (tap = 9(dz+1) + 3(dy+1) + dx+1), then bias[Co]. */
+size_t vg_net_param_count(void);
+vg_status vg_net_set_params(vg_net* net, const float* params, size_t count, float out_scale);
+vg_status vg_net_get_params(vg_net* net, float* params, size_t count, float* out_scale);
+/* Weight file: BF16 weights, FP32 biases and the output scale. */
+vg_status vg_net_save(vg_net* net, const char* path);
+vg_status vg_net_load(vg_net* net, const char* path);
+/* Writes the network's guess into the interior points of vecpot3 (AoS xyz per
+ * point, (edge+1)^3 points), whose boundary points already hold the Dirichlet
+ * values; rhs3 is the solver's right-hand side (minus the vorticity). */
+vg_status vg_net_guess_device(vg_net* net, const vg_grid_geom* g, const float* rhs3, float* vecpot3);
+/* Training: forward + backward on one (right-hand side, converged solution)
+ * pair (FP32, or BF16 when pair_bf16 != 0); the parameter gradients replace
+ * the previous ones, or are added to them when accumulate != 0 (batches).
+ * The loss is the squared error of the interior solution relative to the
+ * solution's own squared norm; loss (optional, host) receives it and makes
+ * the call synchronise. */
+vg_status vg_net_backward_device(vg_net* net, const vg_grid_geom* g, int pair_bf16, const void* rhs3,
+                                 const void* vecpot3, int accumulate, float* loss);
+vg_status vg_net_adam_step(vg_net* net, float lr, float beta1, float beta2, float eps);
+vg_status vg_net_get_grads(vg_net* net, float* grads, size_t count);
+/* FP32 output of the last forward pass: [edge^3][16], channels 0..2 used. */
+vg_status vg_net_get_output(vg_net* net, float* out, size_t count);
+/* BF16 activation `which` of the last forward pass as FP32, channels-last:
+ * 0 input, then enc0a, enc0b, pool1, enc1a, enc1b, pool2, enc2a, enc2b, pool3,
+ * enc3a, enc3b, dec2a, dec2b, dec1a, dec1b, dec0a, dec0b (17). */
+vg_status vg_net_get_activation(vg_net* net, int which, float* out, size_t count);
+/* BF16 gradient of the last backward pass as FP32, channels-last: of_input = 0
+ * the gradient w.r.t. layer `layer`'s pre-activation output (Co channels),
+ * of_input = 1 the gradient w.r.t. its (pooled or concatenated) input
+ * (Ci channels; layers 2, 4, 6, 8, 10, 12 only). */
+vg_status vg_net_get_gradient(vg_net* net, int layer, int of_input, float* out, size_t count);
+vg_status vg_net_synchronize(vg_net* net);
+/* count FP32 values -> BF16 (training pairs), on stream; no context. */
+vg_status vg_net_to_bf16_device(const float* src, void* dst, size_t count, void* stream);
+/* Attach (or detach with NULL) a network; with warm_start = VG_WARM_NETWORK
+ * the Poisson solve starts from its guess whenever the grid has edge+1 points
+ * per axis, and from zero otherwise (vg_step_stats.warm_start_used says which). */
+vg_status vg_set_network(vg_ctx* ctx, vg_net* net);
 
 #ifdef __cplusplus
 }

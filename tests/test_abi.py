@@ -50,7 +50,7 @@ def test_host_calls_without_gpu(built_lib):
     import numpy as np
     import vortegrid_gb300 as vg
     lib = vg.lib()
-    assert lib.vg_abi_version() == 1
+    assert lib.vg_abi_version() == 2
     cfg = vg.Config()
     assert lib.vg_config_default(ctypes.byref(cfg)) == vg.OK
     assert cfg.poisson_tolerance == 1e-6 and cfg.velocity_technique == vg.VELOCITY_POISSON
@@ -77,6 +77,19 @@ def test_create_fails_cleanly_without_gpu(built_lib):
     with pytest.raises(vg.VgError) as e:
         vg.Context()
     assert e.value.status == vg.CUDA_ERROR
+
+
+def test_network_create_fails_cleanly_without_gpu(built_lib):
+    import torch
+    if torch.cuda.is_available():
+        pytest.skip("GPU present")
+    import vortegrid_gb300 as vg
+    assert vg.lib().vg_net_param_count() == 1472976
+    h = ctypes.c_void_p()
+    assert vg.lib().vg_net_create(0, None, 128, ctypes.byref(h)) == vg.CUDA_ERROR
+    assert not h.value
+    assert vg.lib().vg_net_create(0, None, 100, ctypes.byref(h)) == vg.INVALID  # edge/8 must tile
+    assert not h.value
 
 
 def test_invalid_config_rejected(built_lib):

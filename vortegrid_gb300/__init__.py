@@ -105,7 +105,7 @@ class StepStats(ctypes.Structure):
     _fields_ = [("grid", GridGeom), ("tree_depth", ctypes.c_int), ("poisson_cycles", ctypes.c_int),
                 ("poisson_relres", ctypes.c_double), ("poisson_relres0", ctypes.c_double),
                 ("ms_total", ctypes.c_float), ("ms_poisson", ctypes.c_float),
-                ("kernels_launched", ctypes.c_uint)]
+                ("kernels_launched", ctypes.c_uint), ("warm_start_used", ctypes.c_int)]
 
 
 _lib = None
@@ -118,6 +118,11 @@ EXPORTS = [
     "vg_sor_device", "vg_cascade_device", "vg_multigrid_device", "vg_downsample_device", "vg_upsample_device",
     "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
     "vg_evolve_device", "vg_direct_noalloc",
+    "vg_net_create", "vg_net_destroy", "vg_net_last_error", "vg_net_param_count", "vg_net_set_params",
+    "vg_net_get_params", "vg_net_save", "vg_net_load", "vg_net_guess_device", "vg_net_backward_device",
+    "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
+    "vg_net_synchronize",
+    "vg_net_to_bf16_device", "vg_set_network",
 ]
 
 
@@ -177,7 +182,27 @@ def lib():
         L.vg_stretch_device.argtypes = [vp, G, vp, vp, vp, sz, fl]
         L.vg_pse_device.argtypes = [vp, G, vp, vp, sz, fl, fl]
         L.vg_gather_advect_device.argtypes = [vp, G, vp, vp, vp, sz, fl]
-        if L.vg_abi_version() != 1:
+        fp = ctypes.POINTER(ctypes.c_float)
+        L.vg_net_create.argtypes = [i, vp, ctypes.c_uint, ctypes.POINTER(ctypes.c_void_p)]
+        L.vg_net_destroy.argtypes = [vp]
+        L.vg_net_last_error.argtypes = [vp]
+        L.vg_net_last_error.restype = ctypes.c_char_p
+        L.vg_net_param_count.restype = sz
+        L.vg_net_set_params.argtypes = [vp, vp, sz, fl]
+        L.vg_net_get_params.argtypes = [vp, vp, sz, fp]
+        L.vg_net_save.argtypes = [vp, ctypes.c_char_p]
+        L.vg_net_load.argtypes = [vp, ctypes.c_char_p]
+        L.vg_net_guess_device.argtypes = [vp, G, vp, vp]
+        L.vg_net_backward_device.argtypes = [vp, G, i, vp, vp, i, fp]
+        L.vg_net_adam_step.argtypes = [vp, fl, fl, fl, fl]
+        L.vg_net_get_grads.argtypes = [vp, vp, sz]
+        L.vg_net_get_output.argtypes = [vp, vp, sz]
+        L.vg_net_get_activation.argtypes = [vp, i, vp, sz]
+        L.vg_net_get_gradient.argtypes = [vp, i, i, vp, sz]
+        L.vg_net_synchronize.argtypes = [vp]
+        L.vg_net_to_bf16_device.argtypes = [vp, vp, sz, vp]
+        L.vg_set_network.argtypes = [vp, vp]
+        if L.vg_abi_version() != 2:
             raise ImportError("libvortegrid ABI version mismatch")
         _lib = L
     return _lib

@@ -220,7 +220,6 @@ vg_status check_cfg(Ctx* c, const vg_config* cfg) {
   if (cfg->numerics < 0 || cfg->numerics > 1) return fail(c, VG_INVALID, "bad numerics");
   if (cfg->poisson_solver < 0 || cfg->poisson_solver > 1) return fail(c, VG_INVALID, "bad poisson_solver");
   if (cfg->warm_start < 0 || cfg->warm_start > 2) return fail(c, VG_INVALID, "bad warm_start");
-  if (cfg->warm_start == VG_WARM_NETWORK) return fail(c, VG_INVALID, "network warm start needs a loaded network");
   if (!(cfg->viscosity >= 0.0f)) return fail(c, VG_INVALID, "viscosity must be >= 0");
   if (!(cfg->poisson_tolerance > 0.0)) return fail(c, VG_INVALID, "poisson_tolerance must be > 0");
   if (cfg->use_fixed_grid) {
@@ -308,6 +307,7 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
     if ((st = launch_splat(c, g, ps, w, n, cl, -1.0f, radius, negvort)) != VG_OK) return st;
     const bool warm_prev = c->cfg.warm_start == VG_WARM_PREVIOUS && c->have_prev &&
                            memcmp(&c->prev_grid, &g, sizeof(Geom)) == 0;
+    c->stats.warm_start_used = warm_prev ? VG_WARM_PREVIOUS : VG_WARM_ZERO;
     if (warm_prev) {
       float* prev = (float*)c->buf[S_PREV].p;
       VG_CUDA(c, cudaMemcpyAsync(vecpot, prev, pts * 3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
@@ -317,6 +317,11 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
     if ((st = launch_boundary_vecpot(c, t, g, ps, w, n, c->cfg.boundary_copy_odd_x != 0, ref, vecpot)) != VG_OK)
       return st;
     VG_CUDA(c, cudaEventRecord(c->ev2, c->stream));
+    // the network's guess counts as part of the solve's time
+    if (c->cfg.warm_start == VG_WARM_NETWORK && c->net && nn::fits(c->net, g)) {
+      if ((st = nn::guess(c, c->net, g, negvort, vecpot)) != VG_OK) return st;
+      c->stats.warm_start_used = VG_WARM_NETWORK;
+    }
     if (c->cfg.poisson_solver == VG_POISSON_REFERENCE_CASCADE) {
       if ((st = run_cascade(c, g, vecpot, negvort, c->cfg.cascade_steps)) != VG_OK) return st;
     } else {
@@ -483,6 +488,12 @@ vg_status vg_destroy(vg_ctx* c) {
   if (c->ev3) cudaEventDestroy(c->ev3);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c;
+  return VG_OK;
+}
+
+vg_status vg_set_network(vg_ctx* c, vg_net* net) {
+  if (!c) return VG_INVALID;
+  c->net = reinterpret_cast<vg::nn::Net*>(net);
   return VG_OK;
 }
 

@@ -196,8 +196,13 @@ struct MgGraphCache {
   unsigned launches = 0;
 };
 
+namespace nn {
+struct Net;
+}
+
 struct Ctx {
   vg_config cfg;
+  nn::Net* net = nullptr;   // attached warm-start network (not owned)
   MgGraphCache mg_graph[2];  // phase-1 and phase-2 cycle graphs
   cudaStream_t stream = nullptr;
   bool own_stream = false;
@@ -281,5 +286,12 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
                                float dt, bool evolve);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
+
+namespace nn {
+// True when the network applies to grid g ((edge+1)^3 points).
+bool fits(const Net* N, const Geom& g);
+// Writes the network's guess into the interior points of vp (boundary already set).
+vg_status guess(Ctx* c, Net* N, const Geom& g, const float* rhs, float* vp);
+}  // namespace nn
 
 }  // namespace vg
