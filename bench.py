@@ -391,12 +391,12 @@ def vg_grid_points(grid):
 
 
 def poisson_section(vg, torch, stream, local, steps=3):
-    from vortegrid_gb300 import workloads
+    """128^3 vector-potential solve to 1e-6 on the puff workload through the
+    library's own step, from three starts: zero (plain multigrid), the learned
+    network (its guess is timed inside the solve) and the previous frame."""
+    from vortegrid_gb300 import workloads, warmstart
     pos, w, s = workloads.puff(262144, seed=3)
     grid = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [129] * 3)
-    cfg = vg.default_config(fixed_grid=grid, device=local)
-    cfg.stream = stream.cuda_stream
-    ctx = vg.VortonSim(cfg=cfg)
     o = np.zeros((len(pos), 4), np.float32)
     o[:, :3] = pos
     o[:, 3] = s
@@ -404,22 +404,61 @@ def poisson_section(vg, torch, stream, local, steps=3):
     o2 = np.zeros((len(pos), 4), np.float32)
     o2[:, :3] = w
     w0 = torch.from_numpy(o2).cuda()
-    ps, ww, vel = ps0.clone(), w0.clone(), torch.zeros_like(ps0)
-    res = []
-    with torch.cuda.stream(stream):
-        for k in range(steps + 1):
-            ps.copy_(ps0)
-            ww.copy_(w0)
-            ctx.UpdateDevice(ps, ww, vel, float(DT))
-            st = ctx.stats()
-            if k > 0:
-                res.append((st.ms_poisson, st.ms_total, st.poisson_cycles, st.poisson_relres0, st.poisson_relres))
-    ms_p = statistics.median(r[0] for r in res)
-    return {"workload": "puff: 262144 vortons N(0,0.5^2), vorticity N(0,2^2), 129^3 grid on [-2,2]^3 (dx=1/32), "
-                        "treecode boundary, FP32 V(2,2)-cycles in FP64 iterative refinement",
-            "plain_mg_ms": ms_p, "step_ms": statistics.median(r[1] for r in res), "cycles": res[-1][2],
-            "relres0": res[-1][3], "relres": res[-1][4], "tolerance": 1e-6, "nn_warm_start_ms": None,
-            "nn_note": "learned warm start not built yet"}
+
+    def make_ctx(warm):
+        cfg = vg.default_config(fixed_grid=grid, device=local)
+        cfg.stream = stream.cuda_stream
+        cfg.warm_start = warm
+        return vg.VortonSim(cfg=cfg)
+
+    def run(ctx, reset):
+        ps, ww, vel = ps0.clone(), w0.clone(), torch.zeros_like(ps0)
+        res = []
+        with torch.cuda.stream(stream):
+            for k in range(steps + 1):
+                if reset:
+                    ps.copy_(ps0)
+                    ww.copy_(w0)
+                ctx.UpdateDevice(ps, ww, vel, float(DT))
+                st = ctx.stats()
+                if k > 0:
+                    res.append((st.ms_poisson, st.ms_total, st.poisson_cycles, st.poisson_relres0, st.poisson_relres,
+                                st.warm_start_used))
+        return res
+
+    def summary(res):
+        return {"ms": statistics.median(r[0] for r in res), "step_ms": statistics.median(r[1] for r in res),
+                "cycles": res[-1][2], "relres0": res[-1][3], "relres": res[-1][4], "warm_start_used": res[-1][5]}
+
+    def velocity(ctx):
+        v, _ = ctx.GetVelocityGrid()
+        return torch.from_numpy(np.ascontiguousarray(v, np.float64).reshape(-1))
+
+    zero_ctx = make_ctx(0)
+    zero = summary(run(zero_ctx, True))
+    out = {"workload": "puff: 262144 vortons N(0,0.5^2), vorticity N(0,2^2), 129^3 grid on [-2,2]^3 (dx=1/32), "
+                       "treecode boundary, FP32 V(2,2)-cycles in FP64 iterative refinement to 1e-6",
+           "tolerance": 1e-6, "plain_mg_ms": zero["ms"], "step_ms": zero["step_ms"], "cycles": zero["cycles"],
+           "relres0": zero["relres0"], "relres": zero["relres"]}
+    prev = summary(run(make_ctx(1), False))
+    out["previous_frame"] = {"ms": prev["ms"], "cycles": prev["cycles"], "relres0": prev["relres0"],
+                             "relres": prev["relres"], "note": "field evolving one step between solves"}
+    if os.path.exists(warmstart.DEFAULT_WEIGHTS):
+        net = warmstart.Network(warmstart.EDGE, local, stream)
+        net.load(warmstart.DEFAULT_WEIGHTS)
+        nn_ctx = make_ctx(2)
+        nn_ctx.check(vg.lib().vg_set_network(nn_ctx.h, net.h), "vg_set_network")
+        nn = summary(run(nn_ctx, True))
+        v_zero, v_nn = velocity(zero_ctx), velocity(nn_ctx)
+        out["nn_warm_start_ms"] = nn["ms"]
+        out["nn"] = {"ms_including_guess": nn["ms"], "cycles": nn["cycles"], "relres0": nn["relres0"],
+                     "relres": nn["relres"], "warm_start_used": nn["warm_start_used"],
+                     "velocity_rel_diff_vs_plain": float((v_nn - v_zero).norm() / v_zero.norm()),
+                     "speedup_vs_plain_mg": zero["ms"] / nn["ms"]}
+    else:
+        out["nn_warm_start_ms"] = None
+        out["nn_note"] = "no trained weights at " + warmstart.DEFAULT_WEIGHTS
+    return out
 
 
 def main():

@@ -274,3 +274,69 @@ def test_step_uses_network_and_falls_back(ws):
     st = run(EDGE + 9)   # grid does not fit the network: plain zero start
     assert st.warm_start_used == 0
     assert st.poisson_relres <= 1e-6
+
+
+def test_trained_network_gains_over_zero_start(ws):
+    """The committed network on held-out seeded fields (seeds disjoint from
+    training): it starts far closer to the solution than the zero start, never
+    needs more multigrid cycles to the same 1e-6 tolerance, saves cycles in
+    total, and ends at the same solution."""
+    if not os.path.exists(ws.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights")
+    summ, rows = ws.evaluate(ws.DEFAULT_WEIGHTS, fields=4, seed=11, log=None)
+    for r in rows:
+        assert r["zero_relres"] <= 1e-6 and r["nn_relres"] <= 1e-6, r
+        assert r["nn_err0"] < 0.5, r           # the zero start's error is 1 by definition
+        assert r["nn_cycles"] <= r["zero_cycles"], r
+        assert r["nn_vs_zero_solution"] < 1e-3, r
+    assert sum(r["zero_cycles"] - r["nn_cycles"] for r in rows) >= 1, rows
+
+
+def test_network_start_keeps_velocity_error(ws):
+    """Equal velocity error against the FP64 direct-sum oracle: the velocity
+    grids of the zero-start and network-start solves (curl of the vector
+    potential) differ from the FP64 direct sum at sampled interior grid points
+    by the same relative L2 error, to 1e-4 of each other."""
+    import vortegrid_gb300 as vg
+    import oracle
+    if not os.path.exists(ws.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights")
+    oracle.build()
+    s = torch.cuda.Stream()
+    with torch.cuda.stream(s):
+        solver = ws.Solver(0, s)
+        net = ws.Network(ws.EDGE, 0, s)
+        net.load(ws.DEFAULT_WEIGHTS)
+        ps, w = ws.make_field("rings", 9_000_777_001)
+        g = solver.grid
+        n3 = g.capacity * 3
+        rhs = torch.empty(n3, device="cuda")
+        vp0 = torch.empty(n3, device="cuda")
+        solver.rhs(ps, w, rhs)
+        solver.boundary(ps, w, vp0)
+        vels = []
+        for use_net in (False, True):
+            vp = vp0.clone()
+            if use_net:
+                net.guess(g, rhs, vp)
+            cyc, r0, r1 = solver.multigrid(rhs, vp)
+            assert r1 <= 1e-6
+            vel = torch.empty(n3, device="cuda")
+            c = solver.ctx
+            with ws._Ordered(solver.stream):
+                c.check(vg.lib().vg_jacobian_curl_device(c.h, ctypes.byref(g), ctypes.c_void_p(vp.data_ptr()), None,
+                                                         ctypes.c_void_p(vel.data_ptr())), "vg_jacobian_curl_device")
+            vels.append(vel.cpu().numpy().reshape(-1, 3))
+        torch.cuda.synchronize()
+    pos = ps[:, :3].cpu().numpy()
+    angvel = w[:, :3].cpu().numpy()
+    size = ps[:, 3].cpu().numpy()
+    rng = np.random.default_rng(3)
+    np1 = g.points[0]
+    idx = rng.integers(8, np1 - 8, (256, 3))
+    flat = (idx[:, 2] * np1 + idx[:, 1]) * np1 + idx[:, 0]
+    cell = np.float32(g.cell_spacing[0])
+    q = np.float32(g.min_corner[0]) + idx.astype(np.float32) * cell
+    ref = oracle.direct(0, pos, angvel, size, q, f64=True)  # kind 0: velocity
+    errs = [rel(v[flat], ref) for v in vels]
+    assert abs(errs[0] - errs[1]) < 1e-4 * max(1.0, errs[0]) + 1e-6, errs

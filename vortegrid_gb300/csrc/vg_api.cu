@@ -108,6 +108,7 @@ vg_status sync_and_check(Ctx* c, const char* what) {
   VG_CUDA(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
   if (h) {
     VG_CUDA(c, cudaMemset(c->dflag, 0, sizeof(int)));
+    if (h & DF_TIMEOUT) return fail(c, VG_TIMEOUT, std::string(what) + ": a bounded device wait gave up");
     if (h & DF_NONFINITE) return fail(c, VG_NONFINITE, std::string(what) + ": non-finite vorton position");
     return fail(c, VG_OUT_OF_GRID, std::string(what) + ": a particle lies outside the grid's cells");
   }

@@ -220,7 +220,7 @@ struct Ctx {
 };
 
 // Device-side error bits, reported at the next synchronising call.
-enum DevFlag { DF_OUT_OF_GRID = 1, DF_NONFINITE = 2 };
+enum DevFlag { DF_OUT_OF_GRID = 1, DF_NONFINITE = 2, DF_TIMEOUT = 4 };
 vg_status sync_and_check(Ctx* c, const char* what);
 
 // Workspace: returns a device buffer of at least `bytes` for slot s.

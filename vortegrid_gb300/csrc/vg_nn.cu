@@ -593,6 +593,8 @@ vg_status alloc_net(Net* N) {
   if ((st = device_alloc(c, &N->scales, 4)) != VG_OK) return st;
   if ((st = device_alloc(c, &N->partials, kRedBlocks)) != VG_OK) return st;
   if ((st = device_alloc(c, &N->loss, 4)) != VG_OK) return st;
+  if ((st = device_alloc(c, &c->dflag, 64)) != VG_OK) return st;
+  VG_CUDA(c, cudaMemset(c->dflag, 0, 64 * sizeof(int)));
   VG_CUDA(c, cudaMemset(N->master, 0, off * sizeof(float)));
   return VG_OK;
 }
@@ -617,7 +619,7 @@ vg_status alloc_training(Net* N) {
 
 void free_net(Net* N) {
   if (N->ctx.stream) cudaStreamSynchronize(N->ctx.stream);
-  void* ps[] = {N->master, N->grad, N->m1, N->m2, N->w, N->wt, N->out, N->scales, N->partials, N->loss};
+  void* ps[] = {N->master, N->grad, N->m1, N->m2, N->w, N->wt, N->out, N->scales, N->partials, N->loss, N->ctx.dflag};
   for (void* p : ps)
     if (p) cudaFree(p);
   for (int a = 0; a < A_NUM; ++a)
@@ -755,7 +757,7 @@ vg_status vg_net_set_params(vg_net* N, const float* params, size_t count, float 
   N->out_scale = out_scale;
   vg_status st = refresh_bf16(c, N);
   if (st != VG_OK) return net_status(N, st);
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   if (N->m1) {
     VG_CUDA(c, cudaMemset(N->m1, 0, N->nparam * sizeof(float)));
     VG_CUDA(c, cudaMemset(N->m2, 0, N->nparam * sizeof(float)));
@@ -769,7 +771,7 @@ vg_status vg_net_get_params(vg_net* N, float* params, size_t count, float* out_s
   if (!N || !params) return VG_INVALID;
   if (count != N->nparam) return fail(&N->ctx, VG_INVALID, "vg_net_get_params: wrong parameter count");
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   VG_CUDA(c, cudaMemcpy(params, N->master, count * sizeof(float), cudaMemcpyDeviceToHost));
   if (out_scale) *out_scale = N->out_scale;
   return VG_OK;
@@ -779,7 +781,7 @@ vg_status vg_net_get_grads(vg_net* N, float* grads, size_t count) {
   if (!N || !grads) return VG_INVALID;
   if (count != N->nparam || !N->grad) return fail(&N->ctx, VG_INVALID, "vg_net_get_grads: no gradients");
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   VG_CUDA(c, cudaMemcpy(grads, N->grad, count * sizeof(float), cudaMemcpyDeviceToHost));
   return VG_OK;
 }
@@ -788,7 +790,7 @@ vg_status vg_net_get_output(vg_net* N, float* out, size_t count) {
   if (!N || !out) return VG_INVALID;
   if (count != N->vox(0) * 16) return fail(&N->ctx, VG_INVALID, "vg_net_get_output: count must be edge^3 * 16");
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   VG_CUDA(c, cudaMemcpy(out, N->out, count * sizeof(float), cudaMemcpyDeviceToHost));
   return VG_OK;
 }
@@ -798,7 +800,7 @@ vg_status vg_net_get_activation(vg_net* N, int which, float* out, size_t count) 
   const size_t cnt = N->vox(kActLevel[which]) * kActC[which];
   if (count != cnt) return fail(&N->ctx, VG_INVALID, "vg_net_get_activation: wrong count");
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   std::vector<uint16_t> b(cnt);
   VG_CUDA(c, cudaMemcpy(b.data(), N->act[which], cnt * 2, cudaMemcpyDeviceToHost));
   for (size_t i = 0; i < cnt; ++i) out[i] = bf_bits2f(b[i]);
@@ -812,7 +814,7 @@ vg_status vg_net_get_gradient(vg_net* N, int layer, int of_input, float* out, si
   const size_t cnt = N->vox(kNet[layer].level) * (of_input ? kNet[layer].ci : kNet[layer].co);
   if (count != cnt) return fail(&N->ctx, VG_INVALID, "vg_net_get_gradient: wrong count");
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   std::vector<uint16_t> b(cnt);
   VG_CUDA(c, cudaMemcpy(b.data(), src, cnt * 2, cudaMemcpyDeviceToHost));
   for (size_t i = 0; i < cnt; ++i) out[i] = bf_bits2f(b[i]);
@@ -881,7 +883,7 @@ vg_status vg_net_backward_device(vg_net* N, const vg_grid_geom* g, int pair_bf16
                    : backward_pair<float>(c, N, G, (const float*)rhs3, (const float*)vecpot3, accumulate != 0);
   if (st != VG_OK) return net_status(N, st);
   if (loss) {
-    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+    if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
     VG_CUDA(c, cudaMemcpy(loss, N->loss, sizeof(float), cudaMemcpyDeviceToHost));
   }
   return VG_OK;
@@ -911,7 +913,7 @@ vg_status vg_net_to_bf16_device(const float* src, void* dst, size_t count, void*
 vg_status vg_net_synchronize(vg_net* N) {
   if (!N) return VG_INVALID;
   Ctx* c = &N->ctx;
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  if (vg_status sst = sync_and_check(c, "network"); sst != VG_OK) return sst;
   return VG_OK;
 }
 

@@ -40,6 +40,10 @@ struct ConvOut {
 bool conv_shape_ok(int D, int H, int W, int C1, int C2, int Co);
 size_t conv3_fwd_smem(int D, int H, int W, int co_t);
 vg_status conv3_fwd(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const ConvOut& out);
+// The tcgen05 form (tiles of 8 x 16 voxels; needs W % 8 == 0, H % 16 == 0, the
+// weights of one output-channel group within shared memory, and c->dflag for
+// its timeout bit); *handled says whether it ran.
+vg_status conv3_fwd_umma(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const ConvOut& out, bool* handled);
 // dW[27][Co][Ci] += sum over voxels of dY (x) X_tap  (FP32, accumulated atomically)
 vg_status conv3_wgrad(Ctx* c, const ConvIn& in, const __nv_bfloat16* dy, int Co, float* dw);
 

@@ -19,6 +19,8 @@
 //    ldmatrix.trans operands; a CTA owns one 16 x 16 (co, ci) block and strides
 //    over voxel tiles, each warp owns a quarter of the taps, and the FP32
 //    partials are added to dW atomically once per CTA.
+#include <algorithm>
+
 #include "vg_nn.cuh"
 
 namespace vg {
@@ -121,6 +123,48 @@ __device__ __forceinline__ int centre_slot(const Tile& T, int v) {
   return ((vz + 1) * (T.ty + 2) + vy + 1) * (T.tx + 2) + vx + 1;
 }
 
+// Epilogue of one output tile: C fragment rows (voxels) lane/4 and lane/4 + 8,
+// columns 2 (lane % 4) + {0, 1}; + bias, activation, mask, store.
+template <int CO_T>
+__device__ __forceinline__ void store_tile(const float (&acc)[kMT][CO_T / 8][4], const bool (&active)[kMT],
+                                           const ConvIn& in, const ConvOut& out, const Tile& T, int x0, int y0, int z0,
+                                           int co0) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int g = lane >> 2, q2 = (lane & 3) * 2, Co = out.Co;
+#pragma unroll
+  for (int mt = 0; mt < kMT; ++mt) {
+    if (!active[mt]) continue;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int v = (warp * kMT + mt) * 16 + g + 8 * h;
+      const int vx = x0 + v % T.tx, vy = y0 + (v / T.tx) % T.ty, vz = z0 + v / (T.tx * T.ty);
+      const size_t vox = ((size_t)vz * in.H + vy) * in.W + vx;
+#pragma unroll
+      for (int n = 0; n < CO_T / 8; ++n) {
+        const int co = co0 + n * 8 + q2;
+        float v0 = acc[mt][n][2 * h], v1 = acc[mt][n][2 * h + 1];
+        if (out.bias) {
+          v0 += out.bias[co];
+          v1 += out.bias[co + 1];
+        }
+        if (out.relu) {
+          v0 = v0 > 0.f ? v0 : out.slope * v0;
+          v1 = v1 > 0.f ? v1 : out.slope * v1;
+        }
+        if (out.mask) {
+          const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(out.mask + vox * Co + co);
+          if (!(__bfloat162float(mk.x) > 0.f)) v0 *= out.mask_slope;
+          if (!(__bfloat162float(mk.y) > 0.f)) v1 *= out.mask_slope;
+        }
+        if (out.yf)
+          *reinterpret_cast<float2*>(out.yf + vox * Co + co) = make_float2(v0, v1);
+        else
+          *reinterpret_cast<__nv_bfloat162*>(out.y + vox * Co + co) = __floats2bfloat162_rn(v0, v1);
+      }
+    }
+  }
+}
+
 template <int CO_T>
 __global__ void __launch_bounds__(kWarps * 32) k_conv3_fwd(const ConvIn in, const __nv_bfloat16* __restrict__ wt,
                                                            const ConvOut out) {
@@ -176,39 +220,129 @@ __global__ void __launch_bounds__(kWarps * 32) k_conv3_fwd(const ConvIn in, cons
       }
     }
   }
-  // C fragment: rows (voxels) lane/4 and lane/4 + 8, columns 2 (lane % 4) + {0, 1}
-  const int g = lane >> 2, q2 = (lane & 3) * 2;
-#pragma unroll
-  for (int mt = 0; mt < kMT; ++mt) {
-    if (!active[mt]) continue;
-#pragma unroll
-    for (int h = 0; h < 2; ++h) {
-      const int v = (warp * kMT + mt) * 16 + g + 8 * h;
-      const int vx = x0 + v % T.tx, vy = y0 + (v / T.tx) % T.ty, vz = z0 + v / (T.tx * T.ty);
-      const size_t vox = ((size_t)vz * in.H + vy) * in.W + vx;
-#pragma unroll
-      for (int n = 0; n < CO_T / 8; ++n) {
-        const int co = co0 + n * 8 + q2;
-        float v0 = acc[mt][n][2 * h], v1 = acc[mt][n][2 * h + 1];
-        if (out.bias) {
-          v0 += out.bias[co];
-          v1 += out.bias[co + 1];
+  store_tile<CO_T>(acc, active, in, out, T, x0, y0, z0, co0);
+}
+
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem, int src_bytes) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16, %2;\n" ::"r"(smem_u32(smem)), "l"(gmem), "r"(src_bytes));
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::); }
+__device__ __forceinline__ void cp_async_wait_all_but_newest() { asm volatile("cp.async.wait_group 1;\n" ::); }
+
+// Issues asynchronous copies of one 16-channel slice of a tile's halo into sx;
+// voxels outside the volume are zero-filled (a 0-byte source read).
+__device__ __forceinline__ void issue_halo(uint4* sx, const Tile& T, const ConvIn& in, int x0, int y0, int z0,
+                                           int ci0) {
+  const int hx = T.tx + 2, hy = T.ty + 2, nh = hx * hy * (T.tz + 2);
+  for (int s = threadIdx.x; s < nh; s += blockDim.x) {
+    const int ix = s % hx, iy = (s / hx) % hy, iz = s / (hx * hy);
+    const int z = z0 + iz - 1, y = y0 + iy - 1, x = x0 + ix - 1;
+    const bool inside = z >= 0 && y >= 0 && x >= 0 && z < in.D && y < in.H && x < in.W;
+    const __nv_bfloat16* p = in.x1;  // a valid address when nothing is read
+    if (inside) {
+      if (ci0 < in.C1) {
+        if (in.up1) {
+          const int H1 = in.H >> 1, W1 = in.W >> 1;
+          p = in.x1 + (((size_t)(z >> 1) * H1 + (y >> 1)) * W1 + (x >> 1)) * in.C1 + ci0;
+        } else {
+          p = in.x1 + (((size_t)z * in.H + y) * in.W + x) * in.C1 + ci0;
         }
-        if (out.relu) {
-          v0 = v0 > 0.f ? v0 : out.slope * v0;
-          v1 = v1 > 0.f ? v1 : out.slope * v1;
-        }
-        if (out.mask) {
-          const __nv_bfloat162 mk = *reinterpret_cast<const __nv_bfloat162*>(out.mask + vox * Co + co);
-          if (!(__bfloat162float(mk.x) > 0.f)) v0 *= out.mask_slope;
-          if (!(__bfloat162float(mk.y) > 0.f)) v1 *= out.mask_slope;
-        }
-        if (out.yf)
-          *reinterpret_cast<float2*>(out.yf + vox * Co + co) = make_float2(v0, v1);
-        else
-          *reinterpret_cast<__nv_bfloat162*>(out.y + vox * Co + co) = __floats2bfloat162_rn(v0, v1);
+      } else {
+        p = in.x2 + (((size_t)z * in.H + y) * in.W + x) * in.C2 + (ci0 - in.C1);
       }
     }
+    const int nb = inside ? 16 : 0;
+    cp_async16(sx + chunk_at(s, 0), p, nb);
+    cp_async16(sx + chunk_at(s, 1), p + 8, nb);
+  }
+}
+
+// Persistent form of k_conv3_fwd for layers whose weights (one output-channel
+// group, every input slice) fit in shared memory: each CTA keeps its group's
+// weights resident, walks its tiles (blockIdx / ncog, then every
+// gridDim / ncog) slice by slice, and copies the next slice's halo with
+// cp.async while the tensor cores work on the current one (two buffers).
+template <int CO_T>
+__global__ void __launch_bounds__(kWarps * 32) k_conv3_fwd_resident(const ConvIn in,
+                                                                    const __nv_bfloat16* __restrict__ wt,
+                                                                    const ConvOut out, int ncog) {
+  extern __shared__ __align__(16) uint4 smem4[];
+  const Tile T = make_tile(in.D, in.H, in.W);
+  const int hx = T.tx + 2, hy = T.ty + 2, nh = hx * hy * (T.tz + 2);
+  const int Ci = in.C1 + in.C2, nsl = Ci / 16, Co = out.Co;
+  const int wrows = 27 * CO_T;
+  uint4* sw = smem4;  // row i = slice * wrows + tap * CO_T + co, two chunks each
+  uint4* sxb0 = sw + 2 * wrows * nsl;
+  uint4* sxb1 = sxb0 + 2 * nh;
+  const int co0 = (blockIdx.x % ncog) * CO_T;
+  const int t0 = blockIdx.x / ncog, tstride = gridDim.x / ncog;
+  const int ntiles = T.nx * T.ny * T.nz;
+  if (t0 >= ntiles) return;  // whole CTA: no barrier is skipped by part of it
+  const int nst = ((ntiles - t0 + tstride - 1) / tstride) * nsl;
+  for (int i = threadIdx.x; i < wrows * nsl; i += blockDim.x) {
+    const int sl = i / wrows, r = i % wrows, tap = r / CO_T, co = r % CO_T;
+    const __nv_bfloat16* src = wt + ((size_t)tap * Co + co0 + co) * Ci + sl * 16;
+    cp_async16(sw + chunk_at(i, 0), src, 16);
+    cp_async16(sw + chunk_at(i, 1), src + 8, 16);
+  }
+  {
+    int x0, y0, z0;
+    tile_origin(T, t0, x0, y0, z0);
+    issue_halo(sxb0, T, in, x0, y0, z0, 0);
+  }
+  cp_async_commit();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  int cslot[kMT];
+  bool active[kMT];
+#pragma unroll
+  for (int mt = 0; mt < kMT; ++mt) {
+    const int m0 = (warp * kMT + mt) * 16;
+    active[mt] = m0 < T.vox;
+    cslot[mt] = active[mt] ? centre_slot(T, m0 + (lane & 15)) : 0;
+  }
+  float acc[kMT][CO_T / 8][4];
+#pragma unroll
+  for (int mt = 0; mt < kMT; ++mt)
+#pragma unroll
+    for (int n = 0; n < CO_T / 8; ++n) acc[mt][n][0] = acc[mt][n][1] = acc[mt][n][2] = acc[mt][n][3] = 0.f;
+  for (int st = 0; st < nst; ++st) {
+    if (st + 1 < nst) {
+      int x0, y0, z0;
+      tile_origin(T, t0 + ((st + 1) / nsl) * tstride, x0, y0, z0);
+      issue_halo((st + 1) & 1 ? sxb1 : sxb0, T, in, x0, y0, z0, ((st + 1) % nsl) * 16);
+    }
+    cp_async_commit();
+    cp_async_wait_all_but_newest();
+    __syncthreads();
+    const uint4* sx = st & 1 ? sxb1 : sxb0;
+    const int rbase = (st % nsl) * wrows;
+#pragma unroll 1
+    for (int tap = 0; tap < 27; ++tap) {
+      const int off = ((tap / 9 - 1) * hy + ((tap / 3) % 3 - 1)) * hx + (tap % 3 - 1);
+      unsigned a[kMT][4];
+#pragma unroll
+      for (int mt = 0; mt < kMT; ++mt)
+        if (active[mt]) ldsm_x4(sx + chunk_at(cslot[mt] + off, lane >> 4), a[mt][0], a[mt][1], a[mt][2], a[mt][3]);
+#pragma unroll
+      for (int n = 0; n < CO_T / 8; ++n) {
+        const int row = rbase + tap * CO_T + n * 8 + (lane & 7);
+        unsigned b0, b1;
+        ldsm_x2(sw + chunk_at(row, (lane >> 3) & 1), b0, b1);
+#pragma unroll
+        for (int mt = 0; mt < kMT; ++mt)
+          if (active[mt]) mma_bf16(acc[mt][n], a[mt][0], a[mt][1], a[mt][2], a[mt][3], b0, b1);
+      }
+    }
+    if (st % nsl == nsl - 1) {
+      int x0, y0, z0;
+      tile_origin(T, t0 + (st / nsl) * tstride, x0, y0, z0);
+      store_tile<CO_T>(acc, active, in, out, T, x0, y0, z0, co0);
+#pragma unroll
+      for (int mt = 0; mt < kMT; ++mt)
+#pragma unroll
+        for (int n = 0; n < CO_T / 8; ++n) acc[mt][n][0] = acc[mt][n][1] = acc[mt][n][2] = acc[mt][n][3] = 0.f;
+    }
+    __syncthreads();  // the buffer just read is refilled by the next iteration's copies
   }
 }
 
@@ -298,14 +432,62 @@ size_t conv3_fwd_smem(int D, int H, int W, int co_t) {
   return (2 * nh + 2 * 27 * (size_t)co_t) * 16;
 }
 
+namespace {
+
+constexpr size_t kResidentWeightBytes = 100 * 1024;
+
+template <int CO_T>
+vg_status launch_resident(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const ConvOut& out) {
+  const Tile T = make_tile(in.D, in.H, in.W);
+  const int Ci = in.C1 + in.C2, ncog = out.Co / CO_T;
+  const size_t nh = (size_t)(T.tx + 2) * (T.ty + 2) * (T.tz + 2);
+  const size_t smem = (2 * 27 * (size_t)CO_T * (Ci / 16) + 4 * nh) * 16;
+  VG_CUDA(c, cudaFuncSetAttribute(k_conv3_fwd_resident<CO_T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                  (int)smem));
+  int per_sm = 0;
+  VG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_fwd_resident<CO_T>, kWarps * 32, smem));
+  const long items = (long)T.nx * T.ny * T.nz * ncog;
+  long grid = std::min<long>(items, (long)std::max(per_sm, 1) * kSMs);
+  grid = std::max<long>(ncog, grid / ncog * ncog);
+  k_conv3_fwd_resident<CO_T><<<(unsigned)grid, kWarps * 32, smem, c->stream>>>(in, wt, out, ncog);
+  VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+}  // namespace
+
 vg_status conv3_fwd(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const ConvOut& out) {
   if (!conv_shape_ok(in.D, in.H, in.W, in.C1, in.C2, out.Co) || (in.up1 && (in.D % 2 || in.H % 2 || in.W % 2)) ||
       (!out.y && !out.yf))
     return fail(c, VG_INVALID, "conv3: unsupported shape");
+  {
+    bool handled = false;
+    const vg_status st = conv3_fwd_umma(c, in, wt, out, &handled);
+    if (handled || st != VG_OK) return st;
+  }
   const Tile T = make_tile(in.D, in.H, in.W);
-  const int co_t = out.Co % 64 == 0 ? 64 : (out.Co % 32 == 0 ? 32 : 16);
+  const size_t Ci = (size_t)(in.C1 + in.C2);
+  // weights resident in shared memory when one output-channel group's fit
+  for (int co_t : {64, 32, 16}) {
+    if (out.Co % co_t || 27 * (size_t)co_t * Ci * 2 > kResidentWeightBytes) continue;
+    if (co_t == 64) return launch_resident<64>(c, in, wt, out);
+    if (co_t == 32) return launch_resident<32>(c, in, wt, out);
+    return launch_resident<16>(c, in, wt, out);
+  }
+  // otherwise weights stream with the halo, slice by slice; the group width is
+  // the widest that still gives two CTAs per SM
+  const long tiles = (long)T.nx * T.ny * T.nz;
+  int co_t = 16;
+  for (int w : {64, 32}) {
+    if (out.Co % w == 0 && tiles * (out.Co / w) >= 2L * kSMs) {
+      co_t = w;
+      break;
+    }
+  }
+  if (out.Co % 32 && co_t != 16) co_t = 16;
   const size_t smem = conv3_fwd_smem(in.D, in.H, in.W, co_t);
-  const dim3 grid((unsigned)(T.nx * T.ny * T.nz), (unsigned)(out.Co / co_t));
+  const dim3 grid((unsigned)tiles, (unsigned)(out.Co / co_t));
   if (co_t == 64) {
     set_fwd_smem_attr<64>();
     k_conv3_fwd<64><<<grid, kWarps * 32, smem, c->stream>>>(in, wt, out);

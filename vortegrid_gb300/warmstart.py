@@ -446,18 +446,31 @@ def _evaluate(torch, stream, weights, fields, seed, device, log, dt):
         solver.rhs(ps, w, rhs)
         solver.boundary(ps, w, vp0)
         row = {"kind": kind}
-        vp.copy_(vp0)
-        (row["zero_cycles"], _, row["zero_relres"]), row["zero_ms"] = timed(lambda: solver.multigrid(rhs, vp))
-        vp.copy_(prev)
-        # keep this frame's boundary values; interior from the previous frame
         bmask = boundary_mask(torch, pts_axis=solver.grid.num_points[0])
+        interior = ~bmask
+        vp.copy_(vp0)
+        (row["zero_cycles"], row["zero_relres0"], row["zero_relres"]), row["zero_ms"] = timed(
+            lambda: solver.multigrid(rhs, vp))
+        sol = vp[interior].double()
+        sol_norm = float(sol.norm())
+
+        def start_error(start):
+            return float((start[interior].double() - sol).norm()) / sol_norm
+
+        # previous frame: this frame's boundary values, the interior of the previous frame's solution
+        vp.copy_(prev)
         vp[bmask] = vp0[bmask]
-        (row["prev_cycles"], _, row["prev_relres"]), row["prev_ms"] = timed(lambda: solver.multigrid(rhs, vp))
+        row["prev_err0"] = start_error(vp)
+        (row["prev_cycles"], row["prev_relres0"], row["prev_relres"]), row["prev_ms"] = timed(
+            lambda: solver.multigrid(rhs, vp))
         vp.copy_(vp0)
         _, row["nn_guess_ms"] = timed(lambda: net.guess(solver.grid, rhs, vp))
+        row["nn_err0"] = start_error(vp)
         (row["nn_cycles"], row["nn_relres0"], row["nn_relres"]), row["nn_mg_ms"] = timed(
             lambda: solver.multigrid(rhs, vp))
         row["nn_ms"] = row["nn_guess_ms"] + row["nn_mg_ms"]
+        # both solves end at the same tolerance: their solutions agree to about it
+        row["nn_vs_zero_solution"] = float((vp[interior].double() - sol).norm()) / sol_norm
         rows.append(row)
         if log and (f + 1) % 20 == 0:
             log(f"eval {f + 1}/{fields}: " + json.dumps(summarise(rows)))
@@ -481,7 +494,7 @@ def boundary_mask(torch, pts_axis):
 def summarise(rows):
     out = {"fields": len(rows)}
     for k in ("zero_cycles", "prev_cycles", "nn_cycles", "zero_ms", "prev_ms", "nn_guess_ms", "nn_mg_ms", "nn_ms",
-              "nn_relres0"):
+              "zero_relres0", "prev_relres0", "nn_relres0", "prev_err0", "nn_err0", "nn_vs_zero_solution"):
         v = [r[k] for r in rows]
         out[k] = float(np.median(v))
         out[k + "_mean"] = float(np.mean(v))
