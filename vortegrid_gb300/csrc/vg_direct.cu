@@ -117,6 +117,87 @@ __global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restri
   }
 }
 
+// Velocity (KIND 0) with packed FP32x2 arithmetic (FADD2 / FMUL2 / FFMA2):
+// each thread carries its 8 targets as 4 pairs, and every source is staged in
+// shared memory already duplicated into pairs (-p, 1/R, w, -w), so each
+// operation below advances two targets in one instruction.  The per-target
+// operations and their order are those of k_direct_fast<0>, so the results are
+// bit-identical to it; only the instruction count changes (about 11 issue
+// slots per interaction instead of 19).
+// 8 targets per thread with registers capped for 4 resident CTAs per SM was
+// the fastest of the shapes measured on GB300 (4 to 16 targets, 1 to 8 CTAs;
+// scalar accumulation FFMAs mixed in were slower): the FFMA2s all run on the
+// heavy half of the FMA pipe, which the profile shows ~70% busy.
+constexpr int kPairTPT = 8;
+
+__global__ void __launch_bounds__(kThreads, 4)
+    k_direct_pair(const float4* __restrict__ s0, const float4* __restrict__ s1, int n, int chunk,
+                  const float4* __restrict__ q, int m, float* __restrict__ partial) {
+  constexpr int kPairs = kPairTPT / 2;
+  __shared__ float4 sh[5 * kTile];
+  const int base = blockIdx.x * (kThreads * kPairTPT) + threadIdx.x;
+  float2 qx[kPairs], qy[kPairs], qz[kPairs], ax[kPairs], ay[kPairs], az[kPairs];
+#pragma unroll
+  for (int pr = 0; pr < kPairs; ++pr) {
+    const int j0 = base + 2 * pr * kThreads, j1 = j0 + kThreads;
+    const float4 v0 = (j0 < m) ? q[j0] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 v1 = (j1 < m) ? q[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    qx[pr] = make_float2(v0.x, v1.x);
+    qy[pr] = make_float2(v0.y, v1.y);
+    qz[pr] = make_float2(v0.z, v1.z);
+    ax[pr] = ay[pr] = az[pr] = make_float2(0.f, 0.f);
+  }
+  const int k0 = blockIdx.y * chunk;
+  const int k1 = min(n, k0 + chunk);
+  for (int tile = k0; tile < k1; tile += kTile) {
+    const int cnt = min(kTile, k1 - tile);
+    __syncthreads();
+    for (int i = threadIdx.x; i < cnt; i += kThreads) {
+      const float4 p = s0[tile + i], a = s1[tile + i];
+      sh[5 * i + 0] = make_float4(-p.x, -p.x, -p.y, -p.y);
+      sh[5 * i + 1] = make_float4(-p.z, -p.z, p.w, p.w);
+      sh[5 * i + 2] = make_float4(a.x, a.x, a.y, a.y);
+      sh[5 * i + 3] = make_float4(a.z, a.z, -a.x, -a.x);
+      sh[5 * i + 4] = make_float4(-a.y, -a.y, -a.z, -a.z);
+    }
+    __syncthreads();
+#pragma unroll 2
+    for (int i = 0; i < cnt; ++i) {
+      const float4 e0 = sh[5 * i], e1 = sh[5 * i + 1], e2 = sh[5 * i + 2], e3 = sh[5 * i + 3], e4 = sh[5 * i + 4];
+      const float2 np0 = make_float2(e0.x, e0.y), np1 = make_float2(e0.z, e0.w), np2 = make_float2(e1.x, e1.y);
+      const float invr = e1.z;
+      const float2 wx = make_float2(e2.x, e2.y), wy = make_float2(e2.z, e2.w), wz = make_float2(e3.x, e3.y);
+      const float2 nwx = make_float2(e3.z, e3.w), nwy = make_float2(e4.x, e4.y), nwz = make_float2(e4.z, e4.w);
+#pragma unroll
+      for (int pr = 0; pr < kPairs; ++pr) {
+        const float2 d0 = __fadd2_rn(qx[pr], np0), d1 = __fadd2_rn(qy[pr], np1), d2 = __fadd2_rn(qz[pr], np2);
+        const float2 r2 = __ffma2_rn(d0, d0, __ffma2_rn(d1, d1, __fmul2_rn(d2, d2)));
+        const float2 inv = make_float2(fminf(rsqrt_ftz(r2.x), invr), fminf(rsqrt_ftz(r2.y), invr));
+        const float2 law = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+        const float2 b0 = __fmul2_rn(d0, law), b1 = __fmul2_rn(d1, law), b2 = __fmul2_rn(d2, law);
+        ax[pr] = __ffma2_rn(wy, b2, __ffma2_rn(nwz, b1, ax[pr]));
+        ay[pr] = __ffma2_rn(wz, b0, __ffma2_rn(nwx, b2, ay[pr]));
+        az[pr] = __ffma2_rn(wx, b1, __ffma2_rn(nwy, b0, az[pr]));
+      }
+    }
+  }
+  float* out = partial + (size_t)blockIdx.y * m * 3;
+#pragma unroll
+  for (int pr = 0; pr < kPairs; ++pr) {
+    const int j0 = base + 2 * pr * kThreads, j1 = j0 + kThreads;
+    if (j0 < m) {
+      out[3 * j0] = ax[pr].x;
+      out[3 * j0 + 1] = ay[pr].x;
+      out[3 * j0 + 2] = az[pr].x;
+    }
+    if (j1 < m) {
+      out[3 * j1] = ax[pr].y;
+      out[3 * j1 + 1] = ay[pr].y;
+      out[3 * j1 + 2] = az[pr].y;
+    }
+  }
+}
+
 __global__ void k_reduce_partials(const float* __restrict__ partial, int ksplit, int m, float4* __restrict__ out) {
   int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
@@ -161,7 +242,7 @@ unsigned direct_slots(int kind) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (kind == 0)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_fast<0>, kThreads, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_pair, kThreads, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_fast<1>, kThreads, 0);
     cudaGetLastError();
@@ -193,7 +274,7 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
   // Split the sources into `ksplit` chunks so that target blocks x chunks
   // fills the resident CTA slots of the GPU (SMs x CTAs per SM) once, with no
   // partial second wave; every CTA then does the same amount of work.
-  const unsigned tblocks = blocks_for(m, kThreads * kTPT);
+  const unsigned tblocks = blocks_for(m, kThreads * (kind == 0 ? kPairTPT : kTPT));
   const unsigned slots = direct_slots(kind);
   unsigned ksplit = std::max(1u, slots / tblocks);
   const size_t min_chunk = 64;  // keep each CTA's source loop long enough to amortise its set-up
@@ -214,7 +295,7 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
   VG_LAUNCHED(c);
   dim3 grid(tblocks, ksplit);
   if (kind == 0)
-    k_direct_fast<0><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
+    k_direct_pair<<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
   else
     k_direct_fast<1><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
   VG_LAUNCHED(c);
