@@ -188,23 +188,64 @@ __device__ __forceinline__ void rbgs_point(const Geom& g, float r2x, float r2y, 
   }
 }
 
-// Point red-black Gauss-Seidel on L e = r (FP32).  One thread per x-pair:
-// updates the point of `color` among (2j, 2j+1).  zero_first: e is zero
-// before this sweep, so the red points take -r H directly.
+// Point red-black Gauss-Seidel on L e = r (FP32).  One thread per component
+// of a point of `color` (x = 2j + parity, components c = 0..2 adjacent), so a
+// warp reads ~11 points' worth of consecutive floats of the AoS field instead
+// of 32 points 24 bytes apart.  zero_first: e is zero before this sweep, so the
+// red points take -r H directly.
 __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, float r2z, float H,
                                               float* __restrict__ e, const float* __restrict__ r, unsigned color,
                                               int zero_first) {
   const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
-  const unsigned half = (nx + 1) / 2;
+  const unsigned half3 = 3 * ((nx + 1) / 2);
   const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ny * nz * half) return;
-  const unsigned row = t / half;
-  const unsigned j = t - row * half;
+  if (t >= ny * nz * half3) return;
+  const unsigned row = t / half3;
+  const unsigned jc = t - row * half3;
+  const unsigned j = jc / 3, c = jc - 3 * j;
   const unsigned z = row / ny, y = row - z * ny;
   if (y == 0 || z == 0 || y + 1 >= ny || z + 1 >= nz) return;
   const unsigned x = 2 * j + ((y + z + color) & 1u);
   if (x == 0 || x + 1 >= nx) return;
-  rbgs_point(g, r2x, r2y, r2z, H, e, r, x + (size_t)nx * (y + (size_t)ny * z), zero_first != 0);
+  const size_t k = x + (size_t)nx * (y + (size_t)ny * z);
+  const size_t sy = nx, sz = (size_t)nx * ny;
+  float v;
+  if (zero_first) {
+    v = -r[3 * k + c] * H;
+  } else {
+    const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
+    const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
+    const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
+    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[3 * k + c]) * H;
+  }
+  e[3 * k + c] = v;
+}
+
+// The last half sweep of a cycle fused with x += e: threads cover every
+// (point, component); points of `color` take their smoothed value and add it
+// to x, the others (already final) just add theirs.  Boundary points carry no
+// correction.
+__global__ void __launch_bounds__(256) k_rbgs_add(Geom g, float r2x, float r2y, float r2z, float H,
+                                                  float* __restrict__ e, const float* __restrict__ r,
+                                                  unsigned color, float* __restrict__ x_out) {
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
+  if (t >= 3u * (unsigned)g.points()) return;
+  const unsigned k = t / 3u, c = t - 3u * k;
+  unsigned x, y, z;
+  unflat(k, g, x, y, z);
+  if (!interior(g, x, y, z)) return;
+  float v;
+  if (((x + y + z) & 1u) == color) {
+    const unsigned sy = g.np[0], sz = g.np[0] * g.np[1];
+    const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
+    const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
+    const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
+    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[t]) * H;
+    e[t] = v;
+  } else {
+    v = e[t];
+  }
+  x_out[t] += v;
 }
 
 // Fused FP32 residual + full-weighting restriction: coarse interior point
@@ -249,11 +290,40 @@ __device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geo
   rc[3 * k + 2] = acc[2] * s;
 }
 
+// Global-memory form: one thread per (coarse point, component), the same sums
+// in the same order as residual_restrict_point for that component.
 __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float r2x, float r2y, float r2z,
                                                            const float* __restrict__ e, const float* __restrict__ r,
                                                            float* __restrict__ rc) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < C.points()) residual_restrict_point(F, C, r2x, r2y, r2z, e, r, k, rc);
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
+  if (t >= 3u * (unsigned)C.points()) return;
+  const unsigned k = t / 3u;
+  const int c = (int)(t - 3u * k);
+  unsigned x, y, z;
+  unflat(k, C, x, y, z);
+  if (!interior(C, x, y, z)) {
+    rc[t] = 0.f;
+    return;
+  }
+  const ptrdiff_t sy = F.np[0], sz = (ptrdiff_t)F.np[0] * F.np[1];
+  const size_t f0 = (size_t)(2 * x) + sy * (2 * y) + sz * (2 * z);
+  float acc = 0.f;
+#pragma unroll
+  for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+    for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+      for (int dx = -1; dx <= 1; ++dx) {
+        const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
+        const size_t o = f0 + dx + sy * dy + sz * dz;
+        if (!interior(F, 2 * x + dx, 2 * y + dy, 2 * z + dz)) continue;
+        const float ec = e[3 * o + c];
+        const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
+                          (e[3 * (o + sy) + c] + e[3 * (o - sy) + c] - 2.f * ec) * r2y +
+                          (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
+        acc = fmaf(wt, r[3 * o + c] - lap, acc);
+      }
+  rc[t] = acc * (1.0f / 64.0f);
 }
 
 // e_fine += trilinear(e_coarse) on fine interior points.
@@ -280,10 +350,26 @@ __device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, cons
   ef[3 * k + 2] += a2 * wt;
 }
 
+// Global-memory form: one thread per (fine point, component), the same sums in
+// the same order as prolong_point for that component.
 __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
                                                      float* __restrict__ ef) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < F.points()) prolong_point(F, C, ec, ef, k);
+  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
+  if (t >= 3u * (unsigned)F.points()) return;
+  const unsigned k = t / 3u;
+  const int c = (int)(t - 3u * k);
+  unsigned x, y, z;
+  unflat(k, F, x, y, z);
+  if (!interior(F, x, y, z)) return;
+  const unsigned ox = x & 1, oy = y & 1, oz = z & 1;
+  const size_t sy = C.np[0], sz = (size_t)C.np[0] * C.np[1];
+  const size_t c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
+  float a = 0.f;
+  const float wt = 1.0f / (float)(1u << (ox + oy + oz));
+  for (unsigned iz = 0; iz <= oz; ++iz)
+    for (unsigned iy = 0; iy <= oy; ++iy)
+      for (unsigned ix = 0; ix <= ox; ++ix) a += ec[3 * (c0 + ix + sy * iy + sz * iz) + c];
+  ef[t] += a * wt;
 }
 
 // The small levels of a V-cycle in one CTA, their e and r in shared memory:
@@ -291,6 +377,7 @@ __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float
 // FP64 Gauss-Seidel solve there, then prolongation and post-smoothing back up.
 // The first small level reads its r from global memory and writes its e back.
 constexpr int kSmallMax = 8;
+constexpr int kCoarseShared = 1536;  // doubles of the coarsest solve kept in shared memory
 constexpr size_t kSmallLevelPoints = 17 * 17 * 17;
 struct SmallLevels {
   int n;  // levels handled here
@@ -353,6 +440,8 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
     const double H = 0.5 / (cx + cy + cz);
     const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
     const float* r = sm_r(sm, S, l);
+    __shared__ double s_work[kCoarseShared];
+    if (3 * n <= kCoarseShared) work = s_work;  // the usual 3^3..7^3 coarsest grids
     for (size_t k = threadIdx.x; k < 3 * n; k += blockDim.x) work[k] = 0.0;
     __syncthreads();
     for (int it = 0; it < S.coarse_sweeps; ++it)
@@ -463,14 +552,18 @@ struct MgBufs {
 };
 
 // One V(pre, post)-cycle on L e = R[level 0] (level 0's e starts from zero).
-static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsigned* nl) {
+// One V-cycle on L e = r (level 0's e and r in B).  With x, the last half
+// sweep on level 0 also adds e to x (*added says whether that happened: not
+// when every level is small).
+static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float* x, bool* added, unsigned* nl) {
+  *added = false;
   const int pre = 2, post = 2;
   const int fs = P.first_small;
   for (int l = 0; l < fs; ++l) {
     const Lev& L = P.lev[l];
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
-    const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
+    const size_t pairs = 3 * (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);  // (point, component) threads
     for (int s = 0; s < pre; ++s)
       for (unsigned col = 0; col < 2; ++col) {
         k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
@@ -478,7 +571,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
         ++*nl;
       }
     const Lev& Cn = P.lev[l + 1];
-    k_residual_restrict<<<blocks_for(Cn.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e,
+    k_residual_restrict<<<blocks_for(3 * Cn.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e,
                                                                                r, B.R + 3 * Cn.base);
     ++*nl;
   }
@@ -503,7 +596,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const Geom& cg = P.lev[P.nlev - 1].g;
     // Gauss-Seidel on m interior points per axis contracts by about
     // cos^2(pi / (m + 1)) per sweep; 3 (m + 1)^2 sweeps reach ~1e-13.
-    const unsigned m = std::max(cg.np[0], std::max(cg.np[1], cg.np[2])) - 1;
+    const unsigned m = std::max(cg.np[0], std::max(cg.np[1], cg.np[2])) - 2;
     S.coarse_sweeps = (int)std::min(3u * m * m + 2u, 4000u);
     k_vcycle_small<<<1, 1024, P.small_smem, c->stream>>>(S, B.cwork);
     ++*nl;
@@ -513,12 +606,18 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const Lev& Cn = P.lev[l + 1];
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
-    const size_t pairs = (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);
-    k_prolong_add<<<blocks_for(L.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    const size_t pairs = 3 * (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);  // (point, component) threads
+    k_prolong_add<<<blocks_for(3 * L.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+        if (x && l == 0 && s == post - 1 && col == 1) {
+          k_rbgs_add<<<blocks_for(3 * L.g.points(), 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r,
+                                                                             col, x);
+          *added = true;
+        } else {
+          k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+        }
         ++*nl;
       }
   }
@@ -530,14 +629,18 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
 // R = rhs - L x in FP32 with its FP64-accumulated norm.
 static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
                                unsigned* nl) {
-  vg_status st = enqueue_vcycle(c, P, B, nl);
+  bool added = false;
+  vg_status st = enqueue_vcycle(c, P, B, x, &added, nl);
   if (st != VG_OK) return st;
   const size_t n3 = 3 * g.points();
   const Lev& L0 = P.lev[0];
-  k_add_f32<<<blocks_for(n3, 256), 256, 0, c->stream>>>(x, B.E, n3);
+  if (!added) {
+    k_add_f32<<<blocks_for(n3, 256), 256, 0, c->stream>>>(x, B.E, n3);
+    ++*nl;
+  }
   k_residual32n<<<B.nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, x, rhs, B.R, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
-  *nl += 3;
+  *nl += 2;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }
