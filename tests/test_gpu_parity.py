@@ -346,6 +346,17 @@ def test_status_paths(vg):
     with pytest.raises(vg.VgError) as e:
         sim.Advect(far, DT)
     assert e.value.status == vg.OUT_OF_GRID
+    # one to two cells below the minimum corner on one axis (truncation gives
+    # cell -1 there) is outside too
+    _, g = sim.GetVelocityGrid()
+    mn = np.array(g.min_corner[:3], np.float32)
+    cell = np.array(g.cell_spacing[:3], np.float32)
+    below = np.stack([mn + np.float32(3.0) * cell] * 3)
+    for a in range(3):
+        below[a, a] = mn[a] - np.float32(1.5) * cell[a]
+    with pytest.raises(vg.VgError) as e:
+        sim.Advect(vg.make_particles(below.astype(np.float32)), DT)
+    assert e.value.status == vg.OUT_OF_GRID
     # the context stays usable after a reported error
     inside = vg.make_particles(pos[:10])
     sim.Advect(inside, DT)

@@ -131,10 +131,13 @@ __device__ __forceinline__ void interp(const Geom& g, const float* __restrict__ 
 __device__ __forceinline__ bool inside_cells(const Geom& g, float px, float py, float pz) {
   // The reference requires samples strictly inside the grid's cells
   // (uniformGrid.h:1122-1124); report rather than read out of bounds.
+  // bin_axis maps a position one to two cells below the minimum corner to
+  // 0xffffffff (truncation gives -1), so compare against np - 1 rather than
+  // testing ix + 1 < np, which wraps to 0 there.
   const unsigned ix = bin_axis(px, g.mn[0], g.cpe[0]);
   const unsigned iy = bin_axis(py, g.mn[1], g.cpe[1]);
   const unsigned iz = bin_axis(pz, g.mn[2], g.cpe[2]);
-  return ix + 1 < g.np[0] && iy + 1 < g.np[1] && iz + 1 < g.np[2] && px == px && py == py && pz == pz;
+  return ix < g.np[0] - 1u && iy < g.np[1] - 1u && iz < g.np[2] - 1u && px == px && py == py && pz == pz;
 }
 
 __global__ void k_upsample(Geom C, const float* __restrict__ cv, Geom F, int interior, float* __restrict__ fv) {
@@ -242,9 +245,15 @@ __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ 
   const float4 p = ps[i];
   const float4 wi = w0[i];
   const int nx = (int)g.np[0], ny = (int)g.np[1], nz = (int)g.np[2];
-  const int cx = (int)bin_axis(p.x, g.mn[0], g.cpe[0]);
-  const int cy = (int)bin_axis(p.y, g.mn[1], g.cpe[1]);
-  const int cz = (int)bin_axis(p.z, g.mn[2], g.cpe[2]);
+  // cell coordinates clamped to [-2, n + 1]: beyond that every neighbour test
+  // below fails the same way, and ncx = cx + ox cannot overflow
+  const int cx = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.x, g.mn[0]), g.cpe[0])), -2), nx + 1);
+  const int cy = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.y, g.mn[1]), g.cpe[1])), -2), ny + 1);
+  const int cz = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.z, g.mn[2]), g.cpe[2])), -2), nz + 1);
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= nx || cy >= ny || cz >= nz) {
+    w[i] = wi;  // outside the grid's points: in no cell list, so no exchange
+    return;
+  }
   const bool here_ok = cx >= 0 && cy >= 0 && cz >= 0 && cx < nx - 1 && cy < ny - 1 && cz < nz - 1;
   const float twonudt = 2.0f * nu * dt;
   float ax = 0.f, ay = 0.f, az = 0.f;
@@ -455,7 +464,7 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3) {
 vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt) {
   if (0.0f == g.ext[0] || 0.0f == g.ext[1] || 0.0f == g.ext[2]) return VG_OK;  // 2D: no stretching
   if (n == 0) return VG_OK;
-  k_stretch<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, jac9, ps, w, (int)n, dt, c->dflag);
+  k_stretch<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, jac9, ps, w, (int)n, dt, outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -479,7 +488,7 @@ vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4*
   if (m == 0) return VG_OK;
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "advect: more than 2^31 particles");
   k_gather_advect<<<blocks_for(m, 256), 256, 0, c->stream>>>(g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0,
-                                                              c->dflag);
+                                                              outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;

@@ -217,7 +217,20 @@ struct Ctx {
   bool have_prev = false;
   int* dflag = nullptr;     // device error word: bit 0 = a sample left the grid
   bool stats_pending = false;
+  // Multigrid schedule.  mg_fixed_k1 > 0 runs a fixed schedule with no host
+  // round trip (k1 FP32 cycles, then k2 refinement cycles), so that a step can
+  // be captured in a CUDA graph; the adaptive solve records the counts it used.
+  int mg_fixed_k1 = 0, mg_fixed_k2 = 0;
+  int mg_last_k1 = 0, mg_last_k2 = 0;
+  double* mg_relres_dev = nullptr;  // fixed schedule: final and initial relative residuals
+  bool step_captured = false;       // the last step was recorded into a CUDA graph (its events carry no times)
+  // Vortons that leave a fixed grid: an error (false), or stopped and left out
+  // of the solve, with dflag[1] recording that it happened (true).
+  bool freeze_outside = false;
 };
+
+// The word a kernel marks when a sample lies outside the grid's cells.
+inline int* outside_flag(Ctx* c) { return c->freeze_outside ? c->dflag + 1 : c->dflag; }
 
 // Device-side error bits, reported at the next synchronising call.
 enum DevFlag { DF_OUT_OF_GRID = 1, DF_NONFINITE = 2, DF_TIMEOUT = 4 };

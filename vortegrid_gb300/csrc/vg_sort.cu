@@ -29,9 +29,12 @@ __global__ void k_bin(Geom g, const float4* __restrict__ pos, int n, unsigned* _
   const unsigned iy = bin_axis(p.y, g.mn[1], g.cpe[1]);
   const unsigned iz = bin_axis(p.z, g.mn[2], g.cpe[2]);
   unsigned off = ix + g.np[0] * (iy + g.np[1] * iz);
-  // Out-of-grid vortons (undefined behaviour in the reference) are clamped to
-  // the last slot so that no write leaves the arrays; callers check bounds.
-  if (ix >= g.np[0] || iy >= g.np[1] || iz >= g.np[2] || off >= ncells) off = ncells - 1;
+  // Vortons outside the grid's points (undefined behaviour in the reference;
+  // negative cells wrap to large values), and non-finite ones, go to an extra
+  // slot, ncells, that no consumer of the lists reads: they drop out of the
+  // splat, the tree and PSE.
+  if (ix >= g.np[0] || iy >= g.np[1] || iz >= g.np[2] || off >= ncells || !(p.x == p.x && p.y == p.y && p.z == p.z))
+    off = ncells;
   key[i] = off;
   val[i] = (unsigned)i;
   atomicAdd(&count[off], 1u);
@@ -179,26 +182,28 @@ static vg_status exclusive_scan(Ctx* c, const unsigned* in, size_t n, unsigned* 
 
 vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, CellLists* out) {
   const size_t ncells = g.points();
-  if (n > 0x7fffffff || ncells > 0xffffffffu) return fail(c, VG_TOO_LARGE, "cell lists: too many vortons or cells");
+  if (n > 0x7fffffff || ncells >= 0xffffffffu) return fail(c, VG_TOO_LARGE, "cell lists: too many vortons or cells");
   vg_status st = VG_OK;
-  // S_CELL: key, val, key2, val2 (4 n); S_COUNT: count (ncells); S_START: start (ncells+1)
+  // one slot per grid point and one for vortons outside the grid
+  const size_t slots = ncells + 1;
+  // S_CELL: key, val, key2, val2 (4 n); S_COUNT: count (slots); S_START: start (slots+1)
   unsigned* kv = (unsigned*)ws(c, S_CELL, 4 * (n + 1) * sizeof(unsigned), &st);
   if (st != VG_OK) return st;
-  unsigned* count = (unsigned*)ws(c, S_COUNT, ncells * sizeof(unsigned), &st);
+  unsigned* count = (unsigned*)ws(c, S_COUNT, slots * sizeof(unsigned), &st);
   if (st != VG_OK) return st;
-  unsigned* start = (unsigned*)ws(c, S_START, (ncells + 1) * sizeof(unsigned), &st);
+  unsigned* start = (unsigned*)ws(c, S_START, (slots + 1) * sizeof(unsigned), &st);
   if (st != VG_OK) return st;
   unsigned *key = kv, *val = kv + (n + 1), *key2 = kv + 2 * (n + 1), *val2 = kv + 3 * (n + 1);
-  VG_CUDA(c, cudaMemsetAsync(count, 0, ncells * sizeof(unsigned), c->stream));
+  VG_CUDA(c, cudaMemsetAsync(count, 0, slots * sizeof(unsigned), c->stream));
   if (n > 0) {
     k_bin<<<blocks_for(n, 256), 256, 0, c->stream>>>(g, ps, (int)n, key, val, count, (unsigned)ncells);
     VG_LAUNCHED(c);
   }
-  st = exclusive_scan(c, count, ncells, start, true);
+  st = exclusive_scan(c, count, slots, start, true);
   if (st != VG_OK) return st;
-  // Stable radix sort by key: only as many 8-bit passes as the cell count needs.
+  // Stable radix sort by key: only as many 8-bit passes as the largest key (ncells) needs.
   int bits = 0;
-  while (bits < 32 && (ncells - 1) >> bits) ++bits;
+  while (bits < 32 && ncells >> bits) ++bits;
   const int passes = (bits + 7) / 8;
   const int ntiles = (int)((n + kTileKeys - 1) / kTileKeys);
   if (n > 0 && passes > 0) {
