@@ -330,6 +330,57 @@ vg_status vg_net_to_bf16_device(const float* src, void* dst, size_t count, void*
  * per axis, and from zero otherwise (vg_step_stats.warm_start_used says which). */
 vg_status vg_set_network(vg_ctx* ctx, vg_net* net);
 
+/* ------------------------------------------------------------------------
+ * Batched effects (no counterpart in the reference).  Many independent
+ * simulations stepped per frame.  Each simulation is a context with a fixed
+ * grid and the multigrid Poisson step, and its vortons (float4 arrays as in
+ * vg_step_device) stay on the device.  A frame is vg_step_device + the
+ * vortons' Euler advection for every simulation.  After a calibration step
+ * (one adaptive solve each, which fixes each simulation's multigrid schedule
+ * and sizes its workspaces), a frame has no host round trip, so it is
+ * captured once as CUDA graphs and replayed: the simulations are dealt to
+ * `streams` parallel branches, each branch's chain is captured as graphs of at
+ * most a few thousand kernels, and a frame forks into the branches, launches
+ * their graphs and joins.  A vorton that leaves its simulation's fixed grid
+ * stops (zero velocity) and drops out of that simulation's solve instead of
+ * failing the frame (vg_batch_outside reports it).  Errors: vg_batch_last_error. */
+typedef struct vg_batch vg_batch;
+
+vg_status vg_batch_create(int device, int streams /* 1..32 */, vg_batch** out);
+vg_status vg_batch_destroy(vg_batch* batch);
+const char* vg_batch_last_error(const vg_batch* batch);
+/* cfg: use_fixed_grid = 1, VG_VELOCITY_POISSON, VG_POISSON_MULTIGRID (stream and device are the
+ * batch's).  The arrays stay the caller's and must outlive the batch. */
+vg_status vg_batch_add(vg_batch* batch, const vg_config* cfg, float* pos_size, float* angvel, float* vel, size_t n,
+                       int* index);
+/* One network per (grid edge, stream) for the simulations whose grids it fits; others start from zero. */
+vg_status vg_batch_load_network(vg_batch* batch, const char* path);
+/* Stream count and network use (invalidates the graphs; a network change also the calibration). */
+vg_status vg_batch_configure(vg_batch* batch, int streams, int use_network);
+/* One adaptive step of every simulation (it advances them), fixing their multigrid schedules. */
+vg_status vg_batch_calibrate(vg_batch* batch, float dt);
+/* mode 0: the captured graphs (captured on first use and after any change); mode 1: the same work
+ * simulation after simulation on one stream, no graph.  Calibrates first if needed.  Does not
+ * synchronise. */
+vg_status vg_batch_step(vg_batch* batch, float dt, int mode);
+/* Waits for the batch and reports device-side errors of any simulation. */
+vg_status vg_batch_synchronize(vg_batch* batch);
+/* The autotuner: times `frames` graph replays for each stream count in candidates (with and
+ * without the network when one is loaded), keeps the fastest and reports it (best_ms per frame).
+ * Steps the simulations while measuring. */
+vg_status vg_batch_autotune(vg_batch* batch, float dt, int frames, const int* candidates, int ncand,
+                            int* best_streams, int* best_network, float* best_ms);
+/* *outside = 1 when a vorton of simulation `index` has left its grid since the last call, which
+ * clears the record.  Synchronises the batch. */
+vg_status vg_batch_outside(vg_batch* batch, int index, int* outside);
+/* A simulation's context (for vg_get_stats, vg_get_velocity_grid), owned by the batch.  After a
+ * graph frame, call vg_batch_synchronize before reading it; per-step times are then 0. */
+vg_ctx* vg_batch_context(vg_batch* batch, int index);
+int vg_batch_size(const vg_batch* batch);
+/* The captured frame: how many graphs it launches, and their largest and total node counts
+ * (0 before the first graph frame). */
+vg_status vg_batch_graph_info(const vg_batch* batch, int* graphs, size_t* max_nodes, size_t* total_nodes);
+
 #ifdef __cplusplus
 }
 #endif

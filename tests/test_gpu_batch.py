@@ -1,0 +1,117 @@
+"""GPU tests of batched effects (vg_batch_*): frames replayed from the
+captured CUDA graphs (simulations on parallel branches) are bit-identical to
+the same frames stepped simulation after simulation, with and without the
+network warm start; the calibrated fixed multigrid schedules end near the
+tolerance; long branches split into bounded graphs; a vorton that leaves its
+grid stops and drops out; the autotuner returns a measured setting."""
+import os
+
+import numpy as np
+import pytest
+
+torch = pytest.importorskip("torch")
+
+pytestmark = pytest.mark.gpu
+
+DT = 1.0 / 60.0
+
+
+@pytest.fixture(scope="module")
+def mod():
+    import vortegrid_gb300 as vg
+    from vortegrid_gb300 import batch
+    vg.lib()
+    return batch
+
+
+def effects(mod, seeds):
+    return [mod.make_effect(s) for s in seeds]
+
+
+def frames_equal(A, B):
+    for (pa, wa, va), (pb, wb, vb) in zip(A.arrays, B.arrays):
+        if not (torch.equal(pa, pb) and torch.equal(wa, wb) and torch.equal(va, vb)):
+            return False
+    return True
+
+
+@pytest.mark.parametrize("network", [False, True])
+def test_graph_frame_matches_sequential_frame(mod, network):
+    from vortegrid_gb300 import warmstart
+    if network and not os.path.exists(warmstart.DEFAULT_WEIGHTS):
+        pytest.skip("no trained weights")
+    ef = effects(mod, [11, 14, 17, 25, 13, 22])  # grid edges 80, 64, 48, 32, 96, 48
+    A, B = mod.Batch(ef, streams=3), mod.Batch(ef, streams=3)
+    if network:
+        A.load_network(warmstart.DEFAULT_WEIGHTS)
+        B.load_network(warmstart.DEFAULT_WEIGHTS)
+    A.calibrate(DT)
+    B.calibrate(DT)
+    A.synchronize()
+    B.synchronize()
+    assert frames_equal(A, B)
+    for _ in range(2):
+        A.step(DT, graph=True)
+        B.step(DT, graph=False)
+    A.synchronize()
+    B.synchronize()
+    assert frames_equal(A, B)
+    for i in range(len(A)):
+        st = A.stats(i)
+        assert st.poisson_relres < 1e-5, (i, st.poisson_relres, st.poisson_cycles)
+
+
+def test_long_branch_splits_into_bounded_graphs(mod):
+    """Twelve simulations on one branch (~4,000 kernels a frame) are captured
+    as more than one graph, each of bounded size, and still replay exactly
+    the sequential frames."""
+    ef = effects(mod, range(31, 43))
+    A, B = mod.Batch(ef, streams=1), mod.Batch(ef, streams=1)
+    A.calibrate(DT)
+    B.calibrate(DT)
+    for _ in range(2):
+        A.step(DT, graph=True)
+        B.step(DT, graph=False)
+    A.synchronize()
+    B.synchronize()
+    assert frames_equal(A, B)
+    graphs, max_nodes, total = A.graph_info()
+    assert graphs >= 2 and 0 < max_nodes < total and max_nodes < 8000, (graphs, max_nodes, total)
+
+
+def test_vorton_leaving_its_grid_stops_and_drops_out(mod):
+    """A vorton one and a half cells below a batched simulation's grid (the
+    band where truncation gives cell -1) does not fail the frame: it keeps its
+    place and vorticity, gets zero velocity, is reported by outside(), and
+    every other vorton steps bit-identically to the same effect without it."""
+    e = mod.make_effect(25)
+    g = e.grid
+    mn = np.array(g.min_corner[:3], np.float32)
+    cell = np.array(g.cell_spacing[:3], np.float32)
+    stray = (mn + np.float32(5.0) * cell).astype(np.float32)
+    stray[0] = mn[0] - np.float32(1.5) * cell[0]
+    e2 = mod.Effect(np.vstack([e.pos, stray[None]]).astype(np.float32),
+                    np.vstack([e.vort, np.ones((1, 3), np.float32)]).astype(np.float32), e.radius, e.grid)
+    A, B = mod.Batch([e]), mod.Batch([e2])
+    p0 = B.arrays[0][0][-1].clone()
+    w0 = B.arrays[0][1][-1].clone()
+    for X in (A, B):
+        X.calibrate(DT)
+        X.step(DT, graph=True)
+        X.step(DT, graph=True)
+        X.synchronize()
+    assert B.outside(0) and not A.outside(0)
+    assert not B.outside(0)  # the record was cleared
+    n = e.n
+    for a, b in zip(A.arrays[0], B.arrays[0]):
+        assert torch.equal(a, b[:n])
+    assert torch.equal(B.arrays[0][0][-1], p0) and torch.equal(B.arrays[0][1][-1], w0)
+    assert not torch.any(B.arrays[0][2][-1])
+
+
+def test_autotune_picks_a_measured_setting(mod):
+    A = mod.Batch(effects(mod, [21, 22, 23, 24]), streams=2)
+    streams, use_net, ms = A.autotune(DT, frames=2, candidates=(1, 2, 4))
+    assert streams in (1, 2, 4) and not use_net and 0.0 < ms < 1e4
+    A.step(DT)
+    A.synchronize()

@@ -123,6 +123,9 @@ EXPORTS = [
     "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
     "vg_net_synchronize",
     "vg_net_to_bf16_device", "vg_set_network",
+    "vg_batch_create", "vg_batch_destroy", "vg_batch_last_error", "vg_batch_add", "vg_batch_load_network",
+    "vg_batch_configure", "vg_batch_calibrate", "vg_batch_step", "vg_batch_synchronize", "vg_batch_autotune",
+    "vg_batch_outside", "vg_batch_context", "vg_batch_size", "vg_batch_graph_info",
 ]
 
 
@@ -202,6 +205,23 @@ def lib():
         L.vg_net_synchronize.argtypes = [vp]
         L.vg_net_to_bf16_device.argtypes = [vp, vp, sz, vp]
         L.vg_set_network.argtypes = [vp, vp]
+        ip = ctypes.POINTER(ctypes.c_int)
+        L.vg_batch_create.argtypes = [i, i, ctypes.POINTER(ctypes.c_void_p)]
+        L.vg_batch_destroy.argtypes = [vp]
+        L.vg_batch_last_error.argtypes = [vp]
+        L.vg_batch_last_error.restype = ctypes.c_char_p
+        L.vg_batch_add.argtypes = [vp, ctypes.POINTER(Config), vp, vp, vp, sz, ip]
+        L.vg_batch_load_network.argtypes = [vp, ctypes.c_char_p]
+        L.vg_batch_configure.argtypes = [vp, i, i]
+        L.vg_batch_calibrate.argtypes = [vp, fl]
+        L.vg_batch_step.argtypes = [vp, fl, i]
+        L.vg_batch_synchronize.argtypes = [vp]
+        L.vg_batch_autotune.argtypes = [vp, fl, i, ip, i, ip, ip, fp]
+        L.vg_batch_outside.argtypes = [vp, i, ip]
+        L.vg_batch_context.argtypes = [vp, i]
+        L.vg_batch_context.restype = vp
+        L.vg_batch_size.argtypes = [vp]
+        L.vg_batch_graph_info.argtypes = [vp, ip, ctypes.POINTER(sz), ctypes.POINTER(sz)]
         if L.vg_abi_version() != 2:
             raise ImportError("libvortegrid ABI version mismatch")
         _lib = L

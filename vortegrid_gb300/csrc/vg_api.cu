@@ -276,6 +276,9 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
   if (n == 0) return fail(c, VG_EMPTY, "no vortons");
   if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
   c->launches = 0;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
+  c->step_captured = cap != cudaStreamCaptureStatusNone;
   VG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
   Geom g;
   vg_status st = step_geometry(c, ps, n, first_pos, radius, extra_min, extra_max, &g);
@@ -325,6 +328,10 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
     }
     if (c->cfg.poisson_solver == VG_POISSON_REFERENCE_CASCADE) {
       if ((st = run_cascade(c, g, vecpot, negvort, c->cfg.cascade_steps)) != VG_OK) return st;
+    } else if (c->mg_fixed_k1 > 0) {
+      // fixed schedule: no host round trip; the residuals are read at vg_get_stats
+      if ((st = run_multigrid_fixed(c, g, vecpot, negvort)) != VG_OK) return st;
+      c->stats.poisson_cycles = c->mg_fixed_k1 + c->mg_fixed_k2;
     } else {
       int cyc = 0;
       double r0 = 0, r1 = 0;
@@ -464,6 +471,7 @@ vg_status vg_create(const vg_config* cfg, vg_ctx** out) {
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev3);
   if (e == cudaSuccess) e = cudaMalloc(&c->dflag, 256);
   if (e == cudaSuccess) e = cudaMemset(c->dflag, 0, 256);
+  if (e == cudaSuccess) e = cudaMalloc(&c->mg_relres_dev, 2 * sizeof(double));
   if (e != cudaSuccess) {
     g_err_noctx = std::string("vg_create: ") + cudaGetErrorString(e);
     cudaGetLastError();
@@ -483,6 +491,7 @@ vg_status vg_destroy(vg_ctx* c) {
   for (MgGraphCache& G : c->mg_graph)
     if (G.exec) cudaGraphExecDestroy(G.exec);
   if (c->dflag) cudaFree(c->dflag);
+  if (c->mg_relres_dev) cudaFree(c->mg_relres_dev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev2) cudaEventDestroy(c->ev2);
@@ -599,13 +608,26 @@ vg_status vg_get_vector_potential(vg_ctx* c, float* xyz, size_t cap_points, vg_g
 vg_status vg_get_stats(vg_ctx* c, vg_step_stats* s) {
   if (!c || !s) return VG_INVALID;
   if (c->stats_pending) {
-    VG_CUDA(c, cudaEventSynchronize(c->ev1));
-    float ms = 0.f;
-    cudaEventElapsedTime(&ms, c->ev0, c->ev1);
-    c->stats.ms_total = ms;
-    if (c->cfg.velocity_technique == VG_VELOCITY_POISSON && cudaEventElapsedTime(&ms, c->ev2, c->ev3) == cudaSuccess)
-      c->stats.ms_poisson = ms;
-    cudaGetLastError();
+    if (c->step_captured) {
+      // a step replayed from a graph: no per-step times; the caller has
+      // synchronised the graph's stream before asking
+      c->stats.ms_total = c->stats.ms_poisson = 0.f;
+    } else {
+      VG_CUDA(c, cudaEventSynchronize(c->ev1));
+      float ms = 0.f;
+      cudaEventElapsedTime(&ms, c->ev0, c->ev1);
+      c->stats.ms_total = ms;
+      if (c->cfg.velocity_technique == VG_VELOCITY_POISSON && cudaEventElapsedTime(&ms, c->ev2, c->ev3) == cudaSuccess)
+        c->stats.ms_poisson = ms;
+      cudaGetLastError();
+    }
+    if (c->cfg.velocity_technique == VG_VELOCITY_POISSON && c->mg_fixed_k1 > 0 &&
+        c->cfg.poisson_solver == VG_POISSON_MULTIGRID) {
+      double h[2] = {0.0, 0.0};
+      VG_CUDA(c, cudaMemcpy(h, c->mg_relres_dev, sizeof(h), cudaMemcpyDeviceToHost));
+      c->stats.poisson_relres = h[0];
+      c->stats.poisson_relres0 = h[1];
+    }
     c->stats_pending = false;
   }
   *s = c->stats;

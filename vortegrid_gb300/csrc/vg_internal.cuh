@@ -290,6 +290,8 @@ vg_status launch_upsample(Ctx* c, const Geom& coarse, const float* c3, const Geo
 vg_status run_cascade(Ctx* c, const Geom& g, float* soln3, const float* rhs3, int steps);
 vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, double tol, int max_cycles,
                         int* cycles, double* relres0, double* relres);
+// The same solve on a schedule fixed in advance (c->mg_fixed_k1, mg_fixed_k2): no host round trip.
+vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* rhs3);
 
 vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9);
 vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);

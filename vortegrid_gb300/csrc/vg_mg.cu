@@ -697,9 +697,8 @@ static vg_status read_norm(Ctx* c, const MgBufs& B, double* rr, double* bb) {
   return VG_OK;
 }
 
-vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, double tol, int max_cycles,
-                        int* cycles_out, double* relres0_out, double* relres_out) {
-  const MgPlan P = plan_levels(g);
+// Buffers of a solve on grid g (grow-only workspace slot S_MG).
+static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, float** etot, float** rir) {
   const size_t n0 = g.points();
   const unsigned nb0 = blocks_for(n0, kRedThreads);
   const size_t coarse_pts = P.lev[P.nlev - 1].g.points();
@@ -709,7 +708,6 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   vg_status st = VG_OK;
   char* mem = (char*)ws(c, S_MG, bytes, &st);
   if (st != VG_OK) return st;
-  MgBufs B;
   B.E = (float*)mem;
   B.R = B.E + 3 * P.total;
   B.a64 = (double*)(((uintptr_t)(B.R + 3 * P.total) + 255) & ~(uintptr_t)255);
@@ -717,13 +715,75 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   B.sums = B.part + 2 * (size_t)nb0;
   B.cwork = B.sums + 4;
   B.nb0 = nb0;
-  float* etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
-  float* rir = etot + 3 * n0;                                                                 // IR right-hand side
+  *etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
+  *rir = *etot + 3 * n0;                                                                 // IR right-hand side
   static bool smem_set = false;
   if (!smem_set) {
     cudaFuncSetAttribute(k_vcycle_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     smem_set = true;
   }
+  return VG_OK;
+}
+
+// out = sqrt(sums[0] / sums[1]) (sums[1] = ||b||^2 from the solve's first residual)
+__global__ void k_relres(const double* __restrict__ sums, double* __restrict__ out) {
+  if (threadIdx.x == 0 && blockIdx.x == 0) *out = sums[1] > 0.0 ? sqrt(sums[0] / sums[1]) : sqrt(sums[0]);
+}
+
+// The adaptive solve's steps with the cycle counts fixed in advance (k1 FP32
+// cycles, then one refinement round of k2 cycles) and no host round trip; the
+// relative residuals go to mg_relres_dev ([0] final, [1] initial).
+vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* rhs3) {
+  const MgPlan P = plan_levels(g);
+  MgBufs B;
+  float *etot = nullptr, *rir = nullptr;
+  vg_status st = setup_bufs(c, g, P, B, &etot, &rir);
+  if (st != VG_OK) return st;
+  if (!c->mg_relres_dev) return fail(c, VG_INVALID, "multigrid: no device slot for the residual");
+  const size_t n0 = g.points();
+  const unsigned nb0 = B.nb0;
+  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
+               r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
+  const Lev& L0 = P.lev[0];
+  unsigned nl = 0;
+  VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
+  k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
+  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
+  k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev + 1);
+  nl += 3;
+  for (int k = 0; k < c->mg_fixed_k1; ++k)
+    if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl)) != VG_OK) return st;
+  k_to_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.a64, 3 * n0);
+  k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+  nl += 3;
+  if (c->mg_fixed_k2 > 0) {
+    VG_CUDA(c, cudaMemsetAsync(etot, 0, 3 * n0 * sizeof(float), c->stream));
+    VG_CUDA(c, cudaMemcpyAsync(B.R, rir, 3 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+    for (int k = 0; k < c->mg_fixed_k2; ++k)
+      if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl)) != VG_OK) return st;
+    k_add_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, etot, 3 * n0);
+    k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+    nl += 3;
+  }
+  k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev);
+  k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, soln3, 3 * n0);
+  nl += 2;
+  c->launches += nl;
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, double tol, int max_cycles,
+                        int* cycles_out, double* relres0_out, double* relres_out) {
+  const MgPlan P = plan_levels(g);
+  const size_t n0 = g.points();
+  MgBufs B;
+  float *etot = nullptr, *rir = nullptr;
+  vg_status st = setup_bufs(c, g, P, B, &etot, &rir);
+  if (st != VG_OK) return st;
+  const unsigned nb0 = B.nb0;
   const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
                r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
   // e must be zero on every level's boundary (Dirichlet correction); the
@@ -748,6 +808,7 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
     if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
     relres = std::sqrt(rr) / bn;
   }
+  const int k1 = cyc;
   // Phase 2: iterative refinement.  FP64 residual of the FP64 iterate, FP32
   // cycles on the correction equation L e = r (its residual updated in FP32,
   // accurate because r is already small), a64 += e, and an FP64 check.
@@ -779,6 +840,8 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, soln3, 3 * n0);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
+  c->mg_last_k1 = k1;
+  c->mg_last_k2 = cyc - k1;
   if (cycles_out) *cycles_out = cyc;
   if (relres0_out) *relres0_out = relres0;
   if (relres_out) *relres_out = relres;
