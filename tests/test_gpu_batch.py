@@ -62,10 +62,10 @@ def test_graph_frame_matches_sequential_frame(mod, network):
 
 
 def test_long_branch_splits_into_bounded_graphs(mod):
-    """Twelve simulations on one branch (~4,000 kernels a frame) are captured
-    as more than one graph, each of bounded size, and still replay exactly
-    the sequential frames."""
-    ef = effects(mod, range(31, 43))
+    """Twenty-four simulations on one branch (~6,500 graph nodes a frame) are
+    captured as more than one graph, each of bounded size, and still replay
+    exactly the sequential frames."""
+    ef = effects(mod, range(31, 55))
     A, B = mod.Batch(ef, streams=1), mod.Batch(ef, streams=1)
     A.calibrate(DT)
     B.calibrate(DT)
