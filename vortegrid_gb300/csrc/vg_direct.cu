@@ -121,25 +121,36 @@ __global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restri
 // each thread carries its 8 targets as 4 pairs, and every source is staged in
 // shared memory already duplicated into pairs (-p, 1/R, w, -w), so each
 // operation below advances two targets in one instruction.  The per-target
-// operations and their order are those of k_direct_fast<0>, so the results are
-// bit-identical to it; only the instruction count changes (about 11 issue
-// slots per interaction instead of 19).
-// 8 targets per thread with registers capped for 4 resident CTAs per SM was
-// the fastest of the shapes measured on GB300 (4 to 16 targets, 1 to 8 CTAs;
-// scalar accumulation FFMAs mixed in were slower): the FFMA2s all run on the
-// heavy half of the FMA pipe, which the profile shows ~70% busy.
+// operations and their order are those of k_direct_fast<0> (and the source
+// constants those of k_prep_sources<0>, computed here while staging), so the
+// results are bit-identical to it; only the instruction count changes (about
+// 11 issue slots per interaction instead of 19).
+// 8 targets per thread (128 registers) was the fastest of the shapes measured
+// on GB300 (4 to 16 targets; scalar accumulation FFMAs or a scalar law mixed in
+// were slower): the FFMA2s all run on the heavy half of the FMA pipe, which the
+// profile shows ~70% busy.  CTAs of 256 threads, 2 per SM, beat 4 CTAs of 128
+// by ~4%: the tile barriers keep a CTA's warps together, whereas independent
+// small CTAs on one SM finish far apart (measured 39-100 us for equal work)
+// and leave the SM short of warps at the end.
+// With more than one source chunk the partial sums go to a scratch buffer and
+// k_reduce_pair adds them in chunk order.  (Reducing them inside this kernel,
+// by the last CTA of each target block or after a grid-wide barrier, or
+// launching the reduction as a programmatic dependent, measured no faster.)
 constexpr int kPairTPT = 8;
+constexpr int kPairThreads = 256;
 
-__global__ void __launch_bounds__(kThreads, 4)
-    k_direct_pair(const float4* __restrict__ s0, const float4* __restrict__ s1, int n, int chunk,
-                  const float4* __restrict__ q, int m, float* __restrict__ partial) {
+
+
+__global__ void __launch_bounds__(kPairThreads, 2)
+    k_direct_pair(const float4* __restrict__ ps, const float4* __restrict__ w, int n, int chunk, float sr, float sc,
+                  const float4* __restrict__ q, int m, float* __restrict__ partial, float4* __restrict__ out) {
   constexpr int kPairs = kPairTPT / 2;
   __shared__ float4 sh[5 * kTile];
-  const int base = blockIdx.x * (kThreads * kPairTPT) + threadIdx.x;
+  const int base = blockIdx.x * (kPairThreads * kPairTPT) + threadIdx.x;
   float2 qx[kPairs], qy[kPairs], qz[kPairs], ax[kPairs], ay[kPairs], az[kPairs];
 #pragma unroll
   for (int pr = 0; pr < kPairs; ++pr) {
-    const int j0 = base + 2 * pr * kThreads, j1 = j0 + kThreads;
+    const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
     const float4 v0 = (j0 < m) ? q[j0] : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 v1 = (j1 < m) ? q[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
     qx[pr] = make_float2(v0.x, v1.x);
@@ -152,10 +163,15 @@ __global__ void __launch_bounds__(kThreads, 4)
   for (int tile = k0; tile < k1; tile += kTile) {
     const int cnt = min(kTile, k1 - tile);
     __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += kThreads) {
-      const float4 p = s0[tile + i], a = s1[tile + i];
+    for (int i = threadIdx.x; i < cnt; i += kPairThreads) {
+      const float4 p = ps[tile + i], a0 = w[tile + i];
+      // k_prep_sources<0>: 1/R and the scaled angular velocity
+      const float radius = p.w * 0.5f * sr;
+      const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
+      const float invr = 1.0f / radius;
+      const float4 a = make_float4(a0.x * s, a0.y * s, a0.z * s, 0.f);
       sh[5 * i + 0] = make_float4(-p.x, -p.x, -p.y, -p.y);
-      sh[5 * i + 1] = make_float4(-p.z, -p.z, p.w, p.w);
+      sh[5 * i + 1] = make_float4(-p.z, -p.z, invr, invr);
       sh[5 * i + 2] = make_float4(a.x, a.x, a.y, a.y);
       sh[5 * i + 3] = make_float4(a.z, a.z, -a.x, -a.x);
       sh[5 * i + 4] = make_float4(-a.y, -a.y, -a.z, -a.z);
@@ -181,21 +197,60 @@ __global__ void __launch_bounds__(kThreads, 4)
       }
     }
   }
-  float* out = partial + (size_t)blockIdx.y * m * 3;
+  if (gridDim.y == 1) {  // one chunk: the sums are final (0 + sum, as the reduction would give)
+#pragma unroll
+    for (int pr = 0; pr < kPairs; ++pr) {
+      const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
+      if (j0 < m) out[j0] = make_float4(0.f + ax[pr].x, 0.f + ay[pr].x, 0.f + az[pr].x, 0.f);
+      if (j1 < m) out[j1] = make_float4(0.f + ax[pr].y, 0.f + ay[pr].y, 0.f + az[pr].y, 0.f);
+    }
+    return;
+  }
+  float* mine = partial + (size_t)blockIdx.y * (size_t)m * 3;
 #pragma unroll
   for (int pr = 0; pr < kPairs; ++pr) {
-    const int j0 = base + 2 * pr * kThreads, j1 = j0 + kThreads;
+    const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
     if (j0 < m) {
-      out[3 * j0] = ax[pr].x;
-      out[3 * j0 + 1] = ay[pr].x;
-      out[3 * j0 + 2] = az[pr].x;
+      mine[3 * j0] = ax[pr].x;
+      mine[3 * j0 + 1] = ay[pr].x;
+      mine[3 * j0 + 2] = az[pr].x;
     }
     if (j1 < m) {
-      out[3 * j1] = ax[pr].y;
-      out[3 * j1 + 1] = ay[pr].y;
-      out[3 * j1 + 2] = az[pr].y;
+      mine[3 * j1] = ax[pr].y;
+      mine[3 * j1 + 1] = ay[pr].y;
+      mine[3 * j1 + 2] = az[pr].y;
     }
   }
+}
+
+// Sums the chunks' partial sums in chunk order (as k_reduce_partials), with
+// up to 16 chunks' loads issued before the first add: the sum is bound by the
+// latency of these loads, not by their bytes.
+__global__ void __launch_bounds__(256) k_reduce_pair(const float* __restrict__ partial, int ks, int m,
+                                                     float4* __restrict__ out) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  if (j >= m) return;
+  constexpr int kBatch = 16;
+  float x = 0.f, y = 0.f, z = 0.f;
+  for (int k0 = 0; k0 < ks; k0 += kBatch) {
+    float v[kBatch][3];
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k)
+      if (k0 + k < ks) {
+        const float* p = partial + ((size_t)(k0 + k) * m + j) * 3;
+        v[k][0] = p[0];
+        v[k][1] = p[1];
+        v[k][2] = p[2];
+      }
+#pragma unroll
+    for (int k = 0; k < kBatch; ++k)
+      if (k0 + k < ks) {
+        x += v[k][0];
+        y += v[k][1];
+        z += v[k][2];
+      }
+  }
+  out[j] = make_float4(x, y, z, 0.f);
 }
 
 __global__ void k_reduce_partials(const float* __restrict__ partial, int ksplit, int m, float4* __restrict__ out) {
@@ -242,7 +297,7 @@ unsigned direct_slots(int kind) {
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (kind == 0)
-      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_pair, kThreads, 0);
+      cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_pair, kPairThreads, 0);
     else
       cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_direct_fast<1>, kThreads, 0);
     cudaGetLastError();
@@ -274,7 +329,7 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
   // Split the sources into `ksplit` chunks so that target blocks x chunks
   // fills the resident CTA slots of the GPU (SMs x CTAs per SM) once, with no
   // partial second wave; every CTA then does the same amount of work.
-  const unsigned tblocks = blocks_for(m, kThreads * (kind == 0 ? kPairTPT : kTPT));
+  const unsigned tblocks = blocks_for(m, kind == 0 ? kPairThreads * kPairTPT : kThreads * kTPT);
   const unsigned slots = direct_slots(kind);
   unsigned ksplit = std::max(1u, slots / tblocks);
   const size_t min_chunk = 64;  // keep each CTA's source loop long enough to amortise its set-up
@@ -282,22 +337,32 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
   const int chunk = (int)((n + ksplit - 1) / ksplit);
   ksplit = (unsigned)((n + chunk - 1) / chunk);
   vg_status st = VG_OK;
+  if (kind == 0) {
+    float* partial = nullptr;
+    if (ksplit > 1) {
+      partial = (float*)ws(c, S_DIRECT, (size_t)ksplit * m * 3 * sizeof(float), &st);
+      if (st != VG_OK) return st;
+    }
+    dim3 grid(tblocks, ksplit);
+    k_direct_pair<<<grid, kPairThreads, 0, c->stream>>>(ps, w, (int)n, chunk, sr, sc, q, (int)m, partial, out);
+    VG_LAUNCHED(c);
+    if (ksplit > 1) {
+      k_reduce_pair<<<blocks_for(m, 256), 256, 0, c->stream>>>(partial, (int)ksplit, (int)m, out);
+      VG_LAUNCHED(c);
+    }
+    VG_CUDA(c, cudaGetLastError());
+    return VG_OK;
+  }
   const size_t srcb = ((n * sizeof(float4) + 255) / 256) * 256;
   char* scratch = (char*)ws(c, S_DIRECT, 2 * srcb + (size_t)ksplit * m * 3 * sizeof(float), &st);
   if (st != VG_OK) return st;
   float4* s0 = (float4*)scratch;
   float4* s1 = (float4*)(scratch + srcb);
   float* partial = (float*)(scratch + 2 * srcb);
-  if (kind == 0)
-    k_prep_sources<0><<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, sr, sc, s0, s1);
-  else
-    k_prep_sources<1><<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, sr, sc, s0, s1);
+  k_prep_sources<1><<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, sr, sc, s0, s1);
   VG_LAUNCHED(c);
   dim3 grid(tblocks, ksplit);
-  if (kind == 0)
-    k_direct_pair<<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
-  else
-    k_direct_fast<1><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
+  k_direct_fast<1><<<grid, kThreads, 0, c->stream>>>(s0, s1, (int)n, chunk, q, (int)m, partial);
   VG_LAUNCHED(c);
   k_reduce_partials<<<blocks_for(m, 256), 256, 0, c->stream>>>(partial, (int)ksplit, (int)m, out);
   VG_LAUNCHED(c);
