@@ -331,7 +331,7 @@ def run_ours(args, world, rank, local):
     achieved = FLOPS_PER_INTERACTION * interactions() / (kms * 1e-3) / 1e12
     clk_mhz = result["clocks"].get("sm_mhz") or 2070.0
     peak = 2 * 128 * 152 * clk_mhz * 1e6 / 1e12
-    result["roofline"] = {"bound": "fp32", "kernel": "k_direct_pair (+prep, +partial reduce)",
+    result["roofline"] = {"bound": "fp32", "kernel": "k_direct_pair (+ k_reduce_pair)",
                           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                           "traffic": profiled_traffic("direct_pair_ring4096.md"), "ms_per_launch": kms,
                           "peak_basis": f"2 flops x 128 FP32 lanes x 152 SMs x {clk_mhz:.0f} MHz (sampled median)",
