@@ -189,26 +189,23 @@ __device__ __forceinline__ void rbgs_point(const Geom& g, float r2x, float r2y, 
 }
 
 // Point red-black Gauss-Seidel on L e = r (FP32).  One thread per component
-// of a point of `color` (x = 2j + parity, components c = 0..2 adjacent), so a
-// warp reads ~11 points' worth of consecutive floats of the AoS field instead
-// of 32 points 24 bytes apart.  zero_first: e is zero before this sweep, so the
-// red points take -r H directly.
+// of an interior point of `color`: threadIdx.x runs along a row over
+// (point j, component c) pairs -- x = 1 + parity + 2 j, components adjacent --
+// so a warp reads ~11 points' worth of consecutive floats of the AoS field
+// instead of 32 points 24 bytes apart; y and z come from the block index
+// (launch_rows), so no thread divides by a grid size.  zero_first: e is zero
+// before this sweep, so the red points take -r H directly.
 __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, float r2z, float H,
                                               float* __restrict__ e, const float* __restrict__ r, unsigned color,
                                               int zero_first) {
-  const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
-  const unsigned half3 = 3 * ((nx + 1) / 2);
-  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= ny * nz * half3) return;
-  const unsigned row = t / half3;
-  const unsigned jc = t - row * half3;
-  const unsigned j = jc / 3, c = jc - 3 * j;
-  const unsigned z = row / ny, y = row - z * ny;
-  if (y == 0 || z == 0 || y + 1 >= ny || z + 1 >= nz) return;
-  const unsigned x = 2 * j + ((y + z + color) & 1u);
-  if (x == 0 || x + 1 >= nx) return;
-  const size_t k = x + (size_t)nx * (y + (size_t)ny * z);
-  const size_t sy = nx, sz = (size_t)nx * ny;
+  const unsigned nx = g.np[0], ny = g.np[1];
+  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
+  const unsigned j = jc / 3u, c = jc - 3u * j;
+  const unsigned x = 1u + ((color + 1u + y + z) & 1u) + 2u * j;
+  if (y + 1 >= ny || x + 1 >= nx) return;
+  const unsigned k = x + nx * (y + ny * z);
+  const unsigned sy = nx, sz = nx * ny;
   float v;
   if (zero_first) {
     v = -r[3 * k + c] * H;
@@ -228,15 +225,17 @@ __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, floa
 __global__ void __launch_bounds__(256) k_rbgs_add(Geom g, float r2x, float r2y, float r2z, float H,
                                                   float* __restrict__ e, const float* __restrict__ r,
                                                   unsigned color, float* __restrict__ x_out) {
-  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
-  if (t >= 3u * (unsigned)g.points()) return;
-  const unsigned k = t / 3u, c = t - 3u * k;
-  unsigned x, y, z;
-  unflat(k, g, x, y, z);
-  if (!interior(g, x, y, z)) return;
+  // threads over (interior x, component) along a row; y, z from the block
+  const unsigned nx = g.np[0], ny = g.np[1];
+  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
+  const unsigned j = jc / 3u, c = jc - 3u * j;
+  const unsigned x = 1u + j;
+  if (y + 1 >= ny || x + 1 >= nx) return;
+  const unsigned k = x + nx * (y + ny * z), t = 3 * k + c;
   float v;
   if (((x + y + z) & 1u) == color) {
-    const unsigned sy = g.np[0], sz = g.np[0] * g.np[1];
+    const unsigned sy = nx, sz = nx * ny;
     const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
     const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
     const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
@@ -295,18 +294,15 @@ __device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geo
 __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float r2x, float r2y, float r2z,
                                                            const float* __restrict__ e, const float* __restrict__ r,
                                                            float* __restrict__ rc) {
-  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
-  if (t >= 3u * (unsigned)C.points()) return;
-  const unsigned k = t / 3u;
-  const int c = (int)(t - 3u * k);
-  unsigned x, y, z;
-  unflat(k, C, x, y, z);
-  if (!interior(C, x, y, z)) {
-    rc[t] = 0.f;
-    return;
-  }
-  const ptrdiff_t sy = F.np[0], sz = (ptrdiff_t)F.np[0] * F.np[1];
-  const size_t f0 = (size_t)(2 * x) + sy * (2 * y) + sz * (2 * z);
+  // threads over (coarse interior x, component) along a row; y, z from the
+  // block.  Coarse boundary points are never read, so they are not written.
+  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
+  const unsigned j = jc / 3u, c = jc - 3u * j;
+  const unsigned x = 1u + j;
+  if (y + 1 >= C.np[1] || x + 1 >= C.np[0]) return;
+  const unsigned sy = F.np[0], sz = F.np[0] * F.np[1];
+  const unsigned f0 = 2 * x + sy * (2 * y) + sz * (2 * z);
   float acc = 0.f;
 #pragma unroll
   for (int dz = -1; dz <= 1; ++dz)
@@ -315,7 +311,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float
 #pragma unroll
       for (int dx = -1; dx <= 1; ++dx) {
         const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
-        const size_t o = f0 + dx + sy * dy + sz * dz;
+        const unsigned o = f0 + dx + sy * dy + sz * dz;
         if (!interior(F, 2 * x + dx, 2 * y + dy, 2 * z + dz)) continue;
         const float ec = e[3 * o + c];
         const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
@@ -323,7 +319,7 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float
                           (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
         acc = fmaf(wt, r[3 * o + c] - lap, acc);
       }
-  rc[t] = acc * (1.0f / 64.0f);
+  rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = acc * (1.0f / 64.0f);
 }
 
 // e_fine += trilinear(e_coarse) on fine interior points.
@@ -350,26 +346,42 @@ __device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, cons
   ef[3 * k + 2] += a2 * wt;
 }
 
-// Global-memory form: one thread per (fine point, component), the same sums in
-// the same order as prolong_point for that component.
+// Global-memory form: one thread per (fine interior point, component), the
+// same sums in the same order as prolong_point for that component; threads
+// along a row over (x, component), y and z from the block.
 __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
                                                      float* __restrict__ ef) {
-  const unsigned t = blockIdx.x * blockDim.x + threadIdx.x;  // grids hold < 2^30 points
-  if (t >= 3u * (unsigned)F.points()) return;
-  const unsigned k = t / 3u;
-  const int c = (int)(t - 3u * k);
-  unsigned x, y, z;
-  unflat(k, F, x, y, z);
-  if (!interior(F, x, y, z)) return;
+  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
+  const unsigned j = jc / 3u, c = jc - 3u * j;
+  const unsigned x = 1u + j;
+  if (y + 1 >= F.np[1] || x + 1 >= F.np[0]) return;
   const unsigned ox = x & 1, oy = y & 1, oz = z & 1;
-  const size_t sy = C.np[0], sz = (size_t)C.np[0] * C.np[1];
-  const size_t c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
+  const unsigned sy = C.np[0], sz = C.np[0] * C.np[1];
+  const unsigned c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
   float a = 0.f;
   const float wt = 1.0f / (float)(1u << (ox + oy + oz));
   for (unsigned iz = 0; iz <= oz; ++iz)
     for (unsigned iy = 0; iy <= oy; ++iy)
       for (unsigned ix = 0; ix <= ox; ++ix) a += ec[3 * (c0 + ix + sy * iy + sz * iz) + c];
-  ef[t] += a * wt;
+  ef[3 * (x + F.np[0] * (y + F.np[1] * z)) + c] += a * wt;
+}
+
+// Launch shape of the row kernels above over `items` (point, component)
+// pairs per row and the interior rows (ny - 2) x (nz - 2) of a level: rows of
+// up to 256 threads, rounded to whole warps; short rows stack in y.
+struct RowLaunch {
+  dim3 grid, block;
+};
+static RowLaunch launch_rows(unsigned items, unsigned ny, unsigned nz) {
+  const unsigned nb = (items + 255) / 256;
+  const unsigned bx = ((items + nb - 1) / nb + 31) / 32 * 32;
+  unsigned by = std::max(1u, 256u / bx);
+  while (by > 1 && by / 2 >= ny - 2) by >>= 1;
+  RowLaunch L;
+  L.block = dim3(bx, by, 1);
+  L.grid = dim3(nb, (ny - 2 + by - 1) / by, nz - 2);
+  return L;
 }
 
 // The small levels of a V-cycle in one CTA, their e and r in shared memory:
@@ -563,16 +575,17 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     const Lev& L = P.lev[l];
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
-    const size_t pairs = 3 * (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);  // (point, component) threads
+    const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);  // one colour's points
     for (int s = 0; s < pre; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
-                                                              (s == 0 && col == 0) ? 1 : 0);
+        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
+                                                    (s == 0 && col == 0) ? 1 : 0);
         ++*nl;
       }
     const Lev& Cn = P.lev[l + 1];
-    k_residual_restrict<<<blocks_for(3 * Cn.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e,
-                                                                               r, B.R + 3 * Cn.base);
+    const RowLaunch rl = launch_rows(3 * (Cn.g.np[0] - 2), Cn.g.np[1], Cn.g.np[2]);
+    k_residual_restrict<<<rl.grid, rl.block, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r,
+                                                             B.R + 3 * Cn.base);
     ++*nl;
   }
   {
@@ -606,17 +619,17 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     const Lev& Cn = P.lev[l + 1];
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
-    const size_t pairs = 3 * (size_t)L.g.np[1] * L.g.np[2] * ((L.g.np[0] + 1) / 2);  // (point, component) threads
-    k_prolong_add<<<blocks_for(3 * L.g.points(), 256), 256, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    const RowLaunch all = launch_rows(3 * (L.g.np[0] - 2), L.g.np[1], L.g.np[2]);  // every interior point
+    const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);
+    k_prolong_add<<<all.grid, all.block, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
         if (x && l == 0 && s == post - 1 && col == 1) {
-          k_rbgs_add<<<blocks_for(3 * L.g.points(), 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r,
-                                                                             col, x);
+          k_rbgs_add<<<all.grid, all.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, x);
           *added = true;
         } else {
-          k_rbgs<<<blocks_for(pairs, 256), 256, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+          k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
         }
         ++*nl;
       }
