@@ -247,33 +247,26 @@ __global__ void __launch_bounds__(256) k_rbgs_add(Geom g, float r2x, float r2y, 
   x_out[t] += v;
 }
 
-// Fused FP32 residual + full-weighting restriction: coarse interior point
-// (x, y, z) sums the fine residuals r - L e at the 27 fine points around
-// (2x, 2y, 2z) with weights 8/4/2/1 / 64, recomputing them instead of
-// writing the fine residual field.
+// Fused FP32 residual + full-weighting restriction at coarse interior point
+// (x, y, z): the fine residuals r - L e at the 27 fine points around
+// (2x, 2y, 2z) with weights 8/4/2/1 / 64, recomputed instead of writing the
+// fine residual field.  Levels halve exactly (fine n = 2 coarse n - 1 per
+// axis), so those fine points are all interior.
 __device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geom& C, float r2x, float r2y,
                                                         float r2z, const float* __restrict__ e,
-                                                        const float* __restrict__ r, size_t k,
-                                                        float* __restrict__ rc) {
-  unsigned x, y, z;
-  unflat(k, C, x, y, z);
-  if (!interior(C, x, y, z)) {
-    rc[3 * k] = rc[3 * k + 1] = rc[3 * k + 2] = 0.f;
-    return;
-  }
-  const ptrdiff_t sy = F.np[0], sz = (ptrdiff_t)F.np[0] * F.np[1];
-  const size_t f0 = (size_t)(2 * x) + sy * (2 * y) + sz * (2 * z);
+                                                        const float* __restrict__ r, unsigned x, unsigned y,
+                                                        unsigned z, float* __restrict__ rc) {
+  const unsigned sy = F.np[0], sz = F.np[0] * F.np[1];
+  const unsigned f0 = 2 * x + sy * (2 * y) + sz * (2 * z);
   float acc[3] = {0.f, 0.f, 0.f};
-#pragma unroll
+#pragma unroll 1  // the 1024-thread CTA has 64 registers per thread
   for (int dz = -1; dz <= 1; ++dz)
 #pragma unroll
     for (int dy = -1; dy <= 1; ++dy)
 #pragma unroll
       for (int dx = -1; dx <= 1; ++dx) {
         const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
-        const size_t o = f0 + dx + sy * dy + sz * dz;
-        // fine points on the boundary carry no residual (Dirichlet)
-        if (!interior(F, 2 * x + dx, 2 * y + dy, 2 * z + dz)) continue;
+        const unsigned o = f0 + dx + sy * dy + sz * dz;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
           const float ec = e[3 * o + c];
@@ -284,87 +277,138 @@ __device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geo
         }
       }
   const float s = 1.0f / 64.0f;
+  const unsigned k = x + C.np[0] * (y + C.np[1] * z);
   rc[3 * k] = acc[0] * s;
   rc[3 * k + 1] = acc[1] * s;
   rc[3 * k + 2] = acc[2] * s;
 }
 
-// Global-memory form: one thread per (coarse point, component), the same sums
-// in the same order as residual_restrict_point for that component.
+// Global-memory form, tiled: a CTA owns kRTX x kRTY x kRTZ coarse points.  It
+// first computes the fine residuals r - L e of the (2 kRTX + 1) x (2 kRTY + 1)
+// x (2 kRTZ + 1) fine points around them into shared memory (coalesced along
+// fine rows, each fine residual evaluated once per tile instead of once per
+// coarse neighbour), then each (coarse point, component) sums its 27 fine
+// residuals in the order of residual_restrict_point.  Coarse boundary points
+// are never read, so they are not written.
+constexpr int kRTX = 16, kRTY = 4, kRTZ = 2;
+constexpr int kRFX = 2 * kRTX + 1, kRFY = 2 * kRTY + 1, kRFZ = 2 * kRTZ + 1;
 __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float r2x, float r2y, float r2z,
                                                            const float* __restrict__ e, const float* __restrict__ r,
                                                            float* __restrict__ rc) {
-  // threads over (coarse interior x, component) along a row; y, z from the
-  // block.  Coarse boundary points are never read, so they are not written.
-  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
-  const unsigned j = jc / 3u, c = jc - 3u * j;
-  const unsigned x = 1u + j;
-  if (y + 1 >= C.np[1] || x + 1 >= C.np[0]) return;
-  const unsigned sy = F.np[0], sz = F.np[0] * F.np[1];
-  const unsigned f0 = 2 * x + sy * (2 * y) + sz * (2 * z);
-  float acc = 0.f;
+  __shared__ float s_res[kRFX * kRFY * kRFZ * 3];
+  const unsigned cx0 = 1 + blockIdx.x * kRTX, cy0 = 1 + blockIdx.y * kRTY, cz0 = 1 + blockIdx.z * kRTZ;
+  const unsigned nx = F.np[0], ny = F.np[1], nz = F.np[2];
+  const unsigned sy = nx, sz = nx * ny;
+  // fine local (0, 0, 0) is fine (2 cx0 - 1, 2 cy0 - 1, 2 cz0 - 1)
+  for (unsigned p = threadIdx.x; p < (unsigned)(kRFX * kRFY * kRFZ); p += blockDim.x) {
+    const unsigned lx = p % kRFX, q = p / kRFX;
+    const unsigned ly = q % kRFY, lz = q / kRFY;
+    const unsigned fx = 2 * cx0 - 1 + lx, fy = 2 * cy0 - 1 + ly, fz = 2 * cz0 - 1 + lz;
+    float v[3] = {0.f, 0.f, 0.f};
+    if (fx + 1 < nx && fy + 1 < ny && fz + 1 < nz) {  // fx, fy, fz >= 1 by construction
+      const unsigned o = fx + sy * fy + sz * fz;
 #pragma unroll
-  for (int dz = -1; dz <= 1; ++dz)
-#pragma unroll
-    for (int dy = -1; dy <= 1; ++dy)
-#pragma unroll
-      for (int dx = -1; dx <= 1; ++dx) {
-        const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
-        const unsigned o = f0 + dx + sy * dy + sz * dz;
-        if (!interior(F, 2 * x + dx, 2 * y + dy, 2 * z + dz)) continue;
+      for (int c = 0; c < 3; ++c) {
         const float ec = e[3 * o + c];
         const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
                           (e[3 * (o + sy) + c] + e[3 * (o - sy) + c] - 2.f * ec) * r2y +
                           (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
-        acc = fmaf(wt, r[3 * o + c] - lap, acc);
+        v[c] = r[3 * o + c] - lap;
       }
-  rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = acc * (1.0f / 64.0f);
+    }
+    s_res[3 * p] = v[0];
+    s_res[3 * p + 1] = v[1];
+    s_res[3 * p + 2] = v[2];
+  }
+  __syncthreads();
+  // levels halve exactly, so the 27 fine points of a coarse interior point
+  // are all interior
+  for (unsigned i = threadIdx.x; i < (unsigned)(kRTX * kRTY * kRTZ * 3); i += blockDim.x) {
+    const unsigned c = i % 3u, p = i / 3u;
+    const unsigned lx = p % kRTX, q = p / kRTX;
+    const unsigned ly = q % kRTY, lz = q / kRTY;
+    const unsigned x = cx0 + lx, y = cy0 + ly, z = cz0 + lz;
+    if (x + 1 >= C.np[0] || y + 1 >= C.np[1] || z + 1 >= C.np[2]) continue;
+    const float* sr = s_res + 3 * ((2 * lx + 1) + kRFX * ((2 * ly + 1) + kRFY * (2 * lz + 1))) + c;
+    float acc = 0.f;
+#pragma unroll
+    for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+      for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+        for (int dx = -1; dx <= 1; ++dx) {
+          const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
+          acc = fmaf(wt, sr[3 * (dx + kRFX * (dy + kRFY * dz))], acc);
+        }
+    rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = acc * (1.0f / 64.0f);
+  }
 }
 
-// e_fine += trilinear(e_coarse) on fine interior points.
+// e_fine += trilinear(e_coarse) at fine interior point (x, y, z).
 __device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, const float* __restrict__ ec,
-                                              float* __restrict__ ef, size_t k) {
-  unsigned x, y, z;
-  unflat(k, F, x, y, z);
-  if (!interior(F, x, y, z)) return;
+                                              float* __restrict__ ef, unsigned x, unsigned y, unsigned z) {
   const unsigned ox = x & 1, oy = y & 1, oz = z & 1;
-  const size_t sy = C.np[0], sz = (size_t)C.np[0] * C.np[1];
-  const size_t c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
+  const unsigned sy = C.np[0], sz = C.np[0] * C.np[1];
+  const unsigned c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
   float a0 = 0.f, a1 = 0.f, a2 = 0.f;
   const float wt = 1.0f / (float)(1u << (ox + oy + oz));
   for (unsigned iz = 0; iz <= oz; ++iz)
     for (unsigned iy = 0; iy <= oy; ++iy)
       for (unsigned ix = 0; ix <= ox; ++ix) {
-        const size_t o = c0 + ix + sy * iy + sz * iz;
+        const unsigned o = c0 + ix + sy * iy + sz * iz;
         a0 += ec[3 * o];
         a1 += ec[3 * o + 1];
         a2 += ec[3 * o + 2];
       }
+  const unsigned k = x + F.np[0] * (y + F.np[1] * z);
   ef[3 * k] += a0 * wt;
   ef[3 * k + 1] += a1 * wt;
   ef[3 * k + 2] += a2 * wt;
 }
 
-// Global-memory form: one thread per (fine interior point, component), the
-// same sums in the same order as prolong_point for that component; threads
-// along a row over (x, component), y and z from the block.
+// Global-memory form: one thread per coarse cell (cx .. cx+1) x (cy .. cy+1) x
+// (cz .. cz+1), all three components: it reads the cell's 8 corners once and
+// updates the 8 fine points (2 cx + ox, 2 cy + oy, 2 cz + oz) with the same
+// sums in the same order as prolong_point (fine boundary points skipped).
 __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
                                                      float* __restrict__ ef) {
-  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
-  const unsigned j = jc / 3u, c = jc - 3u * j;
-  const unsigned x = 1u + j;
-  if (y + 1 >= F.np[1] || x + 1 >= F.np[0]) return;
-  const unsigned ox = x & 1, oy = y & 1, oz = z & 1;
+  const unsigned cx = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned cy = blockIdx.y * blockDim.y + threadIdx.y, cz = blockIdx.z;
+  if (cx + 1 >= C.np[0] || cy + 1 >= C.np[1]) return;
   const unsigned sy = C.np[0], sz = C.np[0] * C.np[1];
-  const unsigned c0 = (x >> 1) + sy * (y >> 1) + sz * (z >> 1);
-  float a = 0.f;
-  const float wt = 1.0f / (float)(1u << (ox + oy + oz));
-  for (unsigned iz = 0; iz <= oz; ++iz)
-    for (unsigned iy = 0; iy <= oy; ++iy)
-      for (unsigned ix = 0; ix <= ox; ++ix) a += ec[3 * (c0 + ix + sy * iy + sz * iz) + c];
-  ef[3 * (x + F.np[0] * (y + F.np[1] * z)) + c] += a * wt;
+  const unsigned c0 = cx + sy * cy + sz * cz;
+  float v[2][2][2][3];  // [iz][iy][ix][component]
+#pragma unroll
+  for (int iz = 0; iz < 2; ++iz)
+#pragma unroll
+    for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+      for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) v[iz][iy][ix][c] = ec[3 * (c0 + ix + sy * iy + sz * iz) + c];
+  const unsigned fsy = F.np[0], fsz = F.np[0] * F.np[1];
+#pragma unroll
+  for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+    for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+      for (int ox = 0; ox < 2; ++ox) {
+        const unsigned X = 2 * cx + ox, Y = 2 * cy + oy, Z = 2 * cz + oz;
+        if (X == 0 || Y == 0 || Z == 0) continue;  // X <= nx - 2 etc. always
+        const float wt = 1.0f / (float)(1u << (ox + oy + oz));
+        const unsigned k = X + fsy * Y + fsz * Z;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          float a = 0.f;
+#pragma unroll
+          for (int iz = 0; iz <= oz; ++iz)
+#pragma unroll
+            for (int iy = 0; iy <= oy; ++iy)
+#pragma unroll
+              for (int ix = 0; ix <= ox; ++ix) a += v[iz][iy][ix][c];
+          ef[3 * k + c] += a * wt;
+        }
+      }
 }
 
 // Launch shape of the row kernels above over `items` (point, component)
@@ -396,6 +440,10 @@ struct SmallLevels {
   Geom g[kSmallMax];
   float r2x[kSmallMax], r2y[kSmallMax], r2z[kSmallMax], H[kSmallMax];
   unsigned off[kSmallMax];  // float offsets of e (r follows e) in shared memory
+  // Interior rows of a level as work items: row r = t >> sh, lane t & mask.
+  // shc: lanes for one colour's points of a row; sha: for all interior points.
+  unsigned shc[kSmallMax], sha[kSmallMax];
+  float inv_nyi[kSmallMax];  // 1 / (ny - 2): z = r / (ny - 2) by a float product
   const float* r_in;        // first small level's r (global)
   float* e_out;             // first small level's e (global)
   int pre, post, coarse_sweeps;
@@ -406,16 +454,34 @@ __device__ __forceinline__ float* sm_r(float* sm, const SmallLevels& S, int l) {
   return sm + S.off[l] + 3 * S.g[l].points();
 }
 
+// Work item t over the interior rows of small level l with 2^sh lanes per row:
+// lane j, interior row (y, z).  z = r / (ny - 2) by a float product, exact for
+// the row counts of these levels (r < 2^20, ny - 2 < 2^10).
+__device__ __forceinline__ void row_item(const SmallLevels& S, int l, unsigned sh, unsigned t, unsigned& j,
+                                         unsigned& y, unsigned& z) {
+  const unsigned nyi = S.g[l].np[1] - 2;
+  const unsigned r = t >> sh;
+  j = t & ((1u << sh) - 1u);
+  const unsigned zz = __float2uint_rz(((float)r + 0.5f) * S.inv_nyi[l]);
+  y = 1 + r - zz * nyi;
+  z = 1 + zz;
+}
+
+__device__ __forceinline__ unsigned row_items(const SmallLevels& S, int l, unsigned sh) {
+  return ((S.g[l].np[1] - 2) * (S.g[l].np[2] - 2)) << sh;
+}
+
 __device__ void block_rb_sweep(float* sm, const SmallLevels& S, int l, unsigned color, bool zero_first) {
   const Geom& g = S.g[l];
-  const size_t n = g.points();
   float* e = sm_e(sm, S, l);
   const float* r = sm_r(sm, S, l);
-  for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
-    unsigned x, y, z;
-    unflat(k, g, x, y, z);
-    if (!interior(g, x, y, z) || ((x + y + z) & 1u) != color) continue;
-    rbgs_point(g, S.r2x[l], S.r2y[l], S.r2z[l], S.H[l], e, r, k, zero_first);
+  const unsigned sh = S.shc[l], items = row_items(S, l, sh);
+  for (unsigned t = threadIdx.x; t < items; t += blockDim.x) {
+    unsigned j, y, z;
+    row_item(S, l, sh, t, j, y, z);
+    const unsigned x = 1u + ((color + 1u + y + z) & 1u) + 2u * j;
+    if (x + 1 >= g.np[0]) continue;
+    rbgs_point(g, S.r2x[l], S.r2y[l], S.r2z[l], S.H[l], e, r, x + g.np[0] * (y + g.np[1] * z), zero_first);
   }
   __syncthreads();
 }
@@ -438,9 +504,16 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
       block_rb_sweep(sm, S, l, 1, false);
     }
     const Geom& C = S.g[l + 1];
-    for (size_t k = threadIdx.x; k < C.points(); k += blockDim.x)
-      residual_restrict_point(S.g[l], C, S.r2x[l], S.r2y[l], S.r2z[l], sm_e(sm, S, l), sm_r(sm, S, l), k,
-                              sm_r(sm, S, l + 1));
+    {  // coarse interior points only: boundary r is never read (and stays 0)
+      const unsigned sh = S.sha[l + 1], items = row_items(S, l + 1, sh);
+      for (unsigned t = threadIdx.x; t < items; t += blockDim.x) {
+        unsigned j, y, z;
+        row_item(S, l + 1, sh, t, j, y, z);
+        if (j + 2 >= C.np[0]) continue;
+        residual_restrict_point(S.g[l], C, S.r2x[l], S.r2y[l], S.r2z[l], sm_e(sm, S, l), sm_r(sm, S, l), 1 + j,
+                                y, z, sm_r(sm, S, l + 1));
+      }
+    }
     __syncthreads();
   }
   {  // coarsest grid: FP64 red-black Gauss-Seidel from zero
@@ -458,10 +531,13 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
     __syncthreads();
     for (int it = 0; it < S.coarse_sweeps; ++it)
       for (unsigned color = 0; color < 2; ++color) {
-        for (size_t k = threadIdx.x; k < n; k += blockDim.x) {
-          unsigned x, y, z;
-          unflat(k, g, x, y, z);
-          if (!interior(g, x, y, z) || ((x + y + z) & 1u) != color) continue;
+        const unsigned sh = S.shc[l], items = row_items(S, l, sh);
+        for (unsigned t = threadIdx.x; t < items; t += blockDim.x) {
+          unsigned j, y, z;
+          row_item(S, l, sh, t, j, y, z);
+          const unsigned x = 1u + ((color + 1u + y + z) & 1u) + 2u * j;
+          if (x + 1 >= g.np[0]) continue;
+          const size_t k = x + (size_t)g.np[0] * (y + (size_t)g.np[1] * z);
           for (int c = 0; c < 3; ++c) {
             const double sv = (work[3 * (k + 1) + c] + work[3 * (k - 1) + c]) * cx +
                               (work[3 * (k + sy) + c] + work[3 * (k - sy) + c]) * cy +
@@ -477,8 +553,15 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
   }
   for (int l = S.n - 2; l >= 0; --l) {
     const Geom& F = S.g[l];
-    for (size_t k = threadIdx.x; k < F.points(); k += blockDim.x)
-      prolong_point(F, S.g[l + 1], sm_e(sm, S, l + 1), sm_e(sm, S, l), k);
+    {
+      const unsigned sh = S.sha[l], items = row_items(S, l, sh);
+      for (unsigned t = threadIdx.x; t < items; t += blockDim.x) {
+        unsigned j, y, z;
+        row_item(S, l, sh, t, j, y, z);
+        if (j + 2 >= F.np[0]) continue;
+        prolong_point(F, S.g[l + 1], sm_e(sm, S, l + 1), sm_e(sm, S, l), 1 + j, y, z);
+      }
+    }
     __syncthreads();
     for (int s = 0; s < S.post; ++s) {
       block_rb_sweep(sm, S, l, 0, false);
@@ -583,9 +666,9 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
         ++*nl;
       }
     const Lev& Cn = P.lev[l + 1];
-    const RowLaunch rl = launch_rows(3 * (Cn.g.np[0] - 2), Cn.g.np[1], Cn.g.np[2]);
-    k_residual_restrict<<<rl.grid, rl.block, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r,
-                                                             B.R + 3 * Cn.base);
+    const dim3 rg((Cn.g.np[0] - 2 + kRTX - 1) / kRTX, (Cn.g.np[1] - 2 + kRTY - 1) / kRTY,
+                  (Cn.g.np[2] - 2 + kRTZ - 1) / kRTZ);
+    k_residual_restrict<<<rg, 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r, B.R + 3 * Cn.base);
     ++*nl;
   }
   {
@@ -600,6 +683,12 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
       S.r2z[i] = L.r2z;
       S.H[i] = L.H;
       S.off[i] = off;
+      unsigned shc = 0, sha = 0;
+      while ((1u << shc) < (L.g.np[0] - 1) / 2) ++shc;
+      while ((1u << sha) < L.g.np[0] - 2) ++sha;
+      S.shc[i] = shc;
+      S.sha[i] = sha;
+      S.inv_nyi[i] = 1.0f / (float)(L.g.np[1] - 2);
       off += (unsigned)(6 * L.g.points());
     }
     S.r_in = B.R + 3 * P.lev[fs].base;
@@ -610,7 +699,8 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     // Gauss-Seidel on m interior points per axis contracts by about
     // cos^2(pi / (m + 1)) per sweep; 3 (m + 1)^2 sweeps reach ~1e-13.
     const unsigned m = std::max(cg.np[0], std::max(cg.np[1], cg.np[2])) - 2;
-    S.coarse_sweeps = (int)std::min(3u * m * m + 2u, 4000u);
+    // one interior point: a single sweep solves it exactly
+    S.coarse_sweeps = m == 1 ? 1 : (int)std::min(3u * m * m + 2u, 4000u);
     k_vcycle_small<<<1, 1024, P.small_smem, c->stream>>>(S, B.cwork);
     ++*nl;
   }
@@ -621,7 +711,9 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     float* r = B.R + 3 * L.base;
     const RowLaunch all = launch_rows(3 * (L.g.np[0] - 2), L.g.np[1], L.g.np[2]);  // every interior point
     const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);
-    k_prolong_add<<<all.grid, all.block, 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    const unsigned cells_x = Cn.g.np[0] - 1, pbx = cells_x >= 64 ? 64 : 32, pby = 256 / pbx;
+    const dim3 pg((cells_x + pbx - 1) / pbx, (Cn.g.np[1] - 1 + pby - 1) / pby, Cn.g.np[2] - 1);
+    k_prolong_add<<<pg, dim3(pbx, pby), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
