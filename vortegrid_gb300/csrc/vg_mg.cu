@@ -13,13 +13,15 @@
 //     a += e;
 //   * phase 1 iterates on the FP32 field with an FP32 residual while FP32 can
 //     still represent it (relative residual above 1e-4);
-//   * phase 2 (iterative refinement) keeps the iterate in FP64, evaluates
-//     r = b - L a in FP64 arithmetic, solves the correction L e = r with FP32
-//     cycles (the correction's residual is small, so FP32 tracks it well),
-//     adds e in FP64 and checks with another FP64 residual -- reaching
+//   * phase 2 (iterative refinement) keeps the iterate as the FP32 field plus
+//     an FP32 correction field, evaluates r = b - L a to FP64-class accuracy
+//     (float-pair sums with exact FMA-split products; GB300's FP64 pipe runs
+//     at a small fraction of its FP32 rate), solves the correction L e = r
+//     with FP32 cycles (the correction's residual is small, so FP32 tracks it
+//     well), accumulates e and checks with another such residual -- reaching
 //     residuals far below FP32's cancellation floor (~1e-4 at 128^3) with two
-//     FP64 residual evaluations per solve.
-// FP64 is used only for that residual, the coarsest-grid solve and the norms.
+//     accurate residual evaluations per solve.
+// FP64 is used for the coarsest-grid solve and the norms.
 // The levels of at most 17^3 points run inside one CTA with their fields in
 // shared memory; each cycle is captured once as a CUDA graph and replayed.
 // Grids are float[3] per point (x fastest); the three components are three
@@ -113,11 +115,34 @@ __global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, 
   block_sum2(rr, bb, part);
 }
 
-// Phase 2 residual: r = b - L a in FP64 arithmetic from the FP64 iterate,
-// stored as FP32; per-block FP64 partial sums of r^2 (b^2 slot unused).
-__global__ void __launch_bounds__(kRedThreads) k_residual64(Geom g, double r2x, double r2y, double r2z,
-                                                            const double* __restrict__ a, const float* __restrict__ b,
-                                                            float* __restrict__ r, double* __restrict__ part) {
+// Phase 2 residual: r = b - L (hi + lo) for the iterate kept as a pair of
+// FP32 fields (hi: phase 1's FP32 iterate, fixed during refinement; lo: the
+// accumulated corrections).  L hi, where b - L hi cancels to ~1e-6 of the
+// terms, is summed as an unevaluated pair of floats: every product
+// coefficient x value is split exactly by an FMA (the coefficients themselves
+// carried as float pairs) and added with error-free TwoSum, so the sum keeps
+// ~2^-46 relative accuracy -- the FP64-class residual of iterative refinement
+// without GB300's low-rate FP64 pipe.  L lo is small and needs only FP32.
+// Stored as FP32, with per-block FP64 partial sums of r^2 (b^2 slot unused).
+struct PairCoef {
+  float xh, xl, yh, yl, zh, zl, dh, dl;  // r2x, r2y, r2z and -2 (r2x + r2y + r2z) as float pairs
+  float r2x, r2y, r2z;                   // the FP32 operator of the cycles
+};
+
+__device__ __forceinline__ void pair_add_prod(float ch, float cl, float v, float& sh, float& sl) {
+  const float p = __fmul_rn(ch, v);
+  const float pe = __fmaf_rn(ch, v, -p);  // ch v - p exactly
+  const float t = __fadd_rn(sh, p);      // TwoSum(sh, p)
+  const float bv = __fsub_rn(t, sh);
+  const float err = __fadd_rn(__fsub_rn(sh, __fsub_rn(t, bv)), __fsub_rn(p, bv));
+  sh = t;
+  sl = __fadd_rn(sl, __fadd_rn(err, __fmaf_rn(cl, v, pe)));
+}
+
+__global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef cf, const float* __restrict__ hi,
+                                                               const float* __restrict__ lo,
+                                                               const float* __restrict__ b, float* __restrict__ r,
+                                                               double* __restrict__ part) {
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   float rr = 0.f;
   if (k < g.points()) {
@@ -125,14 +150,26 @@ __global__ void __launch_bounds__(kRedThreads) k_residual64(Geom g, double r2x, 
     unflat(k, g, x, y, z);
     if (interior(g, x, y, z)) {
       const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
-      const double d = -2.0 * (r2x + r2y + r2z);
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const double lap = fma(a[3 * k + c], d,
-                               fma(a[3 * (k + 1) + c] + a[3 * (k - 1) + c], r2x,
-                                   fma(a[3 * (k + sy) + c] + a[3 * (k - sy) + c], r2y,
-                                       (a[3 * (k + sz) + c] + a[3 * (k - sz) + c]) * r2z)));
-        const float rv = (float)((double)b[3 * k + c] - lap);
+        float sh = 0.f, sl = 0.f;
+        pair_add_prod(cf.dh, cf.dl, hi[3 * k + c], sh, sl);
+        pair_add_prod(cf.xh, cf.xl, hi[3 * (k + 1) + c], sh, sl);
+        pair_add_prod(cf.xh, cf.xl, hi[3 * (k - 1) + c], sh, sl);
+        pair_add_prod(cf.yh, cf.yl, hi[3 * (k + sy) + c], sh, sl);
+        pair_add_prod(cf.yh, cf.yl, hi[3 * (k - sy) + c], sh, sl);
+        pair_add_prod(cf.zh, cf.zl, hi[3 * (k + sz) + c], sh, sl);
+        pair_add_prod(cf.zh, cf.zl, hi[3 * (k - sz) + c], sh, sl);
+        const float l0 = lo[3 * k + c];
+        const float lap_lo = (lo[3 * (k + 1) + c] + lo[3 * (k - 1) + c] - 2.f * l0) * cf.r2x +
+                             (lo[3 * (k + sy) + c] + lo[3 * (k - sy) + c] - 2.f * l0) * cf.r2y +
+                             (lo[3 * (k + sz) + c] + lo[3 * (k - sz) + c] - 2.f * l0) * cf.r2z;
+        // r = (b - sh) - sl - lap_lo, the first difference by TwoSum
+        const float bv = b[3 * k + c];
+        const float t = __fsub_rn(bv, sh);
+        const float bb = __fsub_rn(t, bv);
+        const float terr = __fadd_rn(__fsub_rn(bv, __fsub_rn(t, bb)), __fsub_rn(-sh, bb));
+        const float rv = __fadd_rn(t, __fsub_rn(__fsub_rn(terr, sl), lap_lo));
         r[3 * k + c] = rv;
         rr = fmaf(rv, rv, rr);
       }
@@ -573,27 +610,13 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
   for (size_t k = threadIdx.x; k < n0; k += blockDim.x) S.e_out[k] = e0[k];
 }
 
-__global__ void k_to_f64(const float* __restrict__ a, double* __restrict__ b, size_t n) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) b[k] = (double)a[k];
-}
 
-__global__ void k_add_f64(double* __restrict__ a, const float* __restrict__ e, size_t n) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) a[k] += (double)e[k];
-}
+}  // namespace
 
 __global__ void k_add_f32(float* __restrict__ a, const float* __restrict__ e, size_t n) {
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) a[k] += e[k];
 }
-
-__global__ void k_to_f32(const double* __restrict__ a, float* __restrict__ b, size_t n) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k < n) b[k] = (float)a[k];
-}
-
-}  // namespace
 
 struct MgPlan {
   int nlev;
@@ -639,7 +662,7 @@ static MgPlan plan_levels(const Geom& g) {
 struct MgBufs {
   float* E;
   float* R;
-  double* a64;
+  float* lo;  // refinement: corrections accumulated on top of the FP32 iterate
   double* part;
   double* sums;
   double* cwork;
@@ -815,8 +838,8 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
   if (st != VG_OK) return st;
   B.E = (float*)mem;
   B.R = B.E + 3 * P.total;
-  B.a64 = (double*)(((uintptr_t)(B.R + 3 * P.total) + 255) & ~(uintptr_t)255);
-  B.part = B.a64 + 3 * n0;
+  B.lo = (float*)(((uintptr_t)(B.R + 3 * P.total) + 255) & ~(uintptr_t)255);
+  B.part = (double*)(((uintptr_t)(B.lo + 3 * n0) + 255) & ~(uintptr_t)255);
   B.sums = B.part + 2 * (size_t)nb0;
   B.cwork = B.sums + 4;
   B.nb0 = nb0;
@@ -838,6 +861,27 @@ __global__ void k_relres(const double* __restrict__ sums, double* __restrict__ o
 // The adaptive solve's steps with the cycle counts fixed in advance (k1 FP32
 // cycles, then one refinement round of k2 cycles) and no host round trip; the
 // relative residuals go to mg_relres_dev ([0] final, [1] initial).
+// The refinement residual's operator constants: FP64 values split into float
+// pairs (hi = nearest float, lo = the rest), and the cycles' FP32 operator.
+static PairCoef pair_coef(const Geom& g, const Lev& L0) {
+  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
+               r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
+  const double d = -2.0 * (r2x + r2y + r2z);
+  PairCoef cf;
+  cf.xh = (float)r2x;
+  cf.xl = (float)(r2x - (double)cf.xh);
+  cf.yh = (float)r2y;
+  cf.yl = (float)(r2y - (double)cf.yh);
+  cf.zh = (float)r2z;
+  cf.zl = (float)(r2z - (double)cf.zh);
+  cf.dh = (float)d;
+  cf.dl = (float)(d - (double)cf.dh);
+  cf.r2x = L0.r2x;
+  cf.r2y = L0.r2y;
+  cf.r2z = L0.r2z;
+  return cf;
+}
+
 vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* rhs3) {
   const MgPlan P = plan_levels(g);
   MgBufs B;
@@ -847,9 +891,8 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
   if (!c->mg_relres_dev) return fail(c, VG_INVALID, "multigrid: no device slot for the residual");
   const size_t n0 = g.points();
   const unsigned nb0 = B.nb0;
-  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
-               r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
   const Lev& L0 = P.lev[0];
+  const PairCoef cf = pair_coef(g, L0);
   unsigned nl = 0;
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
   k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
@@ -858,8 +901,8 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
   nl += 3;
   for (int k = 0; k < c->mg_fixed_k1; ++k)
     if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl)) != VG_OK) return st;
-  k_to_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.a64, 3 * n0);
-  k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+  VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
+  k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
   nl += 3;
   if (c->mg_fixed_k2 > 0) {
@@ -867,13 +910,13 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
     VG_CUDA(c, cudaMemcpyAsync(B.R, rir, 3 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     for (int k = 0; k < c->mg_fixed_k2; ++k)
       if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl)) != VG_OK) return st;
-    k_add_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, etot, 3 * n0);
-    k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+    k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.lo, etot, 3 * n0);
+    k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
     nl += 3;
   }
   k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev);
-  k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, soln3, 3 * n0);
+  k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.lo, 3 * n0);
   nl += 2;
   c->launches += nl;
   VG_CUDA(c, cudaGetLastError());
@@ -889,12 +932,11 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   vg_status st = setup_bufs(c, g, P, B, &etot, &rir);
   if (st != VG_OK) return st;
   const unsigned nb0 = B.nb0;
-  const double r2x = 1.0 / ((double)g.cell[0] * g.cell[0]), r2y = 1.0 / ((double)g.cell[1] * g.cell[1]),
-               r2z = 1.0 / ((double)g.cell[2] * g.cell[2]);
   // e must be zero on every level's boundary (Dirichlet correction); the
   // kernels only ever write interior points.
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
   const Lev& L0 = P.lev[0];
+  const PairCoef cf = pair_coef(g, L0);
   k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
   c->launches += 2;
@@ -914,20 +956,21 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
     relres = std::sqrt(rr) / bn;
   }
   const int k1 = cyc;
-  // Phase 2: iterative refinement.  FP64 residual of the FP64 iterate, FP32
-  // cycles on the correction equation L e = r (its residual updated in FP32,
-  // accurate because r is already small), a64 += e, and an FP64 check.
-  k_to_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.a64, 3 * n0);
-  VG_LAUNCHED(c);
+  // Phase 2: iterative refinement.  The iterate is soln3 + lo (lo from zero);
+  // the residual b - L (soln3 + lo) is evaluated to FP64-class accuracy by
+  // k_residual_pair, FP32 cycles solve the correction equation L e = r (its
+  // residual updated in FP32, accurate because r is already small), lo += e,
+  // and another such residual checks.
+  VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
   for (;;) {
-    k_residual64<<<nb0, kRedThreads, 0, c->stream>>>(g, r2x, r2y, r2z, B.a64, rhs3, rir, B.part);
+    k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
     c->launches += 2;
     if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
     relres = std::sqrt(rr) / bn;
     if (relres <= tol || cyc >= max_cycles) break;
-    // The FP32 residual of the correction equation tracks the FP64 residual of
-    // a64 + e to ~1e-11 relative (its right-hand side is already below 1e-4),
+    // The FP32 residual of the correction equation tracks the accurate residual
+    // of soln3 + lo + e to ~1e-11 relative (its right-hand side is already below 1e-4),
     // so half the tolerance is margin enough for the FP64 check that follows.
     const double inner_tol = std::max(0.5 * tol, 1e-4 * relres);
     VG_CUDA(c, cudaMemsetAsync(etot, 0, 3 * n0 * sizeof(float), c->stream));
@@ -939,10 +982,10 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
       if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
       inner = std::sqrt(rr) / bn;
     }
-    k_add_f64<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, etot, 3 * n0);
+    k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.lo, etot, 3 * n0);
     VG_LAUNCHED(c);
   }
-  k_to_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.a64, soln3, 3 * n0);
+  k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.lo, 3 * n0);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   c->mg_last_k1 = k1;
