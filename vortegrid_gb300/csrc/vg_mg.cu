@@ -59,43 +59,68 @@ __device__ __forceinline__ bool interior(const Geom& g, unsigned x, unsigned y, 
   return x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2];
 }
 
-// Block reduction of two sums into part[2 * blockIdx.x + {0, 1}]: 32-term
-// warp sums in FP32 (relative error ~1e-6, irrelevant for a norm), then FP64
-// across warps, blocks and the grid.
+// Block reduction (kRedThreads threads, any 2D shape) of two sums into
+// part[2 * b + {0, 1}], b the linear block index: 32-term warp sums in FP32
+// (relative error ~1e-6, irrelevant for a norm), then FP64 across warps,
+// blocks and the grid.
 __device__ __forceinline__ void block_sum2(float a32, float b32, double* __restrict__ part) {
   __shared__ double s_a[kRedThreads / 32], s_b[kRedThreads / 32];
+  const unsigned tid = threadIdx.x + blockDim.x * threadIdx.y;
   for (int o = 16; o > 0; o >>= 1) {
     a32 += __shfl_xor_sync(0xffffffffu, a32, o);
     b32 += __shfl_xor_sync(0xffffffffu, b32, o);
   }
-  if ((threadIdx.x & 31) == 0) {
-    s_a[threadIdx.x >> 5] = (double)a32;
-    s_b[threadIdx.x >> 5] = (double)b32;
+  if ((tid & 31) == 0) {
+    s_a[tid >> 5] = (double)a32;
+    s_b[tid >> 5] = (double)b32;
   }
   __syncthreads();
-  if (threadIdx.x == 0) {
+  if (tid == 0) {
     double t1 = 0.0, t2 = 0.0;
     for (int w = 0; w < kRedThreads / 32; ++w) {
       t1 += s_a[w];
       t2 += s_b[w];
     }
-    part[2 * blockIdx.x] = t1;
-    part[2 * blockIdx.x + 1] = t2;
+    const unsigned b = blockIdx.x + gridDim.x * (blockIdx.y + gridDim.y * blockIdx.z);
+    part[2 * b] = t1;
+    part[2 * b + 1] = t2;
   }
 }
 
-// Phase 1 residual: r = b - L a in FP32 from the FP32 iterate; per-block FP64
-// partial sums of r^2 and b^2.
-__global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, float r2y, float r2z,
+// Residual kernels run over interior points in rows: blocks of (bx, by) =
+// kRedThreads threads over (x, y), each thread stepping through `zs` planes.
+struct ResLaunch {
+  dim3 grid, block;
+  unsigned zs, nb;  // planes per thread, blocks (= partial sums)
+};
+static ResLaunch res_launch(const Geom& g) {
+  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, nzi = g.np[2] - 2;
+  unsigned bx = 32;
+  while (bx < nxi && bx < (unsigned)kRedThreads) bx <<= 1;
+  const unsigned by = kRedThreads / bx;
+  const unsigned gx = (nxi + bx - 1) / bx, gy = (nyi + by - 1) / by;
+  const unsigned zs = (size_t)gx * gy * nzi >= 4096 ? 4 : 1;
+  ResLaunch L;
+  L.block = dim3(bx, by, 1);
+  L.grid = dim3(gx, gy, (nzi + zs - 1) / zs);
+  L.zs = zs;
+  L.nb = L.grid.x * L.grid.y * L.grid.z;
+  return L;
+}
+
+// Phase 1 residual: r = b - L a in FP32 from the FP32 iterate at interior
+// points (boundary r is never read); per-block FP64 partial sums of r^2 and b^2.
+__global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, float r2y, float r2z, unsigned zs,
                                                              const float* __restrict__ a, const float* __restrict__ b,
                                                              float* __restrict__ r, double* __restrict__ part) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned x = blockIdx.x * blockDim.x + threadIdx.x + 1, y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
   float rr = 0.f, bb = 0.f;
-  if (k < g.points()) {
-    unsigned x, y, z;
-    unflat(k, g, x, y, z);
-    if (interior(g, x, y, z)) {
-      const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
+  if (x + 1 < nx && y + 1 < ny) {
+    const unsigned sy = nx, sz = nx * ny;
+    const unsigned z0 = 1 + blockIdx.z * zs, z1 = min(nz - 1, z0 + zs);
+    for (unsigned z = z0; z < z1; ++z) {
+      const unsigned k = x + sy * y + sz * z;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         const float ac = a[3 * k + c];
@@ -108,8 +133,6 @@ __global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, 
         rr = fmaf(rv, rv, rr);
         bb = fmaf(bv, bv, bb);
       }
-    } else {
-      r[3 * k] = r[3 * k + 1] = r[3 * k + 2] = 0.f;
     }
   }
   block_sum2(rr, bb, part);
@@ -139,17 +162,19 @@ __device__ __forceinline__ void pair_add_prod(float ch, float cl, float v, float
   sl = __fadd_rn(sl, __fadd_rn(err, __fmaf_rn(cl, v, pe)));
 }
 
-__global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef cf, const float* __restrict__ hi,
+__global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef cf, unsigned zs,
+                                                               const float* __restrict__ hi,
                                                                const float* __restrict__ lo,
                                                                const float* __restrict__ b, float* __restrict__ r,
                                                                double* __restrict__ part) {
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned x = blockIdx.x * blockDim.x + threadIdx.x + 1, y = blockIdx.y * blockDim.y + threadIdx.y + 1;
+  const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
   float rr = 0.f;
-  if (k < g.points()) {
-    unsigned x, y, z;
-    unflat(k, g, x, y, z);
-    if (interior(g, x, y, z)) {
-      const size_t sy = g.np[0], sz = (size_t)g.np[0] * g.np[1];
+  if (x + 1 < nx && y + 1 < ny) {
+    const unsigned sy = nx, sz = nx * ny;
+    const unsigned z0 = 1 + blockIdx.z * zs, z1 = min(nz - 1, z0 + zs);
+    for (unsigned z = z0; z < z1; ++z) {
+      const unsigned k = x + sy * y + sz * z;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
         float sh = 0.f, sl = 0.f;
@@ -173,8 +198,6 @@ __global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef 
         r[3 * k + c] = rv;
         rr = fmaf(rv, rv, rr);
       }
-    } else {
-      r[3 * k] = r[3 * k + 1] = r[3 * k + 2] = 0.f;
     }
   }
   block_sum2(rr, 0.f, part);
@@ -666,7 +689,8 @@ struct MgBufs {
   double* part;
   double* sums;
   double* cwork;
-  unsigned nb0;
+  unsigned nb0;  // residual blocks (partial sums)
+  ResLaunch rl;   // the residual kernels' launch over level 0
 };
 
 // One V(pre, post)-cycle on L e = R[level 0] (level 0's e starts from zero).
@@ -766,7 +790,7 @@ static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgB
     k_add_f32<<<blocks_for(n3, 256), 256, 0, c->stream>>>(x, B.E, n3);
     ++*nl;
   }
-  k_residual32n<<<B.nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, x, rhs, B.R, B.part);
+  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
   *nl += 2;
   VG_CUDA(c, cudaGetLastError());
@@ -828,7 +852,8 @@ static vg_status read_norm(Ctx* c, const MgBufs& B, double* rr, double* bb) {
 // Buffers of a solve on grid g (grow-only workspace slot S_MG).
 static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, float** etot, float** rir) {
   const size_t n0 = g.points();
-  const unsigned nb0 = blocks_for(n0, kRedThreads);
+  const ResLaunch rl = res_launch(g);
+  const unsigned nb0 = rl.nb;
   const size_t coarse_pts = P.lev[P.nlev - 1].g.points();
   const size_t bytes = 2 * P.total * 3 * sizeof(float) + n0 * 3 * sizeof(double) + (size_t)nb0 * 2 * sizeof(double) +
                        4 * sizeof(double) + coarse_pts * 3 * sizeof(double) + 2 * n0 * 3 * sizeof(float) + 4096;
@@ -843,6 +868,7 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
   B.sums = B.part + 2 * (size_t)nb0;
   B.cwork = B.sums + 4;
   B.nb0 = nb0;
+  B.rl = rl;
   *etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
   *rir = *etot + 3 * n0;                                                                 // IR right-hand side
   static bool smem_set = false;
@@ -895,14 +921,15 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
   const PairCoef cf = pair_coef(g, L0);
   unsigned nl = 0;
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
-  k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
+  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
+                                                         B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
   k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev + 1);
   nl += 3;
   for (int k = 0; k < c->mg_fixed_k1; ++k)
     if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl)) != VG_OK) return st;
   VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
-  k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
+  k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
   nl += 3;
   if (c->mg_fixed_k2 > 0) {
@@ -911,7 +938,7 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
     for (int k = 0; k < c->mg_fixed_k2; ++k)
       if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl)) != VG_OK) return st;
     k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.lo, etot, 3 * n0);
-    k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
+    k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
     nl += 3;
   }
@@ -937,7 +964,8 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
   const Lev& L0 = P.lev[0];
   const PairCoef cf = pair_coef(g, L0);
-  k_residual32n<<<nb0, kRedThreads, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, soln3, rhs3, B.R, B.part);
+  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
+                                                         B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
   c->launches += 2;
   double rr = 0.0, bnorm2 = 0.0;
@@ -963,7 +991,7 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   // and another such residual checks.
   VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
   for (;;) {
-    k_residual_pair<<<nb0, kRedThreads, 0, c->stream>>>(g, cf, soln3, B.lo, rhs3, rir, B.part);
+    k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
     c->launches += 2;
     if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
