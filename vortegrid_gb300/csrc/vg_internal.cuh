@@ -185,6 +185,7 @@ enum Slot {
   S_TRACERS,
   S_RED,
   S_PREV,
+  S_MGINV,
   S_NUM
 };
 
@@ -227,6 +228,9 @@ struct Ctx {
   // Vortons that leave a fixed grid: an error (false), or stopped and left out
   // of the solve, with dflag[1] recording that it happened (true).
   bool freeze_outside = false;
+  // the multigrid coarsest-level inverse held in buf[S_MGINV]: its level's shape and 1 / spacing^2
+  unsigned mginv_np[3] = {0, 0, 0};
+  double mginv_r2[3] = {0.0, 0.0, 0.0};
 };
 
 // The word a kernel marks when a sample lies outside the grid's cells.

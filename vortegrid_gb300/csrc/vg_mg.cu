@@ -30,6 +30,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <vector>
 
 #include "vg_internal.cuh"
 
@@ -494,6 +495,7 @@ static RowLaunch launch_rows(unsigned items, unsigned ny, unsigned nz) {
 // The first small level reads its r from global memory and writes its e back.
 constexpr int kSmallMax = 8;
 constexpr int kCoarseShared = 1536;  // doubles of the coarsest solve kept in shared memory
+constexpr unsigned kDirectMax = 512;  // interior points of a coarsest level solved by sine transforms
 constexpr size_t kSmallLevelPoints = 17 * 17 * 17;
 struct SmallLevels {
   int n;  // levels handled here
@@ -504,6 +506,7 @@ struct SmallLevels {
   // shc: lanes for one colour's points of a row; sha: for all interior points.
   unsigned shc[kSmallMax], sha[kSmallMax];
   float inv_nyi[kSmallMax];  // 1 / (ny - 2): z = r / (ny - 2) by a float product
+  const float* dst;         // coarsest level solved exactly: its sine-transform tables (direct_tables), or null
   const float* r_in;        // first small level's r (global)
   float* e_out;             // first small level's e (global)
   int pre, post, coarse_sweeps;
@@ -576,7 +579,56 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
     }
     __syncthreads();
   }
-  {  // coarsest grid: FP64 red-black Gauss-Seidel from zero
+  if (S.dst) {
+    // Coarsest grid solved exactly: L is diagonalised by the discrete sine
+    // transform along each axis, so e = S (D^-1 (S r)) with S = Sx Sy Sz
+    // (orthonormal DST-I, its own inverse) and D the eigenvalues.  Seven
+    // passes over the interior, ping-ponging between this level's r and e
+    // arrays in compact layout (3 (x + nx' (y + ny' z)) + c).
+    const int l = S.n - 1;
+    const Geom& g = S.g[l];
+    const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, nzi = g.np[2] - 2, N = nxi * nyi * nzi;
+    float* E = sm_e(sm, S, l);
+    float* R = sm_r(sm, S, l);
+    const float* Sx = S.dst;
+    const float* Sy = Sx + nxi * nxi;
+    const float* Sz = Sy + nyi * nyi;
+    const float* Dinv = Sz + nzi * nzi;
+    for (unsigned i = threadIdx.x; i < 3 * N; i += blockDim.x) {  // R (full) -> E (compact)
+      const unsigned c = i % 3u, p = i / 3u;
+      const unsigned x = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
+      E[i] = R[3 * ((x + 1) + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c];
+    }
+    __syncthreads();
+    // one transform pass along axis a (stride st, length n, table T): out = T in
+    auto pass = [&](const float* in, float* out, const float* T, unsigned n, unsigned st, bool scale) {
+      for (unsigned i = threadIdx.x; i < 3 * N; i += blockDim.x) {
+        const unsigned c = i % 3u, p = i / 3u;
+        const unsigned k = (p / st) % n, p0 = p - k * st;
+        float acc = 0.f;
+        for (unsigned m = 0; m < n; ++m) acc = fmaf(__ldg(T + k * n + m), in[3 * (p0 + m * st) + c], acc);
+        out[i] = scale ? acc * __ldg(Dinv + p) : acc;
+      }
+      __syncthreads();
+    };
+    pass(E, R, Sx, nxi, 1, false);
+    pass(R, E, Sy, nyi, nxi, false);
+    pass(E, R, Sz, nzi, nxi * nyi, true);
+    pass(R, E, Sz, nzi, nxi * nyi, false);
+    pass(E, R, Sy, nyi, nxi, false);
+    // last pass along x writes e in full layout (interior), zero on the boundary
+    for (unsigned i = threadIdx.x; i < 3 * (unsigned)g.points(); i += blockDim.x) {
+      const unsigned c = i % 3u, k = i / 3u;
+      const unsigned x = k % g.np[0], q = k / g.np[0], y = q % g.np[1], z = q / g.np[1];
+      float v = 0.f;
+      if (x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2]) {
+        const unsigned kx = x - 1, p0 = nxi * ((y - 1) + nyi * (z - 1));
+        for (unsigned m = 0; m < nxi; ++m) v = fmaf(__ldg(Sx + kx * nxi + m), R[3 * (p0 + m) + c], v);
+      }
+      E[i] = v;
+    }
+    __syncthreads();
+  } else {  // coarsest grid: FP64 red-black Gauss-Seidel from zero
     const int l = S.n - 1;
     const Geom& g = S.g[l];
     const size_t n = g.points();
@@ -647,6 +699,7 @@ struct MgPlan {
   size_t total;
   int first_small;    // first level run by k_vcycle_small
   size_t small_smem;  // its dynamic shared memory (bytes)
+  bool direct;        // the coarsest level is solved exactly by its operator's inverse
 };
 
 static MgPlan plan_levels(const Geom& g) {
@@ -671,6 +724,20 @@ static MgPlan plan_levels(const Geom& g) {
     if (!can) break;
     cur = decimate(cur, 2);
   }
+  // Stop at the finest level with at most kDirectMax interior points and solve
+  // it exactly there by sine transforms: the levels below it would cost a
+  // V-cycle of short barrier-bound phases.
+  P.direct = false;
+  for (int l = 0; l < P.nlev; ++l) {
+    const Geom& lg = P.lev[l].g;
+    if ((size_t)(lg.np[0] - 2) * (lg.np[1] - 2) * (lg.np[2] - 2) <= kDirectMax) {
+      P.nlev = l + 1;
+      P.direct = true;
+      break;
+    }
+  }
+  total = 0;
+  for (int l = 0; l < P.nlev; ++l) total += P.lev[l].g.points();
   P.total = total;
   int fs = P.nlev - 1;  // the coarsest level always runs in the CTA kernel
   while (fs > 1 && P.lev[fs - 1].g.points() <= kSmallLevelPoints && P.nlev - (fs - 1) <= kSmallMax) --fs;
@@ -689,6 +756,7 @@ struct MgBufs {
   double* part;
   double* sums;
   double* cwork;
+  const float* dst;  // the coarsest level's sine-transform tables when P.direct
   unsigned nb0;  // residual blocks (partial sums)
   ResLaunch rl;   // the residual kernels' launch over level 0
 };
@@ -738,6 +806,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
       S.inv_nyi[i] = 1.0f / (float)(L.g.np[1] - 2);
       off += (unsigned)(6 * L.g.points());
     }
+    S.dst = P.direct ? B.dst : nullptr;
     S.r_in = B.R + 3 * P.lev[fs].base;
     S.e_out = B.E + 3 * P.lev[fs].base;
     S.pre = pre;
@@ -849,6 +918,52 @@ static vg_status read_norm(Ctx* c, const MgBufs& B, double* rr, double* bb) {
   return VG_OK;
 }
 
+// Tables of the exact coarsest-level solve: per axis the orthonormal DST-I
+// matrix S[k][m] = sqrt(2 / (n + 1)) sin(pi (m + 1) (k + 1) / (n + 1)) of its
+// n interior points, then 1 / eigenvalue of L for every transformed point,
+// eig = -(r2x lx + r2y ly + r2z lz) with l(k) = 2 - 2 cos(pi (k + 1) / (n + 1))
+// (FP64 on the host, stored as FP32).  Uploaded when the level's shape or
+// spacing changes; never during stream capture, which the calibrated
+// schedules guarantee by running the same grid uncaptured first.
+static vg_status direct_tables(Ctx* c, const Geom& lg, const float** out) {
+  const double r2[3] = {1.0 / ((double)lg.cell[0] * lg.cell[0]), 1.0 / ((double)lg.cell[1] * lg.cell[1]),
+                        1.0 / ((double)lg.cell[2] * lg.cell[2])};
+  if (c->mginv_np[0] == lg.np[0] && c->mginv_np[1] == lg.np[1] && c->mginv_np[2] == lg.np[2] &&
+      c->mginv_r2[0] == r2[0] && c->mginv_r2[1] == r2[1] && c->mginv_r2[2] == r2[2] && c->buf[S_MGINV].p) {
+    *out = (const float*)c->buf[S_MGINV].p;
+    return VG_OK;
+  }
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
+  if (cap != cudaStreamCaptureStatusNone)
+    return fail(c, VG_INVALID, "multigrid: the coarsest-level tables are not ready (run this grid uncaptured first)");
+  const unsigned n[3] = {lg.np[0] - 2, lg.np[1] - 2, lg.np[2] - 2};
+  const double pi = 3.14159265358979323846;
+  std::vector<float> h;
+  std::vector<double> lam[3];
+  for (int a = 0; a < 3; ++a) {
+    const double f = std::sqrt(2.0 / (n[a] + 1));
+    for (unsigned k = 0; k < n[a]; ++k)
+      for (unsigned m = 0; m < n[a]; ++m) h.push_back((float)(f * std::sin(pi * (m + 1) * (k + 1) / (n[a] + 1))));
+    for (unsigned k = 0; k < n[a]; ++k) lam[a].push_back(2.0 - 2.0 * std::cos(pi * (k + 1) / (n[a] + 1)));
+  }
+  for (unsigned z = 0; z < n[2]; ++z)
+    for (unsigned y = 0; y < n[1]; ++y)
+      for (unsigned x = 0; x < n[0]; ++x)
+        h.push_back((float)(-1.0 / (r2[0] * lam[0][x] + r2[1] * lam[1][y] + r2[2] * lam[2][z])));
+  vg_status st = VG_OK;
+  float* d = (float*)ws(c, S_MGINV, h.size() * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  VG_CUDA(c, cudaMemcpyAsync(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+  VG_CUDA(c, cudaStreamSynchronize(c->stream));  // h is released on return
+  for (int a = 0; a < 3; ++a) {
+    c->mginv_np[a] = lg.np[a];
+    c->mginv_r2[a] = r2[a];
+  }
+  *out = d;
+  return VG_OK;
+}
+
 // Buffers of a solve on grid g (grow-only workspace slot S_MG).
 static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, float** etot, float** rir) {
   const size_t n0 = g.points();
@@ -869,6 +984,8 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
   B.cwork = B.sums + 4;
   B.nb0 = nb0;
   B.rl = rl;
+  B.dst = nullptr;
+  if (P.direct && (st = direct_tables(c, P.lev[P.nlev - 1].g, &B.dst)) != VG_OK) return st;
   *etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
   *rir = *etot + 3 * n0;                                                                 // IR right-hand side
   static bool smem_set = false;
