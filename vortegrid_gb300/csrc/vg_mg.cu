@@ -279,6 +279,35 @@ __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, floa
   e[3 * k + c] = v;
 }
 
+// The first pre-smoothing sweep from e = 0, both colours in one pass: red
+// points take -r H, black points the Gauss-Seidel update from those red
+// values (recomputed from r, the same float operations as the two half
+// sweeps, so the result is identical).  Threads over every interior (point,
+// component), as k_rbgs_add.
+__global__ void __launch_bounds__(256) k_rbgs_first(Geom g, float r2x, float r2y, float r2z, float H,
+                                                    float* __restrict__ e, const float* __restrict__ r) {
+  const unsigned nx = g.np[0], ny = g.np[1];
+  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
+  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
+  const unsigned j = jc / 3u, c = jc - 3u * j;
+  const unsigned x = 1u + j;
+  if (y + 1 >= ny || x + 1 >= nx) return;
+  const unsigned k = x + nx * (y + ny * z), t = 3 * k + c;
+  float v;
+  if (((x + y + z) & 1u) == 0u) {
+    v = -r[t] * H;
+  } else {
+    const unsigned sy = nx, sz = nx * ny;
+    // red neighbours: -r H (boundary neighbours stay e = 0)
+    auto red = [&](unsigned n, bool in) { return in ? -r[3 * n + c] * H : 0.f; };
+    const float sx = red(k + 1, x + 2 < nx) + red(k - 1, x > 1);
+    const float syv = red(k + sy, y + 2 < ny) + red(k - sy, y > 1);
+    const float szv = red(k + sz, z + 2 < g.np[2]) + red(k - sz, z > 1);
+    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[t]) * H;
+  }
+  e[t] = v;
+}
+
 // The last half sweep of a cycle fused with x += e: threads cover every
 // (point, component); points of `color` take their smoothed value and add it
 // to x, the others (already final) just add theirs.  Boundary points carry no
@@ -774,10 +803,12 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
     const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);  // one colour's points
-    for (int s = 0; s < pre; ++s)
+    const RowLaunch all = launch_rows(3 * (L.g.np[0] - 2), L.g.np[1], L.g.np[2]);     // every interior point
+    k_rbgs_first<<<all.grid, all.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r);
+    ++*nl;
+    for (int s = 1; s < pre; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col,
-                                                    (s == 0 && col == 0) ? 1 : 0);
+        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
         ++*nl;
       }
     const Lev& Cn = P.lev[l + 1];
