@@ -586,6 +586,21 @@ def poisson_section(vg, torch, stream, local, steps=3):
     return out
 
 
+def run_section(name):
+    """One workload section alone on cuda:0 (its own JSON object), for profiling."""
+    import torch
+    import vortegrid_gb300 as vg
+    torch.cuda.set_device(0)
+    stream = torch.cuda.Stream()
+    if name == "poisson":
+        out = poisson_section(vg, torch, stream, 0)
+    elif name == "treecode":
+        out = treecode_section(vg, torch, stream, 0)
+    else:
+        out = batched_section(torch, 0)
+    print(json.dumps({"section": name, name: out}), flush=True)
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -594,7 +609,12 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--skip-poisson", action="store_true")
+    ap.add_argument("--section", choices=["poisson", "treecode", "batched"],
+                    help="run one workload section alone and print its JSON (for profiling)")
     args = ap.parse_args()
+    if args.section:
+        run_section(args.section)
+        return
     args.warmup = max(args.warmup, 3) if args.impl == "ours" else args.warmup
     world, rank, local = dist_setup() if args.impl == "ours" else (int(os.environ.get("WORLD_SIZE", "1")),
                                                                   int(os.environ.get("RANK", "0")), 0)
