@@ -330,6 +330,37 @@ def test_multigrid_reaches_tolerance(vg, oracle_lib, field):
         assert np.linalg.norm(v - d) / np.linalg.norm(d) < 0.08  # measured 4.2%
 
 
+def test_multigrid_anisotropic_box(vg, oracle_lib):
+    """The multigrid stage on a non-cubic box with unequal spacings (33 x 65 x
+    17 points; its coarsest level, 9 x 17 x 5, is solved exactly by sine
+    transforms along each axis) reaches 1e-6 and matches an independent FP64
+    sparse solve of the same discrete problem to 1e-5 relative."""
+    pytest.importorskip("scipy")
+    g = vg.GridGeom.make([-1.0, -1.5, -0.375], [2.0, 3.0, 0.75], [33, 65, 17])
+    n = g.capacity
+    rng = np.random.default_rng(7)
+    b = rng.normal(size=(n, 3)).astype(np.float32)
+    a0 = np.zeros((17, 65, 33, 3), np.float32)
+    bnd = rng.normal(size=a0.shape).astype(np.float32) * 1e-3
+    for sl in ((0,), (-1,)):
+        a0[sl] = bnd[sl]
+        a0[:, sl[0]] = bnd[:, sl[0]]
+        a0[:, :, sl[0]] = bnd[:, :, sl[0]]
+    a0 = a0.reshape(-1, 3)
+    ctx = vg.Context(numerics=vg.NUMERICS_FAST)
+    soln, rhs = dev(a0), dev(b)
+    cyc, r0, r1 = ctypes.c_int(), ctypes.c_double(), ctypes.c_double()
+    ctx.check(vg.lib().vg_multigrid_device(ctx.h, ctypes.byref(g), vg._ptr(soln), vg._ptr(rhs), 1e-6, 50,
+                                           ctypes.byref(cyc), ctypes.byref(r0), ctypes.byref(r1)), "multigrid")
+    sync()
+    a = soln.cpu().numpy()
+    assert r1.value <= 1e-6 and 1 <= cyc.value <= 12, (r1.value, cyc.value)
+    og = oracle_lib.Geom.from12(g.as12(), g.points)
+    assert oracle_lib.relres(og, a, b) < 1e-4  # the FP32 copy of the refined iterate
+    exact = _exact_discrete_solve(og, b, a)
+    assert np.linalg.norm(a - exact) / np.linalg.norm(exact) < 1e-5
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)
