@@ -198,6 +198,78 @@ __device__ float3 tree_walk(const TreeParams& T, const float4* __restrict__ sp, 
   return res;
 }
 
+// FAST form of the same walk.  The opening test is geometric and separable
+// per axis (the query lies in the child's box widened by 1e-4 cells along x,
+// y and z), so the cells opened at a layer always form a box of 1 or 2 cells
+// per axis (2 where the query is within the margin of a face -- every grid
+// point is).  Walk the layers with that box in registers: the children of the
+// open cells that are not themselves opened add their monopoles, the opened
+// ones form the next layer's box.  Same cells as tree_walk, summed layer by
+// layer instead of depth first (FAST numerics sum in any order).
+template <int KIND>
+__device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__ sp, const float4* __restrict__ sw,
+                                 const float4* __restrict__ ps, const float4* __restrict__ w, int n, float qx,
+                                 float qy, float qz, float sr, float sc) {
+  float3 acc = make_float3(0.f, 0.f, 0.f);
+  if (T.depth <= 1) {  // no tree: direct sum (vortonSim.cpp:2125-2128)
+    for (int i = 0; i < n; ++i) fast_accum<KIND>(acc, qx, qy, qz, ps[i], w[i], sr, sc);
+    return acc;
+  }
+  const float mfac = 0.0001f;
+  const float q[3] = {qx, qy, qz};
+  unsigned f0[3] = {0u, 0u, 0u}, fn[3] = {1u, 1u, 1u};  // open box of layer L: [f0, f0 + fn) per axis
+  for (int L = T.depth - 1; L >= 1; --L) {
+    const Geom& C = T.layer[L - 1];
+    unsigned c0[3], cn[3], o0[3], on[3];
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      const unsigned d = T.decim[L][a];
+      c0[a] = f0[a] * d;
+      cn[a] = fn[a] * d;
+      on[a] = 0;
+      o0[a] = 0;
+      if (L > 1) {  // children open along this axis: a contiguous run of 1 or 2
+        const float m = (a == 2) ? __fadd_rn(__fmul_rn(mfac, C.cell[2]), (0.0f == C.cell[2]) ? FLT_MIN : 0.0f)
+                                 : __fmul_rn(mfac, C.cell[a]);
+        for (unsigned i = 0; i < cn[a]; ++i) {
+          const unsigned ch = c0[a] + i;
+          const float lo = __fadd_rn(C.mn[a], __fmul_rn((float)ch, C.cell[a]));
+          const float hi = __fadd_rn(C.mn[a], __fmul_rn((float)(ch + 1), C.cell[a]));
+          if (q[a] >= __fsub_rn(lo, m) && q[a] < __fadd_rn(hi, m)) {
+            if (on[a] == 0) o0[a] = ch;
+            ++on[a];
+          }
+        }
+      }
+    }
+    const bool any = on[0] && on[1] && on[2];
+    for (unsigned iz = 0; iz < cn[2]; ++iz)
+      for (unsigned iy = 0; iy < cn[1]; ++iy)
+        for (unsigned ix = 0; ix < cn[0]; ++ix) {
+          const unsigned chx = c0[0] + ix, chy = c0[1] + iy, chz = c0[2] + iz;
+          if (any && chx - o0[0] < on[0] && chy - o0[1] < on[1] && chz - o0[2] < on[2]) continue;  // opened
+          const size_t o = T.base[L - 1] + chx + (size_t)C.np[0] * (chy + (size_t)C.np[1] * chz);
+          fast_accum<KIND>(acc, qx, qy, qz, sp[o], sw[o], sr, sc);
+        }
+    if (!any) break;
+#pragma unroll
+    for (int a = 0; a < 3; ++a) {
+      f0[a] = o0[a];
+      fn[a] = on[a];
+    }
+  }
+  return acc;
+}
+
+template <int KIND, bool REF>
+__device__ __forceinline__ float3 walk(const TreeParams& T, const float4* __restrict__ sp,
+                                       const float4* __restrict__ sw, const float4* __restrict__ ps,
+                                       const float4* __restrict__ w, int n, float qx, float qy, float qz, float sr,
+                                       float sc) {
+  if (REF) return tree_walk<KIND, true>(T, sp, sw, ps, w, n, qx, qy, qz, sr, sc);
+  return tree_walk_fast<KIND>(T, sp, sw, ps, w, n, qx, qy, qz, sr, sc);
+}
+
 template <int KIND, bool REF>
 __global__ void __launch_bounds__(128) k_tree_eval(const __grid_constant__ TreeParams T, const float4* __restrict__ sp,
                                                     const float4* __restrict__ sw, const float4* __restrict__ ps,
@@ -206,7 +278,7 @@ __global__ void __launch_bounds__(128) k_tree_eval(const __grid_constant__ TreeP
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   const float4 v = q[j];
-  const float3 r = tree_walk<KIND, REF>(T, sp, sw, ps, w, n, v.x, v.y, v.z, sr, sc);
+  const float3 r = walk<KIND, REF>(T, sp, sw, ps, w, n, v.x, v.y, v.z, sr, sc);
   out[j] = make_float4(r.x, r.y, r.z, 0.f);
 }
 
@@ -271,7 +343,7 @@ __global__ void __launch_bounds__(128) k_boundary_vecpot(const __grid_constant__
     const float qx = __fadd_rn(g.mn[0], __fmul_rn((float)xq, __fmul_rn(g.cell[0], nudge)));
     const float qy = __fadd_rn(g.mn[1], __fmul_rn((float)y, __fmul_rn(g.cell[1], nudge)));
     const float qz = __fadd_rn(g.mn[2], __fmul_rn((float)z, __fmul_rn(g.cell[2], nudge)));
-    r = tree_walk<1, REF>(T, sp, sw, ps, w, n, qx, qy, qz, 1.0f, 1.0f);
+    r = walk<1, REF>(T, sp, sw, ps, w, n, qx, qy, qz, 1.0f, 1.0f);
   }
   const size_t o = x + (size_t)g.np[0] * (y + (size_t)g.np[1] * z);
   grid3[3 * o] = r.x;
