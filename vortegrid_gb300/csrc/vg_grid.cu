@@ -240,8 +240,11 @@ __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* _
 __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ ps, const float4* __restrict__ w0,
                                              float4* __restrict__ w, int n, const unsigned* __restrict__ start,
                                              const unsigned* __restrict__ items, float nu, float dt) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  // threads take the vortons in cell order, so a warp's vortons share their
+  // neighbour cells (each vorton's sums are the same whichever thread runs them)
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = (int)items[t];
   const float4 p = ps[i];
   const float4 wi = w0[i];
   const int nx = (int)g.np[0], ny = (int)g.np[1], nz = (int)g.np[2];
