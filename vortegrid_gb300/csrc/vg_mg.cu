@@ -46,20 +46,6 @@ struct Lev {
   size_t base;             // offset (points) into level arrays
 };
 
-// Grids here have fewer than 2^32 points, so index math stays in 32 bits
-// (64-bit integer division costs tens of instructions on the GPU).
-__device__ __forceinline__ void unflat(size_t k, const Geom& g, unsigned& x, unsigned& y, unsigned& z) {
-  const unsigned k32 = (unsigned)k, nx = g.np[0], ny = g.np[1];
-  const unsigned q = k32 / nx;
-  x = k32 - q * nx;
-  z = q / ny;
-  y = q - z * ny;
-}
-
-__device__ __forceinline__ bool interior(const Geom& g, unsigned x, unsigned y, unsigned z) {
-  return x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2];
-}
-
 // Block reduction (kRedThreads threads, any 2D shape) of two sums into
 // part[2 * b + {0, 1}], b the linear block index: 32-term warp sums in FP32
 // (relative error ~1e-6, irrelevant for a norm), then FP64 across warps,
@@ -306,35 +292,6 @@ __global__ void __launch_bounds__(256) k_rbgs_first(Geom g, float r2x, float r2y
     v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[t]) * H;
   }
   e[t] = v;
-}
-
-// The last half sweep of a cycle fused with x += e: threads cover every
-// (point, component); points of `color` take their smoothed value and add it
-// to x, the others (already final) just add theirs.  Boundary points carry no
-// correction.
-__global__ void __launch_bounds__(256) k_rbgs_add(Geom g, float r2x, float r2y, float r2z, float H,
-                                                  float* __restrict__ e, const float* __restrict__ r,
-                                                  unsigned color, float* __restrict__ x_out) {
-  // threads over (interior x, component) along a row; y, z from the block
-  const unsigned nx = g.np[0], ny = g.np[1];
-  const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
-  const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
-  const unsigned j = jc / 3u, c = jc - 3u * j;
-  const unsigned x = 1u + j;
-  if (y + 1 >= ny || x + 1 >= nx) return;
-  const unsigned k = x + nx * (y + ny * z), t = 3 * k + c;
-  float v;
-  if (((x + y + z) & 1u) == color) {
-    const unsigned sy = nx, sz = nx * ny;
-    const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
-    const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
-    const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
-    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[t]) * H;
-    e[t] = v;
-  } else {
-    v = e[t];
-  }
-  x_out[t] += v;
 }
 
 // Fused FP32 residual + full-weighting restriction at coarse interior point
@@ -722,6 +679,33 @@ __global__ void k_add_f32(float* __restrict__ a, const float* __restrict__ e, si
   if (k < n) a[k] += e[k];
 }
 
+// a += e as float4 over the first n4 groups of 4 (both arrays 16-byte
+// aligned), the n - 4 n4 remaining floats one by one.
+__global__ void k_add_f32x4(float* __restrict__ a, const float* __restrict__ e, size_t n4, size_t n) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k < n4) {
+    float4 va = reinterpret_cast<float4*>(a)[k];
+    const float4 ve = reinterpret_cast<const float4*>(e)[k];
+    va.x += ve.x;
+    va.y += ve.y;
+    va.z += ve.z;
+    va.w += ve.w;
+    reinterpret_cast<float4*>(a)[k] = va;
+  } else if (k - n4 < n - 4 * n4) {
+    a[4 * n4 + (k - n4)] += e[4 * n4 + (k - n4)];
+  }
+}
+
+// a[0, n) += e[0, n) on the stream (vectorised when both are 16-byte aligned).
+static void add_f32(Ctx* c, float* a, const float* e, size_t n) {
+  if ((((uintptr_t)a | (uintptr_t)e) & 15) == 0) {
+    const size_t n4 = n / 4;
+    k_add_f32x4<<<blocks_for(n4 + 3, 256), 256, 0, c->stream>>>(a, e, n4, n);
+  } else {
+    k_add_f32<<<blocks_for(n, 256), 256, 0, c->stream>>>(a, e, n);
+  }
+}
+
 struct MgPlan {
   int nlev;
   Lev lev[kMaxLayers];
@@ -790,12 +774,9 @@ struct MgBufs {
   ResLaunch rl;   // the residual kernels' launch over level 0
 };
 
-// One V(pre, post)-cycle on L e = R[level 0] (level 0's e starts from zero).
-// One V-cycle on L e = r (level 0's e and r in B).  With x, the last half
-// sweep on level 0 also adds e to x (*added says whether that happened: not
-// when every level is small).
-static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float* x, bool* added, unsigned* nl) {
-  *added = false;
+// One V(pre, post)-cycle on L e = R[level 0] (level 0's e and r in B; e
+// starts from zero).
+static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsigned* nl) {
   const int pre = 2, post = 2;
   const int fs = P.first_small;
   for (int l = 0; l < fs; ++l) {
@@ -856,7 +837,6 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     const Lev& Cn = P.lev[l + 1];
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
-    const RowLaunch all = launch_rows(3 * (L.g.np[0] - 2), L.g.np[1], L.g.np[2]);  // every interior point
     const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);
     const unsigned cells_x = Cn.g.np[0] - 1, pbx = cells_x >= 64 ? 64 : 32, pby = 256 / pbx;
     const dim3 pg((cells_x + pbx - 1) / pbx, (Cn.g.np[1] - 1 + pby - 1) / pby, Cn.g.np[2] - 1);
@@ -864,12 +844,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        if (x && l == 0 && s == post - 1 && col == 1) {
-          k_rbgs_add<<<all.grid, all.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, x);
-          *added = true;
-        } else {
-          k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
-        }
+        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
         ++*nl;
       }
   }
@@ -881,15 +856,14 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, float*
 // R = rhs - L x in FP32 with its FP64-accumulated norm.
 static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
                                unsigned* nl) {
-  bool added = false;
-  vg_status st = enqueue_vcycle(c, P, B, x, &added, nl);
+  vg_status st = enqueue_vcycle(c, P, B, nl);
   if (st != VG_OK) return st;
   const size_t n3 = 3 * g.points();
   const Lev& L0 = P.lev[0];
-  if (!added) {
-    k_add_f32<<<blocks_for(n3, 256), 256, 0, c->stream>>>(x, B.E, n3);
-    ++*nl;
-  }
+  // x += e as a separate streaming pass: fused into the last half sweep it
+  // measured slower (x is not in L2 by then, and the sweep's gathers wait on it)
+  add_f32(c, x, B.E, n3);
+  ++*nl;
   k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
   *nl += 2;
@@ -1085,13 +1059,13 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
     VG_CUDA(c, cudaMemcpyAsync(B.R, rir, 3 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     for (int k = 0; k < c->mg_fixed_k2; ++k)
       if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl)) != VG_OK) return st;
-    k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.lo, etot, 3 * n0);
+    add_f32(c, B.lo, etot, 3 * n0);
     k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
     nl += 3;
   }
   k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev);
-  k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.lo, 3 * n0);
+  add_f32(c, soln3, B.lo, 3 * n0);
   nl += 2;
   c->launches += nl;
   VG_CUDA(c, cudaGetLastError());
@@ -1158,10 +1132,10 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
       if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
       inner = std::sqrt(rr) / bn;
     }
-    k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(B.lo, etot, 3 * n0);
+    add_f32(c, B.lo, etot, 3 * n0);
     VG_LAUNCHED(c);
   }
-  k_add_f32<<<blocks_for(3 * n0, 256), 256, 0, c->stream>>>(soln3, B.lo, 3 * n0);
+  add_f32(c, soln3, B.lo, 3 * n0);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   c->mg_last_k1 = k1;
