@@ -481,7 +481,8 @@ static RowLaunch launch_rows(unsigned items, unsigned ny, unsigned nz) {
 // The first small level reads its r from global memory and writes its e back.
 constexpr int kSmallMax = 8;
 constexpr int kCoarseShared = 1536;  // doubles of the coarsest solve kept in shared memory
-constexpr unsigned kDirectMax = 512;  // interior points of a coarsest level solved by sine transforms
+constexpr unsigned kDirectMax = 512;         // interior points of a coarsest level solved in the small-level CTA
+constexpr unsigned kDirectGlobalMax = 4096;  // ... or by sine-transform passes over the whole GPU
 constexpr size_t kSmallLevelPoints = 17 * 17 * 17;
 struct SmallLevels {
   int n;  // levels handled here
@@ -706,13 +707,55 @@ static void add_f32(Ctx* c, float* a, const float* e, size_t n) {
   }
 }
 
+// The exact coarsest solve of k_vcycle_small as passes over the whole GPU,
+// for a coarsest level of up to kDirectGlobalMax interior points: gather r
+// into compact order (3 (x + nx' (y + ny' z)) + c), five sine-transform passes
+// (the third scaled by 1 / eigenvalue), and the last x pass writing e in
+// full layout (zero on the boundary).  Same operations as the CTA form.
+__global__ void __launch_bounds__(256) k_dst_gather(Geom g, const float* __restrict__ rfull, float* __restrict__ X) {
+  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * N) return;
+  const unsigned c = i % 3u, p = i / 3u;
+  const unsigned x = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
+  X[i] = rfull[3 * ((x + 1) + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c];
+}
+
+__global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const float* __restrict__ in, float* __restrict__ out,
+                                                  const float* __restrict__ T, unsigned n, unsigned st,
+                                                  const float* __restrict__ Dinv) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * N) return;
+  const unsigned c = i % 3u, p = i / 3u;
+  const unsigned k = (p / st) % n, p0 = p - k * st;
+  float acc = 0.f;
+  for (unsigned m = 0; m < n; ++m) acc = fmaf(__ldg(T + k * n + m), in[3 * (p0 + m * st) + c], acc);
+  out[i] = Dinv ? acc * __ldg(Dinv + p) : acc;
+}
+
+__global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const float* __restrict__ Y, const float* __restrict__ Sx,
+                                                     float* __restrict__ efull) {
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * (unsigned)g.points()) return;
+  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2;
+  const unsigned c = i % 3u, k = i / 3u;
+  const unsigned x = k % g.np[0], q = k / g.np[0], y = q % g.np[1], z = q / g.np[1];
+  float v = 0.f;
+  if (x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2]) {
+    const unsigned kx = x - 1, p0 = nxi * ((y - 1) + nyi * (z - 1));
+    for (unsigned m = 0; m < nxi; ++m) v = fmaf(__ldg(Sx + kx * nxi + m), Y[3 * (p0 + m) + c], v);
+  }
+  efull[i] = v;
+}
+
 struct MgPlan {
   int nlev;
   Lev lev[kMaxLayers];
   size_t total;
   int first_small;    // first level run by k_vcycle_small
   size_t small_smem;  // its dynamic shared memory (bytes)
-  bool direct;        // the coarsest level is solved exactly by its operator's inverse
+  bool direct;        // the coarsest level is solved exactly (sine transforms)
+  bool direct_global;  // ... by kernels over the whole GPU instead of in the small-level CTA
 };
 
 static MgPlan plan_levels(const Geom& g) {
@@ -740,24 +783,30 @@ static MgPlan plan_levels(const Geom& g) {
   // Stop at the finest level with at most kDirectMax interior points and solve
   // it exactly there by sine transforms: the levels below it would cost a
   // V-cycle of short barrier-bound phases.
-  P.direct = false;
+  P.direct = P.direct_global = false;
   for (int l = 0; l < P.nlev; ++l) {
     const Geom& lg = P.lev[l].g;
-    if ((size_t)(lg.np[0] - 2) * (lg.np[1] - 2) * (lg.np[2] - 2) <= kDirectMax) {
+    const size_t interior = (size_t)(lg.np[0] - 2) * (lg.np[1] - 2) * (lg.np[2] - 2);
+    if (interior <= kDirectGlobalMax) {
       P.nlev = l + 1;
       P.direct = true;
+      // a few thousand interior points: seven passes over the GPU cost less
+      // than the single-CTA V-cycle (or transform) of that level
+      P.direct_global = interior > kDirectMax;
       break;
     }
   }
   total = 0;
   for (int l = 0; l < P.nlev; ++l) total += P.lev[l].g.points();
   P.total = total;
-  int fs = P.nlev - 1;  // the coarsest level always runs in the CTA kernel
-  while (fs > 1 && P.lev[fs - 1].g.points() <= kSmallLevelPoints && P.nlev - (fs - 1) <= kSmallMax) --fs;
+  int fs = P.nlev - 1;  // the coarsest level runs in the CTA kernel (or the global transform)
+  if (!P.direct_global)
+    while (fs > 1 && P.lev[fs - 1].g.points() <= kSmallLevelPoints && P.nlev - (fs - 1) <= kSmallMax) --fs;
   if (P.nlev == 1) fs = 0;
   P.first_small = fs;
   size_t floats = 0;
-  for (int l = fs; l < P.nlev; ++l) floats += 6 * P.lev[l].g.points();
+  if (!P.direct_global)
+    for (int l = fs; l < P.nlev; ++l) floats += 6 * P.lev[l].g.points();
   P.small_smem = floats * sizeof(float);
   return P;
 }
@@ -798,7 +847,26 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     k_residual_restrict<<<rg, 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r, B.R + 3 * Cn.base);
     ++*nl;
   }
-  {
+  if (P.direct_global) {
+    const Lev& L = P.lev[fs];
+    const Geom& g = L.g;
+    const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, nzi = g.np[2] - 2, N = nxi * nyi * nzi;
+    float* E = B.E + 3 * L.base;  // ping-pong buffers in compact layout (3 N <= 3 points)
+    float* R = B.R + 3 * L.base;
+    const float* Sx = B.dst;
+    const float* Sy = Sx + nxi * nxi;
+    const float* Sz = Sy + nyi * nyi;
+    const float* Dinv = Sz + nzi * nzi;
+    const unsigned nb = blocks_for(3 * N, 256);
+    k_dst_gather<<<nb, 256, 0, c->stream>>>(g, R, E);
+    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sx, nxi, 1, nullptr);
+    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, R, E, Sy, nyi, nxi, nullptr);
+    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sz, nzi, nxi * nyi, Dinv);
+    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, R, E, Sz, nzi, nxi * nyi, nullptr);
+    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sy, nyi, nxi, nullptr);
+    k_dst_scatter<<<blocks_for(3 * g.points(), 256), 256, 0, c->stream>>>(g, R, Sx, E);
+    *nl += 7;
+  } else {
     SmallLevels S;
     S.n = P.nlev - fs;
     unsigned off = 0;
