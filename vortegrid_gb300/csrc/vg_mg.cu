@@ -482,7 +482,7 @@ static RowLaunch launch_rows(unsigned items, unsigned ny, unsigned nz) {
 constexpr int kSmallMax = 8;
 constexpr int kCoarseShared = 1536;  // doubles of the coarsest solve kept in shared memory
 constexpr unsigned kDirectMax = 512;         // interior points of a coarsest level solved in the small-level CTA
-constexpr unsigned kDirectGlobalMax = 4096;  // ... or by sine-transform passes over the whole GPU
+constexpr unsigned kDirectGlobalMax = 32768;  // ... or by sine-transform passes over the whole GPU
 constexpr size_t kSmallLevelPoints = 17 * 17 * 17;
 struct SmallLevels {
   int n;  // levels handled here
