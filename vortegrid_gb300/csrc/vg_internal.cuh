@@ -186,6 +186,7 @@ enum Slot {
   S_RED,
   S_PREV,
   S_MGINV,
+  S_TREEPREP,
   S_NUM
 };
 

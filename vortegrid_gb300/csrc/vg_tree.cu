@@ -198,6 +198,41 @@ __device__ float3 tree_walk(const TreeParams& T, const float4* __restrict__ sp, 
   return res;
 }
 
+// FAST walk's per-cell constants for one call's spread factors sr, sc:
+// tp = (centroid, 1 / R), tw = (angular velocity x 2/3 R^3 sc, R^2), R =
+// size / 2 x sr -- what fast_accum derives from (sp, sw) at every pair.
+__global__ void k_tree_prep(const float4* __restrict__ sp, const float4* __restrict__ sw, size_t total, float sr,
+                            float sc, float4* __restrict__ tp, float4* __restrict__ tw) {
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= total) return;
+  const float4 p = sp[k], a = sw[k];
+  const float radius = p.w * 0.5f * sr;
+  const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
+  tp[k] = make_float4(p.x, p.y, p.z, 1.0f / radius);
+  tw[k] = make_float4(a.x * s, a.y * s, a.z * s, radius * radius);
+}
+
+// fast_accum's law from prepared constants (the same mathematics, the scale
+// folded into the angular velocity).
+template <int KIND>
+__device__ __forceinline__ void prep_accum(float3& acc, float qx, float qy, float qz, float4 tp, float4 tw) {
+  const float d0 = qx - tp.x, d1 = qy - tp.y, d2 = qz - tp.z;
+  const float dist2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+  if (KIND == 0) {
+    const float inv = fminf(rsqrtf(dist2), tp.w);
+    const float law = inv * inv * inv;
+    const float b0 = d0 * law, b1 = d1 * law, b2 = d2 * law;
+    acc.x = fmaf(tw.y, b2, fmaf(-tw.z, b1, acc.x));
+    acc.y = fmaf(tw.z, b0, fmaf(-tw.x, b2, acc.y));
+    acc.z = fmaf(tw.x, b1, fmaf(-tw.y, b0, acc.z));
+  } else {
+    const float law = (dist2 < tw.w) ? dist2 * tp.w * tp.w * tp.w : rsqrtf(dist2);
+    acc.x = fmaf(tw.x, law, acc.x);
+    acc.y = fmaf(tw.y, law, acc.y);
+    acc.z = fmaf(tw.z, law, acc.z);
+  }
+}
+
 // FAST form of the same walk.  The opening test is geometric and separable
 // per axis (the query lies in the child's box widened by 1e-4 cells along x,
 // y and z), so the cells opened at a layer always form a box of 1 or 2 cells
@@ -207,7 +242,7 @@ __device__ float3 tree_walk(const TreeParams& T, const float4* __restrict__ sp, 
 // ones form the next layer's box.  Same cells as tree_walk, summed layer by
 // layer instead of depth first (FAST numerics sum in any order).
 template <int KIND>
-__device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__ sp, const float4* __restrict__ sw,
+__device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__ tp, const float4* __restrict__ tw,
                                  const float4* __restrict__ ps, const float4* __restrict__ w, int n, float qx,
                                  float qy, float qz, float sr, float sc) {
   float3 acc = make_float3(0.f, 0.f, 0.f);
@@ -249,7 +284,7 @@ __device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__
           const unsigned chx = c0[0] + ix, chy = c0[1] + iy, chz = c0[2] + iz;
           if (any && chx - o0[0] < on[0] && chy - o0[1] < on[1] && chz - o0[2] < on[2]) continue;  // opened
           const size_t o = T.base[L - 1] + chx + (size_t)C.np[0] * (chy + (size_t)C.np[1] * chz);
-          fast_accum<KIND>(acc, qx, qy, qz, sp[o], sw[o], sr, sc);
+          prep_accum<KIND>(acc, qx, qy, qz, tp[o], tw[o]);
         }
     if (!any) break;
 #pragma unroll
@@ -261,24 +296,27 @@ __device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__
   return acc;
 }
 
+// REFERENCE numerics walk the raw cells (sp, sw); FAST the prepared ones (tp, tw).
 template <int KIND, bool REF>
 __device__ __forceinline__ float3 walk(const TreeParams& T, const float4* __restrict__ sp,
-                                       const float4* __restrict__ sw, const float4* __restrict__ ps,
+                                       const float4* __restrict__ sw, const float4* __restrict__ tp,
+                                       const float4* __restrict__ tw, const float4* __restrict__ ps,
                                        const float4* __restrict__ w, int n, float qx, float qy, float qz, float sr,
                                        float sc) {
   if (REF) return tree_walk<KIND, true>(T, sp, sw, ps, w, n, qx, qy, qz, sr, sc);
-  return tree_walk_fast<KIND>(T, sp, sw, ps, w, n, qx, qy, qz, sr, sc);
+  return tree_walk_fast<KIND>(T, tp, tw, ps, w, n, qx, qy, qz, sr, sc);
 }
 
 template <int KIND, bool REF>
 __global__ void __launch_bounds__(128) k_tree_eval(const __grid_constant__ TreeParams T, const float4* __restrict__ sp,
-                                                    const float4* __restrict__ sw, const float4* __restrict__ ps,
+                                                    const float4* __restrict__ sw, const float4* __restrict__ tp,
+                                                    const float4* __restrict__ tw, const float4* __restrict__ ps,
                                                     const float4* __restrict__ w, int n, const float4* __restrict__ q,
                                                     int m, float sr, float sc, float4* __restrict__ out) {
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   const float4 v = q[j];
-  const float3 r = walk<KIND, REF>(T, sp, sw, ps, w, n, v.x, v.y, v.z, sr, sc);
+  const float3 r = walk<KIND, REF>(T, sp, sw, tp, tw, ps, w, n, v.x, v.y, v.z, sr, sc);
   out[j] = make_float4(r.x, r.y, r.z, 0.f);
 }
 
@@ -319,6 +357,7 @@ __device__ __forceinline__ bool face_point(const Geom& g, size_t t, unsigned& x,
 template <bool REF>
 __global__ void __launch_bounds__(128) k_boundary_vecpot(const __grid_constant__ TreeParams T, Geom g,
                                                           const float4* __restrict__ sp, const float4* __restrict__ sw,
+                                                          const float4* __restrict__ tp, const float4* __restrict__ tw,
                                                           const float4* __restrict__ ps, const float4* __restrict__ w,
                                                           int n, int copy_odd_x, size_t nface,
                                                           float* __restrict__ grid3) {
@@ -343,7 +382,7 @@ __global__ void __launch_bounds__(128) k_boundary_vecpot(const __grid_constant__
     const float qx = __fadd_rn(g.mn[0], __fmul_rn((float)xq, __fmul_rn(g.cell[0], nudge)));
     const float qy = __fadd_rn(g.mn[1], __fmul_rn((float)y, __fmul_rn(g.cell[1], nudge)));
     const float qz = __fadd_rn(g.mn[2], __fmul_rn((float)z, __fmul_rn(g.cell[2], nudge)));
-    r = walk<1, REF>(T, sp, sw, ps, w, n, qx, qy, qz, 1.0f, 1.0f);
+    r = walk<1, REF>(T, sp, sw, tp, tw, ps, w, n, qx, qy, qz, 1.0f, 1.0f);
   }
   const size_t o = x + (size_t)g.np[0] * (y + (size_t)g.np[1] * z);
   grid3[3 * o] = r.x;
@@ -467,13 +506,33 @@ vg_status build_tree(Ctx* c, const Geom& g, const float4* ps, const float4* w, s
   return VG_OK;
 }
 
+// The FAST walk's prepared cells (workspace slot S_TREEPREP) for spread
+// factors sr, sc; nothing when the tree has no layers (the walk then sums the
+// vortons directly).
+static vg_status tree_prep(Ctx* c, const Tree& t, float sr, float sc, float4** tp, float4** tw) {
+  if (t.depth <= 1 || t.total == 0) return VG_OK;
+  vg_status st = VG_OK;
+  float4* buf = (float4*)ws(c, S_TREEPREP, 2 * t.total * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  *tp = buf;
+  *tw = buf + t.total;
+  k_tree_prep<<<blocks_for(t.total, 256), 256, 0, c->stream>>>(t.sv_pos, t.sv_w, t.total, sr, sc, *tp, *tw);
+  VG_LAUNCHED(c);
+  return VG_OK;
+}
+
 vg_status launch_tree_eval(Ctx* c, int kind, bool ref, const Tree& t, const float4* ps, const float4* w, size_t n,
                            const float4* q, size_t m, float sr, float sc, float4* out) {
   if (m == 0) return VG_OK;
   const TreeParams T = make_params(t);
   const unsigned blocks = blocks_for(m, 128);
+  float4 *tp = nullptr, *tw = nullptr;
+  if (!ref) {
+    vg_status st = tree_prep(c, t, sr, sc, &tp, &tw);
+    if (st != VG_OK) return st;
+  }
 #define VG_TREE_LAUNCH(K, R) \
-  k_tree_eval<K, R><<<blocks, 128, 0, c->stream>>>(T, t.sv_pos, t.sv_w, ps, w, (int)n, q, (int)m, sr, sc, out)
+  k_tree_eval<K, R><<<blocks, 128, 0, c->stream>>>(T, t.sv_pos, t.sv_w, tp, tw, ps, w, (int)n, q, (int)m, sr, sc, out)
   if (kind == 0) {
     if (ref) VG_TREE_LAUNCH(0, true); else VG_TREE_LAUNCH(0, false);
   } else {
@@ -491,12 +550,16 @@ vg_status launch_boundary_vecpot(Ctx* c, const Tree& t, const Geom& g, const flo
   const size_t nx = g.np[0], ny = g.np[1], nz = g.np[2];
   const size_t nface = 2 * nx * ny + 2 * nx * (nz > 2 ? nz - 2 : 0) + 2 * (ny > 2 ? ny - 2 : 0) * (nz > 2 ? nz - 2 : 0);
   if (nface == 0) return VG_OK;
-  if (ref)
-    k_boundary_vecpot<true><<<blocks_for(nface, 128), 128, 0, c->stream>>>(T, g, t.sv_pos, t.sv_w, ps, w, (int)n,
-                                                                             copy_odd_x ? 1 : 0, nface, grid3);
-  else
-    k_boundary_vecpot<false><<<blocks_for(nface, 128), 128, 0, c->stream>>>(T, g, t.sv_pos, t.sv_w, ps, w, (int)n,
-                                                                              copy_odd_x ? 1 : 0, nface, grid3);
+  if (ref) {
+    k_boundary_vecpot<true><<<blocks_for(nface, 128), 128, 0, c->stream>>>(
+        T, g, t.sv_pos, t.sv_w, nullptr, nullptr, ps, w, (int)n, copy_odd_x ? 1 : 0, nface, grid3);
+  } else {
+    float4 *tp = nullptr, *tw = nullptr;
+    vg_status st = tree_prep(c, t, 1.0f, 1.0f, &tp, &tw);
+    if (st != VG_OK) return st;
+    k_boundary_vecpot<false><<<blocks_for(nface, 128), 128, 0, c->stream>>>(
+        T, g, t.sv_pos, t.sv_w, tp, tw, ps, w, (int)n, copy_odd_x ? 1 : 0, nface, grid3);
+  }
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
