@@ -237,16 +237,28 @@ __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* _
 // Order-independent PSE: vorton i exchanges with every vorton of the pair set
 // the reference visits (same cell, or cells offset by {0,1}^3 either way with
 // the lower cell strictly inside the point range), using pre-step values.
-__global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ ps, const float4* __restrict__ w0,
+// Pre-step positions and angular velocities in cell order (pss[t], w0s[t] of
+// vorton items[t]), so that each cell's vortons are contiguous for k_pse.
+__global__ void k_pse_gather(const float4* __restrict__ ps, const float4* __restrict__ w, int n,
+                             const unsigned* __restrict__ items, float4* __restrict__ pss, float4* __restrict__ w0s) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const unsigned j = items[t];
+  pss[t] = ps[j];
+  w0s[t] = w[j];
+}
+
+__global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ pss, const float4* __restrict__ w0s,
                                              float4* __restrict__ w, int n, const unsigned* __restrict__ start,
                                              const unsigned* __restrict__ items, float nu, float dt) {
   // threads take the vortons in cell order, so a warp's vortons share their
-  // neighbour cells (each vorton's sums are the same whichever thread runs them)
+  // neighbour cells and read them contiguously (each vorton's sums are the
+  // same whichever thread runs them)
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int i = (int)items[t];
-  const float4 p = ps[i];
-  const float4 wi = w0[i];
+  const float4 p = pss[t];
+  const float4 wi = w0s[t];
   const int nx = (int)g.np[0], ny = (int)g.np[1], nz = (int)g.np[2];
   // cell coordinates clamped to [-2, n + 1]: beyond that every neighbour test
   // below fails the same way, and ncx = cx + ox cannot overflow
@@ -273,14 +285,14 @@ __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ 
       for (unsigned kk = b; kk < e; ++kk) {
         const unsigned j = items[kk];
         if (j == (unsigned)i) continue;
-        const float4 pj = ps[j];
+        const float4 pj = pss[kk];
         const unsigned here = (k == 0) ? min((unsigned)i, j) : (s == 1 ? (unsigned)i : j);
         const float range = 4.0f * (here == (unsigned)i ? p.w : pj.w);
         const float dx = p.x - pj.x, dy = p.y - pj.y, dz = p.z - pj.z;
         const float dist2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const float law = __expf(-dist2 / (range * range));
         const float frac = fminf(fmaxf(twonudt * law, -0.5f), 0.5f);
-        const float4 wj = w0[j];
+        const float4 wj = w0s[kk];
         ax = fmaf(frac, wj.x - wi.x, ax);
         ay = fmaf(frac, wj.y - wi.y, ay);
         az = fmaf(frac, wj.z - wi.z, az);
@@ -477,11 +489,12 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
                      float dt) {
   if (n == 0) return VG_OK;
   vg_status st = VG_OK;
-  float4* w0 = (float4*)ws(c, S_WOLD, n * sizeof(float4), &st);
+  float4* pss = (float4*)ws(c, S_WOLD, 2 * n * sizeof(float4), &st);
   if (st != VG_OK) return st;
-  VG_CUDA(c, cudaMemcpyAsync(w0, w, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
-  k_pse<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, ps, w0, w, (int)n, cl.start, cl.items, nu, dt);
-  VG_LAUNCHED(c);
+  float4* w0s = pss + n;
+  k_pse_gather<<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, cl.items, pss, w0s);
+  k_pse<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, pss, w0s, w, (int)n, cl.start, cl.items, nu, dt);
+  c->launches += 2;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }
