@@ -413,11 +413,11 @@ __device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, cons
   ef[3 * k + 2] += a2 * wt;
 }
 
-// Global-memory form: one thread per coarse cell (cx .. cx+1) x (cy .. cy+1) x
+// Global-memory form for small levels: one thread per coarse cell (cx .. cx+1) x (cy .. cy+1) x
 // (cz .. cz+1), all three components: it reads the cell's 8 corners once and
 // updates the 8 fine points (2 cx + ox, 2 cy + oy, 2 cz + oz) with the same
 // sums in the same order as prolong_point (fine boundary points skipped).
-__global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
+__global__ void __launch_bounds__(256) k_prolong_cells(Geom F, Geom C, const float* __restrict__ ec,
                                                      float* __restrict__ ef) {
   const unsigned cx = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned cy = blockIdx.y * blockDim.y + threadIdx.y, cz = blockIdx.z;
@@ -456,6 +456,68 @@ __global__ void __launch_bounds__(256) k_prolong_add(Geom F, Geom C, const float
           ef[3 * k + c] += a * wt;
         }
       }
+}
+
+// Global-memory form: a CTA of kPCX x kPCY x kPCZ threads, one per coarse
+// cell (cx .. cx+1) x (cy .. cy+1) x (cz .. cz+1).  Each thread reads its
+// cell's 8 corners once and forms the increments of the 8 fine points
+// (2 cx + ox, 2 cy + oy, 2 cz + oz), all three components, with the same sums
+// in the same order as prolong_point; the increments go through shared memory
+// so that the read-modify-write of the fine field runs along whole fine rows
+// (per-thread 24-byte runs would write every sector in pieces).  Fine
+// boundary points are skipped.
+template <int kPCX, int kPCY, int kPCZ>
+__global__ void __launch_bounds__(kPCX * kPCY * kPCZ) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
+                                                                   float* __restrict__ ef) {
+  constexpr int kPFX = 2 * kPCX * 3, kPFR = 2 * kPCY * 2 * kPCZ;  // floats per fine row, fine rows per CTA
+  __shared__ float s_inc[kPFR * kPFX];
+  const unsigned tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
+  const unsigned cx0 = blockIdx.x * kPCX, cy0 = blockIdx.y * kPCY, cz0 = blockIdx.z * kPCZ;
+  const unsigned cx = cx0 + tx, cy = cy0 + ty, cz = cz0 + tz;
+  if (cx + 1 < C.np[0] && cy + 1 < C.np[1] && cz + 1 < C.np[2]) {
+    const unsigned sy = C.np[0], sz = C.np[0] * C.np[1];
+    const unsigned c0 = cx + sy * cy + sz * cz;
+    float v[2][2][2][3];  // [iz][iy][ix][component]
+#pragma unroll
+    for (int iz = 0; iz < 2; ++iz)
+#pragma unroll
+      for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) v[iz][iy][ix][c] = ec[3 * (c0 + ix + sy * iy + sz * iz) + c];
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox) {
+          const float wt = 1.0f / (float)(1u << (ox + oy + oz));
+          const unsigned row = (2 * ty + oy) + 2 * kPCY * (2 * tz + oz);
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float a = 0.f;
+#pragma unroll
+            for (int iz = 0; iz <= oz; ++iz)
+#pragma unroll
+              for (int iy = 0; iy <= oy; ++iy)
+#pragma unroll
+                for (int ix = 0; ix <= ox; ++ix) a += v[iz][iy][ix][c];
+            s_inc[row * kPFX + 3 * (2 * tx + ox) + c] = a * wt;
+          }
+        }
+  }
+  __syncthreads();
+  // fine rows Y = 2 cy0 + (0 .. 2 kPCY - 1), Z = 2 cz0 + (0 .. 2 kPCZ - 1);
+  // fine x = 2 cx0 + (0 .. 2 kPCX - 1)
+  const unsigned nthreads = kPCX * kPCY * kPCZ, tid = tx + kPCX * (ty + kPCY * tz);
+  const unsigned X0 = 2 * cx0, Y0 = 2 * cy0, Z0 = 2 * cz0;
+  for (unsigned i = tid; i < (unsigned)(kPFR * kPFX); i += nthreads) {
+    const unsigned row = i / kPFX, col = i - row * kPFX;
+    const unsigned X = X0 + col / 3u, Y = Y0 + row % (2 * kPCY), Z = Z0 + row / (2 * kPCY);
+    if (X == 0 || Y == 0 || Z == 0 || X + 1 >= F.np[0] || Y + 1 >= F.np[1] || Z + 1 >= F.np[2]) continue;
+    ef[3 * (X + F.np[0] * (Y + F.np[1] * Z)) + col % 3u] += s_inc[i];
+  }
 }
 
 // Launch shape of the row kernels above over `items` (point, component)
@@ -906,9 +968,16 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     float* e = B.E + 3 * L.base;
     float* r = B.R + 3 * L.base;
     const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);
-    const unsigned cells_x = Cn.g.np[0] - 1, pbx = cells_x >= 64 ? 64 : 32, pby = 256 / pbx;
-    const dim3 pg((cells_x + pbx - 1) / pbx, (Cn.g.np[1] - 1 + pby - 1) / pby, Cn.g.np[2] - 1);
-    k_prolong_add<<<pg, dim3(pbx, pby), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    // large levels through the shared-memory tile; small ones (few CTAs per
+    // tile) one thread per cell with direct updates, which measured faster there
+    if (Cn.g.points() >= (size_t)1 << 18) {
+      const dim3 pg((Cn.g.np[0] - 1 + 31) / 32, (Cn.g.np[1] - 1 + 3) / 4, (Cn.g.np[2] - 1 + 1) / 2);
+      k_prolong_add<32, 4, 2><<<pg, dim3(32, 4, 2), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    } else {
+      const unsigned cells_x = Cn.g.np[0] - 1, pbx = cells_x >= 64 ? 64 : 32, pby = 256 / pbx;
+      const dim3 pg((cells_x + pbx - 1) / pbx, (Cn.g.np[1] - 1 + pby - 1) / pby, Cn.g.np[2] - 1);
+      k_prolong_cells<<<pg, dim3(pbx, pby), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+    }
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
