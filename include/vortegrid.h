@@ -64,7 +64,7 @@ typedef enum vg_numerics {
 } vg_numerics;
 
 typedef enum vg_poisson_solver {
-  VG_POISSON_MULTIGRID = 0,        /* FP32 V-cycles in FP64 iterative refinement, to a tolerance */
+  VG_POISSON_MULTIGRID = 0,        /* FP32 V-cycles in iterative refinement (FP64-class residual), to a tolerance */
   VG_POISSON_REFERENCE_CASCADE = 1 /* the reference's fixed-work cascade (vortonSim.cpp:2539-2571) */
 } vg_poisson_solver;
 
@@ -108,7 +108,7 @@ typedef struct vg_step_stats {
   vg_grid_geom grid;
   int tree_depth;
   int poisson_cycles;
-  double poisson_relres;     /* FP64 relative residual after the solve */
+  double poisson_relres;     /* relative residual after the solve (FP64-class residual, FP64 norm) */
   double poisson_relres0;    /* before the first cycle (warm start quality) */
   float ms_total;            /* device time of the last step (CUDA events) */
   float ms_poisson;          /* device time of the Poisson solve */
@@ -219,9 +219,12 @@ vg_status vg_boundary_vecpot_device(vg_ctx* ctx, const vg_grid_geom* g, const fl
 vg_status vg_sor_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* lap3, int steps);
 /* The cascade of VortonSim::ComputeVectorPotential (vortonSim.cpp:2539-2571). */
 vg_status vg_cascade_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* rhs3, int steps);
-/* FP32 V-cycles in FP64 iterative refinement to `tolerance` (new; the
- * reference's cascade cannot reach a residual target).  soln3 holds the
- * boundary values and the initial interior guess on entry. */
+/* FP32 V-cycles in iterative refinement to `tolerance` (new; the reference's
+ * cascade cannot reach a residual target).  The refinement residual is
+ * evaluated to FP64-class accuracy in float-pair arithmetic and its norm in
+ * FP64; the coarsest level (at most 32,768 interior points) is solved exactly
+ * by sine transforms.  soln3 holds the boundary values and the initial
+ * interior guess on entry. */
 vg_status vg_multigrid_device(vg_ctx* ctx, const vg_grid_geom* g, float* soln3, const float* rhs3,
                               double tolerance, int max_cycles, int* cycles, double* relres0, double* relres);
 /* DownSampleInto / UpSampleFrom (Core/SpatialPartition/nestedGrid.h:253-293,

@@ -9,7 +9,7 @@
 //     V(2,2)-cycle on L e = r -- point red-black Gauss-Seidel (colour = parity
 //     of x+y+z), 27-point full-weighting restriction fused with the residual
 //     (the reference's SLOWER_MORE_ACCURATE weights, uniformGrid.h:1453-1585),
-//     trilinear prolongation, FP64 Gauss-Seidel on the coarsest grid -- and
+//     trilinear prolongation, an exact solve on the coarsest grid -- and
 //     a += e;
 //   * phase 1 iterates on the FP32 field with an FP32 residual while FP32 can
 //     still represent it (relative residual above 1e-4);
@@ -21,9 +21,13 @@
 //     well), accumulates e and checks with another such residual -- reaching
 //     residuals far below FP32's cancellation floor (~1e-4 at 128^3) with two
 //     accurate residual evaluations per solve.
-// FP64 is used for the coarsest-grid solve and the norms.
-// The levels of at most 17^3 points run inside one CTA with their fields in
-// shared memory; each cycle is captured once as a CUDA graph and replayed.
+// FP64 is used for the norms (and the host-built tables of the coarsest
+// solve).  The hierarchy stops at the finest level with at most 32,768
+// interior points, which is solved exactly by sine transforms (over the whole
+// GPU, or inside the small-level CTA when it has at most 512); levels of at
+// most 17^3 points above such a small one run inside one CTA with their
+// fields in shared memory; each cycle is captured once as a CUDA graph and
+// replayed.
 // Grids are float[3] per point (x fastest); the three components are three
 // independent scalar problems solved together.
 #include <float.h>
