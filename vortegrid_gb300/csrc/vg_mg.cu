@@ -543,7 +543,9 @@ static RowLaunch launch_rows(unsigned items, unsigned ny, unsigned nz) {
 
 // The small levels of a V-cycle in one CTA, their e and r in shared memory:
 // pre-smoothing and fused residual-restriction down to the coarsest grid, an
-// FP64 Gauss-Seidel solve there, then prolongation and post-smoothing back up.
+// exact sine-transform solve there (or FP64 Gauss-Seidel when the hierarchy
+// ends above kDirectMax interior points, e.g. on odd point counts), then
+// prolongation and post-smoothing back up.
 // The first small level reads its r from global memory and writes its e back.
 constexpr int kSmallMax = 8;
 constexpr int kCoarseShared = 1536;  // doubles of the coarsest solve kept in shared memory
