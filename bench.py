@@ -359,8 +359,9 @@ def run_ours(args, world, rank, local):
             e2e_ms.append((t1 - t0) * 1e3)
     e2e_step = statistics.mean(e2e_ms)
     result["e2e"] = {"value": interactions() / (e2e_step * 1e-3) / 1e9, "unit": "Gint/s",
-                     "h2d_bytes_per_step": N_VORTONS * 56 + N_TRACERS * 12,
-                     "d2h_bytes_per_step": N_VORTONS * 36 + N_TRACERS * 24, "ms_per_step": e2e_step,
+                     # 96-byte records travel whole, one contiguous copy each way
+                     "h2d_bytes_per_step": (N_VORTONS + N_TRACERS) * 96,
+                     "d2h_bytes_per_step": (N_VORTONS + N_TRACERS) * 96, "ms_per_step": e2e_step,
                      "path": "vg_step (Particle records) + host Evolve + vg_advect (tracer records), pinned"}
 
     # ---- CPU baseline (reference code, all host threads)

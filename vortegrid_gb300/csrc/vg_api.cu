@@ -527,7 +527,13 @@ vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const flo
   if (!particles || stride < 56 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 56 / unaligned");
   if (!std::isfinite(dt)) return fail(c, VG_INVALID, "dt is not finite");
   vg_status st = VG_OK;
-  unsigned char* stage = (unsigned char*)ws(c, S_HOSTSTAGE, n * 56, &st);
+  // Records of up to 4x the 56 bytes used travel whole, as one contiguous copy
+  // each way (a strided copy of short rows runs far below the link's rate;
+  // kernels reading pinned records in place over the link measured slower
+  // still); wider ones travel as their first 56 bytes.
+  const bool whole = stride <= 4 * 56;
+  const size_t pitch = whole ? stride : 56;
+  unsigned char* stage = (unsigned char*)ws(c, S_HOSTSTAGE, n * pitch, &st);
   if (st != VG_OK) return st;
   float4* ps = (float4*)ws(c, S_POS, n * sizeof(float4), &st);
   if (st != VG_OK) return st;
@@ -536,18 +542,25 @@ vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const flo
   float4* vel = (float4*)ws(c, S_VVEL, n * sizeof(float4), &st);
   if (st != VG_OK) return st;
   // record bytes [0, 56): position, velocity, orientation, angular velocity, density, size
-  VG_CUDA(c, cudaMemcpy2DAsync(stage, 56, particles, stride, 56, n, cudaMemcpyHostToDevice, c->stream));
-  k_unpack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage, 56, (int)n, ps, w);
+  if (whole)
+    VG_CUDA(c, cudaMemcpyAsync(stage, particles, n * stride, cudaMemcpyHostToDevice, c->stream));
+  else
+    VG_CUDA(c, cudaMemcpy2DAsync(stage, 56, particles, stride, 56, n, cudaMemcpyHostToDevice, c->stream));
+  k_unpack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage, pitch, (int)n, ps, w);
   VG_CUDA(c, cudaGetLastError());
   const float* rec0 = (const float*)particles;
   const float radius = rec0[13] * 0.5f;  // Particle::GetRadius of the first vorton
   st = run_step(c, ps, w, vel, n, rec0, radius, extra_min, extra_max, dt);
   if (st != VG_OK) return st;
-  // write back record bytes [12, 48): velocity, (unchanged) orientation, angular velocity
-  k_pack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage + 12, 56, (int)n, vel, w);
+  // write back record bytes [12, 48): velocity, (unchanged) orientation,
+  // angular velocity (whole records carry their other bytes back unchanged)
+  k_pack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage + 12, pitch, (int)n, vel, w);
   VG_CUDA(c, cudaGetLastError());
-  VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + 12, stride, stage + 12, 56, 36, n, cudaMemcpyDeviceToHost,
-                               c->stream));
+  if (whole)
+    VG_CUDA(c, cudaMemcpyAsync(particles, stage, n * stride, cudaMemcpyDeviceToHost, c->stream));
+  else
+    VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + 12, stride, stage + 12, 56, 36, n,
+                                 cudaMemcpyDeviceToHost, c->stream));
   return sync_and_check(c, "vg_step");
 }
 
@@ -646,18 +659,28 @@ vg_status vg_advect(vg_ctx* c, void* particles, size_t m, size_t stride, float d
   if (!particles || stride < 24 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 24 / unaligned");
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
   vg_status st = VG_OK;
-  // staging: records' bytes [0, 24) (position, velocity), then float4 position and velocity
-  const size_t rec_bytes = ((m * 24 + 255) / 256) * 256;
+  // staging: the records (whole when at most 4x the 24 bytes used, as one
+  // contiguous copy each way; else their bytes [0, 24): position, velocity),
+  // then float4 position and velocity
+  const bool whole = stride <= 4 * 24;
+  const size_t pitch = whole ? stride : 24;
+  const size_t rec_bytes = ((m * pitch + 255) / 256) * 256;
   unsigned char* stage = (unsigned char*)ws(c, S_TRACERS, rec_bytes + 2 * m * sizeof(float4), &st);
   if (st != VG_OK) return st;
   float4* p = (float4*)(stage + rec_bytes);
   float4* v = p + m;
-  VG_CUDA(c, cudaMemcpy2DAsync(stage, 24, particles, stride, 12, m, cudaMemcpyHostToDevice, c->stream));
-  k_copy_pos3<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, 24, (int)m, p);
+  if (whole)
+    VG_CUDA(c, cudaMemcpyAsync(stage, particles, m * stride, cudaMemcpyHostToDevice, c->stream));
+  else
+    VG_CUDA(c, cudaMemcpy2DAsync(stage, 24, particles, stride, 12, m, cudaMemcpyHostToDevice, c->stream));
+  k_copy_pos3<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, pitch, (int)m, p);
   if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, p, v, m, dt, true)) != VG_OK) return st;
-  k_store_posvel<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, 24, (int)m, p, v);
+  k_store_posvel<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, pitch, (int)m, p, v);
   VG_CUDA(c, cudaGetLastError());
-  VG_CUDA(c, cudaMemcpy2DAsync(particles, stride, stage, 24, 24, m, cudaMemcpyDeviceToHost, c->stream));
+  if (whole)
+    VG_CUDA(c, cudaMemcpyAsync(particles, stage, m * stride, cudaMemcpyDeviceToHost, c->stream));
+  else
+    VG_CUDA(c, cudaMemcpy2DAsync(particles, stride, stage, 24, 24, m, cudaMemcpyDeviceToHost, c->stream));
   return sync_and_check(c, "vg_advect");
 }
 
