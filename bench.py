@@ -472,8 +472,9 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
     of 16-96 cells per axis from each effect's extent, seeded ring / puff mix),
     each frame: treecode boundary, multigrid interior solve (network warm start
     where it fits and the autotuner keeps it), PSE diffusion, advection.  Frames
-    replayed from captured CUDA graphs on parallel branches vs the same frames
-    stepped sequentially."""
+    replayed from captured CUDA graphs on parallel branches, the Poisson
+    solves in one persistent launch (when the autotuner keeps it), vs the same
+    frames stepped sequentially with per-level launches."""
     from vortegrid_gb300 import batch, warmstart
     effects = [batch.make_effect(1000 + i) for i in range(n_sims)]
     B = batch.Batch(effects, streams=8, device=local)
@@ -496,6 +497,7 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
     seq_ms = (time.perf_counter() - t0) / seq_frames * 1e3
     st = [B.stats(i) for i in range(len(B))]
     graphs, max_nodes, total_nodes = B.graph_info()
+    p_sims, p_teams, p_ctas, p_graph = B.solver_info()
     left = sum(B.outside(i) for i in range(len(B)))
     cells = [int(e.grid.num_points[0]) - 1 for e in effects]
     nv = sum(e.n for e in effects)
@@ -505,7 +507,9 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
                         "(viscosity 0.01), Euler advection",
             "grid_cells_histogram": {str(c): cells.count(c) for c in sorted(set(cells))},
             "autotuned": {"streams": streams, "network_warm_start": use_net, "graph_ms_at_best": tuned_ms,
-                          "seconds": tune_s},
+                          "seconds": tune_s,
+                          "persistent_solve": {"simulations": p_sims, "teams": p_teams, "ctas_per_team": p_ctas,
+                                               "captured_as_graph": p_graph}},
             "graph_ms_per_frame": graph_ms, "sequential_ms_per_frame": seq_ms,
             "speedup_vs_sequential": seq_ms / graph_ms,
             "graphs_per_frame": graphs, "graph_nodes_max": max_nodes, "graph_nodes_total": total_nodes,

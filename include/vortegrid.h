@@ -344,7 +344,12 @@ vg_status vg_set_network(vg_ctx* ctx, vg_net* net);
  * captured once as CUDA graphs and replayed: the simulations are dealt to
  * `streams` parallel branches, each branch's chain is captured as graphs of at
  * most a few thousand kernels, and a frame forks into the branches, launches
- * their graphs and joins.  A vorton that leaves its simulation's fixed grid
+ * their graphs and joins.  With the persistent solve (vg_batch_set_solver), every simulation whose
+ * multigrid hierarchy ends in the sine-transform solve over the GPU has its Poisson solve taken
+ * out of its branch: a frame runs the steps up to the solve on the branches, then one cooperative
+ * launch in which teams of CTAs run all those solves (largest first, a team barrier between
+ * phases, results bit-identical to the per-simulation launches), then the rest of the steps and
+ * the advection on the branches.  A vorton that leaves its simulation's fixed grid
  * stops (zero velocity) and drops out of that simulation's solve instead of
  * failing the frame (vg_batch_outside reports it).  Errors: vg_batch_last_error. */
 typedef struct vg_batch vg_batch;
@@ -369,10 +374,27 @@ vg_status vg_batch_step(vg_batch* batch, float dt, int mode);
 /* Waits for the batch and reports device-side errors of any simulation. */
 vg_status vg_batch_synchronize(vg_batch* batch);
 /* The autotuner: times `frames` graph replays for each stream count in candidates (with and
- * without the network when one is loaded), keeps the fastest and reports it (best_ms per frame).
- * Steps the simulations while measuring. */
+ * without the network when one is loaded), then, at the best of those, with the persistent solve
+ * off and at team sizes of 4, 8, 16 and 32 CTAs; keeps the fastest setting and reports it
+ * (best_ms per frame; vg_batch_solver_info gives the solver setting).  Steps the simulations
+ * while measuring. */
 vg_status vg_batch_autotune(vg_batch* batch, float dt, int frames, const int* candidates, int ncand,
                             int* best_streams, int* best_network, float* best_ms);
+/* persistent: 1 solves qualifying simulations in one persistent launch per frame, 0 inside each
+ * simulation's branch graphs (the default); team_ctas: CTAs per team (0: 8); max_points: only
+ * grids of at most this many points go to the persistent launch (0: any size), the others solve
+ * in their branches.  Invalidates the graphs.  A team barrier that waits more than 2 s gives up;
+ * vg_batch_synchronize then reports VG_TIMEOUT. */
+vg_status vg_batch_set_solver(vg_batch* batch, int persistent, int team_ctas, size_t max_points);
+/* The captured frame's solver: simulations in the persistent launch, its teams and CTAs per team,
+ * and whether the launch was captured as a graph (1) or is launched directly (0). */
+vg_status vg_batch_solver_info(const vg_batch* batch, int* persistent_sims, int* teams, int* team_ctas,
+                               int* captured);
+/* Diagnostics (no counterpart in the reference): the persistent solve's team barrier on one team
+ * of `ctas` CTAs (at most one per SM) of which the last `missing` never arrive, each wait limited
+ * to limit_ms (at most 10 s).  *completed = CTAs that passed two barriers; *gave_up = 1 when a
+ * wait ran out (the CTAs then return, and the device stays usable). */
+vg_status vg_team_barrier_check(int device, int ctas, int missing, float limit_ms, int* completed, int* gave_up);
 /* *outside = 1 when a vorton of simulation `index` has left its grid since the last call, which
  * clears the record.  Synchronises the batch. */
 vg_status vg_batch_outside(vg_batch* batch, int index, int* outside);
@@ -380,8 +402,8 @@ vg_status vg_batch_outside(vg_batch* batch, int index, int* outside);
  * graph frame, call vg_batch_synchronize before reading it; per-step times are then 0. */
 vg_ctx* vg_batch_context(vg_batch* batch, int index);
 int vg_batch_size(const vg_batch* batch);
-/* The captured frame: how many graphs it launches, and their largest and total node counts
- * (0 before the first graph frame). */
+/* The captured frame: how many graphs it launches (the persistent solve's included), and their
+ * largest and total node counts (0 before the first graph frame). */
 vg_status vg_batch_graph_info(const vg_batch* batch, int* graphs, size_t* max_nodes, size_t* total_nodes);
 
 #ifdef __cplusplus

@@ -1,9 +1,11 @@
 """GPU tests of batched effects (vg_batch_*): frames replayed from the
-captured CUDA graphs (simulations on parallel branches) are bit-identical to
-the same frames stepped simulation after simulation, with and without the
-network warm start; the calibrated fixed multigrid schedules end near the
-tolerance; long branches split into bounded graphs; a vorton that leaves its
-grid stops and drops out; the autotuner returns a measured setting."""
+captured CUDA graphs (simulations on parallel branches, their Poisson solves
+in one persistent launch) are bit-identical to the same frames stepped
+simulation after simulation with per-level launches, with and without the
+network warm start, at several team sizes and with the persistent solve off;
+the calibrated fixed multigrid schedules end near the tolerance; long branches
+split into bounded graphs; a vorton that leaves its grid stops and drops out;
+the autotuner returns a measured setting."""
 import os
 
 import numpy as np
@@ -42,6 +44,7 @@ def test_graph_frame_matches_sequential_frame(mod, network):
         pytest.skip("no trained weights")
     ef = effects(mod, [11, 14, 17, 25, 13, 22])  # grid edges 80, 64, 48, 32, 96, 48
     A, B = mod.Batch(ef, streams=3), mod.Batch(ef, streams=3)
+    A.set_solver(True, 8)
     if network:
         A.load_network(warmstart.DEFAULT_WEIGHTS)
         B.load_network(warmstart.DEFAULT_WEIGHTS)
@@ -59,6 +62,34 @@ def test_graph_frame_matches_sequential_frame(mod, network):
     for i in range(len(A)):
         st = A.stats(i)
         assert st.poisson_relres < 1e-5, (i, st.poisson_relres, st.poisson_cycles)
+        sb = B.stats(i)
+        # the persistent launch sums the norms in another order: equal to rounding
+        assert st.poisson_relres == pytest.approx(sb.poisson_relres, rel=1e-6, abs=1e-12)
+    n, teams, ctas, _ = A.solver_info()
+    assert n == len(A) and teams >= 1 and ctas == 8, (n, teams, ctas)
+
+
+@pytest.mark.parametrize("persistent,team", [(True, 1), (True, 3), (True, 32), (False, 0)])
+def test_solver_settings_give_identical_frames(mod, persistent, team):
+    """One CTA per team, odd team sizes, teams larger than a simulation's
+    tiles, and the solve inside the branch graphs: every setting steps the
+    same frames as the per-level launches, bit for bit."""
+    ef = effects(mod, [12, 17, 25, 40, 41])
+    A, B = mod.Batch(ef, streams=2), mod.Batch(ef, streams=2)
+    A.set_solver(persistent, team)
+    A.calibrate(DT)
+    B.calibrate(DT)
+    for _ in range(2):
+        A.step(DT, graph=True)
+        B.step(DT, graph=False)
+    A.synchronize()
+    B.synchronize()
+    assert frames_equal(A, B)
+    n, teams, ctas, _ = A.solver_info()
+    if persistent:
+        assert n == len(A) and ctas == team and 1 <= teams <= len(A), (n, teams, ctas)
+    else:
+        assert n == 0
 
 
 def test_long_branch_splits_into_bounded_graphs(mod):
@@ -113,5 +144,28 @@ def test_autotune_picks_a_measured_setting(mod):
     A = mod.Batch(effects(mod, [21, 22, 23, 24]), streams=2)
     streams, use_net, ms = A.autotune(DT, frames=2, candidates=(1, 2, 4))
     assert streams in (1, 2, 4) and not use_net and 0.0 < ms < 1e4
+    A.step(DT)
+    A.synchronize()
+
+
+def test_team_barrier_gives_up_when_a_cta_never_arrives(mod):
+    """The persistent solve's team barrier is a bounded wait: with every CTA
+    arriving, all pass; with one CTA that never arrives (a count nothing
+    completes), the others give up after the limit and report it, and the
+    device keeps working."""
+    import ctypes
+    import time
+    import vortegrid_gb300 as vg
+    L = vg.lib()
+    done, gave_up = ctypes.c_int(), ctypes.c_int()
+    assert L.vg_team_barrier_check(0, 8, 0, 500.0, ctypes.byref(done), ctypes.byref(gave_up)) == vg.OK
+    assert done.value == 8 and gave_up.value == 0
+    t0 = time.perf_counter()
+    assert L.vg_team_barrier_check(0, 8, 1, 50.0, ctypes.byref(done), ctypes.byref(gave_up)) == vg.OK
+    assert done.value == 0 and gave_up.value == 1
+    assert time.perf_counter() - t0 < 5.0
+    A = mod.Batch(effects(mod, [25]), streams=1)
+    A.set_solver(True, 4)
+    A.calibrate(DT)
     A.step(DT)
     A.synchronize()

@@ -125,7 +125,8 @@ EXPORTS = [
     "vg_net_to_bf16_device", "vg_set_network",
     "vg_batch_create", "vg_batch_destroy", "vg_batch_last_error", "vg_batch_add", "vg_batch_load_network",
     "vg_batch_configure", "vg_batch_calibrate", "vg_batch_step", "vg_batch_synchronize", "vg_batch_autotune",
-    "vg_batch_outside", "vg_batch_context", "vg_batch_size", "vg_batch_graph_info",
+    "vg_batch_outside", "vg_batch_context", "vg_batch_size", "vg_batch_graph_info", "vg_batch_set_solver",
+    "vg_batch_solver_info", "vg_team_barrier_check",
 ]
 
 
@@ -222,6 +223,9 @@ def lib():
         L.vg_batch_context.restype = vp
         L.vg_batch_size.argtypes = [vp]
         L.vg_batch_graph_info.argtypes = [vp, ip, ctypes.POINTER(sz), ctypes.POINTER(sz)]
+        L.vg_batch_set_solver.argtypes = [vp, i, i, sz]
+        L.vg_batch_solver_info.argtypes = [vp, ip, ip, ip, ip]
+        L.vg_team_barrier_check.argtypes = [i, i, i, fl, ip, ip]
         if L.vg_abi_version() != 2:
             raise ImportError("libvortegrid ABI version mismatch")
         _lib = L

@@ -165,5 +165,20 @@ class Batch:
                    "vg_batch_graph_info")
         return g.value, mx.value, tot.value
 
+    def set_solver(self, persistent=True, team_ctas=0, max_points=0):
+        """Poisson solves of qualifying simulations (grids of at most
+        max_points points; 0 = any) in one persistent launch per frame (teams
+        of team_ctas CTAs; 0 = automatic), or inside each simulation's branch
+        graphs."""
+        self.check(lib().vg_batch_set_solver(self.h, 1 if persistent else 0, team_ctas, max_points),
+                   "vg_batch_set_solver")
+
+    def solver_info(self):
+        """(simulations in the persistent launch, teams, CTAs per team, launch captured as a graph)."""
+        n, t, c, g = ctypes.c_int(), ctypes.c_int(), ctypes.c_int(), ctypes.c_int()
+        self.check(lib().vg_batch_solver_info(self.h, ctypes.byref(n), ctypes.byref(t), ctypes.byref(c),
+                                              ctypes.byref(g)), "vg_batch_solver_info")
+        return n.value, t.value, c.value, bool(g.value)
+
     def __len__(self):
         return lib().vg_batch_size(self.h)

@@ -270,45 +270,71 @@ vg_status step_geometry(Ctx* c, const float4* ps, size_t n, const float* first_p
   return VG_OK;
 }
 
-// The step on device-resident vortons (ps: pos+size, w: angvel in place, vel out).
-vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const float* first_pos, float radius,
-                   const float* extra_min, const float* extra_max, float dt) {
-  if (n == 0) return fail(c, VG_EMPTY, "no vortons");
-  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
-  c->launches = 0;
-  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
-  VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
-  c->step_captured = cap != cudaStreamCaptureStatusNone;
-  VG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+}  // namespace
+
+// The state a step carries across its split at the Poisson solve.
+struct vg::StepState {
+  float4 *ps, *w, *vel;
+  size_t n;
+  float radius, dt;
   Geom g;
-  vg_status st = step_geometry(c, ps, n, first_pos, radius, extra_min, extra_max, &g);
+  CellLists cl;
+  Tree t;
+  float* velgrid;
+  float* vecpot;   // Poisson technique: the solution (boundary values and warm start set)
+  float* negvort;  // ... and the right-hand side
+};
+
+bool vg::split_problem(Ctx* c, MgBatchItem* out) {
+  if (!c->split || !c->split->vecpot) return false;
+  out->c = c;
+  out->g = c->split->g;
+  out->soln = c->split->vecpot;
+  out->rhs = c->split->negvort;
+  return true;
+}
+
+namespace {
+
+// The step up to the Poisson solve: grid, cell lists, tree; for the Poisson
+// technique the splat, the boundary values and the warm start; the other
+// techniques evaluate the velocity grid here.
+static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const float* extra_min,
+                            const float* extra_max) {
+  vg_status st = step_geometry(c, s.ps, s.n, first_pos, s.radius, extra_min, extra_max, &s.g);
   if (st != VG_OK) return st;
+  const Geom& g = s.g;
+  float4 *ps = s.ps, *w = s.w, *vel = s.vel;
+  const size_t n = s.n;
+  const float radius = s.radius;
   const size_t pts = g.points();
   const bool ref = c->cfg.numerics == VG_NUMERICS_REFERENCE;
   // Cell lists serve the tree, the splat and PSE; the direct technique
   // without diffusion needs none.
   const int tech = c->cfg.velocity_technique;
-  CellLists cl = {nullptr, nullptr, nullptr};
+  s.cl = {nullptr, nullptr, nullptr};
   if (tech != VG_VELOCITY_DIRECT || c->cfg.enable_diffusion) {
-    if ((st = build_cell_lists(c, g, ps, n, &cl)) != VG_OK) return st;
+    if ((st = build_cell_lists(c, g, ps, n, &s.cl)) != VG_OK) return st;
   }
-  float* velgrid = (float*)ws(c, S_VEL, pts * 3 * sizeof(float), &st);
+  s.velgrid = (float*)ws(c, S_VEL, pts * 3 * sizeof(float), &st);
   if (st != VG_OK) return st;
-  Tree t;
-  t.depth = 0;
+  s.t.depth = 0;
+  s.vecpot = s.negvort = nullptr;
   c->stats.poisson_cycles = 0;
   c->stats.poisson_relres = 0.0;
   c->stats.poisson_relres0 = 0.0;
   c->stats.ms_poisson = 0.f;
   if (tech == VG_VELOCITY_POISSON || tech == VG_VELOCITY_TREE) {
-    if ((st = build_tree(c, g, ps, w, n, cl, &t)) != VG_OK) return st;
+    if ((st = build_tree(c, g, ps, w, n, s.cl, &s.t)) != VG_OK) return st;
   }
   if (tech == VG_VELOCITY_POISSON) {
     float* negvort = (float*)ws(c, S_NEGVORT, pts * 3 * sizeof(float), &st);
     if (st != VG_OK) return st;
     float* vecpot = (float*)ws(c, S_VECPOT, pts * 3 * sizeof(float), &st);
     if (st != VG_OK) return st;
-    if ((st = launch_splat(c, g, ps, w, n, cl, -1.0f, radius, negvort)) != VG_OK) return st;
+    s.negvort = negvort;
+    s.vecpot = vecpot;
+    if ((st = launch_splat(c, g, ps, w, n, s.cl, -1.0f, radius, negvort)) != VG_OK) return st;
     const bool warm_prev = c->cfg.warm_start == VG_WARM_PREVIOUS && c->have_prev &&
                            memcmp(&c->prev_grid, &g, sizeof(Geom)) == 0;
     c->stats.warm_start_used = warm_prev ? VG_WARM_PREVIOUS : VG_WARM_ZERO;
@@ -318,7 +344,7 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
     } else {
       VG_CUDA(c, cudaMemsetAsync(vecpot, 0, pts * 3 * sizeof(float), c->stream));
     }
-    if ((st = launch_boundary_vecpot(c, t, g, ps, w, n, c->cfg.boundary_copy_odd_x != 0, ref, vecpot)) != VG_OK)
+    if ((st = launch_boundary_vecpot(c, s.t, g, ps, w, n, c->cfg.boundary_copy_odd_x != 0, ref, vecpot)) != VG_OK)
       return st;
     VG_CUDA(c, cudaEventRecord(c->ev2, c->stream));
     // the network's guess counts as part of the solve's time
@@ -326,79 +352,134 @@ vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const f
       if ((st = nn::guess(c, c->net, g, negvort, vecpot)) != VG_OK) return st;
       c->stats.warm_start_used = VG_WARM_NETWORK;
     }
-    if (c->cfg.poisson_solver == VG_POISSON_REFERENCE_CASCADE) {
-      if ((st = run_cascade(c, g, vecpot, negvort, c->cfg.cascade_steps)) != VG_OK) return st;
-    } else if (c->mg_fixed_k1 > 0) {
-      // fixed schedule: no host round trip; the residuals are read at vg_get_stats
-      if ((st = run_multigrid_fixed(c, g, vecpot, negvort)) != VG_OK) return st;
-      c->stats.poisson_cycles = c->mg_fixed_k1 + c->mg_fixed_k2;
-    } else {
-      int cyc = 0;
-      double r0 = 0, r1 = 0;
-      st = run_multigrid(c, g, vecpot, negvort, c->cfg.poisson_tolerance, c->cfg.poisson_max_cycles, &cyc, &r0, &r1);
-      c->stats.poisson_cycles = cyc;
-      c->stats.poisson_relres0 = r0;
-      c->stats.poisson_relres = r1;
-      if (st != VG_OK && st != VG_NOT_CONVERGED) return st;
-    }
+    return VG_OK;
+  }
+  // velocity at gridpoints by treecode (auto mollification, vortonSim.cpp:2458-2477) or direct sum;
+  // the direct technique also evaluates every vorton, in the same launch
+  const size_t nq = pts + (tech == VG_VELOCITY_DIRECT ? n : 0);
+  float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
+  if (st != VG_OK) return st;
+  float4* out4 = q + nq;
+  k_grid_points<<<blocks_for(pts, 256), 256, 0, c->stream>>>(g, q);
+  VG_LAUNCHED(c);
+  float sr = 1.0f, sc = 1.0f;
+  if (tech == VG_VELOCITY_TREE) {
+    volatile float cv = g.cell[0] * g.cell[1];
+    cv = cv * g.cell[2];
+    const float cgl = 1.0f * powf(cv, 1.0f / 3.0f);
+    sr = std::max(cgl / radius, 1.0f);
+    volatile float s3 = sr * sr;
+    s3 = s3 * sr;
+    sc = 1.0f / s3;
+    if ((st = launch_tree_eval(c, 0, ref, s.t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
+  } else {
+    // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too
+    VG_CUDA(c, cudaMemcpyAsync(q + pts, ps, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+    if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
+    VG_CUDA(c, cudaMemcpyAsync(vel, out4 + pts, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
+  }
+  k_f4_to_f3<<<blocks_for(pts, 256), 256, 0, c->stream>>>(out4, s.velgrid, pts);
+  VG_LAUNCHED(c);
+  return VG_OK;
+}
+
+// The Poisson solve: the reference cascade, the fixed multigrid schedule, or
+// the adaptive multigrid to the tolerance.
+static vg_status step_solve(Ctx* c, StepState& s) {
+  vg_status st = VG_OK;
+  if (c->cfg.poisson_solver == VG_POISSON_REFERENCE_CASCADE) {
+    if ((st = run_cascade(c, s.g, s.vecpot, s.negvort, c->cfg.cascade_steps)) != VG_OK) return st;
+  } else if (c->mg_fixed_k1 > 0) {
+    // fixed schedule: no host round trip; the residuals are read at vg_get_stats
+    if ((st = run_multigrid_fixed(c, s.g, s.vecpot, s.negvort)) != VG_OK) return st;
+    c->stats.poisson_cycles = c->mg_fixed_k1 + c->mg_fixed_k2;
+  } else {
+    int cyc = 0;
+    double r0 = 0, r1 = 0;
+    st = run_multigrid(c, s.g, s.vecpot, s.negvort, c->cfg.poisson_tolerance, c->cfg.poisson_max_cycles, &cyc, &r0,
+                       &r1);
+    c->stats.poisson_cycles = cyc;
+    c->stats.poisson_relres0 = r0;
+    c->stats.poisson_relres = r1;
+    if (st != VG_OK && st != VG_NOT_CONVERGED) return st;
+  }
+  return VG_OK;
+}
+
+// The step after the solve: curl of the vector potential, stretching, PSE,
+// and the vortons' velocity from the grid.
+static vg_status step_back(Ctx* c, StepState& s) {
+  const Geom& g = s.g;
+  const size_t pts = g.points(), n = s.n;
+  const int tech = c->cfg.velocity_technique;
+  vg_status st = VG_OK;
+  if (tech == VG_VELOCITY_POISSON) {
     VG_CUDA(c, cudaEventRecord(c->ev3, c->stream));
     if (c->cfg.warm_start == VG_WARM_PREVIOUS) {
       float* prev = (float*)ws(c, S_PREV, pts * 3 * sizeof(float), &st);
       if (st != VG_OK) return st;
-      VG_CUDA(c, cudaMemcpyAsync(prev, vecpot, pts * 3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
+      VG_CUDA(c, cudaMemcpyAsync(prev, s.vecpot, pts * 3 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
       c->prev_grid = g;
       c->have_prev = true;
     }
-    if ((st = launch_curl(c, g, vecpot, velgrid)) != VG_OK) return st;
-  } else {
-    // velocity at gridpoints by treecode (auto mollification, vortonSim.cpp:2458-2477) or direct sum;
-    // the direct technique also evaluates every vorton, in the same launch
-    const size_t nq = pts + (tech == VG_VELOCITY_DIRECT ? n : 0);
-    float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
-    if (st != VG_OK) return st;
-    float4* out4 = q + nq;
-    k_grid_points<<<blocks_for(pts, 256), 256, 0, c->stream>>>(g, q);
-    VG_LAUNCHED(c);
-    float sr = 1.0f, sc = 1.0f;
-    if (tech == VG_VELOCITY_TREE) {
-      volatile float cv = g.cell[0] * g.cell[1];
-      cv = cv * g.cell[2];
-      const float cgl = 1.0f * powf(cv, 1.0f / 3.0f);
-      sr = std::max(cgl / radius, 1.0f);
-      volatile float s3 = sr * sr;
-      s3 = s3 * sr;
-      sc = 1.0f / s3;
-      if ((st = launch_tree_eval(c, 0, ref, t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
-    } else {
-      // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too
-      VG_CUDA(c, cudaMemcpyAsync(q + pts, ps, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
-      if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
-      VG_CUDA(c, cudaMemcpyAsync(vel, out4 + pts, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
-    }
-    k_f4_to_f3<<<blocks_for(pts, 256), 256, 0, c->stream>>>(out4, velgrid, pts);
-    VG_LAUNCHED(c);
+    if ((st = launch_curl(c, g, s.vecpot, s.velgrid)) != VG_OK) return st;
   }
   if (c->cfg.enable_stretch) {
     float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), (pts + n) * 2 * sizeof(float4)), &st);
     if (st != VG_OK) return st;
-    if ((st = launch_jacobian(c, g, velgrid, jac)) != VG_OK) return st;
-    if ((st = launch_stretch(c, g, jac, ps, w, n, dt)) != VG_OK) return st;
+    if ((st = launch_jacobian(c, g, s.velgrid, jac)) != VG_OK) return st;
+    if ((st = launch_stretch(c, g, jac, s.ps, s.w, n, s.dt)) != VG_OK) return st;
   }
   if (c->cfg.enable_diffusion) {
-    if ((st = launch_pse(c, g, cl, ps, w, n, c->cfg.viscosity, dt)) != VG_OK) return st;
+    if ((st = launch_pse(c, g, s.cl, s.ps, s.w, n, c->cfg.viscosity, s.dt)) != VG_OK) return st;
   }
   if (tech != VG_VELOCITY_DIRECT) {
     // AssignVelocityFromField(vortons, mVelGrid, 1) (vortonSim.cpp:4251-4255)
-    if ((st = launch_gather_advect(c, g, velgrid, ps, vel, n, 0.0f, false)) != VG_OK) return st;
+    if ((st = launch_gather_advect(c, g, s.velgrid, s.ps, s.vel, n, 0.0f, false)) != VG_OK) return st;
   }
   VG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   c->stats_pending = true;
   c->stats.grid = from_geom(g);
-  c->stats.tree_depth = t.depth;
+  c->stats.tree_depth = s.t.depth;
   c->stats.kernels_launched = c->launches;
   c->grid = g;
   c->have_grid = true;
   return VG_OK;
+}
+
+// The step on device-resident vortons (ps: pos+size, w: angvel in place, vel
+// out).  c->step_split 1 stops before the Poisson solve (the caller solves),
+// 2 resumes after it with the state kept by 1 (the arguments are not read).
+vg_status run_step(Ctx* c, float4* ps, float4* w, float4* vel, size_t n, const float* first_pos, float radius,
+                   const float* extra_min, const float* extra_max, float dt) {
+  if (!c->split) {
+    c->split = new (std::nothrow) StepState();
+    if (!c->split) return fail(c, VG_OOM, "out of host memory");
+  }
+  StepState& s = *c->split;
+  vg_status st;
+  if (c->step_split != 2) {
+    if (n == 0) return fail(c, VG_EMPTY, "no vortons");
+    if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+    c->launches = 0;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
+    c->step_captured = cap != cudaStreamCaptureStatusNone;
+    VG_CUDA(c, cudaEventRecord(c->ev0, c->stream));
+    s.ps = ps;
+    s.w = w;
+    s.vel = vel;
+    s.n = n;
+    s.radius = radius;
+    s.dt = dt;
+    if ((st = step_front(c, s, first_pos, extra_min, extra_max)) != VG_OK) return st;
+    if (c->step_split == 1) {
+      if (s.vecpot) c->stats.poisson_cycles = c->mg_fixed_k1 + c->mg_fixed_k2;
+      return VG_OK;
+    }
+    if (s.vecpot && (st = step_solve(c, s)) != VG_OK) return st;
+  }
+  return step_back(c, s);
 }
 
 }  // namespace
@@ -497,6 +578,7 @@ vg_status vg_destroy(vg_ctx* c) {
   if (c->ev2) cudaEventDestroy(c->ev2);
   if (c->ev3) cudaEventDestroy(c->ev3);
   if (c->own_stream) cudaStreamDestroy(c->stream);
+  delete c->split;
   delete c;
   return VG_OK;
 }

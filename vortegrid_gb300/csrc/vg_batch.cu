@@ -21,6 +21,15 @@
 // and whether the network warm start pays off, by timing replays.  A
 // sequential mode runs the same work simulation after simulation on the main
 // stream without graphs, for comparison.
+//
+// With the persistent solve (vg_batch_set_solver), a frame has three parts: each
+// simulation's step up to its Poisson solve on the branches; one cooperative
+// launch on the main stream that runs every qualifying simulation's
+// fixed-schedule multigrid solve, teams of CTAs taking the simulations longest
+// first (mg_batch_* in vg_mg.cu); then the rest of each step and the
+// advection on the branches.  The solve's results are bit-identical to the
+// per-simulation launches.  The autotuner also decides between the two forms
+// and picks the team size.
 #include <algorithm>
 #include <new>
 #include <vector>
@@ -49,6 +58,7 @@ struct Sim {
 struct Chunk {
   cudaGraphExec_t exec = nullptr;
   int stream = 0;
+  int part = 0;  // 0: before the persistent solve (or whole steps), 1: after it
   size_t nodes = 0;
 };
 
@@ -71,6 +81,16 @@ struct vg_batch {
   float graph_dt = 0.f;
   int graph_streams = 0;
   bool graph_network = false;
+  // persistent solve
+  bool persistent = false;
+  int team_ctas = 0;                   // CTAs per team (0: automatic)
+  size_t max_points = 0;               // largest grid (points) the persistent launch takes (0: any)
+  std::vector<char> split;             // per simulation: solved by the persistent launch
+  MgBatch* mg = nullptr;               // that launch (null: every step whole in the branches)
+  cudaGraphExec_t mg_exec = nullptr;   // ... captured as a graph (null: launched directly)
+  bool graph_persistent = false;
+  int graph_team = 0;
+  size_t graph_max_points = 0;
 };
 
 extern "C" {
@@ -101,6 +121,10 @@ void drop_graph(vg_batch* b) {
   for (Chunk& k : b->chunks)
     if (k.exec) cudaGraphExecDestroy(k.exec);
   b->chunks.clear();
+  if (b->mg_exec) cudaGraphExecDestroy(b->mg_exec);
+  b->mg_exec = nullptr;
+  mg_batch_destroy(b->mg);
+  b->mg = nullptr;
 }
 
 // Points the simulation at stream s and, if the batch uses the network and one
@@ -117,30 +141,37 @@ void bind(vg_batch* b, Sim& sim, int s) {
   sim.ctx->cfg.warm_start = net ? VG_WARM_NETWORK : VG_WARM_ZERO;
 }
 
-vg_status step_one(vg_batch* b, Sim& sim, float dt) {
+// part 0: the whole step and the advection; 1: the step up to its Poisson
+// solve; 2: the rest of the step (resuming part 1) and the advection.
+vg_status step_one(vg_batch* b, Sim& sim, float dt, int part = 0) {
+  sim.ctx->step_split = part;
   vg_status st = vg_step_device(sim.ctx, sim.pos, sim.w, sim.vel, sim.n, nullptr, dt, 0);
+  sim.ctx->step_split = 0;
   if (st != VG_OK) return bfail(b, st, std::string("step: ") + sim.ctx->err);
+  if (part == 1) return VG_OK;
   st = vg_evolve_device(sim.ctx, sim.pos, sim.vel, sim.n, dt);
   if (st != VG_OK) return bfail(b, st, std::string("evolve: ") + sim.ctx->err);
   return VG_OK;
 }
 
-// Captures branch s's simulations *i, *i + K, ... until the graph holds
-// kGraphKernels kernels or the branch ends; *i moves past them.
-vg_status capture_chunk(vg_batch* b, int s, size_t* i, float dt) {
-  const size_t K = (size_t)b->nstreams;
+// Captures branch s's simulations list[*i], list[*i + 1], ... (their `parts`)
+// until the graph holds kGraphKernels kernels or the list ends; *i moves past
+// them.  The chunk runs in frame part `fpart`.
+vg_status capture_chunk(vg_batch* b, int s, const std::vector<size_t>& list, const std::vector<int>& parts,
+                        size_t* i, float dt, int fpart) {
   cudaStream_t cs = b->streams[s];
   vg_status st;
   if ((st = bcuda(b, cudaStreamBeginCapture(cs, cudaStreamCaptureModeThreadLocal), "begin capture")) != VG_OK)
     return st;
   vg_status est = VG_OK;
   unsigned kernels = 0;
-  while (*i < b->sims.size() && kernels < kGraphKernels) {
-    Sim& sim = b->sims[*i];
+  while (*i < list.size() && kernels < kGraphKernels) {
+    Sim& sim = b->sims[list[*i]];
     bind(b, sim, s);
-    if ((est = step_one(b, sim, dt)) != VG_OK) break;
-    kernels += sim.ctx->launches + 1;  // the step's kernels and the advection
-    *i += K;
+    const unsigned before = parts[*i] == 2 ? sim.ctx->launches : 0;
+    if ((est = step_one(b, sim, dt, parts[*i])) != VG_OK) break;
+    kernels += sim.ctx->launches - before + 1;  // the step's kernels and the advection
+    ++*i;
   }
   cudaGraph_t graph = nullptr;
   const cudaError_t ce = cudaStreamEndCapture(cs, &graph);
@@ -152,6 +183,7 @@ vg_status capture_chunk(vg_batch* b, int s, size_t* i, float dt) {
   if ((st = bcuda(b, ce, "end capture")) != VG_OK) return st;
   Chunk k;
   k.stream = s;
+  k.part = fpart;
   cudaGraphGetNodes(graph, nullptr, &k.nodes);
   const cudaError_t ie = cudaGraphInstantiate(&k.exec, graph, 0);
   cudaGraphDestroy(graph);
@@ -160,38 +192,118 @@ vg_status capture_chunk(vg_batch* b, int s, size_t* i, float dt) {
   return VG_OK;
 }
 
+// Captures branch s's simulations in frame part fpart (list: simulation
+// indices, parts: the step part of each).
+vg_status capture_branch(vg_batch* b, int s, const std::vector<size_t>& list, const std::vector<int>& parts, float dt,
+                         int fpart) {
+  size_t i = 0;
+  vg_status st;
+  while (i < list.size())
+    if ((st = capture_chunk(b, s, list, parts, &i, dt, fpart)) != VG_OK) return st;
+  return VG_OK;
+}
+
 vg_status capture(vg_batch* b, float dt) {
   drop_graph(b);
-  vg_status st;
-  for (int s = 0; s < b->nstreams; ++s) {
-    size_t i = (size_t)s;
-    while (i < b->sims.size())
-      if ((st = capture_chunk(b, s, &i, dt)) != VG_OK) {
-        drop_graph(b);
-        return st;
+  vg_status st = VG_OK;
+  const size_t N = b->sims.size();
+  const int K = b->nstreams;
+  // the simulations the persistent launch solves: a calibrated fixed
+  // schedule whose hierarchy ends in the global sine-transform solve
+  b->split.assign(N, 0);
+  size_t nsplit = 0;
+  for (size_t i = 0; i < N && b->persistent; ++i) {
+    const Ctx* c = b->sims[i].ctx;
+    const Geom g = to_geom(c->cfg.fixed_grid);
+    if (c->mg_fixed_k1 > 0 && mg_batch_eligible(g) && (b->max_points == 0 || g.points() <= b->max_points)) {
+      b->split[i] = 1;
+      ++nsplit;
+    }
+  }
+  for (int s = 0; s < K && st == VG_OK; ++s) {
+    std::vector<size_t> list;
+    std::vector<int> parts;
+    for (size_t i = (size_t)s; i < N; i += (size_t)K) {
+      list.push_back(i);
+      parts.push_back(b->split[i] ? 1 : 0);
+    }
+    st = capture_branch(b, s, list, parts, dt, 0);
+  }
+  if (st == VG_OK && nsplit > 0) {
+    std::vector<MgBatchItem> items;
+    for (size_t i = 0; i < N && st == VG_OK; ++i) {
+      MgBatchItem it;
+      if (!b->split[i]) continue;
+      if (split_problem(b->sims[i].ctx, &it))
+        items.push_back(it);
+      else
+        st = bfail(b, VG_INVALID, "persistent solve: a step did not stop before its solve");
+    }
+    std::string err;
+    if (st != VG_OK) {
+    } else if ((st = mg_batch_build(items, b->device, b->team_ctas, &b->mg, &err)) != VG_OK) {
+      bfail(b, st, err);
+    } else {
+      // the launch as a graph of its own where capture takes it; launched directly otherwise
+      cudaGraph_t graph = nullptr;
+      if (cudaStreamBeginCapture(b->main, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+        const vg_status est = mg_batch_enqueue(b->mg, b->main, &err);
+        const cudaError_t ce = cudaStreamEndCapture(b->main, &graph);
+        if (est != VG_OK || ce != cudaSuccess || !graph || cudaGraphInstantiate(&b->mg_exec, graph, 0) != cudaSuccess)
+          b->mg_exec = nullptr;
+        if (graph) cudaGraphDestroy(graph);
       }
+      cudaGetLastError();
+      for (int s = 0; s < K && st == VG_OK; ++s) {
+        std::vector<size_t> list;
+        for (size_t i = (size_t)s; i < N; i += (size_t)K)
+          if (b->split[i]) list.push_back(i);
+        st = capture_branch(b, s, list, std::vector<int>(list.size(), 2), dt, 1);
+      }
+    }
+  }
+  if (st != VG_OK) {
+    drop_graph(b);
+    return st;
   }
   b->graph_dt = dt;
   b->graph_streams = b->nstreams;
   b->graph_network = b->use_network;
+  b->graph_persistent = b->persistent;
+  b->graph_team = b->team_ctas;
+  b->graph_max_points = b->max_points;
   return VG_OK;
 }
 
-// One frame from the captured graphs: fork from main, each branch's graphs in
-// capture order on its stream, join.
-vg_status launch_frame(vg_batch* b) {
+vg_status fork_join_part(vg_batch* b, int part) {
   vg_status st;
   const int K = b->graph_streams;
   if ((st = bcuda(b, cudaEventRecord(b->fork, b->main), "fork")) != VG_OK) return st;
   for (int s = 0; s < K; ++s)
     if ((st = bcuda(b, cudaStreamWaitEvent(b->streams[s], b->fork, 0), "fork wait")) != VG_OK) return st;
   for (const Chunk& k : b->chunks)
-    if ((st = bcuda(b, cudaGraphLaunch(k.exec, b->streams[k.stream]), "graph launch")) != VG_OK) return st;
+    if (k.part == part && (st = bcuda(b, cudaGraphLaunch(k.exec, b->streams[k.stream]), "graph launch")) != VG_OK)
+      return st;
   for (int s = 0; s < K; ++s) {
     if ((st = bcuda(b, cudaEventRecord(b->join[s], b->streams[s]), "join")) != VG_OK) return st;
     if ((st = bcuda(b, cudaStreamWaitEvent(b->main, b->join[s], 0), "join wait")) != VG_OK) return st;
   }
   return VG_OK;
+}
+
+// One frame from the captured graphs: fork from main, each branch's graphs in
+// capture order on its stream, join; with the persistent solve, that for the
+// steps up to the solve, then the solve on main, then again for the rest.
+vg_status launch_frame(vg_batch* b) {
+  vg_status st;
+  if ((st = fork_join_part(b, 0)) != VG_OK || !b->mg) return st;
+  if (b->mg_exec) {
+    if ((st = bcuda(b, cudaGraphLaunch(b->mg_exec, b->main), "graph launch")) != VG_OK) return st;
+  } else {
+    std::string err;
+    if ((st = mg_batch_enqueue(b->mg, b->main, &err)) != VG_OK) return bfail(b, st, err);
+  }
+  return fork_join_part(b, 1);
 }
 
 vg_status calibrate(vg_batch* b, float dt) {
@@ -384,7 +496,9 @@ vg_status vg_batch_step(vg_batch* b, float dt, int mode) {
     }
     return VG_OK;
   }
-  if (b->chunks.empty() || b->graph_dt != dt || b->graph_streams != b->nstreams || b->graph_network != b->use_network)
+  if (b->chunks.empty() || b->graph_dt != dt || b->graph_streams != b->nstreams ||
+      b->graph_network != b->use_network || b->graph_persistent != b->persistent || b->graph_team != b->team_ctas ||
+      b->graph_max_points != b->max_points)
     if ((st = capture(b, dt)) != VG_OK) return st;
   return launch_frame(b);
 }
@@ -393,6 +507,8 @@ vg_status vg_batch_synchronize(vg_batch* b) {
   if (!b) return VG_INVALID;
   vg_status st = bcuda(b, cudaStreamSynchronize(b->main), "synchronize");
   if (st != VG_OK) return st;
+  if (b->mg && mg_batch_failed(b->mg))
+    return bfail(b, VG_TIMEOUT, "persistent solve: a team barrier gave up (its fields are incomplete)");
   for (Sim& s : b->sims)
     if ((st = sync_and_check(s.ctx, "batched step")) != VG_OK) return bfail(b, st, s.ctx->err);
   return VG_OK;
@@ -409,23 +525,46 @@ vg_status vg_batch_autotune(vg_batch* b, float dt, int frames, const int* candid
     if (candidates[k] < 1 || candidates[k] > kMaxStreams) return VG_INVALID;
   float best = 3.4e38f;
   int bs = b->nstreams, bn = b->use_network ? 1 : 0;
+  const bool pers0 = b->persistent;
+  const int team0 = b->team_ctas;
+  bool bp = pers0;
+  int bt = team0;
   const int nets = b->net_edges.empty() ? 1 : 2;
   vg_status st;
+  auto trial = [&](int net) -> vg_status {
+    vg_status s2;
+    if ((s2 = capture(b, dt)) != VG_OK) return s2;
+    float ms = 0.f;
+    if ((s2 = timed_frames(b, frames, &ms)) != VG_OK) return s2;
+    if (ms < best) {
+      best = ms;
+      bs = b->nstreams;
+      bn = net;
+      bp = b->persistent;
+      bt = b->team_ctas;
+    }
+    return VG_OK;
+  };
   for (int net = 0; net < nets; ++net) {
     if ((st = vg_batch_configure(b, candidates[0], net)) != VG_OK) return st;
     if ((st = calibrate(b, dt)) != VG_OK) return st;
     for (int k = 0; k < ncand; ++k) {
       b->nstreams = candidates[k];
-      if ((st = capture(b, dt)) != VG_OK) return st;
-      float ms = 0.f;
-      if ((st = timed_frames(b, frames, &ms)) != VG_OK) return st;
-      if (ms < best) {
-        best = ms;
-        bs = candidates[k];
-        bn = net;
-      }
+      if ((st = trial(net)) != VG_OK) return st;
     }
   }
+  // the solver at the best stream count: in the branches, or persistent with teams of 4-32 CTAs
+  if ((st = vg_batch_configure(b, bs, bn)) != VG_OK) return st;
+  if ((st = calibrate(b, dt)) != VG_OK) return st;
+  const int teams[] = {0, 4, 8, 16, 32};
+  for (int t : teams) {
+    b->persistent = t > 0;
+    b->team_ctas = t > 0 ? t : team0;
+    if (b->persistent == pers0 && (!pers0 || b->team_ctas == team0)) continue;  // measured above
+    if ((st = trial(bn)) != VG_OK) return st;
+  }
+  b->persistent = bp;
+  b->team_ctas = bt;
   if ((st = vg_batch_configure(b, bs, bn)) != VG_OK) return st;
   if ((st = calibrate(b, dt)) != VG_OK) return st;
   if (best_streams) *best_streams = bs;
@@ -454,6 +593,25 @@ vg_ctx* vg_batch_context(vg_batch* b, int index) {
 
 int vg_batch_size(const vg_batch* b) { return b ? (int)b->sims.size() : 0; }
 
+vg_status vg_batch_set_solver(vg_batch* b, int persistent, int team_ctas, size_t max_points) {
+  if (!b || team_ctas < 0 || team_ctas > 1024) return VG_INVALID;
+  b->persistent = persistent != 0;
+  b->team_ctas = team_ctas;
+  b->max_points = max_points;
+  drop_graph(b);
+  return VG_OK;
+}
+
+vg_status vg_batch_solver_info(const vg_batch* b, int* persistent_sims, int* teams, int* team_ctas, int* captured) {
+  if (!b) return VG_INVALID;
+  int n = 0;
+  for (char x : b->split) n += b->mg && x ? 1 : 0;
+  if (persistent_sims) *persistent_sims = n;
+  mg_batch_info(b->mg, teams, team_ctas, nullptr);
+  if (captured) *captured = b->mg_exec ? 1 : 0;
+  return VG_OK;
+}
+
 vg_status vg_batch_graph_info(const vg_batch* b, int* graphs, size_t* max_nodes, size_t* total_nodes) {
   if (!b) return VG_INVALID;
   size_t mx = 0, tot = 0;
@@ -461,7 +619,8 @@ vg_status vg_batch_graph_info(const vg_batch* b, int* graphs, size_t* max_nodes,
     mx = std::max(mx, k.nodes);
     tot += k.nodes;
   }
-  if (graphs) *graphs = (int)b->chunks.size();
+  if (b->mg_exec) tot += 2;  // the persistent solve: barrier clear and the launch
+  if (graphs) *graphs = (int)b->chunks.size() + (b->mg_exec ? 1 : 0);
   if (max_nodes) *max_nodes = mx;
   if (total_nodes) *total_nodes = tot;
   return VG_OK;

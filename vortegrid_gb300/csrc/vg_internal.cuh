@@ -232,6 +232,12 @@ struct Ctx {
   // the multigrid coarsest-level inverse held in buf[S_MGINV]: its level's shape and 1 / spacing^2
   unsigned mginv_np[3] = {0, 0, 0};
   double mginv_r2[3] = {0.0, 0.0, 0.0};
+  // A step split at the Poisson solve, for batched frames that solve every
+  // simulation's problem in one persistent launch between the two halves:
+  // 0 the whole step; 1 up to the solve (its state kept in *split); 2 from
+  // the solve on, resuming *split.
+  int step_split = 0;
+  struct StepState* split = nullptr;
 };
 
 // The word a kernel marks when a sample lies outside the grid's cells.
@@ -297,6 +303,31 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
                         int* cycles, double* relres0, double* relres);
 // The same solve on a schedule fixed in advance (c->mg_fixed_k1, mg_fixed_k2): no host round trip.
 vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* rhs3);
+
+// Persistent batched solve: every qualifying simulation's fixed-schedule
+// solve of one frame in a single cooperative launch, teams of CTAs working
+// through the simulations with a barrier between phases.  A simulation
+// qualifies when its hierarchy ends in the sine-transform solve over the GPU
+// (mg_batch_eligible).  Results are bit-identical to run_multigrid_fixed.
+struct MgBatchItem {
+  Ctx* c;
+  Geom g;
+  float* soln;
+  const float* rhs;
+};
+struct MgBatch;
+// The Poisson problem of the last step that stopped before its solve (step_split 1).
+bool split_problem(Ctx* c, MgBatchItem* out);
+bool mg_batch_eligible(const Geom& g);
+// team_ctas: CTAs per team (0 = automatic).  Not during stream capture (uploads).
+vg_status mg_batch_build(const std::vector<MgBatchItem>& items, int device, int team_ctas, MgBatch** out,
+                         std::string* err);
+// Enqueues the launch on s (capturable): barrier counters cleared, then the kernel.
+vg_status mg_batch_enqueue(MgBatch* mb, cudaStream_t s, std::string* err);
+// Whether a team barrier gave up since the last call (reads and clears the device word; synchronous).
+bool mg_batch_failed(MgBatch* mb);
+void mg_batch_info(const MgBatch* mb, int* teams, int* team_ctas, int* ctas);
+void mg_batch_destroy(MgBatch* mb);
 
 vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9);
 vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);

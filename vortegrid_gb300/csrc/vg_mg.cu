@@ -34,6 +34,7 @@
 
 #include <algorithm>
 #include <cmath>
+#include <cstring>
 #include <vector>
 
 #include "vg_internal.cuh"
@@ -99,6 +100,25 @@ static ResLaunch res_launch(const Geom& g) {
   return L;
 }
 
+// Point arithmetic shared by the per-level kernels and the persistent batched
+// solve, written as explicit round-to-nearest operations so that every caller
+// compiles to the same float operations (no contraction left to the compiler).
+// L v at a point: the 7-point Laplacian from the centre c0 and the neighbours
+// along x, y and z.
+__device__ __forceinline__ float lap7(float c0, float xp, float xm, float yp, float ym, float zp, float zm,
+                                      float r2x, float r2y, float r2z) {
+  const float tx = __fmaf_rn(-2.f, c0, __fadd_rn(xp, xm));
+  const float ty = __fmaf_rn(-2.f, c0, __fadd_rn(yp, ym));
+  const float tz = __fmaf_rn(-2.f, c0, __fadd_rn(zp, zm));
+  return __fmaf_rn(tx, r2x, __fmaf_rn(ty, r2y, __fmul_rn(tz, r2z)));
+}
+
+// The Gauss-Seidel value of a point from its neighbour sums along x, y, z.
+__device__ __forceinline__ float gs_value(float sx, float sy, float sz, float r, float r2x, float r2y, float r2z,
+                                          float H) {
+  return __fmul_rn(__fsub_rn(__fmaf_rn(sx, r2x, __fmaf_rn(sy, r2y, __fmul_rn(sz, r2z))), r), H);
+}
+
 // Phase 1 residual: r = b - L a in FP32 from the FP32 iterate at interior
 // points (boundary r is never read); per-block FP64 partial sums of r^2 and b^2.
 __global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, float r2y, float r2z, unsigned zs,
@@ -114,12 +134,10 @@ __global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, 
       const unsigned k = x + sy * y + sz * z;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float ac = a[3 * k + c];
-        const float lap = (a[3 * (k + 1) + c] + a[3 * (k - 1) + c] - 2.f * ac) * r2x +
-                          (a[3 * (k + sy) + c] + a[3 * (k - sy) + c] - 2.f * ac) * r2y +
-                          (a[3 * (k + sz) + c] + a[3 * (k - sz) + c] - 2.f * ac) * r2z;
+        const float lap = lap7(a[3 * k + c], a[3 * (k + 1) + c], a[3 * (k - 1) + c], a[3 * (k + sy) + c],
+                               a[3 * (k - sy) + c], a[3 * (k + sz) + c], a[3 * (k - sz) + c], r2x, r2y, r2z);
         const float bv = b[3 * k + c];
-        const float rv = bv - lap;
+        const float rv = __fsub_rn(bv, lap);
         r[3 * k + c] = rv;
         rr = fmaf(rv, rv, rr);
         bb = fmaf(bv, bv, bb);
@@ -153,6 +171,25 @@ __device__ __forceinline__ void pair_add_prod(float ch, float cl, float v, float
   sl = __fadd_rn(sl, __fadd_rn(err, __fmaf_rn(cl, v, pe)));
 }
 
+// r = b - L (hi + lo) at a point from the centre and neighbour values of hi
+// and lo, in the order centre, x+, x-, y+, y-, z+, z-.
+__device__ __forceinline__ float pair_residual(const float (&h)[7], const float (&l)[7], float bv, const PairCoef& cf) {
+  float sh = 0.f, sl = 0.f;
+  pair_add_prod(cf.dh, cf.dl, h[0], sh, sl);
+  pair_add_prod(cf.xh, cf.xl, h[1], sh, sl);
+  pair_add_prod(cf.xh, cf.xl, h[2], sh, sl);
+  pair_add_prod(cf.yh, cf.yl, h[3], sh, sl);
+  pair_add_prod(cf.yh, cf.yl, h[4], sh, sl);
+  pair_add_prod(cf.zh, cf.zl, h[5], sh, sl);
+  pair_add_prod(cf.zh, cf.zl, h[6], sh, sl);
+  const float lap_lo = lap7(l[0], l[1], l[2], l[3], l[4], l[5], l[6], cf.r2x, cf.r2y, cf.r2z);
+  // r = (b - sh) - sl - lap_lo, the first difference by TwoSum
+  const float t = __fsub_rn(bv, sh);
+  const float bb = __fsub_rn(t, bv);
+  const float terr = __fadd_rn(__fsub_rn(bv, __fsub_rn(t, bb)), __fsub_rn(-sh, bb));
+  return __fadd_rn(t, __fsub_rn(__fsub_rn(terr, sl), lap_lo));
+}
+
 __global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef cf, unsigned zs,
                                                                const float* __restrict__ hi,
                                                                const float* __restrict__ lo,
@@ -168,24 +205,14 @@ __global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef 
       const unsigned k = x + sy * y + sz * z;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        float sh = 0.f, sl = 0.f;
-        pair_add_prod(cf.dh, cf.dl, hi[3 * k + c], sh, sl);
-        pair_add_prod(cf.xh, cf.xl, hi[3 * (k + 1) + c], sh, sl);
-        pair_add_prod(cf.xh, cf.xl, hi[3 * (k - 1) + c], sh, sl);
-        pair_add_prod(cf.yh, cf.yl, hi[3 * (k + sy) + c], sh, sl);
-        pair_add_prod(cf.yh, cf.yl, hi[3 * (k - sy) + c], sh, sl);
-        pair_add_prod(cf.zh, cf.zl, hi[3 * (k + sz) + c], sh, sl);
-        pair_add_prod(cf.zh, cf.zl, hi[3 * (k - sz) + c], sh, sl);
-        const float l0 = lo[3 * k + c];
-        const float lap_lo = (lo[3 * (k + 1) + c] + lo[3 * (k - 1) + c] - 2.f * l0) * cf.r2x +
-                             (lo[3 * (k + sy) + c] + lo[3 * (k - sy) + c] - 2.f * l0) * cf.r2y +
-                             (lo[3 * (k + sz) + c] + lo[3 * (k - sz) + c] - 2.f * l0) * cf.r2z;
-        // r = (b - sh) - sl - lap_lo, the first difference by TwoSum
-        const float bv = b[3 * k + c];
-        const float t = __fsub_rn(bv, sh);
-        const float bb = __fsub_rn(t, bv);
-        const float terr = __fadd_rn(__fsub_rn(bv, __fsub_rn(t, bb)), __fsub_rn(-sh, bb));
-        const float rv = __fadd_rn(t, __fsub_rn(__fsub_rn(terr, sl), lap_lo));
+        const unsigned o[7] = {k, k + 1, k - 1, k + sy, k - sy, k + sz, k - sz};
+        float h[7], l[7];
+#pragma unroll
+        for (int i = 0; i < 7; ++i) {
+          h[i] = hi[3 * o[i] + c];
+          l[i] = lo[3 * o[i] + c];
+        }
+        const float rv = pair_residual(h, l, b[3 * k + c], cf);
         r[3 * k + c] = rv;
         rr = fmaf(rv, rv, rr);
       }
@@ -228,12 +255,12 @@ __device__ __forceinline__ void rbgs_point(const Geom& g, float r2x, float r2y, 
   for (int c = 0; c < 3; ++c) {
     float v;
     if (zero_first) {
-      v = -r[3 * k + c] * H;
+      v = __fmul_rn(-r[3 * k + c], H);
     } else {
-      const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
-      const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
-      const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
-      v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[3 * k + c]) * H;
+      const float sx = __fadd_rn(e[3 * (k + 1) + c], e[3 * (k - 1) + c]);
+      const float syv = __fadd_rn(e[3 * (k + sy) + c], e[3 * (k - sy) + c]);
+      const float szv = __fadd_rn(e[3 * (k + sz) + c], e[3 * (k - sz) + c]);
+      v = gs_value(sx, syv, szv, r[3 * k + c], r2x, r2y, r2z, H);
     }
     e[3 * k + c] = v;
   }
@@ -259,12 +286,12 @@ __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, floa
   const unsigned sy = nx, sz = nx * ny;
   float v;
   if (zero_first) {
-    v = -r[3 * k + c] * H;
+    v = __fmul_rn(-r[3 * k + c], H);
   } else {
-    const float sx = e[3 * (k + 1) + c] + e[3 * (k - 1) + c];
-    const float syv = e[3 * (k + sy) + c] + e[3 * (k - sy) + c];
-    const float szv = e[3 * (k + sz) + c] + e[3 * (k - sz) + c];
-    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[3 * k + c]) * H;
+    const float sx = __fadd_rn(e[3 * (k + 1) + c], e[3 * (k - 1) + c]);
+    const float syv = __fadd_rn(e[3 * (k + sy) + c], e[3 * (k - sy) + c]);
+    const float szv = __fadd_rn(e[3 * (k + sz) + c], e[3 * (k - sz) + c]);
+    v = gs_value(sx, syv, szv, r[3 * k + c], r2x, r2y, r2z, H);
   }
   e[3 * k + c] = v;
 }
@@ -285,15 +312,15 @@ __global__ void __launch_bounds__(256) k_rbgs_first(Geom g, float r2x, float r2y
   const unsigned k = x + nx * (y + ny * z), t = 3 * k + c;
   float v;
   if (((x + y + z) & 1u) == 0u) {
-    v = -r[t] * H;
+    v = __fmul_rn(-r[t], H);
   } else {
     const unsigned sy = nx, sz = nx * ny;
     // red neighbours: -r H (boundary neighbours stay e = 0)
-    auto red = [&](unsigned n, bool in) { return in ? -r[3 * n + c] * H : 0.f; };
-    const float sx = red(k + 1, x + 2 < nx) + red(k - 1, x > 1);
-    const float syv = red(k + sy, y + 2 < ny) + red(k - sy, y > 1);
-    const float szv = red(k + sz, z + 2 < g.np[2]) + red(k - sz, z > 1);
-    v = (fmaf(sx, r2x, fmaf(syv, r2y, szv * r2z)) - r[t]) * H;
+    auto red = [&](unsigned n, bool in) { return in ? __fmul_rn(-r[3 * n + c], H) : 0.f; };
+    const float sx = __fadd_rn(red(k + 1, x + 2 < nx), red(k - 1, x > 1));
+    const float syv = __fadd_rn(red(k + sy, y + 2 < ny), red(k - sy, y > 1));
+    const float szv = __fadd_rn(red(k + sz, z + 2 < g.np[2]), red(k - sz, z > 1));
+    v = gs_value(sx, syv, szv, r[t], r2x, r2y, r2z, H);
   }
   e[t] = v;
 }
@@ -320,18 +347,16 @@ __device__ __forceinline__ void residual_restrict_point(const Geom& F, const Geo
         const unsigned o = f0 + dx + sy * dy + sz * dz;
 #pragma unroll
         for (int c = 0; c < 3; ++c) {
-          const float ec = e[3 * o + c];
-          const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
-                            (e[3 * (o + sy) + c] + e[3 * (o - sy) + c] - 2.f * ec) * r2y +
-                            (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
-          acc[c] = fmaf(wt, r[3 * o + c] - lap, acc[c]);
+          const float lap = lap7(e[3 * o + c], e[3 * (o + 1) + c], e[3 * (o - 1) + c], e[3 * (o + sy) + c],
+                                 e[3 * (o - sy) + c], e[3 * (o + sz) + c], e[3 * (o - sz) + c], r2x, r2y, r2z);
+          acc[c] = __fmaf_rn(wt, __fsub_rn(r[3 * o + c], lap), acc[c]);
         }
       }
   const float s = 1.0f / 64.0f;
   const unsigned k = x + C.np[0] * (y + C.np[1] * z);
-  rc[3 * k] = acc[0] * s;
-  rc[3 * k + 1] = acc[1] * s;
-  rc[3 * k + 2] = acc[2] * s;
+  rc[3 * k] = __fmul_rn(acc[0], s);
+  rc[3 * k + 1] = __fmul_rn(acc[1], s);
+  rc[3 * k + 2] = __fmul_rn(acc[2], s);
 }
 
 // Global-memory form, tiled: a CTA owns kRTX x kRTY x kRTZ coarse points.  It
@@ -360,11 +385,9 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float
       const unsigned o = fx + sy * fy + sz * fz;
 #pragma unroll
       for (int c = 0; c < 3; ++c) {
-        const float ec = e[3 * o + c];
-        const float lap = (e[3 * (o + 1) + c] + e[3 * (o - 1) + c] - 2.f * ec) * r2x +
-                          (e[3 * (o + sy) + c] + e[3 * (o - sy) + c] - 2.f * ec) * r2y +
-                          (e[3 * (o + sz) + c] + e[3 * (o - sz) + c] - 2.f * ec) * r2z;
-        v[c] = r[3 * o + c] - lap;
+        const float lap = lap7(e[3 * o + c], e[3 * (o + 1) + c], e[3 * (o - 1) + c], e[3 * (o + sy) + c],
+                               e[3 * (o - sy) + c], e[3 * (o + sz) + c], e[3 * (o - sz) + c], r2x, r2y, r2z);
+        v[c] = __fsub_rn(r[3 * o + c], lap);
       }
     }
     s_res[3 * p] = v[0];
@@ -389,9 +412,9 @@ __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float
 #pragma unroll
         for (int dx = -1; dx <= 1; ++dx) {
           const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
-          acc = fmaf(wt, sr[3 * (dx + kRFX * (dy + kRFY * dz))], acc);
+          acc = __fmaf_rn(wt, sr[3 * (dx + kRFX * (dy + kRFY * dz))], acc);
         }
-    rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = acc * (1.0f / 64.0f);
+    rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = __fmul_rn(acc, 1.0f / 64.0f);
   }
 }
 
@@ -1290,4 +1313,826 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   return VG_OK;
 }
 
+// ------------------------------------------------------- persistent batched solve
+//
+// Many simulations' fixed-schedule solves in one cooperative launch.  The
+// CTAs form teams of T; a team takes its simulations (assigned on the host,
+// longest first) one after another and runs every phase of the schedule of
+// run_multigrid_fixed -- zeroing, residuals, smoothing sweeps, residual +
+// restriction, sine-transform passes, prolongation, updates -- as loops over
+// the team's threads, with a team barrier between phases.  The point
+// arithmetic is the shared lap7 / gs_value / pair_residual code, so the
+// result is bit-identical to the per-level launches; only the norm sums
+// (statistics) are accumulated in another order.  Fields written during the
+// launch are read with weak loads (never the non-coherent read-only path),
+// which the barrier's fences order after the writes.
+
+namespace {
+
+constexpr int kPThreads = 512;  // threads per CTA
+constexpr int kPU = 3;          // items a lane has in flight per step of the streaming phases
+constexpr int kPMaxLev = 8;     // levels above and including the sine-transform solve
+
+struct PLev {
+  unsigned np[3];
+  float r2x, r2y, r2z, H;
+  unsigned base;  // points before this level in E and R
+};
+
+struct PSim {
+  PLev lev[kPMaxLev];
+  int nlev;
+  int k1, k2;
+  PairCoef cf;
+  float *E, *R, *x, *lo, *etot, *rir;
+  const float* rhs;
+  const float* dst;  // coarsest level: Sx, Sy, Sz, 1 / eigenvalue (direct_tables)
+  double* relres;    // [0] final, [1] initial relative residual
+  double* acc;       // [0] sum r^2, [1] sum b^2
+  unsigned n0;       // level-0 points
+  unsigned total;    // points over all levels
+};
+
+struct Team {
+  unsigned* ctr;  // arrivals at this team's barriers (cleared before the launch)
+  int* err;       // set when any barrier gives up
+  unsigned T, rank, target;
+  unsigned long long limit_ns;  // a barrier wait gives up after this long
+  __device__ unsigned tid() const { return rank * blockDim.x + threadIdx.x; }
+  __device__ unsigned size() const { return T * blockDim.x; }
+};
+
+__device__ __forceinline__ unsigned long long global_ns() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr unsigned long long kBarrierNs = 2000000000ull;  // the solve's barrier waits give up after 2 s
+constexpr unsigned kBarrierPolls = 1u << 26;              // ... or after this many polls
+
+// Team barrier: each CTA's writes are fenced before it arrives, and after
+// the wait, so the team's next phase sees them.  False (err set) when a wait
+// gives up or another barrier already has; the caller then returns.
+__device__ bool team_sync(Team& tm) {
+  __shared__ int s_ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    tm.target += tm.T;
+    __threadfence();
+    atomicAdd(tm.ctr, 1u);
+    int ok = 1;
+    const unsigned long long t0 = global_ns();
+    for (unsigned it = 0;; ++it) {
+      if ((int)(*(volatile unsigned*)tm.ctr - tm.target) >= 0) break;
+      if (*(volatile int*)tm.err) {
+        ok = 0;
+        break;
+      }
+      if (it >= kBarrierPolls || ((it & 255u) == 255u && global_ns() - t0 > tm.limit_ns)) {
+        atomicExch(tm.err, 1);
+        ok = 0;
+        break;
+      }
+      if (it >= 4096) __nanosleep(64);  // long waits back off
+    }
+    __threadfence();
+    s_ok = ok;
+  }
+  __syncthreads();
+  return s_ok != 0;
+}
+
+// Loads of fields written earlier in the launch: weak loads, cached in L1
+// (the stencils re-read each value up to seven times).  The team barrier's
+// fences order them after the other CTAs' writes; the non-coherent read-only
+// path (ld.global.nc) is never used for these fields.
+__device__ __forceinline__ float ld(const float* p) { return __ldca(p); }
+
+// Interior rows (y, z) of a level taken by the team's warps in turn; the
+// lanes run along the row over `items` (point, component) pairs.
+template <class F>
+__device__ __forceinline__ void team_rows(const Team& tm, unsigned ny, unsigned nz, unsigned items, F f) {
+  const unsigned lane = threadIdx.x & 31u, nyi = ny - 2, rows = nyi * (nz - 2);
+  for (unsigned row = tm.tid() >> 5; row < rows; row += tm.size() >> 5) {
+    const unsigned zz = row / nyi;
+    const unsigned y = 1 + row - zz * nyi, z = 1 + zz;
+    for (unsigned jc = lane; jc < items; jc += 32) f(jc, y, z);
+  }
+}
+
+__device__ void warp_add2(double* a, double* b, float va, float vb) {
+  for (int o = 16; o > 0; o >>= 1) {
+    va += __shfl_xor_sync(0xffffffffu, va, o);
+    vb += __shfl_xor_sync(0xffffffffu, vb, o);
+  }
+  if ((threadIdx.x & 31u) == 0) {
+    if (a) atomicAdd(a, (double)va);
+    if (b) atomicAdd(b, (double)vb);
+  }
+}
+
+// Streaming loops, as float4 where the arrays are 16-byte aligned.
+__device__ __forceinline__ bool aligned16(const void* a, const void* b) {
+  return (((uintptr_t)a | (uintptr_t)b) & 15u) == 0;
+}
+
+__device__ void p_zero(const Team& tm, float* p, unsigned n) {
+  const unsigned n4 = aligned16(p, p) ? n / 4 : 0;
+  for (unsigned i = tm.tid(); i < n4; i += tm.size()) reinterpret_cast<float4*>(p)[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+  for (unsigned i = 4 * n4 + tm.tid(); i < n; i += tm.size()) p[i] = 0.f;
+}
+
+__device__ void p_add(const Team& tm, float* a, const float* e, unsigned n) {  // a += e
+  const unsigned n4 = aligned16(a, e) ? n / 4 : 0;
+  const unsigned step = tm.size();
+  for (unsigned i = tm.tid(); i < n4; i += kPU * step) {
+    float4 va[kPU], ve[kPU];
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const unsigned q = min(i + u * step, n4 - 1);  // past the end: reload the last group, not stored
+      va[u] = __ldcg(reinterpret_cast<const float4*>(a) + q);
+      ve[u] = __ldcg(reinterpret_cast<const float4*>(e) + q);
+    }
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      if (i + u * step >= n4) break;
+      va[u].x = __fadd_rn(va[u].x, ve[u].x);
+      va[u].y = __fadd_rn(va[u].y, ve[u].y);
+      va[u].z = __fadd_rn(va[u].z, ve[u].z);
+      va[u].w = __fadd_rn(va[u].w, ve[u].w);
+      reinterpret_cast<float4*>(a)[i + u * step] = va[u];
+    }
+  }
+  for (unsigned i = 4 * n4 + tm.tid(); i < n; i += tm.size()) a[i] = __fadd_rn(ld(a + i), ld(e + i));
+}
+
+__device__ void p_copy(const Team& tm, float* d, const float* s, unsigned n) {
+  const unsigned n4 = aligned16(d, s) ? n / 4 : 0;
+  for (unsigned i = tm.tid(); i < n4; i += tm.size())
+    reinterpret_cast<float4*>(d)[i] = __ldcg(reinterpret_cast<const float4*>(s) + i);
+  for (unsigned i = 4 * n4 + tm.tid(); i < n; i += tm.size()) d[i] = ld(s + i);
+}
+
+// The team's share of the flattened (interior row, item) space of a level:
+// each warp a contiguous slice of whole warps' worth of items, each lane every
+// 32nd item of it, kPU items per step.  A step first computes all kPU
+// positions, then issues every load (items past the end read a safe interior
+// point), then computes and stores, so each lane keeps kPU items' loads in
+// flight instead of one (the stores would otherwise keep the compiler from
+// hoisting the next item's loads).
+struct Slice {
+  unsigned t, t1;   // this lane's next item and the end of the warp's slice
+  unsigned y, z, jc;  // the item's row and index within the row
+};
+
+__device__ __forceinline__ bool slice_begin(const Team& tm, unsigned ny, unsigned nz, unsigned ipr, Slice& s) {
+  const unsigned nyi = ny - 2, total = nyi * (nz - 2) * ipr;
+  const unsigned nw = tm.size() >> 5, w = tm.tid() >> 5;
+  const unsigned chunk = ((total + nw - 1) / nw + 31u) & ~31u;
+  s.t = w * chunk + (threadIdx.x & 31u);
+  s.t1 = min(total, w * chunk + chunk);
+  if (s.t >= s.t1) return false;
+  const unsigned row = s.t / ipr;
+  s.jc = s.t - row * ipr;
+  s.z = 1 + row / nyi;
+  s.y = 1 + row - (s.z - 1) * nyi;
+  return true;
+}
+
+// The positions of this lane's next kPU items (32 apart); s moves past them.
+__device__ __forceinline__ void slice_step(Slice& s, unsigned ipr, unsigned ny, unsigned (&y)[kPU],
+                                           unsigned (&z)[kPU], unsigned (&jc)[kPU], bool (&in)[kPU]) {
+#pragma unroll
+  for (int u = 0; u < kPU; ++u) {
+    y[u] = s.y;
+    z[u] = s.z;
+    jc[u] = s.jc;
+    in[u] = s.t + 32u * u < s.t1;
+    s.jc += 32u;
+    while (s.jc >= ipr) {
+      s.jc -= ipr;
+      if (++s.y == ny - 1) {
+        s.y = 1;
+        ++s.z;
+      }
+    }
+  }
+  s.t += 32u * kPU;
+}
+
+// One colour's Gauss-Seidel half sweep (k_rbgs).
+__device__ void p_rbgs(const Team& tm, const PLev& L, float* e, const float* r, unsigned col) {
+  const unsigned nx = L.np[0], ny = L.np[1], sy = 3 * nx, sz = 3 * nx * ny;
+  const unsigned ipr = 3 * ((nx - 1) / 2), safe = 3 * (1 + nx * (1 + ny));
+  Slice s;
+  if (!slice_begin(tm, ny, L.np[2], ipr, s)) return;
+  while (s.t < s.t1) {
+    unsigned y[kPU], z[kPU], jc[kPU], k[kPU];
+    bool in[kPU];
+    slice_step(s, ipr, ny, y, z, jc, in);
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const unsigned j = jc[u] / 3u, c = jc[u] - 3u * j;
+      const unsigned x = 1u + ((col + 1u + y[u] + z[u]) & 1u) + 2u * j;
+      in[u] = in[u] && x + 1 < nx;
+      k[u] = in[u] ? 3 * (x + nx * (y[u] + ny * z[u])) + c : safe;
+    }
+    float vx[kPU], vy[kPU], vz[kPU], vr[kPU];
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      vx[u] = __fadd_rn(ld(e + k[u] + 3), ld(e + k[u] - 3));
+      vy[u] = __fadd_rn(ld(e + k[u] + sy), ld(e + k[u] - sy));
+      vz[u] = __fadd_rn(ld(e + k[u] + sz), ld(e + k[u] - sz));
+      vr[u] = ld(r + k[u]);
+    }
+#pragma unroll
+    for (int u = 0; u < kPU; ++u)
+      if (in[u]) e[k[u]] = gs_value(vx[u], vy[u], vz[u], vr[u], L.r2x, L.r2y, L.r2z, L.H);
+  }
+}
+
+// The first sweep from e = 0, both colours (k_rbgs_first).  Red items load
+// their own r in place of the neighbours they do not use.
+__device__ void p_rbgs_first(const Team& tm, const PLev& L, float* e, const float* r) {
+  const unsigned nx = L.np[0], ny = L.np[1], nz = L.np[2], sy = 3 * nx, sz = 3 * nx * ny;
+  const unsigned ipr = 3 * (nx - 2);
+  const float H = L.H;
+  Slice s;
+  if (!slice_begin(tm, ny, nz, ipr, s)) return;
+  while (s.t < s.t1) {
+    unsigned y[kPU], z[kPU], jc[kPU], k[kPU];
+    bool in[kPU], black[kPU];
+    unsigned m[kPU];  // bit i: neighbour i (x+, x-, y+, y-, z+, z-) is a red interior point
+    slice_step(s, ipr, ny, y, z, jc, in);
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const unsigned j = jc[u] / 3u, c = jc[u] - 3u * j, x = 1u + j;
+      k[u] = in[u] ? 3 * (x + nx * (y[u] + ny * z[u])) + c : 3 * (1 + nx * (1 + ny));
+      black[u] = in[u] && ((x + y[u] + z[u]) & 1u);
+      m[u] = black[u] ? (x + 2 < nx) | (x > 1) << 1 | (y[u] + 2 < ny) << 2 | (y[u] > 1) << 3 |
+                            (z[u] + 2 < nz) << 4 | (z[u] > 1) << 5
+                      : 0u;
+    }
+    float nb[kPU][6], vr[kPU];
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      const int off[6] = {3, -3, (int)sy, -(int)sy, (int)sz, -(int)sz};
+      vr[u] = ld(r + k[u]);
+#pragma unroll
+      for (int i = 0; i < 6; ++i) nb[u][i] = ld(r + k[u] + ((m[u] >> i) & 1u ? off[i] : 0));
+    }
+#pragma unroll
+    for (int u = 0; u < kPU; ++u) {
+      if (!in[u]) continue;
+      float v;
+      if (!black[u]) {
+        v = __fmul_rn(-vr[u], H);
+      } else {
+        float red[6];
+#pragma unroll
+        for (int i = 0; i < 6; ++i) red[i] = (m[u] >> i) & 1u ? __fmul_rn(-nb[u][i], H) : 0.f;
+        v = gs_value(__fadd_rn(red[0], red[1]), __fadd_rn(red[2], red[3]), __fadd_rn(red[4], red[5]), vr[u], L.r2x,
+                     L.r2y, L.r2z, H);
+      }
+      e[k[u]] = v;
+    }
+  }
+}
+
+// r = b - L a at level 0 (k_residual32n); sums of r^2 and b^2 into *arr, *abb when given.
+__device__ void p_residual32(const Team& tm, const PLev& L, const float* a, const float* b, float* r, double* arr,
+                             double* abb) {
+  const unsigned nx = L.np[0], ny = L.np[1], sy = 3 * nx, sz = 3 * nx * ny;
+  const unsigned ipr = 3 * (nx - 2);
+  float rr = 0.f, bb = 0.f;
+  Slice s;
+  if (slice_begin(tm, ny, L.np[2], ipr, s)) {
+    while (s.t < s.t1) {
+      unsigned y[kPU], z[kPU], jc[kPU], k[kPU];
+      bool in[kPU];
+      slice_step(s, ipr, ny, y, z, jc, in);
+#pragma unroll
+      for (int u = 0; u < kPU; ++u) {
+        const unsigned j = jc[u] / 3u, c = jc[u] - 3u * j, x = 1u + j;
+        k[u] = in[u] ? 3 * (x + nx * (y[u] + ny * z[u])) + c : 3 * (1 + nx * (1 + ny));
+      }
+      float v[kPU][7], vb[kPU];
+#pragma unroll
+      for (int u = 0; u < kPU; ++u) {
+        v[u][0] = ld(a + k[u]);
+        v[u][1] = ld(a + k[u] + 3);
+        v[u][2] = ld(a + k[u] - 3);
+        v[u][3] = ld(a + k[u] + sy);
+        v[u][4] = ld(a + k[u] - sy);
+        v[u][5] = ld(a + k[u] + sz);
+        v[u][6] = ld(a + k[u] - sz);
+        vb[u] = ld(b + k[u]);
+      }
+#pragma unroll
+      for (int u = 0; u < kPU; ++u) {
+        if (!in[u]) continue;
+        const float lap = lap7(v[u][0], v[u][1], v[u][2], v[u][3], v[u][4], v[u][5], v[u][6], L.r2x, L.r2y, L.r2z);
+        const float rv = __fsub_rn(vb[u], lap);
+        r[k[u]] = rv;
+        rr = fmaf(rv, rv, rr);
+        bb = fmaf(vb[u], vb[u], bb);
+      }
+    }
+  }
+  if (arr || abb) warp_add2(arr, abb, rr, bb);
+}
+
+// r = b - L (x + lo) to FP64-class accuracy (k_residual_pair); r^2 into *arr when given.
+__device__ void p_residual_pair(const Team& tm, const PSim& S, float* r, double* arr) {
+  const PLev& L = S.lev[0];
+  const unsigned nx = L.np[0], ny = L.np[1], sy = nx, sz = nx * ny;
+  float rr = 0.f;
+  team_rows(tm, ny, L.np[2], 3 * (nx - 2), [&](unsigned jc, unsigned y, unsigned z) {
+    const unsigned j = jc / 3u, c = jc - 3u * j, x = 1u + j;
+    const unsigned k = x + nx * (y + ny * z);
+    const unsigned o[7] = {k, k + 1, k - 1, k + sy, k - sy, k + sz, k - sz};
+    float h[7], l[7];
+#pragma unroll
+    for (int i = 0; i < 7; ++i) {
+      h[i] = ld(S.x + 3 * o[i] + c);
+      l[i] = ld(S.lo + 3 * o[i] + c);
+    }
+    const float rv = pair_residual(h, l, ld(S.rhs + 3 * k + c), S.cf);
+    r[3 * k + c] = rv;
+    rr = fmaf(rv, rv, rr);
+  });
+  if (arr) warp_add2(arr, nullptr, rr, 0.f);
+}
+
+// Fused residual + full-weighting restriction (k_residual_restrict), the
+// team's CTAs taking its tiles in turn.
+__device__ void p_restrict(const Team& tm, const PLev& F, const PLev& C, const float* e, const float* r, float* rc,
+                           float* s_res) {
+  const unsigned gx = (C.np[0] - 2 + kRTX - 1) / kRTX, gy = (C.np[1] - 2 + kRTY - 1) / kRTY,
+                 gz = (C.np[2] - 2 + kRTZ - 1) / kRTZ;
+  const unsigned nx = F.np[0], ny = F.np[1], nz = F.np[2], sy = nx, sz = nx * ny;
+  for (unsigned tile = tm.rank; tile < gx * gy * gz; tile += tm.T) {
+    const unsigned bx = tile % gx, q = tile / gx, by = q % gy, bz = q / gy;
+    const unsigned cx0 = 1 + bx * kRTX, cy0 = 1 + by * kRTY, cz0 = 1 + bz * kRTZ;
+    for (unsigned p = threadIdx.x; p < (unsigned)(kRFX * kRFY * kRFZ); p += blockDim.x) {
+      const unsigned lx = p % kRFX, qq = p / kRFX;
+      const unsigned ly = qq % kRFY, lz = qq / kRFY;
+      const unsigned fx = 2 * cx0 - 1 + lx, fy = 2 * cy0 - 1 + ly, fz = 2 * cz0 - 1 + lz;
+      float v[3] = {0.f, 0.f, 0.f};
+      if (fx + 1 < nx && fy + 1 < ny && fz + 1 < nz) {
+        const unsigned o = fx + sy * fy + sz * fz;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) {
+          const float lap = lap7(ld(e + 3 * o + c), ld(e + 3 * (o + 1) + c), ld(e + 3 * (o - 1) + c),
+                                 ld(e + 3 * (o + sy) + c), ld(e + 3 * (o - sy) + c), ld(e + 3 * (o + sz) + c),
+                                 ld(e + 3 * (o - sz) + c), F.r2x, F.r2y, F.r2z);
+          v[c] = __fsub_rn(ld(r + 3 * o + c), lap);
+        }
+      }
+      s_res[3 * p] = v[0];
+      s_res[3 * p + 1] = v[1];
+      s_res[3 * p + 2] = v[2];
+    }
+    __syncthreads();
+    for (unsigned i = threadIdx.x; i < (unsigned)(kRTX * kRTY * kRTZ * 3); i += blockDim.x) {
+      const unsigned c = i % 3u, pp = i / 3u;
+      const unsigned lx = pp % kRTX, qq = pp / kRTX;
+      const unsigned ly = qq % kRTY, lz = qq / kRTY;
+      const unsigned x = cx0 + lx, y = cy0 + ly, z = cz0 + lz;
+      if (x + 1 >= C.np[0] || y + 1 >= C.np[1] || z + 1 >= C.np[2]) continue;
+      const float* sr = s_res + 3 * ((2 * lx + 1) + kRFX * ((2 * ly + 1) + kRFY * (2 * lz + 1))) + c;
+      float acc = 0.f;
+#pragma unroll
+      for (int dz = -1; dz <= 1; ++dz)
+#pragma unroll
+        for (int dy = -1; dy <= 1; ++dy)
+#pragma unroll
+          for (int dx = -1; dx <= 1; ++dx) {
+            const float wt = (float)(8 >> (abs(dx) + abs(dy) + abs(dz)));
+            acc = __fmaf_rn(wt, sr[3 * (dx + kRFX * (dy + kRFY * dz))], acc);
+          }
+      rc[3 * (x + C.np[0] * (y + C.np[1] * z)) + c] = __fmul_rn(acc, 1.0f / 64.0f);
+    }
+    __syncthreads();
+  }
+}
+
+// e_fine += trilinear(e_coarse), one thread per coarse cell (k_prolong_cells).
+__device__ void p_prolong(const Team& tm, const PLev& F, const PLev& C, const float* ec, float* ef) {
+  const unsigned ncx = C.np[0] - 1, ncy = C.np[1] - 1, cells = ncx * ncy * (C.np[2] - 1);
+  const unsigned sy = C.np[0], sz = C.np[0] * C.np[1], fsy = F.np[0], fsz = F.np[0] * F.np[1];
+  for (unsigned i = tm.tid(); i < cells; i += tm.size()) {
+    const unsigned cx = i % ncx, q = i / ncx, cy = q % ncy, cz = q / ncy;
+    const unsigned c0 = cx + sy * cy + sz * cz;
+    float v[2][2][2][3];
+#pragma unroll
+    for (int iz = 0; iz < 2; ++iz)
+#pragma unroll
+      for (int iy = 0; iy < 2; ++iy)
+#pragma unroll
+        for (int ix = 0; ix < 2; ++ix)
+#pragma unroll
+          for (int c = 0; c < 3; ++c) v[iz][iy][ix][c] = ld(ec + 3 * (c0 + ix + sy * iy + sz * iz) + c);
+#pragma unroll
+    for (int oz = 0; oz < 2; ++oz)
+#pragma unroll
+      for (int oy = 0; oy < 2; ++oy)
+#pragma unroll
+        for (int ox = 0; ox < 2; ++ox) {
+          const unsigned X = 2 * cx + ox, Y = 2 * cy + oy, Z = 2 * cz + oz;
+          if (X == 0 || Y == 0 || Z == 0) continue;
+          const float wt = 1.0f / (float)(1u << (ox + oy + oz));
+          const unsigned k = X + fsy * Y + fsz * Z;
+#pragma unroll
+          for (int c = 0; c < 3; ++c) {
+            float a = 0.f;
+#pragma unroll
+            for (int iz = 0; iz <= oz; ++iz)
+#pragma unroll
+              for (int iy = 0; iy <= oy; ++iy)
+#pragma unroll
+                for (int ix = 0; ix <= ox; ++ix) a += v[iz][iy][ix][c];
+            ef[3 * k + c] = __fadd_rn(ld(ef + 3 * k + c), __fmul_rn(a, wt));
+          }
+        }
+  }
+}
+
+// The exact coarsest solve (k_dst_gather, k_dst_pass, k_dst_scatter).
+__device__ bool p_direct(Team& tm, const PSim& S) {
+  const PLev& L = S.lev[S.nlev - 1];
+  const unsigned nx = L.np[0], ny = L.np[1], nz = L.np[2];
+  const unsigned nxi = nx - 2, nyi = ny - 2, nzi = nz - 2, N = nxi * nyi * nzi;
+  float* E = S.E + 3 * L.base;
+  float* R = S.R + 3 * L.base;
+  const float* Sx = S.dst;
+  const float* Sy = Sx + nxi * nxi;
+  const float* Sz = Sy + nyi * nyi;
+  const float* Dinv = Sz + nzi * nzi;
+  for (unsigned i = tm.tid(); i < 3 * N; i += tm.size()) {  // R (full) -> E (compact)
+    const unsigned c = i % 3u, p = i / 3u;
+    const unsigned x = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
+    E[i] = ld(R + 3 * ((x + 1) + nx * ((y + 1) + ny * (z + 1))) + c);
+  }
+  if (!team_sync(tm)) return false;
+  auto pass = [&](const float* in, float* out, const float* T, unsigned n, unsigned st, const float* scale) {
+    for (unsigned i = tm.tid(); i < 3 * N; i += tm.size()) {
+      const unsigned c = i % 3u, p = i / 3u;
+      const unsigned k = (p / st) % n, p0 = p - k * st;
+      float acc = 0.f;
+      for (unsigned m = 0; m < n; ++m) acc = fmaf(__ldg(T + k * n + m), ld(in + 3 * (p0 + m * st) + c), acc);
+      out[i] = scale ? acc * __ldg(scale + p) : acc;
+    }
+    return team_sync(tm);
+  };
+  if (!pass(E, R, Sx, nxi, 1, nullptr) || !pass(R, E, Sy, nyi, nxi, nullptr) ||
+      !pass(E, R, Sz, nzi, nxi * nyi, Dinv) || !pass(R, E, Sz, nzi, nxi * nyi, nullptr) ||
+      !pass(E, R, Sy, nyi, nxi, nullptr))
+    return false;
+  const unsigned pts = nx * ny * nz;
+  for (unsigned i = tm.tid(); i < 3 * pts; i += tm.size()) {  // x pass into e (full layout)
+    const unsigned c = i % 3u, k = i / 3u;
+    const unsigned x = k % nx, q = k / nx, y = q % ny, z = q / ny;
+    float v = 0.f;
+    if (x > 0 && y > 0 && z > 0 && x + 1 < nx && y + 1 < ny && z + 1 < nz) {
+      const unsigned kx = x - 1, p0 = nxi * ((y - 1) + nyi * (z - 1));
+      for (unsigned m = 0; m < nxi; ++m) v = fmaf(__ldg(Sx + kx * nxi + m), ld(R + 3 * (p0 + m) + c), v);
+    }
+    E[i] = v;
+  }
+  return team_sync(tm);
+}
+
+// One V(2,2)-cycle on L e = R[level 0] (enqueue_vcycle).
+__device__ bool p_vcycle(Team& tm, const PSim& S, float* s_res) {
+  const int nl = S.nlev;
+  for (int l = 0; l + 1 < nl; ++l) {
+    const PLev& L = S.lev[l];
+    float* e = S.E + 3 * L.base;
+    const float* r = S.R + 3 * L.base;
+    p_rbgs_first(tm, L, e, r);
+    if (!team_sync(tm)) return false;
+    for (unsigned col = 0; col < 2; ++col) {
+      p_rbgs(tm, L, e, r, col);
+      if (!team_sync(tm)) return false;
+    }
+    p_restrict(tm, L, S.lev[l + 1], e, r, S.R + 3 * S.lev[l + 1].base, s_res);
+    if (!team_sync(tm)) return false;
+  }
+  if (!p_direct(tm, S)) return false;
+  for (int l = nl - 2; l >= 0; --l) {
+    const PLev& L = S.lev[l];
+    float* e = S.E + 3 * L.base;
+    const float* r = S.R + 3 * L.base;
+    p_prolong(tm, L, S.lev[l + 1], S.E + 3 * S.lev[l + 1].base, e);
+    if (!team_sync(tm)) return false;
+    for (int s = 0; s < 2; ++s)
+      for (unsigned col = 0; col < 2; ++col) {
+        p_rbgs(tm, L, e, r, col);
+        if (!team_sync(tm)) return false;
+      }
+  }
+  return true;
+}
+
+// V-cycle, x += e, R = b - L x (enqueue_cycle).
+__device__ bool p_cycle(Team& tm, const PSim& S, float* xv, const float* b, float* s_res) {
+  if (!p_vcycle(tm, S, s_res)) return false;
+  p_add(tm, xv, S.E, 3 * S.n0);
+  if (!team_sync(tm)) return false;
+  p_residual32(tm, S.lev[0], xv, b, S.R, nullptr, nullptr);
+  return team_sync(tm);
+}
+
+__device__ double relres_of(const double* acc) {
+  const double rr = __ldcg(acc), bb = __ldcg(acc + 1);
+  return bb > 0.0 ? sqrt(rr / bb) : sqrt(rr);
+}
+
+// run_multigrid_fixed's schedule for one simulation.
+__device__ bool p_solve(Team& tm, const PSim& S, float* s_res) {
+  const unsigned n3 = 3 * S.n0;
+  const bool lead = tm.tid() == 0;
+  p_zero(tm, S.E, 3 * S.total);  // e is zero on every level's boundary
+  p_zero(tm, S.lo, n3);
+  if (S.k2 > 0) p_zero(tm, S.etot, n3);
+  if (lead) {
+    S.acc[0] = 0.0;
+    S.acc[1] = 0.0;
+  }
+  if (!team_sync(tm)) return false;
+  p_residual32(tm, S.lev[0], S.x, S.rhs, S.R, S.acc, S.acc + 1);
+  if (!team_sync(tm)) return false;
+  if (lead) {
+    S.relres[1] = relres_of(S.acc);
+    S.acc[0] = 0.0;
+  }
+  for (int k = 0; k < S.k1; ++k)
+    if (!p_cycle(tm, S, S.x, S.rhs, s_res)) return false;
+  p_residual_pair(tm, S, S.rir, S.k2 > 0 ? nullptr : S.acc);
+  if (!team_sync(tm)) return false;
+  if (S.k2 > 0) {
+    p_copy(tm, S.R, S.rir, n3);
+    if (!team_sync(tm)) return false;
+    for (int k = 0; k < S.k2; ++k)
+      if (!p_cycle(tm, S, S.etot, S.rir, s_res)) return false;
+    p_add(tm, S.lo, S.etot, n3);
+    if (!team_sync(tm)) return false;
+    p_residual_pair(tm, S, S.rir, S.acc);
+    if (!team_sync(tm)) return false;
+  }
+  if (lead) S.relres[0] = relres_of(S.acc);
+  p_add(tm, S.x, S.lo, n3);
+  return true;
+}
+
+__global__ void __launch_bounds__(kPThreads, 2) k_mg_persistent(const PSim* __restrict__ sims,
+                                                                const int* __restrict__ order,
+                                                                const int* __restrict__ team_first, unsigned T,
+                                                                unsigned* bar, int* err) {
+  __shared__ float s_res[kRFX * kRFY * kRFZ * 3];
+  const unsigned team = blockIdx.x / T;
+  Team tm;
+  tm.ctr = bar + 32 * team;
+  tm.err = err;
+  tm.T = T;
+  tm.rank = blockIdx.x - team * T;
+  tm.target = 0;
+  tm.limit_ns = kBarrierNs;
+  for (int j = team_first[team]; j < team_first[team + 1]; ++j)
+    if (!p_solve(tm, sims[order[j]], s_res)) return;
+}
+
+// The team barrier alone: one team of T CTAs of which the last `missing`
+// never arrive; the others pass two barriers (counted in *passed) or give up
+// after limit_ns and set *err.
+__global__ void k_team_barrier_check(unsigned T, unsigned missing, unsigned long long limit_ns, unsigned* bar,
+                                     int* err, int* passed) {
+  Team tm;
+  tm.ctr = bar;
+  tm.err = err;
+  tm.T = T;
+  tm.rank = blockIdx.x;
+  tm.target = 0;
+  tm.limit_ns = limit_ns;
+  if (blockIdx.x + missing >= T) return;
+  const bool ok = team_sync(tm) && team_sync(tm);
+  if (ok && threadIdx.x == 0) atomicAdd(passed, 1);
+}
+
+}  // namespace
+
+struct MgBatch {
+  int device = 0;
+  unsigned T = 0, teams = 0, nsims = 0;
+  PSim* d_sims = nullptr;
+  int* d_order = nullptr;
+  int* d_first = nullptr;
+  unsigned* d_bar = nullptr;
+  int* d_err = nullptr;
+  double* d_acc = nullptr;
+};
+
+bool mg_batch_eligible(const Geom& g) {
+  const MgPlan P = plan_levels(g);
+  return P.direct && P.direct_global && P.nlev <= kPMaxLev && 3 * P.total < 0xffffffffull;
+}
+
+void mg_batch_destroy(MgBatch* mb) {
+  if (!mb) return;
+  cudaFree(mb->d_sims);
+  cudaFree(mb->d_order);
+  cudaFree(mb->d_first);
+  cudaFree(mb->d_bar);
+  cudaFree(mb->d_err);
+  cudaFree(mb->d_acc);
+  delete mb;
+}
+
+vg_status mg_batch_build(const std::vector<MgBatchItem>& items, int device, int team_ctas, MgBatch** out,
+                         std::string* err) {
+  *out = nullptr;
+  if (items.empty()) {
+    *err = "persistent solve: no simulations";
+    return VG_EMPTY;
+  }
+  std::vector<PSim> hs(items.size());
+  std::vector<double> cost(items.size());
+  for (size_t i = 0; i < items.size(); ++i) {
+    const MgBatchItem& it = items[i];
+    Ctx* c = it.c;
+    const MgPlan P = plan_levels(it.g);
+    if (!(P.direct && P.direct_global && P.nlev <= kPMaxLev) || c->mg_fixed_k1 < 1 || !c->mg_relres_dev) {
+      *err = "persistent solve: a simulation without a calibrated schedule ending in the global sine-transform solve";
+      return VG_INVALID;
+    }
+    MgBufs B;
+    float *etot = nullptr, *rir = nullptr;
+    vg_status st = setup_bufs(c, it.g, P, B, &etot, &rir);
+    if (st != VG_OK) {
+      *err = "persistent solve: " + c->err;
+      return st;
+    }
+    PSim& S = hs[i];
+    memset(&S, 0, sizeof(S));
+    S.nlev = P.nlev;
+    for (int l = 0; l < P.nlev; ++l) {
+      const Lev& L = P.lev[l];
+      for (int a = 0; a < 3; ++a) S.lev[l].np[a] = L.g.np[a];
+      S.lev[l].r2x = L.r2x;
+      S.lev[l].r2y = L.r2y;
+      S.lev[l].r2z = L.r2z;
+      S.lev[l].H = L.H;
+      S.lev[l].base = (unsigned)L.base;
+    }
+    S.k1 = c->mg_fixed_k1;
+    S.k2 = c->mg_fixed_k2;
+    S.cf = pair_coef(it.g, P.lev[0]);
+    S.E = B.E;
+    S.R = B.R;
+    S.x = it.soln;
+    S.lo = B.lo;
+    S.etot = etot;
+    S.rir = rir;
+    S.rhs = it.rhs;
+    S.dst = B.dst;
+    S.relres = c->mg_relres_dev;
+    S.n0 = (unsigned)it.g.points();
+    S.total = (unsigned)P.total;
+    // work ~ level-0 points per cycle plus a fixed cost per barrier (~27 a cycle)
+    cost[i] = (double)(S.k1 + S.k2 + 1) * ((double)P.total + 27.0 * 4096.0);
+  }
+  int sms = 0, occ = 0;
+  cudaError_t e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, k_mg_persistent, kPThreads, 0);
+  if (e != cudaSuccess || occ < 1) {
+    cudaGetLastError();
+    *err = std::string("persistent solve: occupancy query: ") + cudaGetErrorString(e);
+    return VG_CUDA_ERROR;
+  }
+  const unsigned max_ctas = (unsigned)(sms * occ);
+  unsigned T = team_ctas > 0 ? (unsigned)team_ctas : 8u;
+  T = std::min(T, max_ctas);
+  const unsigned teams = std::max(1u, std::min(max_ctas / T, (unsigned)items.size()));
+  // longest first, each to the least-loaded team
+  std::vector<int> idx(items.size());
+  for (size_t i = 0; i < idx.size(); ++i) idx[i] = (int)i;
+  std::stable_sort(idx.begin(), idx.end(), [&](int a, int b) { return cost[a] > cost[b]; });
+  std::vector<double> load(teams, 0.0);
+  std::vector<std::vector<int>> per(teams);
+  for (int i : idx) {
+    const size_t t = std::min_element(load.begin(), load.end()) - load.begin();
+    load[t] += cost[i];
+    per[t].push_back(i);
+  }
+  std::vector<int> order, first(1, 0);
+  for (unsigned t = 0; t < teams; ++t) {
+    order.insert(order.end(), per[t].begin(), per[t].end());
+    first.push_back((int)order.size());
+  }
+  MgBatch* mb = new MgBatch();
+  mb->device = device;
+  mb->T = T;
+  mb->teams = teams;
+  mb->nsims = (unsigned)items.size();
+  e = cudaMalloc(&mb->d_sims, hs.size() * sizeof(PSim));
+  if (e == cudaSuccess) e = cudaMalloc(&mb->d_order, order.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&mb->d_first, first.size() * sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&mb->d_bar, (size_t)teams * 32 * sizeof(unsigned));
+  if (e == cudaSuccess) e = cudaMalloc(&mb->d_err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMalloc(&mb->d_acc, hs.size() * 2 * sizeof(double));
+  if (e == cudaSuccess) {
+    for (size_t i = 0; i < hs.size(); ++i) hs[i].acc = mb->d_acc + 2 * i;
+    e = cudaMemcpy(mb->d_sims, hs.data(), hs.size() * sizeof(PSim), cudaMemcpyHostToDevice);
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(mb->d_order, order.data(), order.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemcpy(mb->d_first, first.data(), first.size() * sizeof(int), cudaMemcpyHostToDevice);
+  if (e == cudaSuccess) e = cudaMemset(mb->d_err, 0, sizeof(int));
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    mg_batch_destroy(mb);
+    *err = std::string("persistent solve: ") + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? VG_OOM : VG_CUDA_ERROR;
+  }
+  *out = mb;
+  return VG_OK;
+}
+
+vg_status mg_batch_enqueue(MgBatch* mb, cudaStream_t s, std::string* err) {
+  cudaError_t e = cudaMemsetAsync(mb->d_bar, 0, (size_t)mb->teams * 32 * sizeof(unsigned), s);
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(mb->teams * mb->T);
+    cfg.blockDim = dim3(kPThreads);
+    cfg.dynamicSmemBytes = 0;
+    cfg.stream = s;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;  // every CTA resident at once: the team barriers need it
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_mg_persistent, (const PSim*)mb->d_sims, (const int*)mb->d_order,
+                           (const int*)mb->d_first, mb->T, mb->d_bar, mb->d_err);
+  }
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    *err = std::string("persistent solve launch: ") + cudaGetErrorString(e);
+    return VG_CUDA_ERROR;
+  }
+  return VG_OK;
+}
+
+bool mg_batch_failed(MgBatch* mb) {
+  int h = 0;
+  if (cudaMemcpy(&h, mb->d_err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess) {
+    cudaGetLastError();
+    return true;
+  }
+  if (h) cudaMemset(mb->d_err, 0, sizeof(int));
+  return h != 0;
+}
+
+void mg_batch_info(const MgBatch* mb, int* teams, int* team_ctas, int* ctas) {
+  if (teams) *teams = mb ? (int)mb->teams : 0;
+  if (team_ctas) *team_ctas = mb ? (int)mb->T : 0;
+  if (ctas) *ctas = mb ? (int)(mb->teams * mb->T) : 0;
+}
+
 }  // namespace vg
+
+extern "C" vg_status vg_team_barrier_check(int device, int ctas, int missing, float limit_ms, int* completed,
+                                           int* gave_up) {
+  using namespace vg;
+  if (ctas < 1 || missing < 0 || missing > ctas || !(limit_ms > 0.f) || limit_ms > 10000.f || !completed || !gave_up)
+    return VG_INVALID;
+  int sms = 0;
+  cudaError_t e = cudaSetDevice(device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, device);
+  if (e == cudaSuccess && ctas > sms) return set_noctx_error(VG_INVALID, "vg_team_barrier_check: more CTAs than SMs");
+  int* d = nullptr;  // [0] err, [1] passed, [2..] barrier counter
+  if (e == cudaSuccess) e = cudaMalloc(&d, 4 * sizeof(int));
+  if (e == cudaSuccess) e = cudaMemset(d, 0, 4 * sizeof(int));
+  if (e == cudaSuccess) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3((unsigned)ctas);
+    cfg.blockDim = dim3(kPThreads);
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeCooperative;
+    at[0].val.cooperative = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    e = cudaLaunchKernelEx(&cfg, k_team_barrier_check, (unsigned)ctas, (unsigned)missing,
+                           (unsigned long long)((double)limit_ms * 1e6), (unsigned*)(d + 2), d, d + 1);
+  }
+  int h[2] = {0, 0};
+  if (e == cudaSuccess) e = cudaMemcpy(h, d, sizeof(h), cudaMemcpyDeviceToHost);
+  if (d) cudaFree(d);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return set_noctx_error(VG_CUDA_ERROR, std::string("vg_team_barrier_check: ") + cudaGetErrorString(e));
+  }
+  *gave_up = h[0] != 0;
+  *completed = h[1];
+  return VG_OK;
+}
