@@ -176,6 +176,19 @@ vg_status vg_advect_device(vg_ctx* ctx, float* pos, float* vel, size_t m, float 
 /* Replaces PclOpEvolve (Particles/Operation/pclOpEvolve.cpp:36-58) on device
  * records: pos4[i].xyz += vel4[i].xyz * dt (w untouched). */
 vg_status vg_evolve_device(vg_ctx* ctx, float* pos4, const float* vel4, size_t m, float dt);
+/* Particle operations on device-resident particles (float4 arrays), for engines that keep vortons
+ * and tracers on the GPU across frames.
+ * Replaces PclOpWind::Operate (Particles/Operation/pclOpWind.cpp:18-42): vel4[i].xyz =
+ * wind_weight * wind + src_weight * vel4[i].xyz, per component in FP32 (nothing when wind_weight
+ * == 0 and src_weight == 1, as there). */
+vg_status vg_wind_device(vg_ctx* ctx, float* vel4, size_t m, const float wind[3], float wind_weight, float src_weight);
+/* Replaces PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47): a particle with
+ * int(frame - birth[i]) > age_max is removed by moving the last particle into its slot
+ * (Particles::Kill, Particles/particle.h:490-495), so the survivors end in the reference's order.
+ * Up to three float4 arrays (any may be NULL) and birth are permuted together in place; *m_out =
+ * survivors.  Synchronises the context's stream. */
+vg_status vg_kill_age_device(vg_ctx* ctx, float* a4, float* b4, float* c4, int* birth, size_t m, unsigned frame,
+                             int age_max, size_t* m_out);
 
 /* ---- Stage entry points on device memory (run on the context's stream).
  * Each replaces one reference function and is what the step composes; they

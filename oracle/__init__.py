@@ -241,6 +241,23 @@ def evolve(pos, vel, dt):
     return p
 
 
+def kill_age(birth, frame, age_max):
+    """Survivors' original indices in the order PclOpKillAge leaves them."""
+    b = np.ascontiguousarray(birth, np.int32)
+    order = np.zeros(len(b), np.uint32)
+    m = ctypes.c_size_t()
+    lib().vgo_kill_age(_p(b), ctypes.c_size_t(len(b)), ctypes.c_uint(frame), ctypes.c_int(age_max), _p(order),
+                       ctypes.byref(m))
+    return order[: m.value].copy()
+
+
+def wind(vel, wind_vec, wind_weight, src_weight):
+    v = f32(vel).copy()
+    lib().vgo_wind(_p(v), ctypes.c_size_t(len(v)), _p(f32(wind_vec)), ctypes.c_float(wind_weight),
+                   ctypes.c_float(src_weight))
+    return v
+
+
 def relres(g, a, b):
     if a.dtype == np.float64:
         return lib().vgo_relres_f64d(ctypes.byref(g), _p(np.ascontiguousarray(a)), _p(f32(b)))

@@ -19,6 +19,8 @@
 #include "VortonFluid/vortonSim.h"
 #include "VortonFluid/pclOpVortonSim.h"
 #include "Particles/Operation/pclOpFindBoundingBox.h"
+#include "Particles/Operation/pclOpKillAge.h"
+#include "Particles/Operation/pclOpWind.h"
 #include "Core/SpatialPartition/uniformGridMath.h"
 #undef private
 #undef protected
@@ -465,6 +467,48 @@ void vgref_last_grids(float* vel_out, float* vecpot_out, float* negvort_out) {
   if (vel_out) grid_to_floats(g_op->mVortonSim.mVelGrid, vel_out);
   if (vecpot_out) grid_to_floats(g_op->mVortonSim.mVectorPotentialMultiGrid[0], vecpot_out);
   if (negvort_out) grid_to_floats(g_op->mVortonSim.mNegativeVorticityMultiGrid[0], negvort_out);
+}
+
+// PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47) on n
+// particles with the given birth times; order_out[0..*m) receives the
+// surviving particles' original indices in the order the operation leaves
+// them (each particle carries its index in mDensity, exact below 2^24).
+void vgref_kill_age(const int* birth, size_t n, unsigned frame, int age_max, unsigned* order_out, size_t* m) {
+  VECTOR<Particle> pcl;
+  pcl.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle p;
+    p.mDensity = (float)i;
+    p.mBirthTime = birth[i];
+    pcl.PushBack(p);
+  }
+  PclOpKillAge op;
+  op.mAgeMax = age_max;
+  op.Operate(pcl, 0.0f, frame);
+  *m = pcl.Size();
+  for (size_t i = 0; i < pcl.Size(); ++i) order_out[i] = (unsigned)pcl[i].mDensity;
+}
+
+// PclOpWind::Operate (Particles/Operation/pclOpWind.cpp:18-42) on n particles'
+// velocities (xyz, in place).
+void vgref_wind(float* vel_inout, size_t n, const float wind[3], float wind_weight, float src_weight) {
+  VECTOR<Particle> pcl;
+  pcl.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle p;
+    p.mVelocity = Vec3(vel_inout[3 * i], vel_inout[3 * i + 1], vel_inout[3 * i + 2]);
+    pcl.PushBack(p);
+  }
+  PclOpWind op;
+  op.mWind = Vec3(wind[0], wind[1], wind[2]);
+  op.mWindWeight = wind_weight;
+  op.mSrcWeight = src_weight;
+  op.Operate(pcl, 0.0f, 0);
+  for (size_t i = 0; i < n; ++i) {
+    vel_inout[3 * i] = pcl[i].mVelocity.x;
+    vel_inout[3 * i + 1] = pcl[i].mVelocity.y;
+    vel_inout[3 * i + 2] = pcl[i].mVelocity.z;
+  }
 }
 
 }  // extern "C"

@@ -956,3 +956,29 @@ void vgo_step_fields(const float* pos, float* vel, float* w, const float* size, 
     vgo_pse_symmetric(pos, w, size, n, g, viscosity, dt);
   vgo_gather(g, velgrid, pos, n, vel);
 }
+
+/* PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47) with
+ * Particles::Kill (Particles/particle.h:490-495): walk the slots; a slot whose
+ * particle is too old takes the last particle and is tested again. */
+void vgo_kill_age(const int* birth, size_t n, unsigned frame, int age_max, unsigned* order, size_t* m) {
+  size_t size = n;
+  for (size_t i = 0; i < n; ++i) order[i] = (unsigned)i;
+  for (size_t i = 0; i < size;) {
+    const int age = (int)(frame - (unsigned)birth[order[i]]);
+    if (age > age_max) {
+      order[i] = order[size - 1];
+      --size;
+    } else {
+      ++i;
+    }
+  }
+  *m = size;
+}
+
+/* PclOpWind::Operate (Particles/Operation/pclOpWind.cpp:18-42). */
+void vgo_wind(float* vel, size_t n, const float wind[3], float wind_weight, float src_weight) {
+  if (wind_weight == 0.0f && src_weight == 1.0f) return;
+  const float term[3] = {wind_weight * wind[0], wind_weight * wind[1], wind_weight * wind[2]};
+  for (size_t i = 0; i < n; ++i)
+    for (int c = 0; c < 3; ++c) vel[3 * i + c] = term[c] + src_weight * vel[3 * i + c];
+}

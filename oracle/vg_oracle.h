@@ -85,6 +85,15 @@ void vgo_pse_symmetric(const float* pos, float* angvel, const float* size, size_
 void vgo_gather(const vgo_geom* g, const float* velgrid, const float* pos, size_t n, float* vel);
 void vgo_evolve(float* pos, const float* vel, size_t n, float dt);
 
+/* PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47): a particle
+ * is removed when int(frame - birth) > age_max, by moving the last particle into
+ * its slot (Particles::Kill, Particles/particle.h:490-495) and re-testing the
+ * slot.  order[0..*m) receives the survivors' original indices in final order. */
+void vgo_kill_age(const int* birth, size_t n, unsigned frame, int age_max, unsigned* order, size_t* m);
+/* PclOpWind::Operate (Particles/Operation/pclOpWind.cpp:18-42): vel = (ww wind)
+ * + sw vel per component; nothing when ww == 0 and sw == 1. */
+void vgo_wind(float* vel, size_t n, const float wind[3], float wind_weight, float src_weight);
+
 /* FP64 relative residual ||b - L a|| / ||b|| over interior points, Dirichlet. */
 double vgo_relres_f64(const vgo_geom* g, const float* a, const float* b);
 double vgo_relres_f64d(const vgo_geom* g, const double* a, const float* b);

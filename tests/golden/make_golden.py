@@ -7,7 +7,8 @@ inputs and outputs in reference.npz.  The inputs are stored too, so the tests
 never depend on the random generator of the machine they run on.
 
 Usage (needs the reference tree or a staged copy; run in this container):
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py              # reference.npz
+    python tests/golden/make_golden.py lifecycle    # lifecycle.npz (PclOpKillAge, PclOpWind)
 """
 import ctypes
 import os
@@ -21,6 +22,7 @@ import oracle  # noqa: E402
 from vortegrid_gb300 import workloads  # noqa: E402
 
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference.npz")
+OUT_LIFE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lifecycle.npz")
 
 
 def P(a):
@@ -189,5 +191,55 @@ def main():
     print(f"wrote {OUT} ({os.path.getsize(OUT) / 1e6:.2f} MB, {len(g)} arrays)")
 
 
+def lifecycle():
+    """PclOpKillAge and PclOpWind from the reference on seeded inputs: birth
+    times around the frame (none, all, the first, the last, alternate and
+    random particles too old; birth -1; a frame past 2^31 where the age wraps
+    negative), and velocities with signed zeros under several weight pairs
+    (including the reference's do-nothing pair 0 / 1)."""
+    oracle.build()
+    R = oracle.ref("serial")
+    rng = np.random.default_rng(20240611)
+    g = {}
+    cases = []
+    n = 1000
+    cases.append((np.full(n, 90, np.int32), 100, 20))                  # none too old
+    cases.append((np.full(n, 10, np.int32), 100, 20))                  # all
+    b = np.full(n, 90, np.int32); b[0] = 0; cases.append((b, 100, 20))  # the first
+    b = np.full(n, 90, np.int32); b[-1] = 0; cases.append((b, 100, 20))  # the last
+    b = np.where(np.arange(n) % 2 == 0, 0, 90).astype(np.int32); cases.append((b, 100, 20))  # alternate
+    for m in (1, 2, 7, 4099):
+        cases.append((rng.integers(50, 101, m).astype(np.int32), 100, int(rng.integers(0, 51))))
+    cases.append((np.array([-1, 5, -1, 7, 99], np.int32), 30, 25))    # birth -1 (age frame + 1)
+    cases.append((np.array([3, 0x7ffffff0, 5, 1], np.int32), 0x80000005, 10))  # ages wrap negative
+    for i, (birth, frame, age_max) in enumerate(cases):
+        order = np.zeros(len(birth), np.uint32)
+        m = ctypes.c_size_t()
+        R.vgref_kill_age(P(birth), ctypes.c_size_t(len(birth)), ctypes.c_uint(frame), ctypes.c_int(age_max), P(order),
+                         ctypes.byref(m))
+        g[f"kill{i}_birth"] = birth
+        g[f"kill{i}_frame_agemax"] = np.array([frame, age_max], np.int64)
+        g[f"kill{i}_order"] = order[: m.value].copy()
+    g["kill_cases"] = np.array(len(cases))
+    vel = rng.normal(0, 3, (777, 3)).astype(np.float32)
+    vel[:5] = -0.0
+    vel[5:9] = 0.0
+    weights = [(0.125, 0.875), (0.0, 1.0), (1.0, 0.0), (0.3, 0.9), (0.0, 0.5)]
+    wind = np.array([1.0, -2.5, 0.375], np.float32)
+    for i, (ww, sw) in enumerate(weights):
+        v = vel.copy()
+        R.vgref_wind(P(v), ctypes.c_size_t(len(v)), P(wind), ctypes.c_float(ww), ctypes.c_float(sw))
+        g[f"wind{i}_weights"] = np.array([ww, sw], np.float32)
+        g[f"wind{i}_out"] = v
+    g["wind_in"] = vel
+    g["wind_vec"] = wind
+    g["wind_cases"] = np.array(len(weights))
+    np.savez_compressed(OUT_LIFE, **g)
+    print(f"wrote {OUT_LIFE} ({os.path.getsize(OUT_LIFE) / 1e3:.1f} kB, {len(g)} arrays)")
+
+
 if __name__ == "__main__":
-    main()
+    if len(sys.argv) > 1 and sys.argv[1] == "lifecycle":
+        lifecycle()
+    else:
+        main()

@@ -165,3 +165,26 @@ def test_full_step_bit_exact(oracle_lib, golden):
     out = golden["step_out"]
     assert np.array_equal(bits(v), bits(out[:, 3:6]))
     assert np.array_equal(bits(w1), bits(out[:, 9:12]))
+
+
+@pytest.fixture(scope="module")
+def lifecycle():
+    """PclOpKillAge / PclOpWind outputs of the reference's own code (make_golden.py lifecycle)."""
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lifecycle.npz")))
+
+
+def test_kill_age_order_bit_exact(oracle_lib, lifecycle):
+    """Survivors and their order after PclOpKillAge: none, all, the first, the
+    last, alternate and random particles too old, birth -1, wrapped ages."""
+    for i in range(int(lifecycle["kill_cases"])):
+        frame, age_max = (int(v) for v in lifecycle[f"kill{i}_frame_agemax"])
+        got = oracle_lib.kill_age(lifecycle[f"kill{i}_birth"], frame, age_max)
+        assert np.array_equal(got, lifecycle[f"kill{i}_order"]), i
+
+
+def test_wind_bit_exact(oracle_lib, lifecycle):
+    for i in range(int(lifecycle["wind_cases"])):
+        ww, sw = (float(v) for v in lifecycle[f"wind{i}_weights"])
+        got = oracle_lib.wind(lifecycle["wind_in"], lifecycle["wind_vec"], ww, sw)
+        assert np.array_equal(bits(got), bits(lifecycle[f"wind{i}_out"])), i

@@ -187,6 +187,7 @@ enum Slot {
   S_PREV,
   S_MGINV,
   S_TREEPREP,
+  S_PCL,
   S_NUM
 };
 
@@ -276,6 +277,8 @@ struct CellLists {
   unsigned* items;  // vorton indices grouped by cell, ascending within a cell
 };
 vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, CellLists* out);
+// Exclusive scan of n values on the context's stream; out[n] receives the total when write_total.
+vg_status exclusive_scan(Ctx* c, const unsigned* in, size_t n, unsigned* out, bool write_total);
 
 struct Tree {
   int depth;

@@ -167,7 +167,7 @@ __global__ void __launch_bounds__(kSortThreads) k_digit_scatter(const unsigned* 
 }  // namespace
 
 // Exclusive scan of n values; out[n] receives the total when out has n+1 slots.
-static vg_status exclusive_scan(Ctx* c, const unsigned* in, size_t n, unsigned* out, bool write_total) {
+vg_status exclusive_scan(Ctx* c, const unsigned* in, size_t n, unsigned* out, bool write_total) {
   const size_t nb = (n + kScanBlock - 1) / kScanBlock;
   vg_status st = VG_OK;
   unsigned* sums = (unsigned*)ws(c, S_SCAN, (nb + 1) * sizeof(unsigned), &st);
