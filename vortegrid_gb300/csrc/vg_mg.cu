@@ -1020,8 +1020,13 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
 
 // One cycle on L x = rhs: V-cycle on the current residual R, x += e, then
 // R = rhs - L x in FP32 with its FP64-accumulated norm.
+// Cycle tails: the residual with its norm (the adaptive solve reads it), the
+// residual alone (a fixed schedule's next cycle needs R, not its norm), or
+// nothing (a fixed schedule's last cycle of a phase: the next step replaces R).
+enum CycleTail { TAIL_NORM, TAIL_RESIDUAL, TAIL_NONE };
+
 static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgBufs& B, float* x, const float* rhs,
-                               unsigned* nl) {
+                               unsigned* nl, CycleTail tail = TAIL_NORM) {
   vg_status st = enqueue_vcycle(c, P, B, nl);
   if (st != VG_OK) return st;
   const size_t n3 = 3 * g.points();
@@ -1030,9 +1035,14 @@ static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgB
   // measured slower (x is not in L2 by then, and the sweep's gathers wait on it)
   add_f32(c, x, B.E, n3);
   ++*nl;
-  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
-  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
-  *nl += 2;
+  if (tail != TAIL_NONE) {
+    k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
+    ++*nl;
+  }
+  if (tail == TAIL_NORM) {
+    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
+    ++*nl;
+  }
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }
@@ -1215,7 +1225,8 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
   k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev + 1);
   nl += 3;
   for (int k = 0; k < c->mg_fixed_k1; ++k)
-    if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl)) != VG_OK) return st;
+    if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl, k + 1 < c->mg_fixed_k1 ? TAIL_RESIDUAL : TAIL_NONE)) != VG_OK)
+      return st;
   VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
   k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
   k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
@@ -1224,7 +1235,9 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
     VG_CUDA(c, cudaMemsetAsync(etot, 0, 3 * n0 * sizeof(float), c->stream));
     VG_CUDA(c, cudaMemcpyAsync(B.R, rir, 3 * n0 * sizeof(float), cudaMemcpyDeviceToDevice, c->stream));
     for (int k = 0; k < c->mg_fixed_k2; ++k)
-      if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl)) != VG_OK) return st;
+      if ((st = enqueue_cycle(c, P, g, B, etot, rir, &nl, k + 1 < c->mg_fixed_k2 ? TAIL_RESIDUAL : TAIL_NONE)) !=
+          VG_OK)
+        return st;
     add_f32(c, B.lo, etot, 3 * n0);
     k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
     k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
@@ -1836,11 +1849,12 @@ __device__ bool p_vcycle(Team& tm, const PSim& S, float* s_res) {
   return true;
 }
 
-// V-cycle, x += e, R = b - L x (enqueue_cycle).
-__device__ bool p_cycle(Team& tm, const PSim& S, float* xv, const float* b, float* s_res) {
+// V-cycle, x += e, R = b - L x unless it is the phase's last cycle (enqueue_cycle).
+__device__ bool p_cycle(Team& tm, const PSim& S, float* xv, const float* b, float* s_res, bool residual) {
   if (!p_vcycle(tm, S, s_res)) return false;
   p_add(tm, xv, S.E, 3 * S.n0);
   if (!team_sync(tm)) return false;
+  if (!residual) return true;
   p_residual32(tm, S.lev[0], xv, b, S.R, nullptr, nullptr);
   return team_sync(tm);
 }
@@ -1869,14 +1883,14 @@ __device__ bool p_solve(Team& tm, const PSim& S, float* s_res) {
     S.acc[0] = 0.0;
   }
   for (int k = 0; k < S.k1; ++k)
-    if (!p_cycle(tm, S, S.x, S.rhs, s_res)) return false;
+    if (!p_cycle(tm, S, S.x, S.rhs, s_res, k + 1 < S.k1)) return false;
   p_residual_pair(tm, S, S.rir, S.k2 > 0 ? nullptr : S.acc);
   if (!team_sync(tm)) return false;
   if (S.k2 > 0) {
     p_copy(tm, S.R, S.rir, n3);
     if (!team_sync(tm)) return false;
     for (int k = 0; k < S.k2; ++k)
-      if (!p_cycle(tm, S, S.etot, S.rir, s_res)) return false;
+      if (!p_cycle(tm, S, S.etot, S.rir, s_res, k + 1 < S.k2)) return false;
     p_add(tm, S.lo, S.etot, n3);
     if (!team_sync(tm)) return false;
     p_residual_pair(tm, S, S.rir, S.acc);
