@@ -261,6 +261,16 @@ vg_status vg_stretch_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel
 vg_status vg_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, float* angvel, size_t n,
                         float viscosity, float dt);
 
+/* DiffuseAndDissipateHeatPSE (vortonSim.cpp:3880-4093) on per-vorton densities (mDensity),
+ * order-independent form: every pair the reference visits (one cell, or face neighbours along +x,
+ * +y, +z) exchanges clamp(2 diffusivity dt exp(-d^2 / (4 size)^2), +-0.5) of its density difference
+ * from the pre-step values; then each vorton of a "here" cell relaxes toward ambient_density by
+ * clamp(diffusivity dt, +-0.5).  Matches the reference's in-place order to O(2 diffusivity dt x
+ * neighbours) of the change; run it after vg_step_device (before the vortons move), where the
+ * reference's step runs it. */
+vg_status vg_heat_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, float* density, size_t n,
+                             float diffusivity, float ambient_density, float dt);
+
 /* AssignParticleVelocityFromField (gain 1) + EvolveParticlesSlice on float4
  * positions with grid vel3; vel4 (optional) receives the gathered velocity. */
 vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel3, float* pos4, float* vel4,

@@ -241,6 +241,14 @@ def evolve(pos, vel, dt):
     return p
 
 
+def heat_pse(pos, density, size, g, diffusivity, ambient, dt, symmetric=False):
+    d = np.ascontiguousarray(density, np.float32).copy()
+    fn = lib().vgo_heat_pse_symmetric if symmetric else lib().vgo_heat_pse_sequential
+    fn(_p(f32(pos)), _p(d), _p(f32(size)), ctypes.c_size_t(len(d)), ctypes.byref(g), ctypes.c_float(diffusivity),
+       ctypes.c_float(ambient), ctypes.c_float(dt))
+    return d
+
+
 def kill_age(birth, frame, age_max):
     """Survivors' original indices in the order PclOpKillAge leaves them."""
     b = np.ascontiguousarray(birth, np.int32)

@@ -469,6 +469,20 @@ void vgref_last_grids(float* vel_out, float* vecpot_out, float* negvort_out) {
   if (negvort_out) grid_to_floats(g_op->mVortonSim.mNegativeVorticityMultiGrid[0], negvort_out);
 }
 
+// DiffuseAndDissipateHeatPSE (VortonFluid/vortonSim.cpp:3954-4093) after
+// PartitionVortons, on vortons carrying density_inout in mDensity.
+void vgref_heat_pse(const float* pos, float* density_inout, const float* size, size_t n, const float geom12[12],
+                    const unsigned np[3], float diffusivity, float ambient, float dt) {
+  std::vector<float> zero(3 * n, 0.0f);
+  Sim s(pos, zero.data(), size, n, geom12, np, 0.0f);
+  for (size_t i = 0; i < n; ++i) s.vortons[i].mDensity = density_inout[i];
+  s.sim.mThermalDiffusivity = diffusivity;
+  s.sim.mAmbientDensity = ambient;
+  s.sim.PartitionVortons(dt, 0, s.sim.mVortonIndicesGrid);
+  s.sim.DiffuseAndDissipateHeatPSE(dt, 0, s.sim.mVortonIndicesGrid);
+  for (size_t i = 0; i < n; ++i) density_inout[i] = s.vortons[i].mDensity;
+}
+
 // PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47) on n
 // particles with the given birth times; order_out[0..*m) receives the
 // surviving particles' original indices in the order the operation leaves

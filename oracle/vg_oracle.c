@@ -957,6 +957,95 @@ void vgo_step_fields(const float* pos, float* vel, float* w, const float* size, 
   vgo_gather(g, velgrid, pos, n, vel);
 }
 
+/* ExchangeHeat (VortonFluid/vortonSim.cpp:3905-3933). */
+static void exchange_heat(const float* pos, float* d, const float* size, unsigned h, unsigned t, float kappa,
+                          float dt) {
+  const float range = 4.0f * size[h];
+  const float range2 = range * range;
+  const float sx = pos[3 * h] - pos[3 * t], sy = pos[3 * h + 1] - pos[3 * t + 1], sz = pos[3 * h + 2] - pos[3 * t + 2];
+  const float dist2 = sx * sx + sy * sy + sz * sz;
+  const float law = expf(-dist2 / range2);
+  const float ratio = clampf_(2.0f * kappa * dt * law, -0.5f, 0.5f);
+  const float ex = ratio * (d[h] - d[t]);
+  d[h] -= ex;
+  d[t] += ex;
+}
+
+/* DiffuseAndDissipateHeatPSESlice (VortonFluid/vortonSim.cpp:3954-4068), PHASE_BOTH over all cells. */
+void vgo_heat_pse_sequential(const float* pos, float* d, const float* size, size_t n, const vgo_geom* g,
+                             float kappa, float ambient, float dt) {
+  cells_t c;
+  cells_build(&c, pos, n, g);
+  const float gain = clampf_(kappa * dt, -0.5f, 0.5f);
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  const size_t fo[3] = {1, nx, nxy};
+  for (size_t z = 0; z + 1 < nz; ++z)
+    for (size_t y = 0; y + 1 < ny; ++y)
+      for (size_t x = 0; x + 1 < nx; ++x) {
+        const size_t cell = x + y * nx + z * nxy;
+        for (unsigned ih = 0; ih < c.count[cell]; ++ih) {
+          const unsigned h = c.items[c.start[cell] + ih];
+          for (unsigned it = ih + 1; it < c.count[cell]; ++it)
+            exchange_heat(pos, d, size, h, c.items[c.start[cell] + it], kappa, dt);
+          for (int k = 0; k < 3; ++k) {
+            const size_t nb = cell + fo[k];
+            for (unsigned it = 0; it < c.count[nb]; ++it)
+              exchange_heat(pos, d, size, h, c.items[c.start[nb] + it], kappa, dt);
+          }
+          d[h] += gain * (ambient - d[h]);
+        }
+      }
+  cells_free(&c);
+}
+
+/* Order-independent form: every pair the reference visits (same cell, or a
+ * face neighbour along +x, +y or +z of a "here" cell strictly inside the point
+ * range) exchanges with the densities from before the step, then every vorton
+ * of a "here" cell relaxes toward ambient.  Differs from the reference's
+ * in-place order by O((2 kappa dt)^2) of the density differences. */
+void vgo_heat_pse_symmetric(const float* pos, float* d, const float* size, size_t n, const vgo_geom* g, float kappa,
+                            float ambient, float dt) {
+  cells_t c;
+  cells_build(&c, pos, n, g);
+  float* d0 = (float*)malloc((n ? n : 1) * sizeof(float));
+  memcpy(d0, d, n * sizeof(float));
+  const float gain = clampf_(kappa * dt, -0.5f, 0.5f);
+  const int nx = (int)g->np[0], ny = (int)g->np[1], nz = (int)g->np[2];
+  for (size_t i = 0; i < n; ++i) {
+    unsigned id[3];
+    vgo_indices_of_position(g, pos + 3 * i, id);
+    const int ci[3] = {(int)id[0], (int)id[1], (int)id[2]};
+    const int here_ok = ci[0] < nx - 1 && ci[1] < ny - 1 && ci[2] < nz - 1;
+    double acc = 0.0;
+    for (int s = -1; s <= 1; s += 2)
+      for (int k = 0; k < 4; ++k) {
+        if (k == 0 && s == 1) continue; /* same cell handled with s == -1 */
+        const int dd[3] = {k == 1 ? s : 0, k == 2 ? s : 0, k == 3 ? s : 0};
+        const int nc[3] = {ci[0] + dd[0], ci[1] + dd[1], ci[2] + dd[2]};
+        if (nc[0] < 0 || nc[1] < 0 || nc[2] < 0 || nc[0] >= nx || nc[1] >= ny || nc[2] >= nz) continue;
+        const int* lower = (s == 1) ? ci : nc;
+        if (!(lower[0] < nx - 1 && lower[1] < ny - 1 && lower[2] < nz - 1)) continue;
+        const size_t cell = (size_t)nc[0] + (size_t)nx * ((size_t)nc[1] + (size_t)ny * nc[2]);
+        for (unsigned it = 0; it < c.count[cell]; ++it) {
+          const unsigned j = c.items[c.start[cell] + it];
+          if (j == i) continue;
+          const unsigned here = (k == 0) ? (i < j ? (unsigned)i : j) : (s == 1 ? (unsigned)i : j);
+          const float range = 4.0f * size[here];
+          const float sx = pos[3 * i] - pos[3 * j], sy = pos[3 * i + 1] - pos[3 * j + 1],
+                      sz = pos[3 * i + 2] - pos[3 * j + 2];
+          const float law = expf(-(sx * sx + sy * sy + sz * sz) / (range * range));
+          const float ratio = clampf_(2.0f * kappa * dt * law, -0.5f, 0.5f);
+          acc += (double)ratio * ((double)d0[j] - (double)d0[i]);
+        }
+      }
+    float v = (float)((double)d0[i] + acc);
+    if (here_ok) v += gain * (ambient - v);
+    d[i] = v;
+  }
+  free(d0);
+  cells_free(&c);
+}
+
 /* PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47) with
  * Particles::Kill (Particles/particle.h:490-495): walk the slots; a slot whose
  * particle is too old takes the last particle and is tested again. */

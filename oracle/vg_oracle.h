@@ -85,6 +85,16 @@ void vgo_pse_symmetric(const float* pos, float* angvel, const float* size, size_
 void vgo_gather(const vgo_geom* g, const float* velgrid, const float* pos, size_t n, float* vel);
 void vgo_evolve(float* pos, const float* vel, size_t n, float dt);
 
+/* DiffuseAndDissipateHeatPSE (VortonFluid/vortonSim.cpp:3880-4093): density
+ * exchange between vortons of one cell and of the +x, +y, +z face-neighbour
+ * cells, ratio clamp(2 kappa dt exp(-d^2 / (4 size_here)^2), +-0.5), then each
+ * vorton of a "here" cell relaxes toward the ambient density by clamp(kappa dt,
+ * +-0.5).  Sequential: the reference's in-place order.  Symmetric: every pair
+ * exchanges with the values from before the step (the GPU form). */
+void vgo_heat_pse_sequential(const float* pos, float* density, const float* size, size_t n, const vgo_geom* g,
+                             float diffusivity, float ambient, float dt);
+void vgo_heat_pse_symmetric(const float* pos, float* density, const float* size, size_t n, const vgo_geom* g,
+                            float diffusivity, float ambient, float dt);
 /* PclOpKillAge::Operate (Particles/Operation/pclOpKillAge.cpp:22-47): a particle
  * is removed when int(frame - birth) > age_max, by moving the last particle into
  * its slot (Particles::Kill, Particles/particle.h:490-495) and re-testing the

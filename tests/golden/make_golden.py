@@ -9,6 +9,7 @@ never depend on the random generator of the machine they run on.
 Usage (needs the reference tree or a staged copy; run in this container):
     python tests/golden/make_golden.py              # reference.npz
     python tests/golden/make_golden.py lifecycle    # lifecycle.npz (PclOpKillAge, PclOpWind)
+    python tests/golden/make_golden.py heat         # heat.npz (DiffuseAndDissipateHeatPSE)
 """
 import ctypes
 import os
@@ -23,6 +24,7 @@ from vortegrid_gb300 import workloads  # noqa: E402
 
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference.npz")
 OUT_LIFE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lifecycle.npz")
+OUT_HEAT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "heat.npz")
 
 
 def P(a):
@@ -238,8 +240,34 @@ def lifecycle():
     print(f"wrote {OUT_LIFE} ({os.path.getsize(OUT_LIFE) / 1e3:.1f} kB, {len(g)} arrays)")
 
 
+def heat():
+    """DiffuseAndDissipateHeatPSE from the reference on the vortons of
+    reference.npz carrying seeded densities (ambient 1 + N(0, 0.2^2)), at a
+    small and a large diffusivity (the second saturates both clamps)."""
+    oracle.build()
+    R = oracle.ref("serial")
+    src = np.load(OUT)
+    pos, s, g12, np3 = src["pos"], src["size"], src["geom"], src["np"]
+    n = len(pos)
+    rng = np.random.default_rng(77)
+    d0 = (1.0 + rng.normal(0, 0.2, n)).astype(np.float32)
+    g = {"heat_density": d0}
+    cases = [(0.01, 1.0, 1.0 / 30.0), (1.8, 1.2, 1.0 / 3.0)]
+    for i, (kappa, ambient, dt) in enumerate(cases):
+        d = d0.copy()
+        R.vgref_heat_pse(P(pos), P(d), P(s), ctypes.c_size_t(n), P(g12), P(np3), ctypes.c_float(kappa),
+                         ctypes.c_float(ambient), ctypes.c_float(dt))
+        g[f"heat{i}_params"] = np.array([kappa, ambient, dt], np.float32)
+        g[f"heat{i}_out"] = d
+    g["heat_cases"] = np.array(len(cases))
+    np.savez_compressed(OUT_HEAT, **g)
+    print(f"wrote {OUT_HEAT} ({os.path.getsize(OUT_HEAT) / 1e3:.1f} kB, {len(g)} arrays)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lifecycle":
         lifecycle()
+    elif len(sys.argv) > 1 and sys.argv[1] == "heat":
+        heat()
     else:
         main()

@@ -188,3 +188,16 @@ def test_wind_bit_exact(oracle_lib, lifecycle):
         ww, sw = (float(v) for v in lifecycle[f"wind{i}_weights"])
         got = oracle_lib.wind(lifecycle["wind_in"], lifecycle["wind_vec"], ww, sw)
         assert np.array_equal(bits(got), bits(lifecycle[f"wind{i}_out"])), i
+
+
+def test_heat_pse_sequential_bit_exact(oracle_lib, golden):
+    """The oracle's heat PSE in the reference's in-place order reproduces the
+    reference's DiffuseAndDissipateHeatPSE bit for bit (tests/golden/heat.npz),
+    including a diffusivity that saturates both clamps."""
+    import os
+    h = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "heat.npz")))
+    g = geom_of(oracle_lib, golden)
+    for i in range(int(h["heat_cases"])):
+        kappa, ambient, dt = (np.float32(v) for v in h[f"heat{i}_params"])
+        got = oracle_lib.heat_pse(golden["pos"], h["heat_density"], golden["size"], g, kappa, ambient, dt)
+        assert np.array_equal(bits(got), bits(h[f"heat{i}_out"])), i

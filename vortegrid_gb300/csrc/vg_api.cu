@@ -942,6 +942,18 @@ vg_status vg_pse_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size
   return launch_pse(c, g, cl, (const float4*)pos_size, (float4*)angvel, n, viscosity, dt);
 }
 
+vg_status vg_heat_pse_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, float* density, size_t n,
+                             float diffusivity, float ambient_density, float dt) {
+  if (!c || !gg || (n && (!pos_size || !density))) return VG_INVALID;
+  if (n == 0) return VG_OK;
+  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+  const Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos_size, n, &cl);
+  if (st != VG_OK) return st;
+  return launch_heat_pse(c, g, cl, (const float4*)pos_size, density, n, diffusivity, ambient_density, dt);
+}
+
 vg_status vg_gather_advect_device(vg_ctx* c, const vg_grid_geom* gg, const float* vel3, float* pos4, float* vel4,
                                   size_t m, float dt) {
   if (!c || !gg || !vel3 || (!pos4 && m)) return VG_INVALID;

@@ -309,6 +309,71 @@ __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ 
   w[i] = make_float4(vx, vy, vz, wi.w);
 }
 
+// DiffuseAndDissipateHeatPSE (vortonSim.cpp:3880-4093) in the order-independent
+// form of k_pse: vorton i (threads in cell order, reading cell-sorted copies)
+// exchanges density with every vorton of its own cell and of the face
+// neighbours along +-x, +-y, +-z that the reference pairs it with (the pair's
+// "here" cell strictly inside the point range; the range 4 x the "here"
+// vorton's size), using the densities from before the step, then relaxes
+// toward the ambient density when its own cell is a "here" cell.
+__global__ void k_heat_gather(const float4* __restrict__ ps, const float* __restrict__ d, int n,
+                              const unsigned* __restrict__ items, float4* __restrict__ pss, float* __restrict__ d0s) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const unsigned j = items[t];
+  pss[t] = ps[j];
+  d0s[t] = d[j];
+}
+
+__global__ void __launch_bounds__(128) k_heat_pse(Geom g, const float4* __restrict__ pss, const float* __restrict__ d0s,
+                                                  float* __restrict__ d, int n, const unsigned* __restrict__ start,
+                                                  const unsigned* __restrict__ items, float kappa, float ambient,
+                                                  float dt) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = (int)items[t];
+  const float4 p = pss[t];
+  const float di = d0s[t];
+  const int nx = (int)g.np[0], ny = (int)g.np[1], nz = (int)g.np[2];
+  const int cx = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.x, g.mn[0]), g.cpe[0])), -2), nx + 1);
+  const int cy = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.y, g.mn[1]), g.cpe[1])), -2), ny + 1);
+  const int cz = min(max(__float2int_rz(__fmul_rn(__fsub_rn(p.z, g.mn[2]), g.cpe[2])), -2), nz + 1);
+  if (cx < 0 || cy < 0 || cz < 0 || cx >= nx || cy >= ny || cz >= nz) {
+    d[i] = di;  // in no cell list: no exchange
+    return;
+  }
+  const bool here_ok = cx < nx - 1 && cy < ny - 1 && cz < nz - 1;
+  const float twokdt = 2.0f * kappa * dt;
+  float acc = 0.f;
+  for (int s = -1; s <= 1; s += 2) {
+    for (int k = 0; k < 4; ++k) {
+      if (k == 0 && s == 1) continue;
+      const int ox = k == 1 ? s : 0, oy = k == 2 ? s : 0, oz = k == 3 ? s : 0;
+      const int ncx = cx + ox, ncy = cy + oy, ncz = cz + oz;
+      if (ncx < 0 || ncy < 0 || ncz < 0 || ncx >= nx || ncy >= ny || ncz >= nz) continue;
+      const int lx = (s == 1) ? cx : ncx, ly = (s == 1) ? cy : ncy, lz = (s == 1) ? cz : ncz;
+      if (!(lx < nx - 1 && ly < ny - 1 && lz < nz - 1)) continue;
+      const size_t cell = (size_t)ncx + (size_t)nx * ((size_t)ncy + (size_t)ny * ncz);
+      const unsigned b = start[cell], e = start[cell + 1];
+      for (unsigned kk = b; kk < e; ++kk) {
+        const unsigned j = items[kk];
+        if (j == (unsigned)i) continue;
+        const float4 pj = pss[kk];
+        const unsigned here = (k == 0) ? min((unsigned)i, j) : (s == 1 ? (unsigned)i : j);
+        const float range = 4.0f * (here == (unsigned)i ? p.w : pj.w);
+        const float dx = p.x - pj.x, dy = p.y - pj.y, dz = p.z - pj.z;
+        const float dist2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float law = __expf(-dist2 / (range * range));
+        const float ratio = fminf(fmaxf(twokdt * law, -0.5f), 0.5f);
+        acc = fmaf(ratio, d0s[kk] - di, acc);
+      }
+    }
+  }
+  float v = di + acc;
+  if (here_ok) v += fminf(fmaxf(kappa * dt, -0.5f), 0.5f) * (ambient - v);
+  d[i] = v;
+}
+
 __global__ void k_gather_advect(Geom g, const float* __restrict__ vel3, float4* __restrict__ pos,
                                 float4* __restrict__ vel, int m, float dt, int evolve, int* __restrict__ flag) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -481,6 +546,21 @@ vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4*
   if (n == 0) return VG_OK;
   k_stretch<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, jac9, ps, w, (int)n, dt, outside_flag(c));
   VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float* density, size_t n,
+                          float kappa, float ambient, float dt) {
+  vg_status st = VG_OK;
+  char* tmp = (char*)ws(c, S_WOLD, n * (sizeof(float4) + sizeof(float)), &st);
+  if (st != VG_OK) return st;
+  float4* pss = (float4*)tmp;
+  float* d0s = (float*)(pss + n);
+  k_heat_gather<<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, density, (int)n, cl.items, pss, d0s);
+  k_heat_pse<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, pss, d0s, density, (int)n, cl.start, cl.items, kappa,
+                                                        ambient, dt);
+  c->launches += 2;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }

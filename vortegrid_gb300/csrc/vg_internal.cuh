@@ -337,6 +337,8 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);
 vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt);
 vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float4* w, size_t n, float nu,
                      float dt);
+vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float* density, size_t n,
+                          float kappa, float ambient, float dt);
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
                                float dt, bool evolve);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
