@@ -361,9 +361,10 @@ vg_status vg_set_network(vg_ctx* ctx, vg_net* net);
  * simulations stepped per frame.  Each simulation is a context with a fixed
  * grid and the multigrid Poisson step, and its vortons (float4 arrays as in
  * vg_step_device) stay on the device.  A frame is vg_step_device + the
- * vortons' Euler advection for every simulation.  After a calibration step
- * (one adaptive solve each, which fixes each simulation's multigrid schedule
- * and sizes its workspaces), a frame has no host round trip, so it is
+ * vortons' Euler advection for every simulation; each solve starts from the
+ * simulation's previous solution (or the network's guess).  After calibration
+ * (two adaptive steps each, which fix each simulation's multigrid schedule and
+ * size its workspaces), a frame has no host round trip, so it is
  * captured once as CUDA graphs and replayed: the simulations are dealt to
  * `streams` parallel branches, each branch's chain is captured as graphs of at
  * most a few thousand kernels, and a frame forks into the branches, launches
@@ -388,7 +389,8 @@ vg_status vg_batch_add(vg_batch* batch, const vg_config* cfg, float* pos_size, f
 vg_status vg_batch_load_network(vg_batch* batch, const char* path);
 /* Stream count and network use (invalidates the graphs; a network change also the calibration). */
 vg_status vg_batch_configure(vg_batch* batch, int streams, int use_network);
-/* One adaptive step of every simulation (it advances them), fixing their multigrid schedules. */
+/* Two adaptive steps of every simulation (they advance them), fixing their multigrid schedules
+ * for solves started from the previous frame's solution (or the network's guess). */
 vg_status vg_batch_calibrate(vg_batch* batch, float dt);
 /* mode 0: the captured graphs (captured on first use and after any change); mode 1: the same work
  * simulation after simulation on one stream, no graph.  Calibrates first if needed.  Does not

@@ -8,8 +8,10 @@
 // the frame can be captured once as CUDA graphs and replayed:
 //   * fixed grids (no bounding-box readback); a vorton that leaves its grid
 //     stops and drops out of the solve instead of failing the frame;
-//   * a fixed multigrid schedule per simulation, calibrated by one adaptive
-//     solve (its phase-1 cycles, and its refinement cycles + 1);
+//   * a fixed multigrid schedule per simulation, calibrated by adaptive
+//     solves (its phase-1 cycles, and its refinement cycles + 1), each solve
+//     starting from the simulation's previous solution (or the network's
+//     guess);
 //   * workspaces grown to their final sizes by the calibration step.
 // The simulations are dealt round-robin to K branch streams.  Each branch's
 // chain of simulations is captured as graphs of at most about kGraphKernels
@@ -138,7 +140,8 @@ void bind(vg_batch* b, Sim& sim, int s) {
       if (b->net_edges[e] == edge) net = b->nets[e][s];
   }
   vg_set_network(sim.ctx, net);
-  sim.ctx->cfg.warm_start = net ? VG_WARM_NETWORK : VG_WARM_ZERO;
+  // without the network, each solve starts from the simulation's previous solution
+  sim.ctx->cfg.warm_start = net ? VG_WARM_NETWORK : VG_WARM_PREVIOUS;
 }
 
 // part 0: the whole step and the advection; 1: the step up to its Poisson
@@ -307,19 +310,22 @@ vg_status launch_frame(vg_batch* b) {
 }
 
 vg_status calibrate(vg_batch* b, float dt) {
-  // one adaptive step per simulation: grows its workspaces, records its schedule
+  // two adaptive steps per simulation: they grow its workspaces, and the
+  // second, started from the first's solution like every later frame,
+  // records its schedule
   vg_status st;
   drop_graph(b);
   // earlier frames may have run on other streams than the ones used below
   if ((st = bcuda(b, cudaStreamSynchronize(b->main), "synchronize")) != VG_OK) return st;
   for (int s = 0; s < kMaxStreams; ++s)
     if ((st = bcuda(b, cudaStreamSynchronize(b->streams[s]), "synchronize")) != VG_OK) return st;
-  for (size_t i = 0; i < b->sims.size(); ++i) {
-    Sim& sim = b->sims[i];
-    sim.ctx->mg_fixed_k1 = sim.ctx->mg_fixed_k2 = 0;
-    bind(b, sim, (int)(i % b->nstreams));
-    if ((st = step_one(b, sim, dt)) != VG_OK) return st;
-  }
+  for (int pass = 0; pass < 2; ++pass)
+    for (size_t i = 0; i < b->sims.size(); ++i) {
+      Sim& sim = b->sims[i];
+      sim.ctx->mg_fixed_k1 = sim.ctx->mg_fixed_k2 = 0;
+      bind(b, sim, (int)(i % b->nstreams));
+      if ((st = step_one(b, sim, dt)) != VG_OK) return st;
+    }
   for (Sim& sim : b->sims) {
     if ((st = sync_and_check(sim.ctx, "calibration")) != VG_OK) return bfail(b, st, sim.ctx->err);
     sim.ctx->mg_fixed_k1 = std::max(1, sim.ctx->mg_last_k1);
