@@ -9,7 +9,9 @@
 //   * fixed grids (no bounding-box readback); a vorton that leaves its grid
 //     stops and drops out of the solve instead of failing the frame;
 //   * a fixed multigrid schedule per simulation, calibrated by adaptive
-//     solves (its phase-1 cycles, and its refinement cycles + 1), each solve
+//     solves (its phase-1 cycles and refinement cycles, plus a spare
+//     refinement cycle when the calibrating solve ended close to the
+//     tolerance), each solve
 //     starting from the simulation's previous solution (or the network's
 //     guess);
 //   * workspaces grown to their final sizes by the calibration step.
@@ -329,7 +331,10 @@ vg_status calibrate(vg_batch* b, float dt) {
   for (Sim& sim : b->sims) {
     if ((st = sync_and_check(sim.ctx, "calibration")) != VG_OK) return bfail(b, st, sim.ctx->err);
     sim.ctx->mg_fixed_k1 = std::max(1, sim.ctx->mg_last_k1);
-    sim.ctx->mg_fixed_k2 = sim.ctx->mg_last_k2 + 1;
+    // a spare refinement cycle (about a tenfold reduction) unless the
+    // calibrating solve already ended ten times below the tolerance
+    const bool close = sim.ctx->stats.poisson_relres > 0.1 * sim.ctx->cfg.poisson_tolerance;
+    sim.ctx->mg_fixed_k2 = sim.ctx->mg_last_k2 + (close ? 1 : 0);
   }
   b->calibrated = true;
   return VG_OK;
