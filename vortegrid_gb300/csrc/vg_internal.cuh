@@ -264,6 +264,33 @@ vg_status cuda_check(Ctx* c, cudaError_t e, const char* what);
 
 inline unsigned blocks_for(size_t n, unsigned threads) { return (unsigned)((n + threads - 1) / threads); }
 
+// Programmatic dependent launch for chains of short kernels: a kernel started
+// by pdl_launch may be launched as the previous kernel of its stream drains
+// (its CTAs' exits trigger it), overlapping the launch with that kernel's
+// completion.  Its first statement is pdl_entry(), which waits until the
+// previous kernel has completed and its writes are visible
+// (griddepcontrol.wait), so the chain's results are those of ordinary
+// launches.  Without a programmatic predecessor the wait returns at once.
+// (Triggering the next launch at kernel entry measured slower: its waiting
+// CTAs held SM slots during the previous kernel's last wave.)
+__device__ __forceinline__ void pdl_entry() { asm volatile("griddepcontrol.wait;" ::: "memory"); }
+
+template <typename... KArgs, typename... Args>
+inline cudaError_t pdl_launch(cudaStream_t s, dim3 grid, dim3 block, size_t smem, void (*kernel)(KArgs...),
+                              Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.dynamicSmemBytes = smem;
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeProgrammaticStreamSerialization;
+  at[0].val.programmaticStreamSerializationAllowed = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
 // ---------------------------------------------------------- stage launchers
 // (device pointers, context stream; defined in the .cu files)
 

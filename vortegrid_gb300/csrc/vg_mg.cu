@@ -124,6 +124,7 @@ __device__ __forceinline__ float gs_value(float sx, float sy, float sz, float r,
 __global__ void __launch_bounds__(kRedThreads) k_residual32n(Geom g, float r2x, float r2y, float r2z, unsigned zs,
                                                              const float* __restrict__ a, const float* __restrict__ b,
                                                              float* __restrict__ r, double* __restrict__ part) {
+  pdl_entry();
   const unsigned x = blockIdx.x * blockDim.x + threadIdx.x + 1, y = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
   float rr = 0.f, bb = 0.f;
@@ -195,6 +196,7 @@ __global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef 
                                                                const float* __restrict__ lo,
                                                                const float* __restrict__ b, float* __restrict__ r,
                                                                double* __restrict__ part) {
+  pdl_entry();
   const unsigned x = blockIdx.x * blockDim.x + threadIdx.x + 1, y = blockIdx.y * blockDim.y + threadIdx.y + 1;
   const unsigned nx = g.np[0], ny = g.np[1], nz = g.np[2];
   float rr = 0.f;
@@ -225,6 +227,7 @@ __global__ void __launch_bounds__(kRedThreads) k_residual_pair(Geom g, PairCoef 
 // ||b||^2 slot is left as phase 1's first residual wrote it.
 __global__ void __launch_bounds__(1024) k_sum_partials(const double* __restrict__ part, int nb,
                                                        double* __restrict__ out2, int keep_b) {
+  pdl_entry();
   __shared__ double s1[1024], s2[1024];
   double a1 = 0.0, a2 = 0.0;
   for (int i = threadIdx.x; i < nb; i += blockDim.x) {
@@ -276,6 +279,7 @@ __device__ __forceinline__ void rbgs_point(const Geom& g, float r2x, float r2y, 
 __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, float r2z, float H,
                                               float* __restrict__ e, const float* __restrict__ r, unsigned color,
                                               int zero_first) {
+  pdl_entry();
   const unsigned nx = g.np[0], ny = g.np[1];
   const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
@@ -303,6 +307,7 @@ __global__ void __launch_bounds__(256) k_rbgs(Geom g, float r2x, float r2y, floa
 // component), as k_rbgs_add.
 __global__ void __launch_bounds__(256) k_rbgs_first(Geom g, float r2x, float r2y, float r2z, float H,
                                                     float* __restrict__ e, const float* __restrict__ r) {
+  pdl_entry();
   const unsigned nx = g.np[0], ny = g.np[1];
   const unsigned jc = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned y = blockIdx.y * blockDim.y + threadIdx.y + 1, z = blockIdx.z + 1;
@@ -371,6 +376,7 @@ constexpr int kRFX = 2 * kRTX + 1, kRFY = 2 * kRTY + 1, kRFZ = 2 * kRTZ + 1;
 __global__ void __launch_bounds__(256) k_residual_restrict(Geom F, Geom C, float r2x, float r2y, float r2z,
                                                            const float* __restrict__ e, const float* __restrict__ r,
                                                            float* __restrict__ rc) {
+  pdl_entry();
   __shared__ float s_res[kRFX * kRFY * kRFZ * 3];
   const unsigned cx0 = 1 + blockIdx.x * kRTX, cy0 = 1 + blockIdx.y * kRTY, cz0 = 1 + blockIdx.z * kRTZ;
   const unsigned nx = F.np[0], ny = F.np[1], nz = F.np[2];
@@ -446,6 +452,7 @@ __device__ __forceinline__ void prolong_point(const Geom& F, const Geom& C, cons
 // sums in the same order as prolong_point (fine boundary points skipped).
 __global__ void __launch_bounds__(256) k_prolong_cells(Geom F, Geom C, const float* __restrict__ ec,
                                                      float* __restrict__ ef) {
+  pdl_entry();
   const unsigned cx = blockIdx.x * blockDim.x + threadIdx.x;
   const unsigned cy = blockIdx.y * blockDim.y + threadIdx.y, cz = blockIdx.z;
   if (cx + 1 >= C.np[0] || cy + 1 >= C.np[1]) return;
@@ -496,6 +503,7 @@ __global__ void __launch_bounds__(256) k_prolong_cells(Geom F, Geom C, const flo
 template <int kPCX, int kPCY, int kPCZ>
 __global__ void __launch_bounds__(kPCX * kPCY * kPCZ) k_prolong_add(Geom F, Geom C, const float* __restrict__ ec,
                                                                    float* __restrict__ ef) {
+  pdl_entry();
   constexpr int kPFX = 2 * kPCX * 3, kPFR = 2 * kPCY * 2 * kPCZ;  // floats per fine row, fine rows per CTA
   __shared__ float s_inc[kPFR * kPFX];
   const unsigned tx = threadIdx.x, ty = threadIdx.y, tz = threadIdx.z;
@@ -629,6 +637,7 @@ __device__ void block_rb_sweep(float* sm, const SmallLevels& S, int l, unsigned 
 
 __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ SmallLevels S,
                                                        double* __restrict__ work) {
+  pdl_entry();
   extern __shared__ float sm[];
   {  // e = 0 everywhere (boundaries stay 0), r of the first level from global
     const size_t total = S.off[S.n - 1] + 6 * S.g[S.n - 1].points();
@@ -767,6 +776,7 @@ __global__ void __launch_bounds__(1024) k_vcycle_small(const __grid_constant__ S
 }  // namespace
 
 __global__ void k_add_f32(float* __restrict__ a, const float* __restrict__ e, size_t n) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n) a[k] += e[k];
 }
@@ -774,6 +784,7 @@ __global__ void k_add_f32(float* __restrict__ a, const float* __restrict__ e, si
 // a += e as float4 over the first n4 groups of 4 (both arrays 16-byte
 // aligned), the n - 4 n4 remaining floats one by one.
 __global__ void k_add_f32x4(float* __restrict__ a, const float* __restrict__ e, size_t n4, size_t n) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k < n4) {
     float4 va = reinterpret_cast<float4*>(a)[k];
@@ -792,9 +803,9 @@ __global__ void k_add_f32x4(float* __restrict__ a, const float* __restrict__ e, 
 static void add_f32(Ctx* c, float* a, const float* e, size_t n) {
   if ((((uintptr_t)a | (uintptr_t)e) & 15) == 0) {
     const size_t n4 = n / 4;
-    k_add_f32x4<<<blocks_for(n4 + 3, 256), 256, 0, c->stream>>>(a, e, n4, n);
+    pdl_launch(c->stream, blocks_for(n4 + 3, 256), 256, 0, k_add_f32x4, a, e, n4, n);
   } else {
-    k_add_f32<<<blocks_for(n, 256), 256, 0, c->stream>>>(a, e, n);
+    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_add_f32, a, e, n);
   }
 }
 
@@ -804,6 +815,7 @@ static void add_f32(Ctx* c, float* a, const float* e, size_t n) {
 // (the third scaled by 1 / eigenvalue), and the last x pass writing e in
 // full layout (zero on the boundary).  Same operations as the CTA form.
 __global__ void __launch_bounds__(256) k_dst_gather(Geom g, const float* __restrict__ rfull, float* __restrict__ X) {
+  pdl_entry();
   const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * N) return;
@@ -815,6 +827,7 @@ __global__ void __launch_bounds__(256) k_dst_gather(Geom g, const float* __restr
 __global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const float* __restrict__ in, float* __restrict__ out,
                                                   const float* __restrict__ T, unsigned n, unsigned st,
                                                   const float* __restrict__ Dinv) {
+  pdl_entry();
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * N) return;
   const unsigned c = i % 3u, p = i / 3u;
@@ -826,6 +839,7 @@ __global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const float* __res
 
 __global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const float* __restrict__ Y, const float* __restrict__ Sx,
                                                      float* __restrict__ efull) {
+  pdl_entry();
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * (unsigned)g.points()) return;
   const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2;
@@ -925,17 +939,17 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     float* r = B.R + 3 * L.base;
     const RowLaunch sw = launch_rows(3 * ((L.g.np[0] - 1) / 2), L.g.np[1], L.g.np[2]);  // one colour's points
     const RowLaunch all = launch_rows(3 * (L.g.np[0] - 2), L.g.np[1], L.g.np[2]);     // every interior point
-    k_rbgs_first<<<all.grid, all.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r);
+    pdl_launch(c->stream, all.grid, all.block, 0, k_rbgs_first, L.g, L.r2x, L.r2y, L.r2z, L.H, e, r);
     ++*nl;
     for (int s = 1; s < pre; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+        pdl_launch(c->stream, sw.grid, sw.block, 0, k_rbgs, L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
         ++*nl;
       }
     const Lev& Cn = P.lev[l + 1];
     const dim3 rg((Cn.g.np[0] - 2 + kRTX - 1) / kRTX, (Cn.g.np[1] - 2 + kRTY - 1) / kRTY,
                   (Cn.g.np[2] - 2 + kRTZ - 1) / kRTZ);
-    k_residual_restrict<<<rg, 256, 0, c->stream>>>(L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r, B.R + 3 * Cn.base);
+    pdl_launch(c->stream, rg, 256, 0, k_residual_restrict, L.g, Cn.g, L.r2x, L.r2y, L.r2z, e, r, B.R + 3 * Cn.base);
     ++*nl;
   }
   if (P.direct_global) {
@@ -949,13 +963,13 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const float* Sz = Sy + nyi * nyi;
     const float* Dinv = Sz + nzi * nzi;
     const unsigned nb = blocks_for(3 * N, 256);
-    k_dst_gather<<<nb, 256, 0, c->stream>>>(g, R, E);
-    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sx, nxi, 1, nullptr);
-    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, R, E, Sy, nyi, nxi, nullptr);
-    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sz, nzi, nxi * nyi, Dinv);
-    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, R, E, Sz, nzi, nxi * nyi, nullptr);
-    k_dst_pass<<<nb, 256, 0, c->stream>>>(N, E, R, Sy, nyi, nxi, nullptr);
-    k_dst_scatter<<<blocks_for(3 * g.points(), 256), 256, 0, c->stream>>>(g, R, Sx, E);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_gather, g, R, E);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sx, nxi, 1, nullptr);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sy, nyi, nxi, nullptr);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sz, nzi, nxi * nyi, Dinv);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sz, nzi, nxi * nyi, nullptr);
+    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sy, nyi, nxi, nullptr);
+    pdl_launch(c->stream, blocks_for(3 * g.points(), 256), 256, 0, k_dst_scatter, g, R, Sx, E);
     *nl += 7;
   } else {
     SmallLevels S;
@@ -988,7 +1002,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const unsigned m = std::max(cg.np[0], std::max(cg.np[1], cg.np[2])) - 2;
     // one interior point: a single sweep solves it exactly
     S.coarse_sweeps = m == 1 ? 1 : (int)std::min(3u * m * m + 2u, 4000u);
-    k_vcycle_small<<<1, 1024, P.small_smem, c->stream>>>(S, B.cwork);
+    pdl_launch(c->stream, 1, 1024, P.small_smem, k_vcycle_small, S, B.cwork);
     ++*nl;
   }
   for (int l = fs - 1; l >= 0; --l) {
@@ -1001,16 +1015,16 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     // tile) one thread per cell with direct updates, which measured faster there
     if (Cn.g.points() >= (size_t)1 << 18) {
       const dim3 pg((Cn.g.np[0] - 1 + 31) / 32, (Cn.g.np[1] - 1 + 3) / 4, (Cn.g.np[2] - 1 + 1) / 2);
-      k_prolong_add<32, 4, 2><<<pg, dim3(32, 4, 2), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+      pdl_launch(c->stream, pg, dim3(32, 4, 2), 0, k_prolong_add<32, 4, 2>, L.g, Cn.g, B.E + 3 * Cn.base, e);
     } else {
       const unsigned cells_x = Cn.g.np[0] - 1, pbx = cells_x >= 64 ? 64 : 32, pby = 256 / pbx;
       const dim3 pg((cells_x + pbx - 1) / pbx, (Cn.g.np[1] - 1 + pby - 1) / pby, Cn.g.np[2] - 1);
-      k_prolong_cells<<<pg, dim3(pbx, pby), 0, c->stream>>>(L.g, Cn.g, B.E + 3 * Cn.base, e);
+      pdl_launch(c->stream, pg, dim3(pbx, pby), 0, k_prolong_cells, L.g, Cn.g, B.E + 3 * Cn.base, e);
     }
     ++*nl;
     for (int s = 0; s < post; ++s)
       for (unsigned col = 0; col < 2; ++col) {
-        k_rbgs<<<sw.grid, sw.block, 0, c->stream>>>(L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
+        pdl_launch(c->stream, sw.grid, sw.block, 0, k_rbgs, L.g, L.r2x, L.r2y, L.r2z, L.H, e, r, col, 0);
         ++*nl;
       }
   }
@@ -1036,11 +1050,11 @@ static vg_status enqueue_cycle(Ctx* c, const MgPlan& P, const Geom& g, const MgB
   add_f32(c, x, B.E, n3);
   ++*nl;
   if (tail != TAIL_NONE) {
-    k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
+    pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual32n, g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, x, rhs, B.R, B.part);
     ++*nl;
   }
   if (tail == TAIL_NORM) {
-    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)B.nb0, B.sums, 1);
+    pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)B.nb0, B.sums, 1);
     ++*nl;
   }
   VG_CUDA(c, cudaGetLastError());
@@ -1179,6 +1193,7 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
 
 // out = sqrt(sums[0] / sums[1]) (sums[1] = ||b||^2 from the solve's first residual)
 __global__ void k_relres(const double* __restrict__ sums, double* __restrict__ out) {
+  pdl_entry();
   if (threadIdx.x == 0 && blockIdx.x == 0) *out = sums[1] > 0.0 ? sqrt(sums[0] / sums[1]) : sqrt(sums[0]);
 }
 
@@ -1219,17 +1234,17 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
   const PairCoef cf = pair_coef(g, L0);
   unsigned nl = 0;
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
-  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
+  pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual32n, g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
                                                          B.part);
-  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
-  k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev + 1);
+  pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)nb0, B.sums, 0);
+  pdl_launch(c->stream, 1, 32, 0, k_relres, B.sums, c->mg_relres_dev + 1);
   nl += 3;
   for (int k = 0; k < c->mg_fixed_k1; ++k)
     if ((st = enqueue_cycle(c, P, g, B, soln3, rhs3, &nl, k + 1 < c->mg_fixed_k1 ? TAIL_RESIDUAL : TAIL_NONE)) != VG_OK)
       return st;
   VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
-  k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
-  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+  pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual_pair, g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
+  pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)nb0, B.sums, 1);
   nl += 3;
   if (c->mg_fixed_k2 > 0) {
     VG_CUDA(c, cudaMemsetAsync(etot, 0, 3 * n0 * sizeof(float), c->stream));
@@ -1239,11 +1254,11 @@ vg_status run_multigrid_fixed(Ctx* c, const Geom& g, float* soln3, const float* 
           VG_OK)
         return st;
     add_f32(c, B.lo, etot, 3 * n0);
-    k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
-    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+    pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual_pair, g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
+    pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)nb0, B.sums, 1);
     nl += 3;
   }
-  k_relres<<<1, 32, 0, c->stream>>>(B.sums, c->mg_relres_dev);
+  pdl_launch(c->stream, 1, 32, 0, k_relres, B.sums, c->mg_relres_dev);
   add_f32(c, soln3, B.lo, 3 * n0);
   nl += 2;
   c->launches += nl;
@@ -1265,9 +1280,9 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   VG_CUDA(c, cudaMemsetAsync(B.E, 0, P.total * 3 * sizeof(float), c->stream));
   const Lev& L0 = P.lev[0];
   const PairCoef cf = pair_coef(g, L0);
-  k_residual32n<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
+  pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual32n, g, L0.r2x, L0.r2y, L0.r2z, B.rl.zs, soln3, rhs3, B.R,
                                                          B.part);
-  k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 0);
+  pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)nb0, B.sums, 0);
   c->launches += 2;
   double rr = 0.0, bnorm2 = 0.0;
   if ((st = read_norm(c, B, &rr, &bnorm2)) != VG_OK) return st;
@@ -1292,8 +1307,8 @@ vg_status run_multigrid(Ctx* c, const Geom& g, float* soln3, const float* rhs3, 
   // and another such residual checks.
   VG_CUDA(c, cudaMemsetAsync(B.lo, 0, 3 * n0 * sizeof(float), c->stream));
   for (;;) {
-    k_residual_pair<<<B.rl.grid, B.rl.block, 0, c->stream>>>(g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
-    k_sum_partials<<<1, 1024, 0, c->stream>>>(B.part, (int)nb0, B.sums, 1);
+    pdl_launch(c->stream, B.rl.grid, B.rl.block, 0, k_residual_pair, g, cf, B.rl.zs, soln3, B.lo, rhs3, rir, B.part);
+    pdl_launch(c->stream, 1, 1024, 0, k_sum_partials, B.part, (int)nb0, B.sums, 1);
     c->launches += 2;
     if ((st = read_norm(c, B, &rr, nullptr)) != VG_OK) return st;
     relres = std::sqrt(rr) / bn;
