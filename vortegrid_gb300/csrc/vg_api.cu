@@ -157,6 +157,7 @@ namespace {
 
 __global__ void k_unpack_records(const unsigned char* __restrict__ rec, size_t pitch, int n, float4* __restrict__ ps,
                                  float4* __restrict__ w) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* r = (const float*)(rec + (size_t)i * pitch);
@@ -166,6 +167,7 @@ __global__ void k_unpack_records(const unsigned char* __restrict__ rec, size_t p
 
 __global__ void k_pack_records(unsigned char* __restrict__ rec, size_t pitch, int n, const float4* __restrict__ v,
                                const float4* __restrict__ w) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float* r = (float*)(rec + (size_t)i * pitch);  // record bytes [12, 48)
@@ -178,6 +180,7 @@ __global__ void k_pack_records(unsigned char* __restrict__ rec, size_t pitch, in
 }
 
 __global__ void k_grid_points(Geom g, float4* __restrict__ q) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= g.points()) return;
   const unsigned x = (unsigned)(k % g.np[0]), y = (unsigned)((k / g.np[0]) % g.np[1]),
@@ -190,6 +193,7 @@ __global__ void k_grid_points(Geom g, float4* __restrict__ q) {
 }
 
 __global__ void k_f4_to_f3(const float4* __restrict__ a, float* __restrict__ b, size_t n) {
+  pdl_entry();
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (i < n) {
     b[3 * i] = a[i].x;
@@ -199,6 +203,7 @@ __global__ void k_f4_to_f3(const float4* __restrict__ a, float* __restrict__ b, 
 }
 
 __global__ void k_copy_pos3(const unsigned char* __restrict__ rec, size_t pitch, int n, float4* __restrict__ p) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float* r = (const float*)(rec + (size_t)i * pitch);
@@ -207,6 +212,7 @@ __global__ void k_copy_pos3(const unsigned char* __restrict__ rec, size_t pitch,
 
 __global__ void k_store_posvel(unsigned char* __restrict__ rec, size_t pitch, int n, const float4* __restrict__ p,
                                const float4* __restrict__ v) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   float* r = (float*)(rec + (size_t)i * pitch);  // bytes [0, 24): position, velocity
@@ -360,7 +366,7 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
   float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
   if (st != VG_OK) return st;
   float4* out4 = q + nq;
-  k_grid_points<<<blocks_for(pts, 256), 256, 0, c->stream>>>(g, q);
+  pdl_launch(c->stream, blocks_for(pts, 256), 256, 0, k_grid_points, g, q);
   VG_LAUNCHED(c);
   float sr = 1.0f, sc = 1.0f;
   if (tech == VG_VELOCITY_TREE) {
@@ -378,7 +384,7 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
     if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
     VG_CUDA(c, cudaMemcpyAsync(vel, out4 + pts, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
   }
-  k_f4_to_f3<<<blocks_for(pts, 256), 256, 0, c->stream>>>(out4, s.velgrid, pts);
+  pdl_launch(c->stream, blocks_for(pts, 256), 256, 0, k_f4_to_f3, out4, s.velgrid, pts);
   VG_LAUNCHED(c);
   return VG_OK;
 }
@@ -628,7 +634,7 @@ vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const flo
     VG_CUDA(c, cudaMemcpyAsync(stage, particles, n * stride, cudaMemcpyHostToDevice, c->stream));
   else
     VG_CUDA(c, cudaMemcpy2DAsync(stage, 56, particles, stride, 56, n, cudaMemcpyHostToDevice, c->stream));
-  k_unpack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage, pitch, (int)n, ps, w);
+  pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_unpack_records, stage, pitch, (int)n, ps, w);
   VG_CUDA(c, cudaGetLastError());
   const float* rec0 = (const float*)particles;
   const float radius = rec0[13] * 0.5f;  // Particle::GetRadius of the first vorton
@@ -636,7 +642,7 @@ vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const flo
   if (st != VG_OK) return st;
   // write back record bytes [12, 48): velocity, (unchanged) orientation,
   // angular velocity (whole records carry their other bytes back unchanged)
-  k_pack_records<<<blocks_for(n, 256), 256, 0, c->stream>>>(stage + 12, pitch, (int)n, vel, w);
+  pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records, stage + 12, pitch, (int)n, vel, w);
   VG_CUDA(c, cudaGetLastError());
   if (whole)
     VG_CUDA(c, cudaMemcpyAsync(particles, stage, n * stride, cudaMemcpyDeviceToHost, c->stream));
@@ -755,9 +761,9 @@ vg_status vg_advect(vg_ctx* c, void* particles, size_t m, size_t stride, float d
     VG_CUDA(c, cudaMemcpyAsync(stage, particles, m * stride, cudaMemcpyHostToDevice, c->stream));
   else
     VG_CUDA(c, cudaMemcpy2DAsync(stage, 24, particles, stride, 12, m, cudaMemcpyHostToDevice, c->stream));
-  k_copy_pos3<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, pitch, (int)m, p);
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, stage, pitch, (int)m, p);
   if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, p, v, m, dt, true)) != VG_OK) return st;
-  k_store_posvel<<<blocks_for(m, 256), 256, 0, c->stream>>>(stage, pitch, (int)m, p, v);
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, stage, pitch, (int)m, p, v);
   VG_CUDA(c, cudaGetLastError());
   if (whole)
     VG_CUDA(c, cudaMemcpyAsync(particles, stage, m * stride, cudaMemcpyDeviceToHost, c->stream));
@@ -775,6 +781,7 @@ vg_status vg_advect_device(vg_ctx* c, float* pos, float* vel, size_t m, float dt
 
 namespace {
 __global__ void k_evolve(float4* __restrict__ pos, const float4* __restrict__ vel, int m, float dt) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   float4 p = pos[i];
@@ -790,7 +797,7 @@ vg_status vg_evolve_device(vg_ctx* c, float* pos4, const float* vel4, size_t m, 
   if (!c || (m && (!pos4 || !vel4))) return VG_INVALID;
   if (m == 0) return VG_OK;
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
-  k_evolve<<<blocks_for(m, 256), 256, 0, c->stream>>>((float4*)pos4, (const float4*)vel4, (int)m, dt);
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_evolve, (float4*)pos4, (const float4*)vel4, (int)m, dt);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }
@@ -806,6 +813,7 @@ vg_status vg_define_shape(size_t n, const float vmin[3], const float vmax[3], in
 namespace {
 __global__ void k_bin_only(Geom g, const float4* __restrict__ pos, int m, unsigned* __restrict__ idx3,
                            unsigned* __restrict__ off) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   const float4 p = pos[i];
@@ -825,7 +833,7 @@ vg_status vg_bin_device(vg_ctx* c, const vg_grid_geom* g, const float* pos4, siz
                         unsigned* offset) {
   if (!c || !g || (!pos4 && m)) return VG_INVALID;
   if (m == 0) return VG_OK;
-  k_bin_only<<<blocks_for(m, 256), 256, 0, c->stream>>>(to_geom(*g), (const float4*)pos4, (int)m, idx3, offset);
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_bin_only, to_geom(*g), (const float4*)pos4, (int)m, idx3, offset);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }

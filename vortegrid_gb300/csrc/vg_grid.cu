@@ -29,6 +29,7 @@ namespace {
 
 __global__ void k_sor_rows(Geom g, float* __restrict__ s, const float* __restrict__ lap, unsigned color, float r2x,
                            float r2y, float r2z, float H) {
+  pdl_entry();
   // rows (y, z) interior with (z % 2 == color) ? y odd-shifted : ...
   const unsigned ny = g.np[1], nz = g.np[2], nx = g.np[0];
   const unsigned rows_per_z = (ny - 2 + 1) / 2 + 1;
@@ -57,6 +58,7 @@ __global__ void k_sor_rows(Geom g, float* __restrict__ s, const float* __restric
 
 __global__ void k_downsample(Geom F, const float* __restrict__ f, Geom C, uint3 cd, int inject,
                              float* __restrict__ out) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= C.points()) return;
   const unsigned x = (unsigned)(k % C.np[0]), y = (unsigned)((k / C.np[0]) % C.np[1]),
@@ -141,6 +143,7 @@ __device__ __forceinline__ bool inside_cells(const Geom& g, float px, float py, 
 }
 
 __global__ void k_upsample(Geom C, const float* __restrict__ cv, Geom F, int interior, float* __restrict__ fv) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= F.points()) return;
   const unsigned x = (unsigned)(k % F.np[0]), y = (unsigned)((k / F.np[0]) % F.np[1]),
@@ -175,6 +178,7 @@ __device__ __forceinline__ void diff_axis(size_t c, unsigned i, unsigned n, size
 
 __global__ void k_jacobian(Geom g, float rsx, float rsy, float rsz, const float* __restrict__ v,
                            float* __restrict__ jac) {
+  pdl_entry();
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.points()) return;
   const unsigned nx = g.np[0], ny = g.np[1];
@@ -193,6 +197,7 @@ __global__ void k_jacobian(Geom g, float rsx, float rsy, float rsz, const float*
 
 __global__ void k_curl(Geom g, float rsx, float rsy, float rsz, const float* __restrict__ v,
                        float* __restrict__ curl) {
+  pdl_entry();
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.points()) return;
   const unsigned nx = g.np[0], ny = g.np[1];
@@ -215,6 +220,7 @@ __global__ void k_curl(Geom g, float rsx, float rsy, float rsz, const float* __r
 
 __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* __restrict__ ps,
                           float4* __restrict__ w, int n, float dt, int* __restrict__ flag) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 p = ps[i];
@@ -241,6 +247,7 @@ __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* _
 // vorton items[t]), so that each cell's vortons are contiguous for k_pse.
 __global__ void k_pse_gather(const float4* __restrict__ ps, const float4* __restrict__ w, int n,
                              const unsigned* __restrict__ items, float4* __restrict__ pss, float4* __restrict__ w0s) {
+  pdl_entry();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const unsigned j = items[t];
@@ -251,6 +258,7 @@ __global__ void k_pse_gather(const float4* __restrict__ ps, const float4* __rest
 __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ pss, const float4* __restrict__ w0s,
                                              float4* __restrict__ w, int n, const unsigned* __restrict__ start,
                                              const unsigned* __restrict__ items, float nu, float dt) {
+  pdl_entry();
   // threads take the vortons in cell order, so a warp's vortons share their
   // neighbour cells and read them contiguously (each vorton's sums are the
   // same whichever thread runs them)
@@ -318,6 +326,7 @@ __global__ void __launch_bounds__(128) k_pse(Geom g, const float4* __restrict__ 
 // toward the ambient density when its own cell is a "here" cell.
 __global__ void k_heat_gather(const float4* __restrict__ ps, const float* __restrict__ d, int n,
                               const unsigned* __restrict__ items, float4* __restrict__ pss, float* __restrict__ d0s) {
+  pdl_entry();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const unsigned j = items[t];
@@ -329,6 +338,7 @@ __global__ void __launch_bounds__(128) k_heat_pse(Geom g, const float4* __restri
                                                   float* __restrict__ d, int n, const unsigned* __restrict__ start,
                                                   const unsigned* __restrict__ items, float kappa, float ambient,
                                                   float dt) {
+  pdl_entry();
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= n) return;
   const int i = (int)items[t];
@@ -376,6 +386,7 @@ __global__ void __launch_bounds__(128) k_heat_pse(Geom g, const float4* __restri
 
 __global__ void k_gather_advect(Geom g, const float* __restrict__ vel3, float4* __restrict__ pos,
                                 float4* __restrict__ vel, int m, float dt, int evolve, int* __restrict__ flag) {
+  pdl_entry();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= m) return;
   float4 p = pos[i];
@@ -402,6 +413,7 @@ __device__ __forceinline__ unsigned f2key(float f) {
 }
 
 __global__ void k_bbox(const float4* __restrict__ pos, int n, unsigned* __restrict__ keys, int* __restrict__ flag) {
+  pdl_entry();
   float mn[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, mx[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
     const float4 p = pos[i];
@@ -425,6 +437,7 @@ __global__ void k_bbox(const float4* __restrict__ pos, int n, unsigned* __restri
 }
 
 __global__ void k_bbox_finish(const unsigned* __restrict__ keys, float* __restrict__ out6) {
+  pdl_entry();
   const int a = threadIdx.x;
   if (a < 6) {
     const unsigned k = keys[a];
@@ -434,6 +447,7 @@ __global__ void k_bbox_finish(const unsigned* __restrict__ keys, float* __restri
 }
 
 __global__ void k_bbox_init(unsigned* keys) {
+  pdl_entry();
   const int a = threadIdx.x;
   if (a < 3) keys[a] = 0xffffffffu;
   else if (a < 6) keys[a] = 0u;
@@ -460,7 +474,7 @@ vg_status launch_sor(Ctx* c, const Geom& g, float* s, const float* lap, int step
   const size_t threads = (size_t)rows_per_z * (g.np[2] - 2);
   for (int it = 0; it < steps; ++it)
     for (unsigned color = 0; color < 2; ++color) {
-      k_sor_rows<<<blocks_for(threads, 64), 64, 0, c->stream>>>(g, s, lap, color, r2x, r2y, r2z, H);
+      pdl_launch(c->stream, blocks_for(threads, 64), 64, 0, k_sor_rows, g, s, lap, color, r2x, r2y, r2z, H);
       VG_LAUNCHED(c);
     }
   VG_CUDA(c, cudaGetLastError());
@@ -469,14 +483,14 @@ vg_status launch_sor(Ctx* c, const Geom& g, float* s, const float* lap, int step
 
 vg_status launch_downsample(Ctx* c, const Geom& F, const float* f3, const Geom& C, bool inject, float* c3) {
   const uint3 cd = make_uint3((F.np[0] - 1) / (C.np[0] - 1), (F.np[1] - 1) / (C.np[1] - 1), (F.np[2] - 1) / (C.np[2] - 1));
-  k_downsample<<<blocks_for(C.points(), 128), 128, 0, c->stream>>>(F, f3, C, cd, inject ? 1 : 0, c3);
+  pdl_launch(c->stream, blocks_for(C.points(), 128), 128, 0, k_downsample, F, f3, C, cd, inject ? 1 : 0, c3);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
 }
 
 vg_status launch_upsample(Ctx* c, const Geom& C, const float* c3, const Geom& F, bool interior, float* f3) {
-  k_upsample<<<blocks_for(F.points(), 128), 128, 0, c->stream>>>(C, c3, F, interior ? 1 : 0, f3);
+  pdl_launch(c->stream, blocks_for(F.points(), 128), 128, 0, k_upsample, C, c3, F, interior ? 1 : 0, f3);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -526,7 +540,7 @@ vg_status run_cascade(Ctx* c, const Geom& g, float* soln3, const float* rhs3, in
 vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9) {
   float rs[3];
   recip_spacing(g, rs);
-  k_jacobian<<<blocks_for(g.points(), 128), 128, 0, c->stream>>>(g, rs[0], rs[1], rs[2], v3, jac9);
+  pdl_launch(c->stream, blocks_for(g.points(), 128), 128, 0, k_jacobian, g, rs[0], rs[1], rs[2], v3, jac9);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -535,7 +549,7 @@ vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9) {
 vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3) {
   float rs[3];
   recip_spacing(g, rs);
-  k_curl<<<blocks_for(g.points(), 128), 128, 0, c->stream>>>(g, rs[0], rs[1], rs[2], v3, curl3);
+  pdl_launch(c->stream, blocks_for(g.points(), 128), 128, 0, k_curl, g, rs[0], rs[1], rs[2], v3, curl3);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -544,7 +558,7 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3) {
 vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt) {
   if (0.0f == g.ext[0] || 0.0f == g.ext[1] || 0.0f == g.ext[2]) return VG_OK;  // 2D: no stretching
   if (n == 0) return VG_OK;
-  k_stretch<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, jac9, ps, w, (int)n, dt, outside_flag(c));
+  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_stretch, g, jac9, ps, w, (int)n, dt, outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -557,8 +571,8 @@ vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const floa
   if (st != VG_OK) return st;
   float4* pss = (float4*)tmp;
   float* d0s = (float*)(pss + n);
-  k_heat_gather<<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, density, (int)n, cl.items, pss, d0s);
-  k_heat_pse<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, pss, d0s, density, (int)n, cl.start, cl.items, kappa,
+  pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_heat_gather, ps, density, (int)n, cl.items, pss, d0s);
+  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_heat_pse, g, pss, d0s, density, (int)n, cl.start, cl.items, kappa,
                                                         ambient, dt);
   c->launches += 2;
   VG_CUDA(c, cudaGetLastError());
@@ -572,8 +586,8 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
   float4* pss = (float4*)ws(c, S_WOLD, 2 * n * sizeof(float4), &st);
   if (st != VG_OK) return st;
   float4* w0s = pss + n;
-  k_pse_gather<<<blocks_for(n, 256), 256, 0, c->stream>>>(ps, w, (int)n, cl.items, pss, w0s);
-  k_pse<<<blocks_for(n, 128), 128, 0, c->stream>>>(g, pss, w0s, w, (int)n, cl.start, cl.items, nu, dt);
+  pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pse_gather, ps, w, (int)n, cl.items, pss, w0s);
+  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_pse, g, pss, w0s, w, (int)n, cl.start, cl.items, nu, dt);
   c->launches += 2;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -583,7 +597,7 @@ vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4*
                                bool evolve) {
   if (m == 0) return VG_OK;
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "advect: more than 2^31 particles");
-  k_gather_advect<<<blocks_for(m, 256), 256, 0, c->stream>>>(g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0,
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect, g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0,
                                                               outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
@@ -594,13 +608,13 @@ vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6) {
   vg_status st = VG_OK;
   unsigned* keys = (unsigned*)ws(c, S_BBOX, 64, &st);
   if (st != VG_OK) return st;
-  k_bbox_init<<<1, 32, 0, c->stream>>>(keys);
+  pdl_launch(c->stream, 1, 32, 0, k_bbox_init, keys);
   if (n > 0) {
     unsigned blocks = blocks_for(n, 256);
     if (blocks > 4u * kSMs) blocks = 4u * kSMs;
-    k_bbox<<<blocks, 256, 0, c->stream>>>(pos, (int)n, keys, c->dflag);
+    pdl_launch(c->stream, blocks, 256, 0, k_bbox, pos, (int)n, keys, c->dflag);
   }
-  k_bbox_finish<<<1, 32, 0, c->stream>>>(keys, out6);
+  pdl_launch(c->stream, 1, 32, 0, k_bbox_finish, keys, out6);
   c->launches += 3;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;

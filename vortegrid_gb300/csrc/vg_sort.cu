@@ -22,6 +22,7 @@ constexpr int kScanBlock = 1024;
 
 __global__ void k_bin(Geom g, const float4* __restrict__ pos, int n, unsigned* __restrict__ key,
                       unsigned* __restrict__ val, unsigned* __restrict__ count, unsigned ncells) {
+  pdl_entry();
   int i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= n) return;
   const float4 p = pos[i];
@@ -71,6 +72,7 @@ __device__ unsigned block_exclusive_scan(unsigned v, unsigned* total) {
 __global__ void __launch_bounds__(kScanBlock) k_scan_blocks(const unsigned* __restrict__ in, size_t n,
                                                             unsigned* __restrict__ out,
                                                             unsigned* __restrict__ block_sums) {
+  pdl_entry();
   const size_t i = (size_t)blockIdx.x * kScanBlock + threadIdx.x;
   const unsigned v = i < n ? in[i] : 0;
   unsigned total;
@@ -82,6 +84,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_blocks(const unsigned* __re
 // Single-block scan of the block sums (any count), in place.
 __global__ void __launch_bounds__(kScanBlock) k_scan_sums(unsigned* __restrict__ sums, size_t nb,
                                                           unsigned* __restrict__ grand_total) {
+  pdl_entry();
   __shared__ unsigned carry;
   if (threadIdx.x == 0) carry = 0;
   __syncthreads();
@@ -99,6 +102,7 @@ __global__ void __launch_bounds__(kScanBlock) k_scan_sums(unsigned* __restrict__
 }
 
 __global__ void k_scan_add(unsigned* __restrict__ out, size_t n, const unsigned* __restrict__ sums) {
+  pdl_entry();
   const size_t i = (size_t)blockIdx.x * kScanBlock + threadIdx.x;
   if (i < n) out[i] += sums[blockIdx.x];
 }
@@ -110,6 +114,7 @@ constexpr int kTileKeys = kSortThreads * kSortItems;
 
 __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const unsigned* __restrict__ key, int n, int shift,
                                                              int ntiles, unsigned* __restrict__ hist) {
+  pdl_entry();
   __shared__ unsigned h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -130,6 +135,7 @@ __global__ void __launch_bounds__(kSortThreads) k_digit_scatter(const unsigned* 
                                                                 int ntiles, const unsigned* __restrict__ offsets,
                                                                 unsigned* __restrict__ key_out,
                                                                 unsigned* __restrict__ val_out) {
+  pdl_entry();
   constexpr int kWarps = kSortThreads / 32;
   __shared__ unsigned running[256];
   __shared__ unsigned warp_cnt[kWarps][256];
@@ -172,9 +178,9 @@ vg_status exclusive_scan(Ctx* c, const unsigned* in, size_t n, unsigned* out, bo
   vg_status st = VG_OK;
   unsigned* sums = (unsigned*)ws(c, S_SCAN, (nb + 1) * sizeof(unsigned), &st);
   if (st != VG_OK) return st;
-  k_scan_blocks<<<(unsigned)nb, kScanBlock, 0, c->stream>>>(in, n, out, sums);
-  k_scan_sums<<<1, kScanBlock, 0, c->stream>>>(sums, nb, write_total ? out + n : nullptr);
-  k_scan_add<<<(unsigned)nb, kScanBlock, 0, c->stream>>>(out, n, sums);
+  pdl_launch(c->stream, (unsigned)nb, kScanBlock, 0, k_scan_blocks, in, n, out, sums);
+  pdl_launch(c->stream, 1, kScanBlock, 0, k_scan_sums, sums, nb, write_total ? out + n : nullptr);
+  pdl_launch(c->stream, (unsigned)nb, kScanBlock, 0, k_scan_add, out, n, sums);
   c->launches += 3;
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -196,7 +202,7 @@ vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, Ce
   unsigned *key = kv, *val = kv + (n + 1), *key2 = kv + 2 * (n + 1), *val2 = kv + 3 * (n + 1);
   VG_CUDA(c, cudaMemsetAsync(count, 0, slots * sizeof(unsigned), c->stream));
   if (n > 0) {
-    k_bin<<<blocks_for(n, 256), 256, 0, c->stream>>>(g, ps, (int)n, key, val, count, (unsigned)ncells);
+    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_bin, g, ps, (int)n, key, val, count, (unsigned)ncells);
     VG_LAUNCHED(c);
   }
   st = exclusive_scan(c, count, slots, start, true);
@@ -211,11 +217,11 @@ vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, Ce
     if (st != VG_OK) return st;
     unsigned* offs = hist + (size_t)256 * ntiles;
     for (int p = 0; p < passes; ++p) {
-      k_digit_hist<<<ntiles, kSortThreads, 0, c->stream>>>(key, (int)n, 8 * p, ntiles, hist);
+      pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_hist, key, (int)n, 8 * p, ntiles, hist);
       VG_LAUNCHED(c);
       st = exclusive_scan(c, hist, (size_t)256 * ntiles, offs, false);
       if (st != VG_OK) return st;
-      k_digit_scatter<<<ntiles, kSortThreads, 0, c->stream>>>(key, val, (int)n, 8 * p, ntiles, offs, key2, val2);
+      pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_scatter, key, val, (int)n, 8 * p, ntiles, offs, key2, val2);
       VG_LAUNCHED(c);
       unsigned* t = key; key = key2; key2 = t;
       t = val; val = val2; val2 = t;

@@ -47,6 +47,7 @@ __device__ __forceinline__ float ref_vort_mag(float4 w) {
 __global__ void k_leaf(Geom g, const float4* __restrict__ ps, const float4* __restrict__ w,
                        const unsigned* __restrict__ start, const unsigned* __restrict__ items,
                        float4* __restrict__ out_pos, float4* __restrict__ out_w) {
+  pdl_entry();
   const size_t c = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (c >= g.points()) return;
   float px = 0.f, py = 0.f, pz = 0.f, wx = 0.f, wy = 0.f, wz = 0.f, size = 0.f, aux = FLT_MIN;
@@ -77,6 +78,7 @@ __global__ void k_leaf(Geom g, const float4* __restrict__ ps, const float4* __re
 
 __global__ void k_aggregate(Geom P, Geom C, uint3 d, const float4* __restrict__ cpos, const float4* __restrict__ cw,
                             float4* __restrict__ ppos, float4* __restrict__ pw) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= P.points()) return;
   const unsigned px = (unsigned)(k % P.np[0]);
@@ -203,6 +205,7 @@ __device__ float3 tree_walk(const TreeParams& T, const float4* __restrict__ sp, 
 // size / 2 x sr -- what fast_accum derives from (sp, sw) at every pair.
 __global__ void k_tree_prep(const float4* __restrict__ sp, const float4* __restrict__ sw, size_t total, float sr,
                             float sc, float4* __restrict__ tp, float4* __restrict__ tw) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= total) return;
   const float4 p = sp[k], a = sw[k];
@@ -313,6 +316,7 @@ __global__ void __launch_bounds__(128) k_tree_eval(const __grid_constant__ TreeP
                                                     const float4* __restrict__ tw, const float4* __restrict__ ps,
                                                     const float4* __restrict__ w, int n, const float4* __restrict__ q,
                                                     int m, float sr, float sc, float4* __restrict__ out) {
+  pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   const float4 v = q[j];
@@ -361,6 +365,7 @@ __global__ void __launch_bounds__(128) k_boundary_vecpot(const __grid_constant__
                                                           const float4* __restrict__ ps, const float4* __restrict__ w,
                                                           int n, int copy_odd_x, size_t nface,
                                                           float* __restrict__ grid3) {
+  pdl_entry();
   const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (t >= nface) return;
   unsigned x, y, z;
@@ -396,6 +401,7 @@ __global__ void __launch_bounds__(128) k_splat(Geom g, const float4* __restrict_
                                                const unsigned* __restrict__ start, const unsigned* __restrict__ items,
                                                float scale, float four_pi_over3, float cell_volume,
                                                float* __restrict__ grid3) {
+  pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (k >= g.points()) return;
   // volumeCorrection = scale * (4 pi / 3 * r^3) / cellVolume, r = first vorton's radius
@@ -491,13 +497,13 @@ vg_status build_tree(Ctx* c, const Geom& g, const float4* ps, const float4* w, s
   t->sv_pos = mem;
   t->sv_w = mem + total;
   const Geom& leaf = t->layer[0];
-  k_leaf<<<blocks_for(leaf.points(), 256), 256, 0, c->stream>>>(leaf, ps, w, cl.start, cl.items, t->sv_pos,
+  pdl_launch(c->stream, blocks_for(leaf.points(), 256), 256, 0, k_leaf, leaf, ps, w, cl.start, cl.items, t->sv_pos,
                                                                   t->sv_w);
   VG_LAUNCHED(c);
   for (int l = 1; l < t->depth; ++l) {
     const Geom& P = t->layer[l];
     const uint3 d = make_uint3(t->decim[l][0], t->decim[l][1], t->decim[l][2]);
-    k_aggregate<<<blocks_for(P.points(), 128), 128, 0, c->stream>>>(P, t->layer[l - 1], d, t->sv_pos + t->base[l - 1],
+    pdl_launch(c->stream, blocks_for(P.points(), 128), 128, 0, k_aggregate, P, t->layer[l - 1], d, t->sv_pos + t->base[l - 1],
                                                                      t->sv_w + t->base[l - 1], t->sv_pos + t->base[l],
                                                                      t->sv_w + t->base[l]);
     VG_LAUNCHED(c);
@@ -516,7 +522,7 @@ static vg_status tree_prep(Ctx* c, const Tree& t, float sr, float sc, float4** t
   if (st != VG_OK) return st;
   *tp = buf;
   *tw = buf + t.total;
-  k_tree_prep<<<blocks_for(t.total, 256), 256, 0, c->stream>>>(t.sv_pos, t.sv_w, t.total, sr, sc, *tp, *tw);
+  pdl_launch(c->stream, blocks_for(t.total, 256), 256, 0, k_tree_prep, t.sv_pos, t.sv_w, t.total, sr, sc, *tp, *tw);
   VG_LAUNCHED(c);
   return VG_OK;
 }
@@ -532,7 +538,7 @@ vg_status launch_tree_eval(Ctx* c, int kind, bool ref, const Tree& t, const floa
     if (st != VG_OK) return st;
   }
 #define VG_TREE_LAUNCH(K, R) \
-  k_tree_eval<K, R><<<blocks, 128, 0, c->stream>>>(T, t.sv_pos, t.sv_w, tp, tw, ps, w, (int)n, q, (int)m, sr, sc, out)
+  pdl_launch(c->stream, blocks, 128, 0, k_tree_eval<K, R>, T, t.sv_pos, t.sv_w, tp, tw, ps, w, (int)n, q, (int)m, sr, sc, out)
   if (kind == 0) {
     if (ref) VG_TREE_LAUNCH(0, true); else VG_TREE_LAUNCH(0, false);
   } else {
@@ -551,13 +557,13 @@ vg_status launch_boundary_vecpot(Ctx* c, const Tree& t, const Geom& g, const flo
   const size_t nface = 2 * nx * ny + 2 * nx * (nz > 2 ? nz - 2 : 0) + 2 * (ny > 2 ? ny - 2 : 0) * (nz > 2 ? nz - 2 : 0);
   if (nface == 0) return VG_OK;
   if (ref) {
-    k_boundary_vecpot<true><<<blocks_for(nface, 128), 128, 0, c->stream>>>(
+    pdl_launch(c->stream, blocks_for(nface, 128), 128, 0, k_boundary_vecpot<true>, 
         T, g, t.sv_pos, t.sv_w, nullptr, nullptr, ps, w, (int)n, copy_odd_x ? 1 : 0, nface, grid3);
   } else {
     float4 *tp = nullptr, *tw = nullptr;
     vg_status st = tree_prep(c, t, 1.0f, 1.0f, &tp, &tw);
     if (st != VG_OK) return st;
-    k_boundary_vecpot<false><<<blocks_for(nface, 128), 128, 0, c->stream>>>(
+    pdl_launch(c->stream, blocks_for(nface, 128), 128, 0, k_boundary_vecpot<false>, 
         T, g, t.sv_pos, t.sv_w, tp, tw, ps, w, (int)n, copy_odd_x ? 1 : 0, nface, grid3);
   }
   VG_LAUNCHED(c);
@@ -579,7 +585,7 @@ vg_status launch_splat(Ctx* c, const Geom& g, const float4* ps, const float4* w,
   const float four_pi = 4.0f * 3.1415926535897932384626433832795f;
   const float four_pi_over3 = four_pi / 3.0f;
   (void)radius;
-  k_splat<<<blocks_for(pts, 128), 128, 0, c->stream>>>(g, ps, w, cl.start, cl.items, scale, four_pi_over3,
+  pdl_launch(c->stream, blocks_for(pts, 128), 128, 0, k_splat, g, ps, w, cl.start, cl.items, scale, four_pi_over3,
                                                         cell_volume, grid3);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
