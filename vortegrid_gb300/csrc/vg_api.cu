@@ -179,10 +179,15 @@ __global__ void k_pack_records(unsigned char* __restrict__ rec, size_t pitch, in
   r[8] = w[i].z;
 }
 
-__global__ void k_grid_points(Geom g, float4* __restrict__ q) {
+// Targets of the grid-point evaluation: every gridpoint, then (when ps is
+// given) the n vortons' position records after them.
+__global__ void k_grid_points(Geom g, float4* __restrict__ q, const float4* __restrict__ ps, size_t n) {
   pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= g.points()) return;
+  if (k >= g.points()) {
+    if (ps && k - g.points() < n) q[k] = ps[k - g.points()];
+    return;
+  }
   const unsigned x = (unsigned)(k % g.np[0]), y = (unsigned)((k / g.np[0]) % g.np[1]),
                  z = (unsigned)(k / ((size_t)g.np[0] * g.np[1]));
   // gridpoint positions min + i * spacing * (1 - 2 eps) (vortonSim.cpp:2229-2252)
@@ -192,10 +197,17 @@ __global__ void k_grid_points(Geom g, float4* __restrict__ q) {
                      __fadd_rn(g.mn[2], __fmul_rn((float)z, __fmul_rn(g.cell[2], nudge))), 0.f);
 }
 
-__global__ void k_f4_to_f3(const float4* __restrict__ a, float* __restrict__ b, size_t n) {
+// Velocities at the targets: the first n (gridpoints) as float[3] into b,
+// the next m (vortons, when vel is given) as float4 records into vel.
+__global__ void k_f4_to_f3(const float4* __restrict__ a, float* __restrict__ b, size_t n, float4* __restrict__ vel,
+                           size_t m) {
   pdl_entry();
   const size_t i = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (i < n) {
+  if (i >= n) {
+    if (vel && i - n < m) vel[i - n] = a[i];
+    return;
+  }
+  {
     b[3 * i] = a[i].x;
     b[3 * i + 1] = a[i].y;
     b[3 * i + 2] = a[i].z;
@@ -366,7 +378,9 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
   float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
   if (st != VG_OK) return st;
   float4* out4 = q + nq;
-  pdl_launch(c->stream, blocks_for(pts, 256), 256, 0, k_grid_points, g, q);
+  // the direct technique also evaluates every vorton, whose records follow the gridpoints
+  pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_grid_points, g, q,
+             tech == VG_VELOCITY_DIRECT ? (const float4*)ps : nullptr, nq - pts);
   VG_LAUNCHED(c);
   float sr = 1.0f, sc = 1.0f;
   if (tech == VG_VELOCITY_TREE) {
@@ -380,11 +394,11 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
     if ((st = launch_tree_eval(c, 0, ref, s.t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
   } else {
     // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too
-    VG_CUDA(c, cudaMemcpyAsync(q + pts, ps, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
     if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
-    VG_CUDA(c, cudaMemcpyAsync(vel, out4 + pts, n * sizeof(float4), cudaMemcpyDeviceToDevice, c->stream));
   }
-  pdl_launch(c->stream, blocks_for(pts, 256), 256, 0, k_f4_to_f3, out4, s.velgrid, pts);
+  // gridpoint velocities to the grid, and (direct technique) the vortons' velocities to vel
+  pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_f4_to_f3, out4, s.velgrid, pts,
+             tech == VG_VELOCITY_DIRECT ? vel : (float4*)nullptr, nq - pts);
   VG_LAUNCHED(c);
   return VG_OK;
 }

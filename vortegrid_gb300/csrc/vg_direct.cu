@@ -144,6 +144,7 @@ constexpr int kPairThreads = 256;
 __global__ void __launch_bounds__(kPairThreads, 2)
     k_direct_pair(const float4* __restrict__ ps, const float4* __restrict__ w, int n, int chunk, float sr, float sc,
                   const float4* __restrict__ q, int m, float* __restrict__ partial, float4* __restrict__ out) {
+  pdl_entry();
   constexpr int kPairs = kPairTPT / 2;
   __shared__ float4 sh[5 * kTile];
   const int base = blockIdx.x * (kPairThreads * kPairTPT) + threadIdx.x;
@@ -228,6 +229,7 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 // latency of these loads, not by their bytes.
 __global__ void __launch_bounds__(256) k_reduce_pair(const float* __restrict__ partial, int ks, int m,
                                                      float4* __restrict__ out) {
+  pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
   constexpr int kBatch = 16;
@@ -344,10 +346,11 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
       if (st != VG_OK) return st;
     }
     dim3 grid(tblocks, ksplit);
-    k_direct_pair<<<grid, kPairThreads, 0, c->stream>>>(ps, w, (int)n, chunk, sr, sc, q, (int)m, partial, out);
+    pdl_launch(c->stream, grid, dim3(kPairThreads), 0, k_direct_pair, ps, w, (int)n, chunk, sr, sc, q, (int)m, partial,
+               out);
     VG_LAUNCHED(c);
     if (ksplit > 1) {
-      k_reduce_pair<<<blocks_for(m, 256), 256, 0, c->stream>>>(partial, (int)ksplit, (int)m, out);
+      pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_reduce_pair, (const float*)partial, (int)ksplit, (int)m, out);
       VG_LAUNCHED(c);
     }
     VG_CUDA(c, cudaGetLastError());
