@@ -105,6 +105,37 @@ def test_direct_fast_vs_fp64(vg, fast_ctx, oracle_lib, kind):
     assert rel < 1e-5, rel
 
 
+def test_direct_step_matches_fp64(vg, oracle_lib):
+    """The direct-technique step (FAST numerics; the ring of the bench's direct
+    workload on its 33^3 grid): the velocity grid and every vorton's velocity,
+    which the multi-chunk reduction writes straight into the grid and the
+    vortons' records, against the FP64 direct sum at the step's gridpoint
+    positions (min + i x spacing x (1 - 2 FLT_EPSILON)): rel-L2 <= 1e-5."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(4096, seed=1)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+    cfg = vg.default_config(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid, enable_stretch=0,
+                            enable_diffusion=0, device=0)
+    ctx = vg.VortonSim(cfg=cfg)
+    ps, wd = dev(f4(pos, s)), dev(f4(w))
+    vel = torch.zeros_like(ps)
+    ctx.UpdateDevice(ps, wd, vel, float(DT))
+    vgrid, g = ctx.GetVelocityGrid()
+    nudge = np.float32(1.0) - np.float32(2.0) * np.finfo(np.float32).eps
+    axes = []
+    for a in range(3):
+        step = np.float32(g.cell_spacing[a]) * nudge
+        axes.append(np.float32(g.min_corner[a]) + np.arange(g.num_points[a], dtype=np.float32) * step)
+    z, y, x = np.meshgrid(axes[2], axes[1], axes[0], indexing="ij")
+    q = np.stack([x.ravel(), y.ravel(), z.ravel()], 1).astype(np.float32)
+    ref_grid = oracle_lib.direct(0, pos, w, s, q, f64=True)
+    ref_vort = oracle_lib.direct(0, pos, w, s, pos, f64=True)
+    got_v = vel.cpu().numpy()[:, :3].astype(np.float64)
+    assert np.linalg.norm(vgrid - ref_grid) / np.linalg.norm(ref_grid) < 1e-5
+    assert np.linalg.norm(got_v - ref_vort) / np.linalg.norm(ref_vort) < 1e-5
+    assert np.all(vel.cpu().numpy()[:, 3] == 0.0)
+
+
 def test_tree_reference_bit_exact(vg, ref_ctx, golden):
     g = geom(vg, golden)
     ps, w = vortons(golden)

@@ -393,8 +393,12 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
     sc = 1.0f / s3;
     if ((st = launch_tree_eval(c, 0, ref, s.t, ps, w, n, q, pts, sr, sc, out4)) != VG_OK) return st;
   } else {
-    // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too
-    if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4)) != VG_OK) return st;
+    // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too;
+    // the multi-chunk reduction writes the grid and vortons directly
+    const DirectSplit split = {s.velgrid, pts, vel};
+    bool done = false;
+    if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4, &split, &done)) != VG_OK) return st;
+    if (done) return VG_OK;
   }
   // gridpoint velocities to the grid, and (direct technique) the vortons' velocities to vel
   pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_f4_to_f3, out4, s.velgrid, pts,

@@ -228,7 +228,8 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 // up to 16 chunks' loads issued before the first add: the sum is bound by the
 // latency of these loads, not by their bytes.
 __global__ void __launch_bounds__(256) k_reduce_pair(const float* __restrict__ partial, int ks, int m,
-                                                     float4* __restrict__ out) {
+                                                     float4* __restrict__ out, float* __restrict__ grid3, int pts,
+                                                     float4* __restrict__ vel) {
   pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= m) return;
@@ -252,7 +253,15 @@ __global__ void __launch_bounds__(256) k_reduce_pair(const float* __restrict__ p
         z += v[k][2];
       }
   }
-  out[j] = make_float4(x, y, z, 0.f);
+  if (!grid3) {
+    out[j] = make_float4(x, y, z, 0.f);
+  } else if (j < pts) {  // the velocity step's split: gridpoints as float[3], vortons as records
+    grid3[3 * j] = x;
+    grid3[3 * j + 1] = y;
+    grid3[3 * j + 2] = z;
+  } else {
+    vel[j - pts] = make_float4(x, y, z, 0.f);
+  }
 }
 
 __global__ void k_reduce_partials(const float* __restrict__ partial, int ksplit, int m, float4* __restrict__ out) {
@@ -311,7 +320,7 @@ unsigned direct_slots(int kind) {
 }  // namespace
 
 vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
-                        size_t m, float sr, float sc, float4* out) {
+                        size_t m, float sr, float sc, float4* out, const DirectSplit* split, bool* split_done) {
   if (m == 0) return VG_OK;
   if (n == 0) {
     VG_CUDA(c, cudaMemsetAsync(out, 0, m * sizeof(float4), c->stream));
@@ -350,7 +359,11 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
                out);
     VG_LAUNCHED(c);
     if (ksplit > 1) {
-      pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_reduce_pair, (const float*)partial, (int)ksplit, (int)m, out);
+      const bool to_split = split != nullptr;
+      pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_reduce_pair, (const float*)partial, (int)ksplit, (int)m, out,
+                 to_split ? split->grid3 : (float*)nullptr, to_split ? (int)split->pts : 0,
+                 to_split ? split->vel : (float4*)nullptr);
+      if (split_done) *split_done = to_split;
       VG_LAUNCHED(c);
     }
     VG_CUDA(c, cudaGetLastError());

@@ -294,8 +294,18 @@ inline cudaError_t pdl_launch(cudaStream_t s, dim3 grid, dim3 block, size_t smem
 // ---------------------------------------------------------- stage launchers
 // (device pointers, context stream; defined in the .cu files)
 
+// Where the velocity step wants the direct sum's results: targets [0, pts)
+// as float[3] into grid3, the rest as float4 records into vel.
+struct DirectSplit {
+  float* grid3;
+  size_t pts;
+  float4* vel;
+};
+// With split, *split_done says whether the results went there (the
+// multi-chunk packed path writes them from its reduction) or to out.
 vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
-                        size_t m, float sr, float sc, float4* out);
+                        size_t m, float sr, float sc, float4* out, const DirectSplit* split = nullptr,
+                        bool* split_done = nullptr);
 
 // Cell lists: stable counting sort of vortons by leaf cell (OffsetOfPosition).
 struct CellLists {
