@@ -127,13 +127,21 @@ def dist_setup():
 
 
 def max_over_ranks(x, world):
+    """The largest x over the ranks (a step's time: the job waits for the slowest replica)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
+
+
+def whole_job_gint_per_s(interactions_per_rank, ms_per_step, world):
+    """Replicas: every rank evaluates the same number of interactions per step;
+    the job's throughput is their sum over the slowest rank's step time."""
+    return world * interactions_per_rank / (ms_per_step * 1e-3) / 1e9
 
 
 def barrier(world):
@@ -297,7 +305,7 @@ def run_ours(args, world, rank, local):
         ms_steps = [a.elapsed_time(b) for a, b in ev]
     ms_total = max_over_ranks(sum(ms_steps), world)
     ms_per_step = ms_total / args.steps
-    value = world * interactions() / (ms_per_step * 1e-3) / 1e9
+    value = whole_job_gint_per_s(interactions(), ms_per_step, world)
 
     result = {"metric": METRIC, "value": value, "unit": "Gint/s", "n_gpus": world, "steps": args.steps,
               "warmup": args.warmup, "ms_per_step": ms_per_step, "higher_is_better": True, "scaling": "weak",
