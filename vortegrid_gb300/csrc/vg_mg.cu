@@ -837,6 +837,51 @@ __global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const float* __res
   out[i] = Dinv ? acc * __ldg(Dinv + p) : acc;
 }
 
+// The first x pass reading r in full layout (the gather folded in): the same
+// sums as k_dst_gather followed by k_dst_pass along x.
+__global__ void __launch_bounds__(256) k_dst_first(Geom g, const float* __restrict__ rfull, float* __restrict__ out,
+                                                   const float* __restrict__ Sx) {
+  pdl_entry();
+  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
+  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= 3 * N) return;
+  const unsigned c = i % 3u, p = i / 3u;
+  const unsigned k = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
+  const unsigned row = 3 * (1 + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c;  // r at (1, y + 1, z + 1)
+  float acc = 0.f;
+  for (unsigned m = 0; m < nxi; ++m) acc = fmaf(__ldg(Sx + k * nxi + m), rfull[row + 3 * m], acc);
+  out[i] = acc;
+}
+
+// The two z passes around the eigenvalue scaling, fused: a CTA owns whole z
+// columns (32 x's, one y, one component), keeps the first pass's results in
+// shared memory and runs the second from there -- the same sums as two
+// k_dst_pass launches.  Dynamic shared memory: nzi x 32 floats.
+constexpr unsigned kZZMaxN = 384;
+__global__ void __launch_bounds__(256) k_dst_zz(unsigned nxi, unsigned nyi, unsigned nzi, const float* __restrict__ in,
+                                                float* __restrict__ out, const float* __restrict__ Sz,
+                                                const float* __restrict__ Dinv) {
+  pdl_entry();
+  extern __shared__ float col[];  // [z][x - x0]
+  const unsigned x0 = blockIdx.x * 32, y = blockIdx.y, c = blockIdx.z, st = nxi * nyi;
+  for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
+    const unsigned xl = it % 32, z = it / 32, x = x0 + xl;
+    if (x >= nxi) continue;
+    const unsigned p0 = x + nxi * y;
+    float acc = 0.f;
+    for (unsigned m = 0; m < nzi; ++m) acc = fmaf(__ldg(Sz + z * nzi + m), in[3 * (p0 + m * st) + c], acc);
+    col[z * 32 + xl] = acc * __ldg(Dinv + p0 + z * st);
+  }
+  __syncthreads();
+  for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
+    const unsigned xl = it % 32, z = it / 32, x = x0 + xl;
+    if (x >= nxi) continue;
+    float acc = 0.f;
+    for (unsigned m = 0; m < nzi; ++m) acc = fmaf(__ldg(Sz + z * nzi + m), col[m * 32 + xl], acc);
+    out[3 * (x + nxi * y + z * st) + c] = acc;
+  }
+}
+
 __global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const float* __restrict__ Y, const float* __restrict__ Sx,
                                                      float* __restrict__ efull) {
   pdl_entry();
@@ -963,14 +1008,25 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const float* Sz = Sy + nyi * nyi;
     const float* Dinv = Sz + nzi * nzi;
     const unsigned nb = blocks_for(3 * N, 256);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_gather, g, R, E);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sx, nxi, 1, nullptr);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sy, nyi, nxi, nullptr);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sz, nzi, nxi * nyi, Dinv);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sz, nzi, nxi * nyi, nullptr);
-    pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sy, nyi, nxi, nullptr);
+    if (nzi <= kZZMaxN) {
+      // x pass from r (full layout) -> E, y -> R, z (scaled) z -> E, y -> R, x -> e (full)
+      pdl_launch(c->stream, nb, 256, 0, k_dst_first, g, (const float*)R, E, Sx);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, (const float*)E, R, Sy, nyi, nxi, (const float*)nullptr);
+      pdl_launch(c->stream, dim3((nxi + 31) / 32, nyi, 3), 256, (size_t)nzi * 32 * sizeof(float), k_dst_zz, nxi, nyi,
+                 nzi, (const float*)R, E, Sz, Dinv);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, (const float*)E, R, Sy, nyi, nxi, (const float*)nullptr);
+      *nl += 4;
+    } else {
+      pdl_launch(c->stream, nb, 256, 0, k_dst_gather, g, R, E);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sx, nxi, 1, nullptr);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sy, nyi, nxi, nullptr);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sz, nzi, nxi * nyi, Dinv);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sz, nzi, nxi * nyi, nullptr);
+      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sy, nyi, nxi, nullptr);
+      *nl += 6;
+    }
     pdl_launch(c->stream, blocks_for(3 * g.points(), 256), 256, 0, k_dst_scatter, g, R, Sx, E);
-    *nl += 7;
+    ++*nl;
   } else {
     SmallLevels S;
     S.n = P.nlev - fs;
