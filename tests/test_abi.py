@@ -99,3 +99,22 @@ def test_invalid_config_rejected(built_lib):
     with pytest.raises(vg.VgError) as e:
         vg.Context(cfg)
     assert e.value.status == vg.INVALID
+
+
+def test_batch_and_particle_entry_points_reject_bad_arguments(built_lib):
+    """Argument checks of the batch solver, team-barrier, wind, kill-age and
+    heat-PSE entry points happen before any device call, so they hold
+    without a GPU."""
+    import vortegrid_gb300 as vg
+    L = vg.lib()
+    i = ctypes.c_int()
+    assert L.vg_batch_set_solver(None, 1, 8, 0) == vg.INVALID
+    assert L.vg_batch_solver_info(None, ctypes.byref(i), None, None, None) == vg.INVALID
+    for ctas, missing, ms in ((0, 0, 10.0), (4, 5, 10.0), (4, -1, 10.0), (4, 0, 0.0), (4, 0, 20000.0)):
+        assert L.vg_team_barrier_check(0, ctas, missing, ms, ctypes.byref(i), ctypes.byref(i)) == vg.INVALID
+    wind = (ctypes.c_float * 3)(1.0, 0.0, 0.0)
+    assert L.vg_wind_device(None, None, 0, wind, 0.1, 0.9) == vg.INVALID
+    m = ctypes.c_size_t()
+    assert L.vg_kill_age_device(None, None, None, None, None, 0, 0, 0, ctypes.byref(m)) == vg.INVALID
+    g = vg.GridGeom.make([0.0] * 3, [1.0] * 3, [5] * 3)
+    assert L.vg_heat_pse_device(None, ctypes.byref(g), None, None, 0, 0.01, 1.0, 0.1) == vg.INVALID
