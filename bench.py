@@ -15,7 +15,7 @@ Keys beyond the base contract:
     reference's 96-byte Particle records + vg_advect on tracer records, from
     pinned host memory, copies included);
   * "roofline": the direct-sum kernel against the FP32 pipe (2 flops x 128
-    lanes x 152 SMs x the SM clock sampled during the run), 26 algorithmic
+    lanes x the device's SM count x the SM clock sampled during the run), 26 algorithmic
     flops per interaction;
   * "cpu_baseline": the reference's own direct sum (built from its sources,
     std::thread TBB stand-in, all host threads) on the same workload;
@@ -338,11 +338,13 @@ def run_ours(args, world, rank, local):
     kms = a.elapsed_time(b) / reps
     achieved = FLOPS_PER_INTERACTION * interactions() / (kms * 1e-3) / 1e12
     clk_mhz = result["clocks"].get("sm_mhz") or 2070.0
-    peak = 2 * 128 * 152 * clk_mhz * 1e6 / 1e12
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = 2 * 128 * sms * clk_mhz * 1e6 / 1e12
     result["roofline"] = {"bound": "fp32", "kernel": "k_direct_pair (+ k_reduce_pair)",
                           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                           "traffic": profiled_traffic("direct_pair_ring4096.md"), "ms_per_launch": kms,
-                          "peak_basis": f"2 flops x 128 FP32 lanes x 152 SMs x {clk_mhz:.0f} MHz (sampled median)",
+                          "peak_basis": f"2 flops x 128 FP32 lanes x {sms} SMs (device attribute) x {clk_mhz:.0f} MHz "
+                                        "(sampled median)",
                           "flops_per_interaction": FLOPS_PER_INTERACTION,
                           "gint_per_s_kernel": interactions() / (kms * 1e-3) / 1e9}
 
@@ -460,19 +462,129 @@ def treecode_section(vg, torch, stream, local, steps=3):
         lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), ps0.shape[0], vg._ptr(q), q.shape[0], 1.0, 1.0,
                              vg._ptr(refg))
         ctx.synchronize()
+        # the treecode alone (cell lists, tree build, walk) at every gridpoint and vorton, for its roofline
+        gq = f4(workloads.grid_points(list(geom.min_corner), list(geom.cell_spacing), geom.points))
+        qa = torch.cat([gq, ps0]).contiguous()
+        outa = torch.zeros_like(qa)
+        npts = ctypes.c_size_t()
+        tms = []
+        for k in range(4):
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            ctx.check(lib.vg_tree_device(ctx.h, 0, ctypes.byref(geom), vg._ptr(ps0), vg._ptr(w0), ps0.shape[0],
+                                         vg._ptr(qa), qa.shape[0], 1.0, 1.0, vg._ptr(outa), None, 0,
+                                         ctypes.byref(npts)), "vg_tree_device")
+            b.record(stream)
+            ctx.synchronize()
+            if k > 0:
+                tms.append(a.elapsed_time(b))
     v = vel[:, :3].cpu().double()
     r = ref[:, :3].cpu().double()
     vg_s = torch.from_numpy(vgrid[idx].astype(np.float64))
     rg = refg[:, :3].cpu().double()
     t = statistics.median(ms)
     nq = geom.capacity + len(pos)
-    return {"workload": "8 rings, 65536 vortons in [-2,2]^3; treecode (NestedGrid, bit-exact binning) at every "
-                        "gridpoint and vorton; 1048576 tracers gathered + Euler; stretch and diffusion off",
-            "grid_points": grid_np, "tree_depth": st.tree_depth, "step_ms": t,
-            "queries_per_s": nq / (t * 1e-3), "tracers_per_s": len(tr) / (t * 1e-3),
-            "rel_l2_vs_direct_at_vortons": float((v - r).norm() / r.norm()),
-            "rel_l2_vs_direct_at_gridpoints": float((vg_s - rg).norm() / rg.norm()),
-            "note": "treecode error is the far-field monopole approximation plus the grid's auto-mollification"}
+    qh = qa.cpu().numpy()[:, :3]
+    per_query = tree_interactions(geom.points, list(geom.min_corner), list(geom.extent), qh) / len(qh)
+    tree_ms = statistics.median(tms)
+    sms = torch.cuda.get_device_properties(local).multi_processor_count
+    peak = 2 * 128 * sms * 2070.0 * 1e6 / 1e12
+    achieved = FLOPS_PER_INTERACTION * per_query * qa.shape[0] / (tree_ms * 1e-3) / 1e12
+    out = {"workload": "8 rings, 65536 vortons in [-2,2]^3; treecode (NestedGrid, bit-exact binning) at every "
+                       "gridpoint and vorton; 1048576 tracers gathered + Euler; stretch and diffusion off",
+           "grid_points": grid_np, "tree_depth": st.tree_depth, "step_ms": t,
+           "queries_per_s": nq / (t * 1e-3), "tracers_per_s": len(tr) / (t * 1e-3),
+           "rel_l2_vs_direct_at_vortons": float((v - r).norm() / r.norm()),
+           "rel_l2_vs_direct_at_gridpoints": float((vg_s - rg).norm() / rg.norm()),
+           "note": "treecode error is the far-field monopole approximation plus the grid's auto-mollification "
+                   "(the reference's own treecode has the same error: tests/test_gpu_config_parity.py)",
+           "roofline": {"bound": "fp32 (issue: a dependent walk of few interactions per query)",
+                        "kernel": "vg_tree_device: cell lists, tree build and walk at every gridpoint and vorton",
+                        "ms_per_call": tree_ms, "interactions_per_query": per_query,
+                        "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
+                        "peak_basis": f"2 flops x 128 FP32 lanes x {sms} SMs x 2070 MHz (maximum clock)"}}
+    out["cpu_baseline"] = treecode_cpu_baseline(pos, w, s, geom, qh, tr, vgrid)
+    return out
+
+
+def tree_interactions(points, min_corner, extent, q):
+    """Pair laws the NestedGrid walk (vortonSim.cpp:1650-1905) evaluates over
+    the queries q.  From the root, each layer examines every child of the
+    cells opened above it; a child containing the query (its cell widened by
+    1e-4 spacings, vortonSim.cpp:1707-1719) is opened, the others add one
+    pair law each, and the leaf's parent adds all its children.  The open test
+    is a conjunction over axes, so the examined and opened sets are products
+    of per-axis ranges; the test is evaluated in FP32 as the walk does.  The
+    layer rule is NestedGrid's (nestedGrid.h:69-85, uniformGrid.h:398-412,
+    794-809)."""
+    f32 = np.float32
+    q = np.ascontiguousarray(q, f32)
+    layers = [np.array([int(v) for v in points], np.int64)]
+    while np.prod(layers[-1]) > 8:
+        layers.append(np.maximum(2, (layers[-1] - 1) // 2 + 1))
+    depth = len(layers)
+    if depth < 2:
+        return 0
+    mn = np.array(min_corner[:3], f32)
+    ext = np.array(extent[:3], f32)
+    cell = [(ext / (L - 1).astype(f32)).astype(f32) for L in layers]
+    dec = [None] + [(layers[l - 1] - 1) // (layers[l] - 1) for l in range(1, depth)]
+    lo = np.zeros((len(q), 3), np.int64)
+    hi = np.zeros((len(q), 3), np.int64)
+    alive = np.ones(len(q), bool)
+    total = 0
+    for layer in range(depth - 1, 0, -1):
+        c_cell = cell[layer - 1]
+        d = dec[layer]
+        elo, ehi = lo * d, hi * d + d - 1
+        examined = np.where(alive, np.prod(ehi - elo + 1, axis=1), 0)
+        if layer == 1:
+            total += int(examined.sum())
+            break
+        margin = (f32(0.0001) * c_cell).astype(f32)
+        olo = np.full_like(lo, np.iinfo(np.int64).max)
+        ohi = np.full_like(hi, -1)
+        for k in range(int((ehi - elo).max()) + 1):
+            c = elo + k
+            cmin = (mn + (c.astype(f32) * c_cell).astype(f32)).astype(f32)
+            cmax = (mn + ((c + 1).astype(f32) * c_cell).astype(f32)).astype(f32)
+            inside = (c <= ehi) & (q >= (cmin - margin).astype(f32)) & (q < (cmax + margin).astype(f32))
+            olo = np.where(inside & (c < olo), c, olo)
+            ohi = np.where(inside & (c > ohi), c, ohi)
+        nopen = np.prod(np.where(ohi >= olo, ohi - olo + 1, 0), axis=1)
+        nopen = np.where(alive, nopen, 0)
+        total += int((examined - nopen).sum())
+        alive = alive & (nopen > 0)
+        lo, hi = np.where(alive[:, None], olo, 0), np.where(alive[:, None], ohi, 0)
+    return total
+
+
+def treecode_cpu_baseline(pos, w, s, geom, q, tr, vgrid):
+    """The reference's treecode (CreateInfluenceTree + ComputeVelocity_Tree at
+    every gridpoint and vorton, vortonSim.cpp:1192-1905) and its tracer
+    advection through the same velocity grid, on all host threads."""
+    L = reference_lib()
+    if L is None:
+        return None
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    g12 = geom.as12()
+    np3 = np.array(geom.points, np.uint32)
+    q = np.ascontiguousarray(q, np.float32)
+    out = np.zeros((len(q), 3), np.float32)
+    t0 = time.perf_counter()
+    L.vgref_tree(0, P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), P(q), ctypes.c_size_t(len(q)),
+                 ctypes.c_float(1.0), ctypes.c_float(1.0), P(out))
+    t1 = time.perf_counter()
+    t = np.ascontiguousarray(tr, np.float32).copy()
+    tv = np.zeros_like(t)
+    vg3 = np.ascontiguousarray(vgrid, np.float32)
+    t2 = time.perf_counter()
+    L.vgref_advect(P(t), P(tv), ctypes.c_size_t(len(t)), P(g12), P(np3), P(vg3), ctypes.c_float(DT))
+    t3 = time.perf_counter()
+    return {"value": (t1 - t0 + t3 - t2) * 1e3, "unit": "ms per step (treecode at every query + tracer advection)",
+            "cores": int(os.environ["NUMBER_OF_PROCESSORS"]), "kind": "reference", "tree_ms": (t1 - t0) * 1e3,
+            "advect_ms": (t3 - t2) * 1e3, "queries_per_s": len(q) / (t1 - t0),
+            "sample": f"one step: {len(q)} treecode queries, {len(t)} tracers"}
 
 
 def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 60.0):
@@ -528,10 +640,66 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
             "timing": "host wall clock over the frames plus one synchronisation (graph launches are asynchronous)"}
 
 
+MG_BYTES_PER_POINT_CYCLE = 250  # V(2,2) over the levels: smoothing, residual + restriction, prolongation + correction
+ADVECT_BYTES_PER_TRACER = 48     # float4 position read and written, float4 velocity written
+N_TRACERS_POISSON = 1 << 22
+
+
+def measured_peaks():
+    """HBM and BF16 peaks measured on this GPU type (MEASURED_PEAKS.json), else the stated fallback."""
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            d = json.load(fh)
+        return {"hbm_gbs": float(d["hbm_gbs"]), "bf16_tflops": float(d["bf16_tflops"]), "basis": "measured"}
+    except (OSError, KeyError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "basis": "fallback"}
+
+
+def poisson_cpu_baseline(pos, w, s, g12, np3, tr):
+    """The reference's own solve on the same problem, all host threads: its
+    boundary vector potential (ComputeVectorPotentialAtGridpoints_Slice,
+    boundaries only) and its multigrid cascade at its fixed work (16 SOR
+    sweeps per level, vortonSim.cpp:2523-2608), with the relative residual it
+    reaches; and its tracer advection (AssignVelocityFromField + Evolve,
+    pclOpAdvect.cpp:42-81, pclOpEvolve.cpp:36-58) of the same tracers."""
+    import oracle
+    L = reference_lib()
+    if L is None:
+        return None
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    cores = int(os.environ["NUMBER_OF_PROCESSORS"])
+    npts = int(np3[0]) * int(np3[1]) * int(np3[2])
+    b = np.zeros((npts, 3), np.float32)
+    L.vgref_splat(P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), ctypes.c_float(-1.0), P(b))
+    a = np.zeros((npts, 3), np.float32)
+    t0 = time.perf_counter()
+    L.vgref_boundary_vecpot(P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), 1, P(a))
+    t1 = time.perf_counter()
+    L.vgref_cascade(P(g12), P(np3), P(a), P(b), 16)
+    t2 = time.perf_counter()
+    og = oracle.Geom.from12(g12, np3)
+    relres = oracle.relres(og, a, b)
+    vel = np.zeros((npts, 3), np.float32)
+    jac = np.zeros((npts, 9), np.float32)
+    L.vgref_jacobian_curl(P(g12), P(np3), P(a), P(jac), P(vel))
+    t = np.ascontiguousarray(tr, np.float32).copy()
+    tv = np.zeros_like(t)
+    t3 = time.perf_counter()
+    L.vgref_advect(P(t), P(tv), ctypes.c_size_t(len(t)), P(g12), P(np3), P(vel), ctypes.c_float(DT))
+    t4 = time.perf_counter()
+    return {"value": (t2 - t0) * 1e3, "unit": "ms per solve (boundary + cascade)", "cores": cores,
+            "kind": "reference", "boundary_ms": (t1 - t0) * 1e3, "cascade_ms": (t2 - t1) * 1e3,
+            "relres": relres, "advect_ms": (t4 - t3) * 1e3, "advect_tracers_per_s": len(t) / (t4 - t3),
+            "sample": f"one solve of the same 129^3 problem; {len(t)} tracers advected once"}
+
+
 def poisson_section(vg, torch, stream, local, steps=3):
     """128^3 vector-potential solve to 1e-6 on the puff workload through the
     library's own step, from three starts: zero (plain multigrid), the learned
-    network (its guess is timed inside the solve) and the previous frame."""
+    network (its guess is timed inside the solve) and the previous frame; the
+    same zero-start solve on the fixed schedule (no host round trip); 4M
+    tracers advected through the step's velocity grid; the reference's own
+    solve and advection on the host cores beside it."""
     from vortegrid_gb300 import workloads, warmstart
     pos, w, s = workloads.puff(262144, seed=3)
     grid = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [129] * 3)
@@ -542,6 +710,10 @@ def poisson_section(vg, torch, stream, local, steps=3):
     o2 = np.zeros((len(pos), 4), np.float32)
     o2[:, :3] = w
     w0 = torch.from_numpy(o2).cuda()
+    tr = np.random.default_rng(6).uniform(-1.9, 1.9, (N_TRACERS_POISSON, 3)).astype(np.float32)
+    o3 = np.zeros((len(tr), 4), np.float32)
+    o3[:, :3] = tr
+    tr0 = torch.from_numpy(o3).cuda()
 
     def make_ctx(warm):
         cfg = vg.default_config(fixed_grid=grid, device=local)
@@ -575,9 +747,65 @@ def poisson_section(vg, torch, stream, local, steps=3):
     zero_ctx = make_ctx(0)
     zero = summary(run(zero_ctx, True))
     out = {"workload": "puff: 262144 vortons N(0,0.5^2), vorticity N(0,2^2), 129^3 grid on [-2,2]^3 (dx=1/32), "
-                       "treecode boundary, FP32 V(2,2)-cycles in FP64 iterative refinement to 1e-6",
+                       "treecode boundary, FP32 V(2,2)-cycles in FP64-class iterative refinement to 1e-6; "
+                       "4194304 tracers advected",
            "tolerance": 1e-6, "plain_mg_ms": zero["ms"], "step_ms": zero["step_ms"], "cycles": zero["cycles"],
-           "relres0": zero["relres0"], "relres": zero["relres"]}
+           "relres0": zero["relres0"], "relres": zero["relres"],
+           "timing": "CUDA events around the solve inside the step; the adaptive schedule reads a residual back "
+                     "to the host after each phase (fixed_schedule below has no round trip)"}
+    # velocity error at 512 interior points against the FP64 direct sum (tests/golden/puff129_exact.npz)
+    try:
+        fx = np.load(os.path.join(ROOT, "tests", "golden", "puff129_exact.npz"))
+        vz, _ = zero_ctx.GetVelocityGrid()
+        got = vz[fx["flat"]].astype(np.float64)
+        d = fx["direct"]
+        out["velocity_rel_l2_vs_fp64_direct"] = float(np.linalg.norm(got - d) / np.linalg.norm(d))
+        out["velocity_rel_l2_vs_exact_discrete"] = float(np.linalg.norm(got - fx["exact_vel"]) /
+                                                         np.linalg.norm(fx["exact_vel"]))
+        out["exact_discrete_rel_l2_vs_fp64_direct"] = float(np.linalg.norm(fx["exact_vel"] - d) / np.linalg.norm(d))
+        out["velocity_note"] = ("512 interior gridpoints; the puff's vortons lie closer than dx, so the grid "
+                                "discretisation error dominates (the exact discrete solution has the same)")
+    except OSError:
+        pass
+    # the same solve on the fixed schedule the adaptive one used (no host round trip)
+    k1, k2 = zero_ctx.poisson_schedule()
+    zero_ctx.set_poisson_schedule(k1, k2)
+    fixed = summary(run(zero_ctx, True))
+    zero_ctx.set_poisson_schedule(0, 0)
+    st_fixed = zero_ctx.stats()
+    out["fixed_schedule"] = {"ms": fixed["ms"], "fp32_cycles": k1, "refinement_cycles": k2,
+                             "relres": st_fixed.poisson_relres}
+    peaks = measured_peaks()
+    pts = grid.capacity
+    best_ms = min(zero["ms"], fixed["ms"])
+    achieved = MG_BYTES_PER_POINT_CYCLE * pts * zero["cycles"] / (best_ms * 1e-3) / 1e9
+    out["roofline"] = {"bound": "hbm", "kernel": "multigrid solve (all its kernels)", "achieved": achieved,
+                       "peak": peaks["hbm_gbs"], "unit": "GB/s", "frac": achieved / peaks["hbm_gbs"],
+                       "peak_basis": peaks["basis"], "traffic": None,
+                       "algorithmic_bytes": f"{MG_BYTES_PER_POINT_CYCLE} B per fine point per V(2,2) cycle x "
+                                            f"{pts} points x {zero['cycles']} cycles",
+                       "note": "the level-0 fields (52 MB) stay in the 129 MB L2; the fraction is of HBM peak"}
+    # 4M tracers through the step's velocity grid (AssignVelocityFromField + Evolve)
+    trp, trv = tr0.clone(), torch.zeros_like(tr0)
+    ams = []
+    with torch.cuda.stream(stream):
+        for k in range(4):
+            trp.copy_(tr0)
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            zero_ctx.AdvectDevice(trp, trv, float(DT))
+            b.record(stream)
+            zero_ctx.synchronize()
+            if k > 0:
+                ams.append(a.elapsed_time(b))
+    adv = statistics.median(ams)
+    adv_bytes = ADVECT_BYTES_PER_TRACER * len(tr) + pts * 12
+    out["tracers"] = {"count": len(tr), "advect_ms": adv, "tracers_per_s": len(tr) / (adv * 1e-3),
+                      "roofline": {"bound": "hbm", "achieved": adv_bytes / (adv * 1e-3) / 1e9,
+                                   "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                                   "frac": adv_bytes / (adv * 1e-3) / 1e9 / peaks["hbm_gbs"],
+                                   "algorithmic_bytes": f"{ADVECT_BYTES_PER_TRACER} B per tracer + the grid once"}}
+    out["step_with_tracers_ms"] = zero["step_ms"] + adv
     prev = summary(run(make_ctx(1), False))
     out["previous_frame"] = {"ms": prev["ms"], "cycles": prev["cycles"], "relres0": prev["relres0"],
                              "relres": prev["relres"], "note": "field evolving one step between solves"}
@@ -596,6 +824,11 @@ def poisson_section(vg, torch, stream, local, steps=3):
     else:
         out["nn_warm_start_ms"] = None
         out["nn_note"] = "no trained weights at " + warmstart.DEFAULT_WEIGHTS
+    g12 = grid.as12()
+    np3 = np.array(grid.points, np.uint32)
+    cpu = poisson_cpu_baseline(pos, w, s, g12, np3, tr)
+    if cpu is not None:
+        out["cpu_baseline"] = cpu
     return out
 
 

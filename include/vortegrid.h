@@ -158,6 +158,19 @@ vg_status vg_get_velocity_grid_device(vg_ctx* ctx, const float** dev_xyz, vg_gri
 vg_status vg_get_vector_potential(vg_ctx* ctx, float* xyz, size_t cap_points, vg_grid_geom* geom);
 /* Statistics of the last step (waits for that step to finish). */
 vg_status vg_get_stats(vg_ctx* ctx, vg_step_stats* stats);
+
+/* Multigrid schedule of a context's Poisson solves.  The default (0, 0) is
+ * adaptive: FP32 cycles until the relative residual is near FP32's reach,
+ * then refinement rounds until poisson_tolerance, with a residual read back to
+ * the host after each phase.  A fixed schedule (fp32_cycles > 0) runs exactly
+ * fp32_cycles FP32 cycles and then refinement_cycles refinement cycles with no
+ * host round trip, so a step can be captured in a CUDA graph; its residuals
+ * are read at vg_get_stats.  vg_get_poisson_schedule returns the counts the
+ * last adaptive solve used (a calibration for the fixed schedule).  No
+ * counterpart in the reference, whose cascade runs a fixed sweep count
+ * (vortonSim.cpp:2539-2571). */
+vg_status vg_set_poisson_schedule(vg_ctx* ctx, int fp32_cycles, int refinement_cycles);
+vg_status vg_get_poisson_schedule(const vg_ctx* ctx, int* fp32_cycles, int* refinement_cycles);
 /* Wait for the context's stream and report any error a device stage flagged
  * since the last synchronising call (VG_OUT_OF_GRID, VG_NONFINITE).  The
  * *_device entry points do not synchronise; host-buffer calls do this
@@ -202,6 +215,18 @@ vg_status vg_define_shape(size_t n, const float vmin[3], const float vmax[3], in
  * idx3 uint32[3 m] and offset uint32[m] for m float4 positions. */
 vg_status vg_bin_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos4, size_t m, unsigned* idx3,
                         unsigned* offset);
+
+/* Particles::PartitionParticles as called by VortonSim::PartitionVortons
+ * (Particles/particle.cpp:398-437, VortonFluid/vortonSim.cpp:3578-3607): the
+ * cell lists of n float4 positions on grid g.  For each point offset c
+ * (OffsetOfPosition), items[start[c] .. start[c+1]) are the indices binned
+ * there in ascending order, as the reference's push_back in index order
+ * leaves them.  start has points + 2 entries: list `points` holds vortons
+ * outside the grid or not finite (undefined behaviour in the reference), and
+ * start[points + 1] = n.  items has n entries.  Device pointers, context
+ * stream. */
+vg_status vg_partition_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos4, size_t n, unsigned* start,
+                              unsigned* items);
 
 /* ComputeVelocity_Direct / ComputeVectorPotential_Direct
  * (VortonFluid/vortonSim.cpp:1113-1158) at m query points (float4) from n
@@ -281,19 +306,29 @@ vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const floa
  * application that gives this library a fixed memory budget up front, a
  * real-time frame that must not stall on the allocator's implicit device
  * synchronisation, or an embedding that forbids the CUDA allocator.  Same
- * arguments and results as vg_direct_device (FAST numerics), but it takes no
- * context and allocates nothing: its scratch is one fixed 8 MiB device array
- * inside this library, held by every GPU that loads the library until the
- * process exits.
+ * arguments as vg_direct_device (FAST numerics), but it takes no context and
+ * allocates nothing: its scratch is one fixed 8 MiB device array inside this
+ * library, reserved when the library's device code is loaded on a device
+ * (with lazy module loading, at the first call there) and held by that device
+ * until the process exits.
+ *  - Results: the kernels and source split of vg_direct_device, so they are
+ *    bit-identical to it unless the 8 MiB cap forces fewer source chunks; then
+ *    they are equal within rounding (the partial sums are grouped
+ *    differently).
  *  - Limits: n <= 32768 sources and m <= (8 MiB - 32 n) / 12 targets;
  *    larger calls return VG_TOO_LARGE (use vg_direct_device).
- *  - The first call on each device looks up that array's device address on
- *    the current device; make that first call before any stream capture.
- *  - Every call uses the same array: calls that can overlap on the GPU (on
- *    different streams, or on one stream from different host threads) race
- *    and must be ordered by the caller.
+ *  - Each call looks up the array's address on the current device (this
+ *    allocates nothing).  On a device where the library's device code is not
+ *    loaded yet, that lookup loads it: make the first call on each device
+ *    before any stream capture.
+ *  - Every call uses the same array and leaves its contents behind; nothing
+ *    in it needs clearing, since each call writes every byte it reads.  Calls
+ *    that can overlap on the GPU (on different streams, or on one stream from
+ *    different host threads) race and must be ordered by the caller.
  *  - Runs on `stream` (a cudaStream_t; NULL = the legacy default stream) and
- *    returns without synchronising.  Errors: vg_last_error(NULL). */
+ *    returns without synchronising.  Errors: vg_last_error(NULL); a launch
+ *    failure is reported from that launch's own return code, so errors other
+ *    code left pending are not consumed. */
 vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_size, const float* angvel, size_t n,
                             const float* q4, size_t m, float spread_range, float spread_circ, float* out4);
 

@@ -24,7 +24,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "liboracle.so")
 REF_DIR = os.path.join(HERE, "_ref")
-REF_TREE = "/root/reference/Samples/MjgIntelFluidDemo_Part20"
+# Location of a VorteGrid checkout to stage the reference build from (no default:
+# hosts without it use an already staged copy in _ref/src, or the C oracle alone).
+REF_TREE = os.environ.get("VG_REFERENCE_TREE", "")
 
 
 def build(quiet=True):
@@ -37,7 +39,7 @@ def build(quiet=True):
         subprocess.check_call(["gcc", "-O2", "-std=c99", "-fPIC", "-shared", "-ffp-contract=off",
                                "-o", LIB, src, "-lm"])
     staged = os.path.join(REF_DIR, "src", ".staged")
-    if not os.path.exists(staged) and os.path.isdir(REF_TREE):
+    if not os.path.exists(staged) and REF_TREE and os.path.isdir(REF_TREE):
         subprocess.check_call(["python3", os.path.join(HERE, "ref_build", "prepare.py"), REF_TREE],
                               stdout=subprocess.DEVNULL if quiet else None)
     if os.path.exists(staged):
@@ -92,6 +94,7 @@ def lib():
         _lib.vgo_nested_shape.restype = ctypes.c_int
         _lib.vgo_relres_f64.restype = ctypes.c_double
         _lib.vgo_relres_f64d.restype = ctypes.c_double
+        _lib.vgo_tree_interactions.restype = ctypes.c_size_t
     return _lib
 
 
@@ -126,6 +129,15 @@ def indices_of_position(g, pos):
     return idx, off
 
 
+def partition(g, pos):
+    """PartitionParticles cell lists: (start[points + 2], items[n])."""
+    pos = f32(pos)
+    start = np.zeros(g.capacity + 2, np.uint32)
+    items = np.zeros(max(len(pos), 1), np.uint32)
+    lib().vgo_partition(ctypes.byref(g), _p(pos), ctypes.c_size_t(len(pos)), _p(start), _p(items))
+    return start, items[: len(pos)]
+
+
 def nested_shape(g):
     layers = (Geom * 32)()
     dec = np.zeros(96, np.uint32)
@@ -156,6 +168,12 @@ def tree(kind, pos, angvel, size, g, q, spread_range=1.0, spread_circ=1.0):
     lib().vgo_tree(ctypes.c_int(kind), _p(pos), _p(angvel), _p(size), ctypes.c_size_t(len(pos)), ctypes.byref(g),
                    _p(q), ctypes.c_size_t(len(q)), ctypes.c_float(spread_range), ctypes.c_float(spread_circ), _p(out))
     return out
+
+
+def tree_interactions(g, q):
+    """Pair laws the treecode walk evaluates over the queries q."""
+    q = f32(q)
+    return int(lib().vgo_tree_interactions(ctypes.byref(g), _p(q), ctypes.c_size_t(len(q))))
 
 
 def splat(pos, angvel, size, g, scale=-1.0):

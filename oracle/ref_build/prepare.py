@@ -23,7 +23,7 @@ import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE = os.path.dirname(HERE)
-DEFAULT_REF = "/root/reference/Samples/MjgIntelFluidDemo_Part20"
+SAMPLE = os.path.join("Samples", "MjgIntelFluidDemo_Part20")
 DST = os.path.join(ORACLE, "_ref", "src")
 
 SUBDIRS = ["Core", "VortonFluid", "Particles", "Sim", "FluidBodySim",
@@ -138,8 +138,21 @@ def apply_edits():
                 fh.write(t)
 
 
+def reference_sample(root):
+    """The newest sample snapshot inside a VorteGrid checkout at `root` (or
+    `root` itself when it already is that snapshot)."""
+    inner = os.path.join(root, SAMPLE)
+    return inner if os.path.isdir(inner) else root
+
+
 def main():
-    ref = sys.argv[1] if len(sys.argv) > 1 else DEFAULT_REF
+    # The checkout's location comes from the command line or VG_REFERENCE_TREE;
+    # there is no built-in default.
+    root = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("VG_REFERENCE_TREE", "")
+    if not root:
+        print("prepare.py: give the VorteGrid checkout as an argument or in VG_REFERENCE_TREE; nothing staged")
+        return 1
+    ref = reference_sample(root)
     if not os.path.isdir(ref):
         print(f"prepare.py: reference tree not found at {ref}; nothing staged")
         return 1

@@ -123,6 +123,39 @@ void vgo_indices_batch(const vgo_geom* g, const float* pos, size_t n, unsigned* 
 
 static size_t capacity(const vgo_geom* g) { return (size_t)g->np[0] * g->np[1] * g->np[2]; }
 
+/* Particles::PartitionParticles (Particles/particle.cpp:398-437), as called by
+ * VortonSim::PartitionVortons (VortonFluid/vortonSim.cpp:3578-3607): walking
+ * the particles in index order, each index is appended to the list of the
+ * grid point OffsetOfPosition names, so every list is in ascending index
+ * order.  Lists are returned flattened: items[start[c] .. start[c+1]) for
+ * point c.  A particle whose indices fall outside the points (undefined
+ * behaviour in the reference) or whose position is not finite goes to the
+ * extra list `points`; start has points + 2 entries. */
+void vgo_partition(const vgo_geom* g, const float* pos, size_t n, unsigned* start, unsigned* items) {
+  const size_t pts = capacity(g);
+  size_t c;
+  unsigned* fill;
+  for (c = 0; c < pts + 2; ++c) start[c] = 0;
+  unsigned* cell = (unsigned*)malloc(n * sizeof(unsigned) + 1);
+  for (size_t k = 0; k < n; ++k) {
+    const float* p = pos + 3 * k;
+    unsigned i[3];
+    vgo_indices_of_position(g, p, i);
+    size_t off = i[0] + (size_t)g->np[0] * (i[1] + (size_t)g->np[1] * i[2]);
+    if (i[0] >= g->np[0] || i[1] >= g->np[1] || i[2] >= g->np[2] || off >= pts || p[0] != p[0] || p[1] != p[1] ||
+        p[2] != p[2])
+      off = pts;
+    cell[k] = (unsigned)off;
+    start[off + 1]++;
+  }
+  for (c = 0; c < pts + 1; ++c) start[c + 1] += start[c];
+  fill = (unsigned*)malloc((pts + 1) * sizeof(unsigned));
+  for (c = 0; c < pts + 1; ++c) fill[c] = start[c];
+  for (size_t k = 0; k < n; ++k) items[fill[cell[k]]++] = (unsigned)k;
+  free(fill);
+  free(cell);
+}
+
 /* NestedGrid::Initialize + PrecomputeDecimations (nestedGrid.h:69-85, 355-391):
  * layer 0 copies g; each parent decimates its child by 2 until the child has
  * at most 8 points.  decim3[3l..3l+2] = child cells / parent cells (l >= 1). */
@@ -418,6 +451,54 @@ static void tree_query(const tree_t* t, int kind, const float* pos, const float*
     for (size_t i = 0; i < n; ++i) accum(kind, acc, q, pos + 3 * i, angvel + 3 * i, size[i], sr, sc);
     memcpy(out, acc, sizeof(acc));
   }
+}
+
+/* The number of pair laws the walk of tree_eval evaluates for query q: the
+ * same open test (vortonSim.cpp:1707-1719), counting instead of adding. */
+static size_t tree_count(const vgo_geom* layers, const unsigned* decim, const float q[3], const unsigned idx[3],
+                         int layer) {
+  const vgo_geom* C = &layers[layer - 1];
+  const unsigned* d = decim + 3 * layer;
+  const float margin_factor = 0.0001f;
+  float margin[3] = {margin_factor * C->cell[0], margin_factor * C->cell[1], margin_factor * C->cell[2]};
+  margin[2] = margin[2] + (0.0f == C->cell[2] ? FLT_MIN : 0.0f);
+  size_t count = 0;
+  for (unsigned iz = 0; iz < d[2]; ++iz) {
+    unsigned ch[3];
+    ch[2] = idx[2] * d[2] + iz;
+    const float mnz = C->mn[2] + (float)ch[2] * C->cell[2];
+    const float mxz = C->mn[2] + (float)(ch[2] + 1) * C->cell[2];
+    for (unsigned iy = 0; iy < d[1]; ++iy) {
+      ch[1] = idx[1] * d[1] + iy;
+      const float mny = C->mn[1] + (float)ch[1] * C->cell[1];
+      const float mxy = C->mn[1] + (float)(ch[1] + 1) * C->cell[1];
+      for (unsigned ix = 0; ix < d[0]; ++ix) {
+        ch[0] = idx[0] * d[0] + ix;
+        const float mnx = C->mn[0] + (float)ch[0] * C->cell[0];
+        const float mxx = C->mn[0] + (float)(ch[0] + 1) * C->cell[0];
+        if (layer > 1 && q[0] >= mnx - margin[0] && q[1] >= mny - margin[1] && q[2] >= mnz - margin[2] &&
+            q[0] < mxx + margin[0] && q[1] < mxy + margin[1] && q[2] < mxz + margin[2])
+          count += tree_count(layers, decim, q, ch, layer - 1);
+        else
+          count += 1;
+      }
+    }
+  }
+  return count;
+}
+
+/* Total pair laws of the treecode walk (ComputeVelocity_Tree from the root)
+ * over m queries on the NestedGrid of g: the interaction count behind the
+ * treecode's FP32 roofline. */
+size_t vgo_tree_interactions(const vgo_geom* g, const float* q, size_t m) {
+  vgo_geom layers[VGO_MAX_LAYERS];
+  unsigned dec[3 * VGO_MAX_LAYERS];
+  static const unsigned zeros[3] = {0, 0, 0};
+  const int depth = vgo_nested_shape(g, layers, dec);
+  size_t total = 0;
+  if (depth < 2) return 0;
+  for (size_t j = 0; j < m; ++j) total += tree_count(layers, dec, q + 3 * j, zeros, depth - 1);
+  return total;
 }
 
 void vgo_tree(int kind, const float* pos, const float* angvel, const float* size, size_t n, const vgo_geom* g,

@@ -42,6 +42,10 @@ void vgo_decimate(const vgo_geom* src, unsigned dec, vgo_geom* dst);
 void vgo_indices_of_position(const vgo_geom* g, const float p[3], unsigned idx[3]);
 unsigned vgo_offset_of_position(const vgo_geom* g, const float p[3]);
 void vgo_indices_batch(const vgo_geom* g, const float* pos, size_t n, unsigned* idx3, unsigned* offset);
+/* Pair laws the treecode walk evaluates over m queries (its interaction count). */
+size_t vgo_tree_interactions(const vgo_geom* g, const float* q, size_t m);
+/* PartitionParticles cell lists: items[start[c]..start[c+1]) per point c; start has points+2 entries. */
+void vgo_partition(const vgo_geom* g, const float* pos, size_t n, unsigned* start, unsigned* items);
 int vgo_nested_shape(const vgo_geom* g, vgo_geom* layers, unsigned* decim3);
 void vgo_bbox(const float* pos, size_t n, float mn[3], float mx[3]);
 void vgo_step_geometry(const float* pos, size_t n, float radius, const float* extra_min, const float* extra_max,

@@ -237,3 +237,47 @@ def test_kill_age_permutation_properties(oracle_lib, n, seed):
     for k, i in enumerate(holes):
         want[i] = movers[k]
     assert np.array_equal(order, want)
+
+
+def test_partition_is_stable_index_order(oracle_lib, golden):
+    """PartitionParticles (Particles/particle.cpp:398-437) appends indices in
+    particle order, so each list is ascending: the oracle's lists equal a
+    stable sort of the particles by OffsetOfPosition, with the extra list
+    (index `points`) for positions outside the grid."""
+    O = oracle_lib
+    g = geom_of(O, golden)
+    pos = np.concatenate([golden["bin_pos"], np.array([[1e6, 0, 0], [np.nan, 0, 0]], np.float32)])
+    idx, off = O.indices_of_position(g, pos)
+    inside = (idx < np.array(g.points, np.uint32)).all(1) & np.isfinite(pos).all(1)
+    key = np.where(inside, off, g.capacity)
+    start, items = O.partition(g, pos)
+    assert np.array_equal(items, np.argsort(key, kind="stable"))
+    assert np.array_equal(np.diff(start.astype(np.int64)), np.bincount(key, minlength=g.capacity + 1))
+    assert start[-1] == len(pos) and key[-1] == key[-2] == g.capacity
+
+
+def test_tree_matches_reference_at_treecode_workload_size(oracle_lib):
+    """The oracle's influence tree and treecode walk equal the reference's own
+    code on the treecode workload (65,536 vortons in 8 rings, 64^3 cells,
+    depth-7 NestedGrid), bit for bit."""
+    import ctypes
+    O = oracle_lib
+    if not O.ref_available("serial"):
+        pytest.skip("reference code not built on this host")
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.rings(65536, count=8, seed=2, box=2.0)
+    g = O.step_geometry(pos, float(s[0]) * 0.5)
+    assert g.points == (65, 65, 65)
+    L = O.ref("serial")
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    g12, np3 = g.as12(), np.array(g.points, np.uint32)
+    n = L.vgref_influence_tree(P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), None, ctypes.c_size_t(0))
+    rt = np.zeros((n, 7), np.float32)
+    L.vgref_influence_tree(P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), P(rt), ctypes.c_size_t(n))
+    assert np.array_equal(bits(O.influence_tree(pos, w, s, g)), bits(rt))
+    q = np.concatenate([workloads.grid_points(list(g.mn), list(g.cell), g.points)[::97], pos[::31]]).astype(np.float32)
+    for kind in (0, 1):
+        out = np.zeros((len(q), 3), np.float32)
+        L.vgref_tree(kind, P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), P(q), ctypes.c_size_t(len(q)),
+                     ctypes.c_float(2.5), ctypes.c_float(0.6), P(out))
+        assert np.array_equal(bits(O.tree(kind, pos, w, s, g, q, 2.5, 0.6)), bits(out)), kind

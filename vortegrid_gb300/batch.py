@@ -158,6 +158,20 @@ class Batch:
             raise VgError(st, "vg_get_stats: " + lib().vg_last_error(ctx).decode())
         return s
 
+    def velocity_grid(self, i):
+        """Simulation i's velocity grid from its last step (after synchronize()):
+        (float32[points, 3], GridGeom)."""
+        ctx = lib().vg_batch_context(self.h, i)
+        g = GridGeom()
+        st = lib().vg_get_velocity_grid(ctx, None, 0, ctypes.byref(g))
+        if st != OK:
+            raise VgError(st, "vg_get_velocity_grid: " + lib().vg_last_error(ctx).decode())
+        out = np.zeros((g.capacity, 3), np.float32)
+        st = lib().vg_get_velocity_grid(ctx, out.ctypes.data_as(ctypes.c_void_p), g.capacity, ctypes.byref(g))
+        if st != OK:
+            raise VgError(st, "vg_get_velocity_grid: " + lib().vg_last_error(ctx).decode())
+        return out, g
+
     def graph_info(self):
         """(graphs launched per frame, largest graph's nodes, total nodes)."""
         g, mx, tot = ctypes.c_int(), ctypes.c_size_t(), ctypes.c_size_t()

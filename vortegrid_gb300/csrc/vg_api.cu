@@ -91,6 +91,24 @@ int nested_shape(const Geom& g, Geom* layers, unsigned (*decim)[3]) {  // nested
 
 // ------------------------------------------------------------------ context
 
+int sm_count() {
+  static int cached[64] = {0};
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    cudaGetLastError();
+    return 1;
+  }
+  if (!cached[dev]) {
+    int sms = 0;
+    if (cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess || sms < 1) {
+      cudaGetLastError();
+      sms = 1;
+    }
+    cached[dev] = sms;
+  }
+  return cached[dev];
+}
+
 vg_status fail(Ctx* c, vg_status s, const std::string& msg) {
   if (c) c->err = msg;
   return s;
@@ -853,6 +871,33 @@ vg_status vg_bin_device(vg_ctx* c, const vg_grid_geom* g, const float* pos4, siz
   if (m == 0) return VG_OK;
   pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_bin_only, to_geom(*g), (const float4*)pos4, (int)m, idx3, offset);
   VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status vg_set_poisson_schedule(vg_ctx* c, int k1, int k2) {
+  if (!c || k1 < 0 || k2 < 0 || (k1 == 0 && k2 != 0)) return VG_INVALID;
+  c->mg_fixed_k1 = k1;
+  c->mg_fixed_k2 = k2;
+  return VG_OK;
+}
+
+vg_status vg_get_poisson_schedule(const vg_ctx* c, int* k1, int* k2) {
+  if (!c || !k1 || !k2) return VG_INVALID;
+  *k1 = c->mg_last_k1;
+  *k2 = c->mg_last_k2;
+  return VG_OK;
+}
+
+vg_status vg_partition_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos4, size_t n, unsigned* start,
+                              unsigned* items) {
+  if (!c || !gg || !start || (n && (!pos4 || !items))) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, (const float4*)pos4, n, &cl);
+  if (st != VG_OK) return st;
+  VG_CUDA(c, cudaMemcpyAsync(start, cl.start, (g.points() + 2) * sizeof(unsigned), cudaMemcpyDeviceToDevice,
+                             c->stream));
+  if (n) VG_CUDA(c, cudaMemcpyAsync(items, cl.items, n * sizeof(unsigned), cudaMemcpyDeviceToDevice, c->stream));
   return VG_OK;
 }
 

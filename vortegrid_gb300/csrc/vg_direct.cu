@@ -19,7 +19,7 @@
 // Reference path: one thread per query, sources in index order, the
 // reference's operation order (bit-identical to the CPU).
 #include <algorithm>
-#include <mutex>
+#include <string>
 
 #include "vg_internal.cuh"
 
@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(kThreads) k_direct_ref(const float4* __restric
 unsigned direct_slots(int kind) {
   static unsigned cached[2] = {0, 0};
   if (!cached[kind]) {
-    int dev = 0, sms = kSMs, per_sm = 1;
+    int dev = 0, sms = sm_count(), per_sm = 1;
     cudaGetDevice(&dev);
     cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
     if (kind == 0)
@@ -315,6 +315,22 @@ unsigned direct_slots(int kind) {
     cached[kind] = (unsigned)std::max(1, sms) * (unsigned)std::max(1, per_sm);
   }
   return cached[kind];
+}
+
+// Split the sources into `ksplit` chunks so that target blocks x chunks
+// fills the resident CTA slots of the GPU (SMs x CTAs per SM) once, with no
+// partial second wave; every CTA then does the same amount of work.  Returns
+// the chunk length.
+int direct_split(int kind, size_t n, size_t m, unsigned* tblocks_out, unsigned* ksplit_out) {
+  const unsigned tblocks = blocks_for(m, kind == 0 ? kPairThreads * kPairTPT : kThreads * kTPT);
+  const unsigned slots = direct_slots(kind);
+  unsigned ksplit = std::max(1u, slots / tblocks);
+  const size_t min_chunk = 64;  // keep each CTA's source loop long enough to amortise its set-up
+  if (n / ksplit < min_chunk) ksplit = (unsigned)std::max<size_t>(1, n / min_chunk);
+  const int chunk = (int)((n + ksplit - 1) / ksplit);
+  *ksplit_out = (unsigned)((n + chunk - 1) / chunk);
+  *tblocks_out = tblocks;
+  return chunk;
 }
 
 }  // namespace
@@ -337,16 +353,8 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
     VG_CUDA(c, cudaGetLastError());
     return VG_OK;
   }
-  // Split the sources into `ksplit` chunks so that target blocks x chunks
-  // fills the resident CTA slots of the GPU (SMs x CTAs per SM) once, with no
-  // partial second wave; every CTA then does the same amount of work.
-  const unsigned tblocks = blocks_for(m, kind == 0 ? kPairThreads * kPairTPT : kThreads * kTPT);
-  const unsigned slots = direct_slots(kind);
-  unsigned ksplit = std::max(1u, slots / tblocks);
-  const size_t min_chunk = 64;  // keep each CTA's source loop long enough to amortise its set-up
-  if (n / ksplit < min_chunk) ksplit = (unsigned)std::max<size_t>(1, n / min_chunk);
-  const int chunk = (int)((n + ksplit - 1) / ksplit);
-  ksplit = (unsigned)((n + chunk - 1) / chunk);
+  unsigned tblocks = 0, ksplit = 0;
+  const int chunk = direct_split(kind, n, m, &tblocks, &ksplit);
   vg_status st = VG_OK;
   if (kind == 0) {
     float* partial = nullptr;
@@ -396,9 +404,11 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
 // up front, code running inside a real-time frame where an allocation's
 // implicit device synchronisation would stall the frame, or an embedding that
 // forbids the CUDA allocator altogether.  For them the scratch that the
-// split-source direct sum needs (per-source constants and per-target partial
-// sums) lives in one file-scope device array, reserved when the library is
-// loaded and held by every GPU that loads it until the process exits.
+// split-source direct sum needs (per-target partial sums, and for the vector
+// potential the per-source constants) lives in one file-scope device array.
+// It is reserved when this library's device code is loaded on a device --
+// with lazy module loading, at the first call that needs it there -- and is
+// held by that device until the process exits.
 namespace vg {
 namespace {
 
@@ -406,9 +416,20 @@ constexpr size_t kNoAllocScratchBytes = size_t(8) << 20;  // 8 MiB
 constexpr size_t kNoAllocMaxSources = 32768;              // 1 MiB of per-source constants
 static __device__ __align__(256) unsigned char g_noalloc_scratch[kNoAllocScratchBytes];
 
-std::mutex g_noalloc_mu;
-void* g_noalloc_ptr[64];  // per device: g_noalloc_scratch's device address
-bool g_noalloc_ready[64];
+// A plain launch whose own error code is returned (no stream-wide error query
+// that could report, and clear, an error some other code left behind).
+template <typename... KArgs, typename... Args>
+cudaError_t launch_plain(cudaStream_t s, dim3 grid, dim3 block, void (*kernel)(KArgs...), Args... args) {
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = grid;
+  cfg.blockDim = block;
+  cfg.stream = s;
+  return cudaLaunchKernelEx(&cfg, kernel, args...);
+}
+
+vg_status noalloc_fail(cudaError_t e, const char* what) {
+  return set_noctx_error(VG_CUDA_ERROR, std::string("vg_direct_noalloc: ") + what + ": " + cudaGetErrorString(e));
+}
 
 }  // namespace
 
@@ -425,63 +446,64 @@ extern "C" vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_
   if (n > kNoAllocMaxSources)
     return set_noctx_error(VG_TOO_LARGE, "vg_direct_noalloc: more than 32768 sources (the fixed scratch holds "
                                          "32768 sources' constants); use vg_direct_device");
+  if (m > 0x7fffffff) return set_noctx_error(VG_TOO_LARGE, "vg_direct_noalloc: more than 2^31 targets");
   const size_t src_bytes = ((n * sizeof(float4) + 255) / 256) * 256;
   const size_t room = kNoAllocScratchBytes - 2 * src_bytes;
   if (m * 3 * sizeof(float) > room)
     return set_noctx_error(VG_TOO_LARGE, "vg_direct_noalloc: too many targets for the fixed 8 MiB scratch "
                                          "(at most (8 MiB - 32 n) / 12 targets); use vg_direct_device");
-  int dev = 0;
-  cudaError_t e = cudaGetDevice(&dev);
-  if (e != cudaSuccess || dev < 0 || dev >= 64)
-    return set_noctx_error(VG_CUDA_ERROR, "vg_direct_noalloc: no current CUDA device");
+  // The array's device address on the current device.  Host code holds only
+  // a stand-in for the symbol; the address is looked up on every call (it
+  // allocates nothing), so it stays right after cudaDeviceReset or a change
+  // of context.  On a device where this library's device code is not loaded
+  // yet, the lookup loads it: make the first call on each device before any
+  // stream capture.
   void* base = nullptr;
-  {
-    // First call on this device: look up where the loader placed the array
-    // on this device (host code only holds a stand-in for the symbol).
-    std::lock_guard<std::mutex> lock(g_noalloc_mu);
-    if (!g_noalloc_ready[dev]) {
-      void* p = nullptr;
-      e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
-      if (e != cudaSuccess || !p) {
-        cudaGetLastError();
-        return set_noctx_error(VG_CUDA_ERROR, std::string("vg_direct_noalloc: cudaGetSymbolAddress failed: ") +
-                                                  cudaGetErrorString(e));
-      }
-      g_noalloc_ptr[dev] = p;
-      g_noalloc_ready[dev] = true;
-    }
-    base = g_noalloc_ptr[dev];
-  }
+  cudaError_t e = cudaGetSymbolAddress(&base, g_noalloc_scratch);
+  if (e != cudaSuccess || !base) return noalloc_fail(e, "cudaGetSymbolAddress");
   cudaStream_t st = (cudaStream_t)stream;
   if (n == 0) {
     e = cudaMemsetAsync(out4, 0, m * sizeof(float4), st);
-    return e == cudaSuccess ? VG_OK : set_noctx_error(VG_CUDA_ERROR, cudaGetErrorString(e));
+    return e == cudaSuccess ? VG_OK : noalloc_fail(e, "cudaMemsetAsync");
   }
-  // Same split as vg_direct_device, capped so the partial sums fit the array.
-  const unsigned tblocks = blocks_for(m, kThreads * kTPT);
-  unsigned ksplit = 1;
-  while (tblocks * ksplit < 4u * kSMs && (n / (ksplit * 2)) >= (size_t)kTile &&
-         (size_t)(ksplit * 2) * m * 3 * sizeof(float) <= room)
-    ksplit *= 2;
-  const int chunk = (int)((n + ksplit - 1) / ksplit);
+  // The kernels and the split of vg_direct_device, with the split capped so
+  // the partial sums fit the array: wherever the cap does not bind, the
+  // results are bit-identical to vg_direct_device's.
+  unsigned tblocks = 0, ksplit = 0;
+  int chunk = direct_split(kind, n, m, &tblocks, &ksplit);
+  while (ksplit > 1 && (size_t)ksplit * m * 3 * sizeof(float) > room) {
+    const unsigned k = ksplit - 1;
+    chunk = (int)((n + k - 1) / k);
+    ksplit = (unsigned)((n + chunk - 1) / chunk);
+  }
   float4* s0 = (float4*)base;
   float4* s1 = (float4*)((char*)base + src_bytes);
   float* partial = (float*)((char*)base + 2 * src_bytes);
   // Every scratch byte read below is written earlier in this call, so nothing
   // needs clearing between calls.
-  if (kind == 0)
-    k_prep_sources<0><<<blocks_for(n, 256), 256, 0, st>>>((const float4*)pos_size, (const float4*)angvel, (int)n,
-                                                           spread_range, spread_circ, s0, s1);
-  else
-    k_prep_sources<1><<<blocks_for(n, 256), 256, 0, st>>>((const float4*)pos_size, (const float4*)angvel, (int)n,
-                                                           spread_range, spread_circ, s0, s1);
-  dim3 grid(tblocks, ksplit);
-  if (kind == 0)
-    k_direct_fast<0><<<grid, kThreads, 0, st>>>(s0, s1, (int)n, chunk, (const float4*)q4, (int)m, partial);
-  else
-    k_direct_fast<1><<<grid, kThreads, 0, st>>>(s0, s1, (int)n, chunk, (const float4*)q4, (int)m, partial);
-  k_reduce_partials<<<blocks_for(m, 256), 256, 0, st>>>(partial, (int)ksplit, (int)m, (float4*)out4);
-  e = cudaGetLastError();
-  if (e != cudaSuccess) return set_noctx_error(VG_CUDA_ERROR, cudaGetErrorString(e));
+  const float4* ps = (const float4*)pos_size;
+  const float4* w = (const float4*)angvel;
+  const float4* q = (const float4*)q4;
+  float4* out = (float4*)out4;
+  if (kind == 0) {
+    e = launch_plain(st, dim3(tblocks, ksplit), dim3(kPairThreads), k_direct_pair, ps, w, (int)n, chunk, spread_range,
+                     spread_circ, q, (int)m, ksplit > 1 ? partial : (float*)nullptr, out);
+    if (e != cudaSuccess) return noalloc_fail(e, "k_direct_pair launch");
+    if (ksplit > 1) {
+      e = launch_plain(st, dim3(blocks_for(m, 256)), dim3(256), k_reduce_pair, (const float*)partial, (int)ksplit,
+                       (int)m, out, (float*)nullptr, 0, (float4*)nullptr);
+      if (e != cudaSuccess) return noalloc_fail(e, "k_reduce_pair launch");
+    }
+    return VG_OK;
+  }
+  e = launch_plain(st, dim3(blocks_for(n, 256)), dim3(256), k_prep_sources<1>, ps, w, (int)n, spread_range,
+                   spread_circ, s0, s1);
+  if (e != cudaSuccess) return noalloc_fail(e, "k_prep_sources launch");
+  e = launch_plain(st, dim3(tblocks, ksplit), dim3(kThreads), k_direct_fast<1>, (const float4*)s0, (const float4*)s1,
+                   (int)n, chunk, q, (int)m, partial);
+  if (e != cudaSuccess) return noalloc_fail(e, "k_direct_fast launch");
+  e = launch_plain(st, dim3(blocks_for(m, 256)), dim3(256), k_reduce_partials, (const float*)partial, (int)ksplit,
+                   (int)m, out);
+  if (e != cudaSuccess) return noalloc_fail(e, "k_reduce_partials launch");
   return VG_OK;
 }

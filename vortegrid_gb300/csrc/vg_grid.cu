@@ -611,7 +611,7 @@ vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6) {
   pdl_launch(c->stream, 1, 32, 0, k_bbox_init, keys);
   if (n > 0) {
     unsigned blocks = blocks_for(n, 256);
-    if (blocks > 4u * kSMs) blocks = 4u * kSMs;
+    if (blocks > 4u * (unsigned)sm_count()) blocks = 4u * (unsigned)sm_count();
     pdl_launch(c->stream, blocks, 256, 0, k_bbox, pos, (int)n, keys, c->dflag);
   }
   pdl_launch(c->stream, 1, 32, 0, k_bbox_finish, keys, out6);

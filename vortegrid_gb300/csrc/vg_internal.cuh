@@ -19,7 +19,9 @@
 namespace vg {
 
 constexpr int kMaxLayers = 24;
-constexpr int kSMs = 152;  // GB300
+// Streaming multiprocessors of the current device (cudaDevAttrMultiProcessorCount,
+// queried once per device); grids sized in whole waves use it.
+int sm_count();
 
 // Grid geometry on the device: identical fields to vg_grid_geom.
 struct Geom {

@@ -40,7 +40,7 @@ namespace nn {
 namespace {
 
 constexpr int kLayers = 15;
-constexpr int kRedBlocks = 2 * kSMs;
+constexpr int kRedBlocks = 304;  // partial sums of the norm reductions (a fixed width)
 constexpr float kSlope = 0.1f;  // leaky ReLU: v > 0 ? v : kSlope v
 
 struct LayerDesc {
@@ -469,7 +469,7 @@ vg_status backward(Ctx* c, Net* N) {
     if ((st = conv3_wgrad(c, layer_input(N, l), N->g[l], L.co, N->grad + N->wofs[l])) != VG_OK) return st;
     {
       const int lanes = 256 / L.co;
-      unsigned nb = (unsigned)std::min<size_t>((nv + lanes - 1) / lanes, 4 * kSMs);
+      unsigned nb = (unsigned)std::min<size_t>((nv + lanes - 1) / lanes, 4 * (size_t)sm_count());
       k_colsum<<<nb, 256, 0, c->stream>>>(N->g[l], nv, L.co, N->grad + N->bofs[l]);
       VG_LAUNCHED(c);
     }

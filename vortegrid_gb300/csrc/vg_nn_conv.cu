@@ -447,7 +447,7 @@ vg_status launch_resident(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, con
   int per_sm = 0;
   VG_CUDA(c, cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_conv3_fwd_resident<CO_T>, kWarps * 32, smem));
   const long items = (long)T.nx * T.ny * T.nz * ncog;
-  long grid = std::min<long>(items, (long)std::max(per_sm, 1) * kSMs);
+  long grid = std::min<long>(items, (long)std::max(per_sm, 1) * sm_count());
   grid = std::max<long>(ncog, grid / ncog * ncog);
   k_conv3_fwd_resident<CO_T><<<(unsigned)grid, kWarps * 32, smem, c->stream>>>(in, wt, out, ncog);
   VG_LAUNCHED(c);
@@ -480,7 +480,7 @@ vg_status conv3_fwd(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const Con
   const long tiles = (long)T.nx * T.ny * T.nz;
   int co_t = 16;
   for (int w : {64, 32}) {
-    if (out.Co % w == 0 && tiles * (out.Co / w) >= 2L * kSMs) {
+    if (out.Co % w == 0 && tiles * (out.Co / w) >= 2L * sm_count()) {
       co_t = w;
       break;
     }
@@ -509,7 +509,7 @@ vg_status conv3_wgrad(Ctx* c, const ConvIn& in, const __nv_bfloat16* dy, int Co,
   const Tile T = make_tile(in.D, in.H, in.W);
   const int ntiles = T.nx * T.ny * T.nz;
   const int blocks_cc = (Co / 16) * ((in.C1 + in.C2) / 16);
-  int splits = (4 * kSMs + blocks_cc - 1) / blocks_cc;
+  int splits = (4 * sm_count() + blocks_cc - 1) / blocks_cc;
   if (splits > ntiles) splits = ntiles;
   if (splits < 1) splits = 1;
   k_conv3_wgrad<<<dim3((unsigned)blocks_cc, (unsigned)splits), kWarps * 32, 0, c->stream>>>(in, dy, Co, dw);

@@ -273,7 +273,7 @@ vg_status launch_umma(Ctx* c, const ConvIn& in, const __nv_bfloat16* wt, const C
   constexpr int kCols = CO_T <= 32 ? 32 : 64;
   const int per_sm = std::max(1, std::min<int>(std::min<int>((228 * 1024) / (int)(smem + 1024), 512 / kCols), 8));
   const long items = (long)(in.W / kTX) * (in.H / kTY) * in.D * ncog;
-  long grid = std::min<long>(items, (long)std::max(per_sm, 1) * kSMs);
+  long grid = std::min<long>(items, (long)std::max(per_sm, 1) * sm_count());
   grid = std::max<long>(ncog, grid / ncog * ncog);
   k_conv3_umma<CO_T><<<(unsigned)grid, 128, smem, c->stream>>>(in, wt, out, ncog, c->dflag);
   VG_LAUNCHED(c);
