@@ -55,24 +55,32 @@ def rel(a, b):
     return np.linalg.norm(np.asarray(a, np.float64) - b) / np.linalg.norm(b)
 
 
-def test_noalloc_matches_direct_device_and_fp64_twice(oracle_lib):
+@pytest.mark.parametrize("kind,n", [(0, 4096), (1, 4096), (1, 1024)])
+def test_noalloc_matches_direct_device_and_fp64_twice(oracle_lib, kind, n):
+    """The direct-sum workload's ring and targets (the 33^3 gridpoints and the
+    vortons).  Where vg_direct_device's source split fits the 8 MiB array
+    (velocity; vector potential from 1,024 sources) the sums are bit-identical
+    to it; where the array caps the split (vector potential from 4,096
+    sources: ~30 chunks x 40k targets x 12 B) the partial sums are grouped
+    differently and equal within rounding."""
     import vortegrid_gb300 as vg
     from vortegrid_gb300 import workloads
-    pos, w, s = workloads.ring(4096, seed=1)
+    pos, w, s = workloads.ring(n, seed=1)
     q = np.concatenate([workloads.grid_points([-1.5] * 3, [3 / 32] * 3, [33] * 3), pos]).astype(np.float32)
     ps, wd, qd = f4(pos, s), f4(w), f4(q)
     ctx = vg.Context()
-    for kind in (0, 1):
-        r = device_sum(vg, ctx, kind, ps, wd, qd)
-        exact = oracle_lib.direct(kind, pos, w, s, q, f64=True)
-        for call in range(2):
-            out = torch.full((len(q), 4), float("nan"), dtype=torch.float32, device="cuda")
-            got = noalloc(vg, kind, ps, wd, len(pos), qd, out)
-            assert np.all(np.isfinite(got))
+    r = device_sum(vg, ctx, kind, ps, wd, qd)
+    exact = oracle_lib.direct(kind, pos, w, s, q, f64=True)
+    capped = kind == 1 and n > 1024
+    for call in range(2):
+        out = torch.full((len(q), 4), float("nan"), dtype=torch.float32, device="cuda")
+        got = noalloc(vg, kind, ps, wd, len(pos), qd, out)
+        assert np.all(np.isfinite(got))
+        if not capped:
             assert np.array_equal(got.view(np.uint32), r.view(np.uint32)), (kind, call)
-            # the direct-sum tolerance used throughout the tests (rel-L2 1e-5)
-            assert rel(got, r) < 1e-5, (kind, call)
-            assert rel(got, exact) < 1e-5, (kind, call, rel(got, exact))
+        # the direct-sum tolerance used throughout the tests (rel-L2 1e-5)
+        assert rel(got, r) < 1e-5, (kind, call)
+        assert rel(got, exact) < 1e-5, (kind, call, rel(got, exact))
 
 
 def test_noalloc_at_the_size_limit():
