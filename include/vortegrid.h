@@ -296,6 +296,59 @@ vg_status vg_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_siz
 vg_status vg_heat_pse_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, float* density, size_t n,
                              float diffusivity, float ambient_density, float dt);
 
+/* VortonSim::PopulateDensityAndMassFractionGrids, density part
+ * (vortonSim.cpp:2911-3016): n vortons' densities (mDensity) times their
+ * volume (pi/6 size^3 of the first vorton, particle.h:225-228) over the cell
+ * volume, spread trilinearly onto grid g (UniformGrid::Accumulate,
+ * uniformGrid.h:1278-1342, summed at each point in vorton order), plus the
+ * ambient density times max(1 - contribution, 0) at every point.  density_grid
+ * has one float per point.  Mass fractions (combustion) are not computed. */
+vg_status vg_density_grid_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, const float* density,
+                                 size_t n, float ambient_density, float* density_grid);
+
+/* ComputeGradient (uniformGridMath.cpp:468-503, 650-800) of a scalar grid:
+ * centred differences inside, one-sided on the faces; grad3 float[3] per point. */
+vg_status vg_gradient_device(vg_ctx* ctx, const vg_grid_geom* g, const float* scalar, float* grad3);
+
+/* Baroclinic generation of vorticity on the density-grid path of
+ * VortonSim::GenerateBaroclinicVorticity (vortonSim.cpp:3407-3547) and
+ * GenerateBaroclinicVorticitySlice (vortonSim.cpp:3318-3392): the density grid
+ * of the vortons (vg_density_grid_device), its gradient, the gradient at each
+ * vorton, then angvel += 0.5 (grad x (grav / ambient_density)) dt.  *applied is
+ * 0 when the grid has no extent along gravity (the reference's early return).
+ * Combustion (CombustAndSetMassFractions) is not run. */
+vg_status vg_baroclinic_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, const float* density,
+                               float* angvel, size_t n, const float grav[3], float ambient_density, float dt,
+                               int* applied);
+
+/* PopulateSignedDistanceGridFromDensityGrid (vortonSim.cpp:3266-3290) with
+ * ComputeImmediateSDFFromDensity_Nearest and
+ * ComputeRemainingSDFFromImmediateSDF_Nearest (pclOpEmit.cpp:696-1060): the
+ * signed distance (negative inside the heavy fluid) of a density grid, NaN
+ * where no surface is reached.  reference_stats = 1 sums the density
+ * statistics in FP32 point order as the reference does (one GPU thread; the
+ * result is then the reference's bit for bit); 0 sums them in FP64 in
+ * parallel (the surface moves by ~1e-6 of the distances). */
+vg_status vg_signed_distance_device(vg_ctx* ctx, const vg_grid_geom* g, const float* density_grid,
+                                    float ambient_density, int reference_stats, float* sdf);
+
+/* Isosurface of a scalar grid by marching cubes, as ExtractIsoLevel /
+ * PolygoniseCellWithNormal do (Render/Resource/marchingCubes.cpp:580-866),
+ * into device buffers instead of a vertex buffer: cells in z, y, x order; per
+ * triangle 9 floats of vertex positions (the reference's VertexInterp on each
+ * crossing edge, corners at min + index x spacing) and, when normals is not
+ * NULL, 9 floats of its unit face normal repeated per vertex.  Corners below
+ * iso_level are inside; normals point away from them.  The triangulation of
+ * each cell is generated by this library (the reference's lookup tables are
+ * not used), so triangle connectivity can differ from the reference's in
+ * cells with an ambiguous face; the vertex positions on each crossing edge
+ * follow the reference's arithmetic.  *triangles receives the count; if it
+ * exceeds max_triangles nothing is written and VG_TOO_LARGE is returned (the
+ * reference's RESULT_INSUFFICIENT_CAPACITY).  Synchronises the context's
+ * stream. */
+vg_status vg_marching_cubes_device(vg_ctx* ctx, const vg_grid_geom* g, const float* values, float iso_level,
+                                   float* vertices, float* normals, size_t max_triangles, size_t* triangles);
+
 /* AssignParticleVelocityFromField (gain 1) + EvolveParticlesSlice on float4
  * positions with grid vel3; vel4 (optional) receives the gathered velocity. */
 vg_status vg_gather_advect_device(vg_ctx* ctx, const vg_grid_geom* g, const float* vel3, float* pos4, float* vel4,

@@ -95,6 +95,8 @@ def lib():
         _lib.vgo_relres_f64.restype = ctypes.c_double
         _lib.vgo_relres_f64d.restype = ctypes.c_double
         _lib.vgo_tree_interactions.restype = ctypes.c_size_t
+        _lib.vgo_baroclinic.restype = ctypes.c_int
+        _lib.vgo_marching_cubes.restype = ctypes.c_size_t
     return _lib
 
 
@@ -265,6 +267,57 @@ def heat_pse(pos, density, size, g, diffusivity, ambient, dt, symmetric=False):
     fn(_p(f32(pos)), _p(d), _p(f32(size)), ctypes.c_size_t(len(d)), ctypes.byref(g), ctypes.c_float(diffusivity),
        ctypes.c_float(ambient), ctypes.c_float(dt))
     return d
+
+
+def density_grid(pos, size, density, g, ambient):
+    """PopulateDensityAndMassFractionGrids (density): float32[points]."""
+    out = np.zeros(g.capacity, np.float32)
+    d = np.ascontiguousarray(density, np.float32)
+    lib().vgo_density_grid(_p(f32(pos)), _p(f32(size)), _p(d), ctypes.c_size_t(len(d)), ctypes.byref(g),
+                           ctypes.c_float(ambient), _p(out))
+    return out
+
+
+def gradient(g, v):
+    """ComputeGradient of a scalar grid: float32[points, 3]."""
+    out = np.zeros((g.capacity, 3), np.float32)
+    lib().vgo_gradient(ctypes.byref(g), _p(np.ascontiguousarray(v, np.float32)), _p(out))
+    return out
+
+
+def baroclinic(pos, angvel, size, density, g, grav, ambient, dt):
+    """Baroclinic generation on the density-grid path: (applied, new angvel)."""
+    w = f32(angvel).copy()
+    d = np.ascontiguousarray(density, np.float32)
+    r = lib().vgo_baroclinic(_p(f32(pos)), _p(w), _p(f32(size)), _p(d), ctypes.c_size_t(len(d)), ctypes.byref(g),
+                             _p(f32(grav)), ctypes.c_float(ambient), ctypes.c_float(dt))
+    return bool(r), w
+
+
+def signed_distance(g, density, ambient, sumstats=0):
+    """PopulateSignedDistanceGridFromDensityGrid: float32[points] (NaN where unreached).
+    sumstats 0: the reference's float sums for the density statistics; 1: double sums."""
+    out = np.zeros(g.capacity, np.float32)
+    lib().vgo_signed_distance(ctypes.byref(g), _p(np.ascontiguousarray(density, np.float32)), ctypes.c_float(ambient),
+                              ctypes.c_int(sumstats), _p(out))
+    return out
+
+
+def marching_cubes(g, v, iso):
+    """Isosurface triangles: (positions float32[t, 3, 3], normals float32[t, 3, 3])."""
+    v = np.ascontiguousarray(v, np.float32)
+    n = lib().vgo_marching_cubes(ctypes.byref(g), _p(v), ctypes.c_float(iso), None, None, ctypes.c_size_t(0))
+    verts = np.zeros((max(n, 1), 3, 3), np.float32)
+    norms = np.zeros((max(n, 1), 3, 3), np.float32)
+    lib().vgo_marching_cubes(ctypes.byref(g), _p(v), ctypes.c_float(iso), _p(verts), _p(norms), ctypes.c_size_t(n))
+    return verts[:n], norms[:n]
+
+
+def marching_cubes_table():
+    cnt = np.zeros(256, np.int32)
+    tri = np.zeros((256, 15), np.int32)
+    lib().vgo_marching_cubes_table(_p(cnt), _p(tri))
+    return cnt, tri
 
 
 def kill_age(birth, frame, age_max):

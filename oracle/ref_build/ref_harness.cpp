@@ -525,4 +525,86 @@ void vgref_wind(float* vel_inout, size_t n, const float wind[3], float wind_weig
   }
 }
 
+// PopulateDensityAndMassFractionGrids (VortonFluid/vortonSim.cpp:2911-3057):
+// the density grid on the grid template from n vortons with per-vorton
+// densities (mass fractions are not returned).
+void vgref_density_grid(const float* pos, const float* size, const float* density, size_t n, const float geom12[12],
+                        const unsigned np[3], float ambient, float* out) {
+  std::vector<float> zeros(3 * n, 0.0f);
+  Sim s(pos, zeros.data(), size, n, geom12, np, 0.0f);
+  for (size_t i = 0; i < n; ++i) s.vortons[i].mDensity = density[i];
+  s.sim.mAmbientDensity = ambient;
+  UniformGrid<float> dg;
+  s.sim.PopulateDensityAndMassFractionGrids(dg, reinterpret_cast<VECTOR<Particle>&>(s.vortons), 0);
+  for (size_t i = 0; i < dg.GetGridCapacity(); ++i) out[i] = dg[i];
+}
+
+// ComputeGradient (Core/SpatialPartition/uniformGridMath.cpp:650-800) of a scalar grid.
+void vgref_gradient(const float geom12[12], const unsigned np[3], const float* scalar, float* out3) {
+  UniformGrid<float> v;
+  load_geom(v, geom12, np);
+  v.Init(0.0f);
+  for (size_t i = 0; i < v.GetGridCapacity(); ++i) v[i] = scalar[i];
+  UniformGrid<Vec3> g;
+  g.CopyShape(v);
+  g.Init();
+  ComputeGradient(g, v);
+  grid_to_floats(g, out3);
+}
+
+// Baroclinic generation on the grid-density path of
+// VortonSim::GenerateBaroclinicVorticity (vortonSim.cpp:3407-3547, the branch
+// without per-vorton SPH gradients): density grid, its gradient
+// (ComputeGradient), the gradient interpolated at each vorton
+// (UniformGrid::Interpolate), then the reference's own
+// GenerateBaroclinicVorticitySlice (vortonSim.cpp:3318-3392) on those
+// gradients.  Returns 0 when the grid has no extent along gravity (the
+// reference's early return, vortonSim.cpp:3417-3421).
+int vgref_baroclinic(const float* pos, float* angvel_inout, const float* size, const float* density, size_t n,
+                     const float geom12[12], const unsigned np[3], const float grav[3], float ambient, float dt) {
+  Sim s(pos, angvel_inout, size, n, geom12, np, 0.0f);
+  for (size_t i = 0; i < n; ++i) s.vortons[i].mDensity = density[i];
+  s.sim.mAmbientDensity = ambient;
+  s.sim.mGravAccel = Vec3(grav[0], grav[1], grav[2]);
+  s.sim.mVelGrid.CopyShape(s.sim.mGridTemplate);
+  if (fabsf(s.sim.mGravAccel * s.sim.mVelGrid.GetExtent()) < FLT_EPSILON) return 0;
+  s.sim.PopulateDensityAndMassFractionGrids(s.sim.mDensityGrid, reinterpret_cast<VECTOR<Particle>&>(s.vortons), 0);
+  s.sim.mDensityGradientGrid.Clear();
+  s.sim.mDensityGradientGrid.CopyShape(s.sim.mGridTemplate);
+  s.sim.mDensityGradientGrid.Init();
+  ComputeGradient(s.sim.mDensityGradientGrid, s.sim.mDensityGrid);
+  VECTOR<Vec3> grads;
+  grads.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Vec3 g;
+    s.sim.mDensityGradientGrid.Interpolate(g, s.vortons[i].mPosition);
+    grads.PushBack(g);
+  }
+  s.sim.GenerateBaroclinicVorticitySlice(dt, &grads, 0, n);
+  for (size_t i = 0; i < n; ++i) {
+    angvel_inout[3 * i] = s.vortons[i].mAngularVelocity.x;
+    angvel_inout[3 * i + 1] = s.vortons[i].mAngularVelocity.y;
+    angvel_inout[3 * i + 2] = s.vortons[i].mAngularVelocity.z;
+  }
+  return 1;
+}
+
+// PopulateSignedDistanceGridFromDensityGrid (vortonSim.cpp:3266-3290): the
+// signed distance grid of a density grid (negative inside the heavy fluid;
+// points no crossing reaches come back as NaN).
+void vgref_signed_distance(const float geom12[12], const unsigned np[3], const float* density, float ambient,
+                           float* out) {
+  std::vector<float> zeros(3, 0.0f);
+  float one = 1.0f;
+  Sim s(zeros.data(), zeros.data(), &one, 1, geom12, np, 0.0f);
+  s.sim.mAmbientDensity = ambient;
+  s.sim.mDensityGrid.Clear();
+  load_geom(s.sim.mDensityGrid, geom12, np);
+  s.sim.mDensityGrid.Init(0.0f);
+  for (size_t i = 0; i < s.sim.mDensityGrid.GetGridCapacity(); ++i) s.sim.mDensityGrid[i] = density[i];
+  UniformGrid<float> sdf;
+  s.sim.PopulateSignedDistanceGridFromDensityGrid(sdf, s.sim.mDensityGrid, 0);
+  for (size_t i = 0; i < sdf.GetGridCapacity(); ++i) out[i] = sdf[i];
+}
+
 }  // extern "C"

@@ -1152,3 +1152,429 @@ void vgo_wind(float* vel, size_t n, const float wind[3], float wind_weight, floa
   for (size_t i = 0; i < n; ++i)
     for (int c = 0; c < 3; ++c) vel[3 * i + c] = term[c] + src_weight * vel[3 * i + c];
 }
+
+/* ---------------------------------------------- density, baroclinic, surface */
+
+/* UniformGrid<float>::Accumulate (uniformGrid.h:1278-1342): item spread over
+ * the 8 corners of the containing cell with clamped trilinear weights, each
+ * weight formed as ((wx * wy) * wz) * item. */
+static void accumulate1(const vgo_geom* g, float* grid, const float p[3], float item) {
+  unsigned idx[3];
+  vgo_indices_of_position(g, p, idx);
+  float tw[3], om[3];
+  for (int a = 0; a < 3; ++a) {
+    const float cmin = g->mn[a] + (float)idx[a] * g->cell[a];
+    const float diff = p[a] - cmin;
+    tw[a] = clampf_(diff * g->cpe[a], 0.0f, 1.0f);
+    om[a] = 1.0f - tw[a];
+  }
+  const size_t nx = g->np[0], nxy = (size_t)g->np[0] * g->np[1];
+  const size_t o = idx[0] + nx * (idx[1] + (size_t)g->np[1] * idx[2]);
+  grid[o] += om[0] * om[1] * om[2] * item;
+  grid[o + 1] += tw[0] * om[1] * om[2] * item;
+  grid[o + nx] += om[0] * tw[1] * om[2] * item;
+  grid[o + nx + 1] += tw[0] * tw[1] * om[2] * item;
+  grid[o + nxy] += om[0] * om[1] * tw[2] * item;
+  grid[o + nxy + 1] += tw[0] * om[1] * tw[2] * item;
+  grid[o + nxy + nx] += om[0] * tw[1] * tw[2] * item;
+  grid[o + nxy + nx + 1] += tw[0] * tw[1] * tw[2] * item;
+}
+
+/* VortonSim::PopulateDensityAndMassFractionGrids, density part
+ * (VortonFluid/vortonSim.cpp:2911-3016): each particle's density times
+ * (particle volume / cell volume), the particle volume taken from the first
+ * particle (pi/6 size^3, Particles/particle.h:225-228), accumulated in
+ * particle order together with a contribution grid of unit items; then
+ * every point gains the ambient density times max(1 - contribution x
+ * volume ratio, 0). */
+void vgo_density_grid(const float* pos, const float* size, const float* density, size_t n, const vgo_geom* g,
+                      float ambient, float* out) {
+  const size_t pts = capacity(g);
+  float* contrib = (float*)calloc(pts, sizeof(float));
+  memset(out, 0, pts * sizeof(float));
+  if (n > 0) {
+    const float one_over_cell_volume = 1.0f / (g->cell[0] * g->cell[1] * g->cell[2]);
+    const float pi_over_6 = PI_F / 6.0f;
+    const float vorton_volume = pi_over_6 * size[0] * size[0] * size[0];
+    const float volume_ratio = vorton_volume * one_over_cell_volume;
+    for (size_t i = 0; i < n; ++i) {
+      accumulate1(g, out, pos + 3 * i, density[i] * volume_ratio);
+      accumulate1(g, contrib, pos + 3 * i, 1.0f);
+    }
+    for (size_t o = 0; o < pts; ++o) {
+      const float pcls = contrib[o] * volume_ratio;
+      const float clamped = minf_(pcls, 1.0f);
+      out[o] += (1.0f - clamped) * ambient;
+    }
+  } else {
+    for (size_t o = 0; o < pts; ++o) out[o] += 1.0f * ambient;
+  }
+  free(contrib);
+}
+
+/* ComputeGradient (Core/SpatialPartition/uniformGridMath.cpp:468-503,
+ * 650-800): centred differences times half the reciprocal spacing inside,
+ * one-sided differences times the reciprocal spacing on each face. */
+void vgo_gradient(const vgo_geom* g, const float* v, float* grad3) {
+  const float rs[3] = {1.0f / g->cell[0], 1.0f / g->cell[1], g->cell[2] > FLT_EPSILON ? 1.0f / g->cell[2] : 0.0f};
+  const float hrs[3] = {0.5f * rs[0], 0.5f * rs[1], 0.5f * rs[2]};
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2];
+  const size_t st[3] = {1, nx, nx * ny};
+  for (size_t z = 0; z < nz; ++z)
+    for (size_t y = 0; y < ny; ++y)
+      for (size_t x = 0; x < nx; ++x) {
+        const size_t o = x + nx * (y + ny * z);
+        const size_t id[3] = {x, y, z};
+        const size_t last[3] = {nx - 1, ny - 1, nz - 1};
+        for (int a = 0; a < 3; ++a) {
+          float d;
+          if (id[a] == 0)
+            d = (v[o + st[a]] - v[o]) * rs[a];
+          else if (id[a] == last[a])
+            d = (v[o] - v[o - st[a]]) * rs[a];
+          else
+            d = (v[o + st[a]] - v[o - st[a]]) * hrs[a];
+          grad3[3 * o + a] = d;
+        }
+      }
+}
+
+/* Baroclinic generation on the density-grid path of
+ * VortonSim::GenerateBaroclinicVorticity (vortonSim.cpp:3407-3547) with
+ * GenerateBaroclinicVorticitySlice (vortonSim.cpp:3318-3392): density grid,
+ * its gradient, the gradient interpolated at each vorton, then
+ * angvel += (0.5 * (grad x (g * (1 / ambient)))) * dt where the gradient is
+ * finite.  Returns 0 (and changes nothing) when the grid has no extent along
+ * gravity (|g . extent| < FLT_EPSILON, vortonSim.cpp:3417-3421). */
+int vgo_baroclinic(const float* pos, float* angvel, const float* size, const float* density, size_t n,
+                   const vgo_geom* g, const float grav[3], float ambient, float dt) {
+  const float gdot = grav[0] * g->ext[0] + grav[1] * g->ext[1] + grav[2] * g->ext[2];
+  if (fabsf(gdot) < FLT_EPSILON) return 0;
+  const size_t pts = capacity(g);
+  float* dens = (float*)malloc(pts * sizeof(float));
+  float* grad = (float*)malloc(pts * 3 * sizeof(float));
+  vgo_density_grid(pos, size, density, n, g, ambient, dens);
+  vgo_gradient(g, dens, grad);
+  const float one_over_density = 1.0f / ambient;
+  const float pg[3] = {grav[0] * one_over_density, grav[1] * one_over_density, grav[2] * one_over_density};
+  for (size_t i = 0; i < n; ++i) {
+    float d[3];
+    vgo_interpolate3(g, grad, pos + 3 * i, d);
+    if (!(isfinite(d[0]) && isfinite(d[1]) && isfinite(d[2]))) continue;
+    const float b[3] = {d[1] * pg[2] - d[2] * pg[1], d[2] * pg[0] - d[0] * pg[2], d[0] * pg[1] - d[1] * pg[0]};
+    for (int a = 0; a < 3; ++a) angvel[3 * i + a] = angvel[3 * i + a] + 0.5f * b[a] * dt;
+  }
+  free(dens);
+  free(grad);
+  return 1;
+}
+
+/* FindValueStats (uniformGridMath.cpp:554-590): min, max and the mean and
+ * standard deviation from float sums in point order. */
+static void value_stats(const float* v, size_t n, float* mn, float* mx, float* mean, float* sd) {
+  float lo = FLT_MAX, hi = -FLT_MAX, sum = 0.0f, sum2 = 0.0f;
+  for (size_t i = 0; i < n; ++i) {
+    lo = minf_(v[i], lo);
+    hi = maxf_(v[i], hi);
+    sum += v[i];
+    sum2 += v[i] * v[i];
+  }
+  *mn = lo;
+  *mx = hi;
+  *mean = sum / (float)n;
+  const float mean2 = sum2 / (float)n;
+  const float variance = mean2 - *mean * *mean;
+  *sd = sqrtf(maxf_(variance, 0.0f));
+}
+
+static void update_sdf(float* here, float cand) {
+  if (fabsf(cand) < fabsf(*here)) *here = cand;
+}
+
+/* PopulateSignedDistanceGridFromDensityGrid (vortonSim.cpp:3266-3290) with
+ * ComputeImmediateSDFFromDensity_Nearest and
+ * ComputeRemainingSDFFromImmediateSDF_Nearest (Particles/Operation/
+ * pclOpEmit.cpp:696-881, 882-1060), serial form:
+ *   1. density statistics; inside density = min(max, mean + stddev);
+ *   2. every cell's +x, +y, +z edges from its min corner that cross the
+ *      surface (density - ambient changes sign) pin both end points with the
+ *      fraction of a spacing to the crossing (negative inside), keeping the
+ *      value of least magnitude;
+ *   3. two sweeps (all axes forward, then all backward) set each unpinned
+ *      point from its backward neighbour of least |value| plus one spacing
+ *      of that neighbour's sign, where that is closer;
+ *   4. points still at FLT_MAX become NaN.
+ * `sumstats` selects the statistics' summation: 0 float sums in point order
+ * (the reference's), 1 double sums (a parallel reduction's reference). */
+void vgo_signed_distance(const vgo_geom* g, const float* density, float ambient, int sumstats, float* sdf) {
+  const size_t pts = capacity(g);
+  float dmin, dmax, dmean, dsd;
+  if (sumstats == 0) {
+    value_stats(density, pts, &dmin, &dmax, &dmean, &dsd);
+  } else {
+    double s = 0.0, s2 = 0.0;
+    dmin = FLT_MAX;
+    dmax = -FLT_MAX;
+    for (size_t i = 0; i < pts; ++i) {
+      dmin = minf_(density[i], dmin);
+      dmax = maxf_(density[i], dmax);
+      s += density[i];
+      s2 += (double)density[i] * density[i];
+    }
+    dmean = (float)(s / (double)pts);
+    const float mean2 = (float)(s2 / (double)pts);
+    const float variance = mean2 - dmean * dmean;
+    dsd = sqrtf(maxf_(variance, 0.0f));
+  }
+  const float inside = minf_(dmax, dmean + dsd);
+  const float denom = inside - ambient;
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  int* pinned = (int*)calloc(pts, sizeof(int));
+  for (size_t i = 0; i < pts; ++i) sdf[i] = FLT_MAX;
+  for (size_t z = 0; z + 1 < nz; ++z)
+    for (size_t y = 0; y + 1 < ny; ++y)
+      for (size_t x = 0; x + 1 < nx; ++x) {
+        const size_t o = x + nx * (y + ny * z);
+        const size_t nb[3] = {o + 1, o + nx, o + nxy};
+        const float here = density[o] - ambient;
+        for (int a = 0; a < 3; ++a) {
+          const float other = density[nb[a]] - ambient;
+          float ch, cn;
+          if (here <= 0.0f && 0.0f < other) {
+            const float t = minf_(other / denom, 1.0f);
+            ch = (1.0f - t) * g->cell[a];
+            cn = -t * g->cell[a];
+          } else if (here > 0.0f && 0.0f >= other) {
+            const float t = minf_(here / denom, 1.0f);
+            ch = -t * g->cell[a];
+            cn = (1.0f - t) * g->cell[a];
+          } else {
+            continue;
+          }
+          pinned[o] = 1;
+          pinned[nb[a]] = 1;
+          update_sdf(&sdf[o], ch);
+          update_sdf(&sdf[nb[a]], cn);
+        }
+      }
+  for (int pass = 0; pass < 2; ++pass) {
+    const long inc = pass ? -1 : 1;
+    const long b[3] = {pass ? (long)nx - 1 : 0, pass ? (long)ny - 1 : 0, pass ? (long)nz - 1 : 0};
+    const long e[3] = {pass ? -1 : (long)nx, pass ? -1 : (long)ny, pass ? -1 : (long)nz};
+    for (long z = b[2]; z != e[2]; z += inc)
+      for (long y = b[1]; y != e[1]; y += inc)
+        for (long x = b[0]; x != e[0]; x += inc) {
+          const size_t o = (size_t)x + nx * ((size_t)y + ny * (size_t)z);
+          if (pinned[o]) continue;
+          const float sx = (x != b[0]) ? sdf[o - inc] : FLT_MAX;
+          const float sy = (y != b[1]) ? sdf[o - inc * (long)nx] : FLT_MAX;
+          const float sz = (z != b[2]) ? sdf[o - inc * (long)nxy] : FLT_MAX;
+          const float ax = fabsf(sx), ay = fabsf(sy), az = fabsf(sz);
+          float nbv, sp;
+          if (ax <= ay) {
+            if (ax <= az) {
+              nbv = sx;
+              sp = g->cell[0];
+            } else {
+              nbv = sz;
+              sp = g->cell[2];
+            }
+          } else if (ay <= az) {
+            nbv = sy;
+            sp = g->cell[1];
+          } else {
+            nbv = sz;
+            sp = g->cell[2];
+          }
+          update_sdf(&sdf[o], nbv + copysignf(sp, nbv));
+        }
+  }
+  for (size_t i = 0; i < pts; ++i)
+    if (sdf[i] == FLT_MAX) sdf[i] = NAN;
+  free(pinned);
+}
+
+/* ------------------------------------------------------------ marching cubes */
+
+/* Cell corners (x, y, z offsets) and edges (corner pairs in the order the
+ * reference interpolates them), the layout of Render/Resource/
+ * marchingCubes.cpp:590-622, 800-816.  The triangulation itself is generated
+ * here, not taken from a table: on each cube face the crossing edges are
+ * joined into segments (on a face with four crossings, each segment cuts off
+ * one corner below the iso level), segments are oriented so that the
+ * corners below the iso level lie on one fixed side, chained into loops, and
+ * each loop is fanned from its first edge. */
+static const int mc_corner[8][3] = {{0, 0, 0}, {1, 0, 0}, {1, 1, 0}, {0, 1, 0},
+                                    {0, 0, 1}, {1, 0, 1}, {1, 1, 1}, {0, 1, 1}};
+static const int mc_edge[12][2] = {{0, 1}, {1, 2}, {2, 3}, {3, 0}, {4, 5}, {5, 6},
+                                   {6, 7}, {7, 4}, {0, 4}, {1, 5}, {2, 6}, {3, 7}};
+static const int mc_face[6][5] = {{0, 1, 2, 3, -3}, {4, 5, 6, 7, 3}, {0, 1, 5, 4, -2},
+                                  {3, 2, 6, 7, 2},  {0, 3, 7, 4, -1}, {1, 2, 6, 5, 1}};  /* corners, then +-axis */
+
+static int mc_edge_of(int a, int b) {
+  for (int e = 0; e < 12; ++e)
+    if ((mc_edge[e][0] == a && mc_edge[e][1] == b) || (mc_edge[e][0] == b && mc_edge[e][1] == a)) return e;
+  return -1;
+}
+
+/* Orientation of segment a -> b on a face with outward normal axis `ax`
+ * (+-1..3): the sign of ((B - A) x (P - A)) . n for the edge midpoints A, B and
+ * a corner P below the iso level.  Coordinates are doubled so they stay integers. */
+static int mc_side(int a, int b, int pin, int ax) {
+  int A[3], B[3], P[3], u[3], v[3], cr[3];
+  for (int k = 0; k < 3; ++k) {
+    A[k] = mc_corner[mc_edge[a][0]][k] + mc_corner[mc_edge[a][1]][k];
+    B[k] = mc_corner[mc_edge[b][0]][k] + mc_corner[mc_edge[b][1]][k];
+    P[k] = 2 * mc_corner[pin][k];
+    u[k] = B[k] - A[k];
+    v[k] = P[k] - A[k];
+  }
+  cr[0] = u[1] * v[2] - u[2] * v[1];
+  cr[1] = u[2] * v[0] - u[0] * v[2];
+  cr[2] = u[0] * v[1] - u[1] * v[0];
+  const int axis = (ax > 0 ? ax : -ax) - 1;
+  return ax > 0 ? cr[axis] : -cr[axis];
+}
+
+/* Triangles of case `mask` (bit c set: corner c below the iso level) as edge
+ * triples; returns their count. */
+static int mc_case(int mask, int tri[15]) {
+  int next[12];
+  for (int e = 0; e < 12; ++e) next[e] = -1;
+  for (int f = 0; f < 6; ++f) {
+    const int* cc = mc_face[f];
+    int ee[4], cr[4], nc = 0;
+    for (int k = 0; k < 4; ++k) {
+      ee[k] = mc_edge_of(cc[k], cc[(k + 1) % 4]);
+      if (((mask >> cc[k]) & 1) != ((mask >> cc[(k + 1) % 4]) & 1)) cr[nc++] = k;
+    }
+    int seg[2][3], ns = 0;
+    if (nc == 2) {
+      int pin = -1;
+      for (int k = 0; k < 4 && pin < 0; ++k)
+        if ((mask >> cc[k]) & 1) pin = cc[k];
+      seg[0][0] = ee[cr[0]];
+      seg[0][1] = ee[cr[1]];
+      seg[0][2] = pin;
+      ns = 1;
+    } else if (nc == 4) {
+      for (int k = 0; k < 4; ++k)
+        if ((mask >> cc[k]) & 1) {
+          seg[ns][0] = ee[(k + 3) % 4];
+          seg[ns][1] = ee[k];
+          seg[ns][2] = cc[k];
+          ++ns;
+        }
+    }
+    for (int s = 0; s < ns; ++s) {
+      const int a = seg[s][0], b = seg[s][1];
+      if (mc_side(a, b, seg[s][2], cc[4]) < 0)
+        next[a] = b;
+      else
+        next[b] = a;
+    }
+  }
+  int seen[12] = {0}, nt = 0;
+  for (int e = 0; e < 12; ++e) {
+    if (next[e] < 0 || seen[e]) continue;
+    int loop[12], n = 0, x = e;
+    do {
+      loop[n++] = x;
+      seen[x] = 1;
+      x = next[x];
+    } while (x != e && n < 12);
+    for (int i = 1; i + 1 < n; ++i) {
+      tri[3 * nt] = loop[0];
+      tri[3 * nt + 1] = loop[i];
+      tri[3 * nt + 2] = loop[i + 1];
+      ++nt;
+    }
+  }
+  return nt;
+}
+
+/* VertexInterp (marchingCubes.cpp:228-250): the end point itself within 1e-5
+ * (compared in double, as the double literal makes it), else the linear
+ * crossing p1 + mu (p2 - p1). */
+static void mc_interp(float iso, const float p1[3], const float p2[3], float v1, float v2, float out[3]) {
+  if ((double)fabsf(iso - v1) < 0.00001) {
+    memcpy(out, p1, 3 * sizeof(float));
+    return;
+  }
+  if ((double)fabsf(iso - v2) < 0.00001) {
+    memcpy(out, p2, 3 * sizeof(float));
+    return;
+  }
+  if ((double)fabsf(v1 - v2) < 0.00001) {
+    memcpy(out, p1, 3 * sizeof(float));
+    return;
+  }
+  const float mu = (iso - v1) / (v2 - v1);
+  for (int k = 0; k < 3; ++k) out[k] = p1[k] + mu * (p2[k] - p1[k]);
+}
+
+/* ExtractIsoLevel_Slice + PolygoniseCellWithNormal (marchingCubes.cpp:
+ * 580-760, 762-866) on grid g of scalar values: cells in z, y, x order; for
+ * each triangle the three vertex positions (9 floats) and its unit face
+ * normal (p1 - p0) x (p2 - p0) / sqrt(|.|^2 + FLT_MIN) repeated for the three
+ * vertices (9 floats).  Corner positions are min + index x spacing.  Writes
+ * at most cap triangles; returns how many the grid makes. */
+size_t vgo_marching_cubes(const vgo_geom* g, const float* v, float iso, float* verts, float* normals, size_t cap) {
+  static int table_ready = 0;
+  static int cnt[256], tri[256][15];
+  if (!table_ready) {
+    for (int m = 0; m < 256; ++m) cnt[m] = mc_case(m, tri[m]);
+    table_ready = 1;
+  }
+  const size_t nx = g->np[0], ny = g->np[1], nz = g->np[2], nxy = nx * ny;
+  size_t out = 0;
+  for (size_t z = 0; z + 1 < nz; ++z)
+    for (size_t y = 0; y + 1 < ny; ++y)
+      for (size_t x = 0; x + 1 < nx; ++x) {
+        const size_t o = x + nx * (y + ny * z);
+        float val[8], p[8][3];
+        int mask = 0;
+        const float gp[3] = {(float)x * g->cell[0] + g->mn[0], (float)y * g->cell[1] + g->mn[1],
+                             (float)z * g->cell[2] + g->mn[2]};
+        const float hi[3] = {gp[0] + g->cell[0], gp[1] + g->cell[1], gp[2] + g->cell[2]};
+        for (int c = 0; c < 8; ++c) {
+          const int* d = mc_corner[c];
+          val[c] = v[o + d[0] + nx * d[1] + nxy * d[2]];
+          for (int k = 0; k < 3; ++k) p[c][k] = d[k] ? hi[k] : gp[k];
+          if (val[c] < iso) mask |= 1 << c;
+        }
+        if (cnt[mask] == 0) continue;
+        float vl[12][3];
+        for (int e = 0; e < 12; ++e) {
+          const int a = mc_edge[e][0], b = mc_edge[e][1];
+          if (((mask >> a) & 1) != ((mask >> b) & 1)) mc_interp(iso, p[a], p[b], val[a], val[b], vl[e]);
+        }
+        for (int t = 0; t < cnt[mask]; ++t, ++out) {
+          if (out >= cap) continue;
+          const float* q0 = vl[tri[mask][3 * t]];
+          const float* q1 = vl[tri[mask][3 * t + 1]];
+          const float* q2 = vl[tri[mask][3 * t + 2]];
+          float* dst = verts + 9 * out;
+          memcpy(dst, q0, 12);
+          memcpy(dst + 3, q1, 12);
+          memcpy(dst + 6, q2, 12);
+          if (normals) {
+            const float u[3] = {q1[0] - q0[0], q1[1] - q0[1], q1[2] - q0[2]};
+            const float w[3] = {q2[0] - q0[0], q2[1] - q0[1], q2[2] - q0[2]};
+            const float n[3] = {u[1] * w[2] - u[2] * w[1], u[2] * w[0] - u[0] * w[2], u[0] * w[1] - u[1] * w[0]};
+            const float r = 1.0f / sqrtf(n[0] * n[0] + n[1] * n[1] + n[2] * n[2] + FLT_MIN);
+            for (int k = 0; k < 3; ++k) {
+              normals[9 * out + 3 * k] = n[0] * r;
+              normals[9 * out + 3 * k + 1] = n[1] * r;
+              normals[9 * out + 3 * k + 2] = n[2] * r;
+            }
+          }
+        }
+      }
+  return out;
+}
+
+/* The generated triangulation: count[256] and up to 5 edge triples per case. */
+void vgo_marching_cubes_table(int* count, int* tri15) {
+  for (int m = 0; m < 256; ++m) count[m] = mc_case(m, tri15 + 15 * m);
+}

@@ -119,7 +119,19 @@ double vgo_relres_f64d(const vgo_geom* g, const double* a, const float* b);
 void vgo_step_fields(const float* pos, float* vel, float* angvel, const float* size, size_t n, const vgo_geom* g,
                      float dt, float viscosity, int pse_mode, float* velgrid, float* vecpot, float* negvort);
 
+/* Density grid, gradient, baroclinic generation and signed distance (grid path). */
+void vgo_density_grid(const float* pos, const float* size, const float* density, size_t n, const vgo_geom* g,
+                      float ambient, float* out);
+void vgo_gradient(const vgo_geom* g, const float* v, float* grad3);
+int vgo_baroclinic(const float* pos, float* angvel, const float* size, const float* density, size_t n,
+                   const vgo_geom* g, const float grav[3], float ambient, float dt);
+void vgo_signed_distance(const vgo_geom* g, const float* density, float ambient, int sumstats, float* sdf);
+/* Marching cubes: up to cap triangles (9 floats of positions, 9 of normals each); returns the count. */
+size_t vgo_marching_cubes(const vgo_geom* g, const float* v, float iso, float* verts, float* normals, size_t cap);
+void vgo_marching_cubes_table(int* count, int* tri15);
+
 #ifdef __cplusplus
 }
 #endif
+
 #endif

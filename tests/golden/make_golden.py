@@ -10,6 +10,7 @@ Usage (needs the reference tree or a staged copy; run in this container):
     python tests/golden/make_golden.py              # reference.npz
     python tests/golden/make_golden.py lifecycle    # lifecycle.npz (PclOpKillAge, PclOpWind)
     python tests/golden/make_golden.py heat         # heat.npz (DiffuseAndDissipateHeatPSE)
+    python tests/golden/make_golden.py surface      # surface.npz (density grid, gradient, baroclinic, SDF)
 """
 import ctypes
 import os
@@ -25,6 +26,7 @@ from vortegrid_gb300 import workloads  # noqa: E402
 OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference.npz")
 OUT_LIFE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lifecycle.npz")
 OUT_HEAT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "heat.npz")
+OUT_SURF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "surface.npz")
 
 
 def P(a):
@@ -264,10 +266,53 @@ def heat():
     print(f"wrote {OUT_HEAT} ({os.path.getsize(OUT_HEAT) / 1e3:.1f} kB, {len(g)} arrays)")
 
 
+def surface():
+    """PopulateDensityAndMassFractionGrids (density), ComputeGradient, the
+    density-grid baroclinic path of GenerateBaroclinicVorticity and
+    PopulateSignedDistanceGridFromDensityGrid, from the reference's own code
+    (oracle/ref_build/ref_harness.cpp), on two seeded fields: a ring with
+    densities in [1, 1.5) and a heavy puff (density 2 in ambient 1)."""
+    oracle.build()
+    R = oracle.ref("serial")
+    R.vgref_baroclinic.restype = ctypes.c_int
+    g = {}
+    rng = np.random.default_rng(41)
+    ring = workloads.ring(3000, seed=7)
+    puff = workloads.puff(3000, seed=8, sigma=0.3, clip=0.9)
+    cases = [(ring, (1.0 + 0.5 * rng.random(3000)).astype(np.float32), [0.0, 0.0, -9.8]),
+             (puff, np.full(3000, 2.0, np.float32), [1.0, -3.0, 2.0])]
+    dt, ambient = np.float32(1.0 / 30.0), np.float32(1.0)
+    for i, ((pos, w, s), dens, grav) in enumerate(cases):
+        geo = oracle.step_geometry(pos, float(s[0]) * 0.5)
+        g12, np3 = geo.as12(), np.array(geo.points, np.uint32)
+        n, npts = len(pos), geo.capacity
+        grav = np.array(grav, np.float32)
+        dg = np.zeros(npts, np.float32)
+        R.vgref_density_grid(P(pos), P(s), P(dens), ctypes.c_size_t(n), P(g12), P(np3), ctypes.c_float(ambient),
+                             P(dg))
+        gr = np.zeros((npts, 3), np.float32)
+        R.vgref_gradient(P(g12), P(np3), P(dg), P(gr))
+        wv = w.copy()
+        applied = R.vgref_baroclinic(P(pos), P(wv), P(s), P(dens), ctypes.c_size_t(n), P(g12), P(np3), P(grav),
+                                     ctypes.c_float(ambient), ctypes.c_float(dt))
+        sdf = np.zeros(npts, np.float32)
+        R.vgref_signed_distance(P(g12), P(np3), P(dg), ctypes.c_float(ambient), P(sdf))
+        g.update({f"s{i}_pos": pos, f"s{i}_angvel": w, f"s{i}_size": s, f"s{i}_density": dens,
+                  f"s{i}_geom": g12, f"s{i}_np": np3, f"s{i}_grav": grav, f"s{i}_density_grid": dg,
+                  f"s{i}_gradient": gr, f"s{i}_baroclinic": wv, f"s{i}_applied": np.array(applied),
+                  f"s{i}_sdf": sdf})
+    g["surface_params"] = np.array([dt, ambient], np.float32)
+    g["surface_cases"] = np.array(len(cases))
+    np.savez_compressed(OUT_SURF, **g)
+    print(f"wrote {OUT_SURF} ({os.path.getsize(OUT_SURF) / 1e3:.1f} kB, {len(g)} arrays)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lifecycle":
         lifecycle()
     elif len(sys.argv) > 1 and sys.argv[1] == "heat":
         heat()
+    elif len(sys.argv) > 1 and sys.argv[1] == "surface":
+        surface()
     else:
         main()

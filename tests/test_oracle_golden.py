@@ -281,3 +281,71 @@ def test_tree_matches_reference_at_treecode_workload_size(oracle_lib):
         L.vgref_tree(kind, P(pos), P(w), P(s), ctypes.c_size_t(len(pos)), P(g12), P(np3), P(q), ctypes.c_size_t(len(q)),
                      ctypes.c_float(2.5), ctypes.c_float(0.6), P(out))
         assert np.array_equal(bits(O.tree(kind, pos, w, s, g, q, 2.5, 0.6)), bits(out)), kind
+
+
+def _surface():
+    import os
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "surface.npz")))
+
+
+def test_density_gradient_baroclinic_sdf_bit_exact(oracle_lib):
+    """The oracle's density grid (PopulateDensityAndMassFractionGrids),
+    gradient (ComputeGradient), density-grid baroclinic generation and signed
+    distance grid (PopulateSignedDistanceGridFromDensityGrid, with the
+    reference's float statistics) equal the reference's own code on a ring
+    with varying densities and a heavy puff (tests/golden/surface.npz)."""
+    O = oracle_lib
+    h = _surface()
+    dt, ambient = (float(v) for v in h["surface_params"])
+    for i in range(int(h["surface_cases"])):
+        g = O.Geom.from12(h[f"s{i}_geom"], h[f"s{i}_np"])
+        pos, size, dens = h[f"s{i}_pos"], h[f"s{i}_size"], h[f"s{i}_density"]
+        dg = O.density_grid(pos, size, dens, g, ambient)
+        assert np.array_equal(bits(dg), bits(h[f"s{i}_density_grid"])), i
+        assert np.array_equal(bits(O.gradient(g, dg)), bits(h[f"s{i}_gradient"])), i
+        applied, w = O.baroclinic(pos, h[f"s{i}_angvel"], size, dens, g, h[f"s{i}_grav"], ambient, np.float32(dt))
+        assert applied == bool(h[f"s{i}_applied"])
+        assert np.array_equal(bits(w), bits(h[f"s{i}_baroclinic"])), i
+        sdf = O.signed_distance(g, dg, ambient, sumstats=0)
+        assert np.array_equal(bits(sdf), bits(h[f"s{i}_sdf"])), i
+        # double-precision statistics (a parallel reduction's) move the pinned
+        # values, and the distances swept from them, by ~1e-6 relative
+        sdf1 = O.signed_distance(g, dg, ambient, sumstats=1)
+        assert np.nanmax(np.abs(sdf1 - sdf)) <= 1e-5 * float(np.nanmax(np.abs(sdf)))
+    # no gravity along the grid: the reference returns before any change
+    g = O.Geom.from12(h["s0_geom"], h["s0_np"])
+    applied, w = O.baroclinic(h["s0_pos"], h["s0_angvel"], h["s0_size"], h["s0_density"], g, [0, 0, 0], ambient,
+                              np.float32(dt))
+    assert not applied and np.array_equal(w, h["s0_angvel"])
+
+
+def test_marching_cubes_table_is_closed(oracle_lib):
+    """The generated triangulation: every case's triangles use exactly the
+    edges whose end points lie on opposite sides of the iso level, each
+    triangle edge between two crossing edges is used once in each direction
+    within a case's loops (closed loops), at most 5 triangles per cell, and a
+    sphere's surface on a 65^3 grid is closed with outward normals."""
+    from collections import Counter
+    from vortegrid_gb300 import workloads
+    cnt, tri = oracle_lib.marching_cubes_table()
+    corner = [(0, 0, 0), (1, 0, 0), (1, 1, 0), (0, 1, 0), (0, 0, 1), (1, 0, 1), (1, 1, 1), (0, 1, 1)]
+    edge = [(0, 1), (1, 2), (2, 3), (3, 0), (4, 5), (5, 6), (6, 7), (7, 4), (0, 4), (1, 5), (2, 6), (3, 7)]
+    assert cnt.max() <= 5 and cnt[0] == 0 and cnt[255] == 0
+    for m in range(256):
+        crossing = {e for e, (a, b) in enumerate(edge) if ((m >> a) & 1) != ((m >> b) & 1)}
+        used = set(tri[m][: 3 * cnt[m]].tolist())
+        assert used == crossing, m
+    n = 65
+    g = oracle_lib.Geom.from12(np.array([-1, -1, -1, 2, 2, 2, 2 / 64, 2 / 64, 2 / 64, 32, 32, 32], np.float32),
+                               (n, n, n))
+    pts = workloads.grid_points([-1.0] * 3, [2 / 64] * 3, [n] * 3)
+    sdf = (np.linalg.norm(pts.astype(np.float64), axis=1) - 0.6).astype(np.float32)
+    V, N = oracle_lib.marching_cubes(g, sdf, 0.0)
+    assert np.all(np.einsum("ij,ij->i", N[:, 0], V.mean(1)) > 0)
+    edges = Counter()
+    for t in np.round(V.astype(np.float64), 5):
+        k = [tuple(p) for p in t]
+        for i in range(3):
+            edges[tuple(sorted((k[i], k[(i + 1) % 3])))] += 1
+    assert set(edges.values()) == {2}
+    assert corner[6] == (1, 1, 1)

@@ -119,6 +119,8 @@ EXPORTS = [
     "vg_sor_device", "vg_cascade_device", "vg_multigrid_device", "vg_downsample_device", "vg_upsample_device",
     "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
     "vg_evolve_device", "vg_direct_noalloc", "vg_wind_device", "vg_kill_age_device", "vg_heat_pse_device",
+    "vg_density_grid_device", "vg_gradient_device", "vg_baroclinic_device", "vg_signed_distance_device",
+    "vg_marching_cubes_device",
     "vg_net_create", "vg_net_destroy", "vg_net_last_error", "vg_net_param_count", "vg_net_set_params",
     "vg_net_get_params", "vg_net_save", "vg_net_load", "vg_net_guess_device", "vg_net_backward_device",
     "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
@@ -168,6 +170,17 @@ def lib():
                                        ctypes.c_float]
         L.vg_heat_pse_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p, ctypes.c_void_p,
                                          ctypes.c_size_t, ctypes.c_float, ctypes.c_float, ctypes.c_float]
+        L.vg_density_grid_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p,
+                                             ctypes.c_void_p, ctypes.c_size_t, ctypes.c_float, ctypes.c_void_p]
+        L.vg_gradient_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p, ctypes.c_void_p]
+        L.vg_baroclinic_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p,
+                                           ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
+                                           ctypes.c_float, ctypes.c_float, ctypes.POINTER(ctypes.c_int)]
+        L.vg_signed_distance_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p,
+                                                ctypes.c_float, ctypes.c_int, ctypes.c_void_p]
+        L.vg_marching_cubes_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p,
+                                               ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
+                                               ctypes.POINTER(ctypes.c_size_t)]
         L.vg_wind_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                      ctypes.c_float, ctypes.c_float]
         L.vg_kill_age_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

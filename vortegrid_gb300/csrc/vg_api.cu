@@ -1031,4 +1031,71 @@ vg_status vg_gather_advect_device(vg_ctx* c, const vg_grid_geom* gg, const float
   return launch_gather_advect(c, to_geom(*gg), vel3, (float4*)pos4, (float4*)vel4, m, dt, true);
 }
 
+vg_status vg_density_grid_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, const float* density,
+                                 size_t n, float ambient_density, float* density_grid) {
+  if (!c || !gg || !density_grid || (n && (!pos_size || !density))) return VG_INVALID;
+  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+  return launch_density_grid(c, to_geom(*gg), (const float4*)pos_size, density, n, ambient_density, density_grid);
+}
+
+vg_status vg_gradient_device(vg_ctx* c, const vg_grid_geom* gg, const float* scalar, float* grad3) {
+  if (!c || !gg || !scalar || !grad3) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  if (g.np[0] < 2 || g.np[1] < 2 || g.np[2] < 2) return fail(c, VG_INVALID, "gradient: fewer than 2 points on an axis");
+  return launch_gradient(c, g, scalar, grad3);
+}
+
+vg_status vg_baroclinic_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, const float* density,
+                               float* angvel, size_t n, const float grav[3], float ambient_density, float dt,
+                               int* applied) {
+  if (!c || !gg || !grav || (n && (!pos_size || !density || !angvel))) return VG_INVALID;
+  if (applied) *applied = 0;
+  if (n == 0) return VG_OK;
+  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+  if (!(ambient_density > 0.0f)) return fail(c, VG_INVALID, "baroclinic: ambient density must be positive");
+  const Geom g = to_geom(*gg);
+  if (g.np[0] < 2 || g.np[1] < 2 || g.np[2] < 2) return fail(c, VG_INVALID, "baroclinic: fewer than 2 points on an axis");
+  // no extent along gravity: nothing to generate (vortonSim.cpp:3417-3421)
+  const float gdot = grav[0] * g.ext[0] + grav[1] * g.ext[1] + grav[2] * g.ext[2];
+  if (fabsf(gdot) < FLT_EPSILON) return VG_OK;
+  vg_status st = VG_OK;
+  const size_t pts = g.points();
+  float* dens = (float*)ws(c, S_DENS, pts * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  float* grad = (float*)ws(c, S_GRAD, pts * 3 * sizeof(float), &st);
+  if (st != VG_OK) return st;
+  if ((st = launch_density_grid(c, g, (const float4*)pos_size, density, n, ambient_density, dens)) != VG_OK) return st;
+  if ((st = launch_gradient(c, g, dens, grad)) != VG_OK) return st;
+  if ((st = launch_baroclinic(c, g, grad, (const float4*)pos_size, (float4*)angvel, n, grav, ambient_density, dt)) !=
+      VG_OK)
+    return st;
+  if (applied) *applied = 1;
+  return VG_OK;
+}
+
+vg_status vg_signed_distance_device(vg_ctx* c, const vg_grid_geom* gg, const float* density_grid,
+                                    float ambient_density, int reference_stats, float* sdf) {
+  if (!c || !gg || !density_grid || !sdf) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  if (g.np[0] < 2 || g.np[1] < 2 || g.np[2] < 2) return fail(c, VG_INVALID, "signed distance: fewer than 2 points on an axis");
+  const size_t pts = g.points();
+  if (pts > 0x7fffffff) return fail(c, VG_TOO_LARGE, "signed distance: more than 2^31 points");
+  const int nb = 2 * sm_count();
+  vg_status st = VG_OK;
+  const size_t pin_bytes = (pts + 255) / 256 * 256;
+  char* w = (char*)ws(c, S_SDF, pin_bytes + 64 + (size_t)nb * 4 * sizeof(double), &st);
+  if (st != VG_OK) return st;
+  return launch_signed_distance(c, g, density_grid, ambient_density, reference_stats != 0, sdf, (unsigned char*)w,
+                                (float*)(w + pin_bytes), (double*)(w + pin_bytes + 64), nb);
+}
+
+vg_status vg_marching_cubes_device(vg_ctx* c, const vg_grid_geom* gg, const float* values, float iso_level,
+                                   float* vertices, float* normals, size_t max_triangles, size_t* triangles) {
+  if (!c || !gg || !values || !triangles || (max_triangles && !vertices)) return VG_INVALID;
+  const Geom g = to_geom(*gg);
+  if (g.np[0] < 2 || g.np[1] < 2 || g.np[2] < 2) return fail(c, VG_INVALID, "marching cubes: fewer than 2 points on an axis");
+  if (g.points() > 0x7fffffff) return fail(c, VG_TOO_LARGE, "marching cubes: more than 2^31 points");
+  return launch_marching_cubes(c, g, values, iso_level, vertices, normals, max_triangles, triangles);
+}
+
 }  // extern "C"

@@ -101,47 +101,6 @@ __global__ void k_downsample(Geom F, const float* __restrict__ f, Geom C, uint3 
   out[3 * k + 2] = __fmul_rn(az, r);
 }
 
-// UniformGrid::Interpolate (uniformGrid.h:1117-1148) of K floats per point.
-template <int K>
-__device__ __forceinline__ void interp(const Geom& g, const float* __restrict__ f, float px, float py, float pz,
-                                       float* out) {
-  const float p[3] = {px, py, pz};
-  unsigned idx[3];
-  float tw[3], om[3];
-#pragma unroll
-  for (int a = 0; a < 3; ++a) {
-    idx[a] = bin_axis(p[a], g.mn[a], g.cpe[a]);
-    const float cmin = __fadd_rn(g.mn[a], __fmul_rn((float)idx[a], g.cell[a]));
-    tw[a] = __fmul_rn(__fsub_rn(p[a], cmin), g.cpe[a]);
-    om[a] = __fsub_rn(1.0f, tw[a]);
-  }
-  const size_t nx = g.np[0], nxy = (size_t)g.np[0] * g.np[1];
-  const size_t o = idx[0] + nx * (idx[1] + (size_t)g.np[1] * idx[2]);
-#pragma unroll
-  for (int a = 0; a < K; ++a) {
-    const float v000 = f[K * o + a], v100 = f[K * (o + 1) + a], v010 = f[K * (o + nx) + a],
-                v110 = f[K * (o + nx + 1) + a], v001 = f[K * (o + nxy) + a], v101 = f[K * (o + nxy + 1) + a],
-                v011 = f[K * (o + nxy + nx) + a], v111 = f[K * (o + nxy + nx + 1) + a];
-    const float y0 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], v000), __fmul_rn(tw[0], v100)), om[1]),
-                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], v010), __fmul_rn(tw[0], v110)), tw[1]));
-    const float y1 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], v001), __fmul_rn(tw[0], v101)), om[1]),
-                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], v011), __fmul_rn(tw[0], v111)), tw[1]));
-    out[a] = __fadd_rn(__fmul_rn(y0, om[2]), __fmul_rn(y1, tw[2]));
-  }
-}
-
-__device__ __forceinline__ bool inside_cells(const Geom& g, float px, float py, float pz) {
-  // The reference requires samples strictly inside the grid's cells
-  // (uniformGrid.h:1122-1124); report rather than read out of bounds.
-  // bin_axis maps a position one to two cells below the minimum corner to
-  // 0xffffffff (truncation gives -1), so compare against np - 1 rather than
-  // testing ix + 1 < np, which wraps to 0 there.
-  const unsigned ix = bin_axis(px, g.mn[0], g.cpe[0]);
-  const unsigned iy = bin_axis(py, g.mn[1], g.cpe[1]);
-  const unsigned iz = bin_axis(pz, g.mn[2], g.cpe[2]);
-  return ix < g.np[0] - 1u && iy < g.np[1] - 1u && iz < g.np[2] - 1u && px == px && py == py && pz == pz;
-}
-
 __global__ void k_upsample(Geom C, const float* __restrict__ cv, Geom F, int interior, float* __restrict__ fv) {
   pdl_entry();
   const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;

@@ -81,6 +81,47 @@ __device__ __forceinline__ float ref_dot_self(float a, float b, float c) {
   return __fadd_rn(__fadd_rn(__fmul_rn(a, a), __fmul_rn(b, b)), __fmul_rn(c, c));
 }
 
+// UniformGrid::Interpolate (uniformGrid.h:1117-1148) of K floats per point.
+template <int K>
+__device__ __forceinline__ void interp(const Geom& g, const float* __restrict__ f, float px, float py, float pz,
+                                       float* out) {
+  const float p[3] = {px, py, pz};
+  unsigned idx[3];
+  float tw[3], om[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    idx[a] = bin_axis(p[a], g.mn[a], g.cpe[a]);
+    const float cmin = __fadd_rn(g.mn[a], __fmul_rn((float)idx[a], g.cell[a]));
+    tw[a] = __fmul_rn(__fsub_rn(p[a], cmin), g.cpe[a]);
+    om[a] = __fsub_rn(1.0f, tw[a]);
+  }
+  const size_t nx = g.np[0], nxy = (size_t)g.np[0] * g.np[1];
+  const size_t o = idx[0] + nx * (idx[1] + (size_t)g.np[1] * idx[2]);
+#pragma unroll
+  for (int a = 0; a < K; ++a) {
+    const float v000 = f[K * o + a], v100 = f[K * (o + 1) + a], v010 = f[K * (o + nx) + a],
+                v110 = f[K * (o + nx + 1) + a], v001 = f[K * (o + nxy) + a], v101 = f[K * (o + nxy + 1) + a],
+                v011 = f[K * (o + nxy + nx) + a], v111 = f[K * (o + nxy + nx + 1) + a];
+    const float y0 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], v000), __fmul_rn(tw[0], v100)), om[1]),
+                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], v010), __fmul_rn(tw[0], v110)), tw[1]));
+    const float y1 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], v001), __fmul_rn(tw[0], v101)), om[1]),
+                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], v011), __fmul_rn(tw[0], v111)), tw[1]));
+    out[a] = __fadd_rn(__fmul_rn(y0, om[2]), __fmul_rn(y1, tw[2]));
+  }
+}
+
+__device__ __forceinline__ bool inside_cells(const Geom& g, float px, float py, float pz) {
+  // The reference requires samples strictly inside the grid's cells
+  // (uniformGrid.h:1122-1124); report rather than read out of bounds.
+  // bin_axis maps a position one to two cells below the minimum corner to
+  // 0xffffffff (truncation gives -1), so compare against np - 1 rather than
+  // testing ix + 1 < np, which wraps to 0 there.
+  const unsigned ix = bin_axis(px, g.mn[0], g.cpe[0]);
+  const unsigned iy = bin_axis(py, g.mn[1], g.cpe[1]);
+  const unsigned iz = bin_axis(pz, g.mn[2], g.cpe[2]);
+  return ix < g.np[0] - 1u && iy < g.np[1] - 1u && iz < g.np[2] - 1u && px == px && py == py && pz == pz;
+}
+
 // 2/3 as the reference's float constant (VortonFluid/vorton.h:92).
 #define VG_TWO_THIRDS (2.0f / 3.0f)
 
@@ -190,6 +231,10 @@ enum Slot {
   S_MGINV,
   S_TREEPREP,
   S_PCL,
+  S_DENS,   // density grid (baroclinic)
+  S_GRAD,   // density gradient grid (baroclinic)
+  S_SDF,    // signed distance: pinned flags, statistics, partial sums
+  S_MC,     // marching cubes: per-cell counts and offsets
   S_NUM
 };
 
@@ -381,6 +426,19 @@ vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const floa
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
                                float dt, bool evolve);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
+// Density grid (PopulateDensityAndMassFractionGrids), gradient (ComputeGradient),
+// baroclinic generation and the signed distance grid (vg_surface.cu).
+vg_status launch_density_grid(Ctx* c, const Geom& g, const float4* ps, const float* density, size_t n,
+                              float ambient, float* out);
+vg_status launch_gradient(Ctx* c, const Geom& g, const float* v, float* grad3);
+vg_status launch_baroclinic(Ctx* c, const Geom& g, const float* grad3, const float4* ps, float4* w, size_t n,
+                            const float grav[3], float ambient, float dt);
+vg_status launch_signed_distance(Ctx* c, const Geom& g, const float* dens, float ambient, bool reference_stats,
+                                 float* sdf, unsigned char* pinned, float* stats, double* partials,
+                                 int partial_blocks);
+// Marching cubes: *triangles receives the count; VG_TOO_LARGE when it exceeds cap (nothing written).  Synchronous.
+vg_status launch_marching_cubes(Ctx* c, const Geom& g, const float* v, float iso, float* verts, float* normals,
+                                size_t cap, size_t* triangles);
 
 namespace nn {
 // True when the network applies to grid g ((edge+1)^3 points).
