@@ -332,6 +332,50 @@ vg_status vg_baroclinic_device(vg_ctx* ctx, const vg_grid_geom* g, const float* 
 vg_status vg_signed_distance_device(vg_ctx* ctx, const vg_grid_geom* g, const float* density_grid,
                                     float ambient_density, int reference_stats, float* sdf);
 
+/* Fluid-body boundary conditions (FluidBodySim/fluidBodySim.cpp) on
+ * device-resident particles.  Bodies are given on the host, nb <= 16, as 32
+ * floats each:
+ *   [0] shape: 0 sphere, 1 box (a ConvexPolytope_MakeBox, Collision/
+ *       convexPolytope.cpp:346-376); [1] 1 for a hollow box (a container the
+ *       fluid fills); [2..4] position; [5..7] velocity; [8..10] angular
+ *       velocity; [11..19] orientation matrix rows; [20] sphere radius, or
+ *       [20..22] box dimensions; [23] temperature; [24] thermal conductivity;
+ *       [25] one over heat capacity (0: 1); the rest unused.
+ * Particles are float4 pos_size (position, diameter), vel4 and angvel4 (the
+ * reference's angular velocity, vorticity / 2), and density per particle. */
+
+/* CollideVortonsSlice (fluidBodySim.cpp:759-1180) for each body in turn over
+ * all vortons, as SolveBoundaryConditions runs it (fluidBodySim.cpp:
+ * 1651-1715): a vorton within 1.5 radii of a body is placed outside it,
+ * bounced, given the Brinkman-penalty vorticity blended with the body's spin,
+ * and exchanges heat with the body through its density (temperature =
+ * 300 ambient / density).  Per body, body_out receives 9 floats: linear
+ * impulse (zero in the reference's smoothed-particle form), angular impulse,
+ * heat to the body, the sum of the collided vortons' temperatures and the
+ * body's new temperature (fluidBodySim.cpp:1703-1714); collided (may be NULL)
+ * the collision counts.  The particle results equal the reference's bit for
+ * bit; the body sums are FP64 reductions in a fixed order (the reference adds
+ * in vorton order in FP32).  Synchronises the context's stream. */
+vg_status vg_collide_vortons_device(vg_ctx* ctx, const float* bodies, int nb, float* pos_size, float* vel4,
+                                    float* angvel4, float* density, size_t n, float ambient_density,
+                                    float specific_heat, float* body_out, unsigned long long* collided);
+
+/* CollideTracersSlice (fluidBodySim.cpp:1300-1455) for each body in turn: a
+ * tracer in contact is placed outside the body and bounced; per body body_out
+ * receives 6 floats, the linear and angular impulses on the body (tracer mass
+ * = density x pi/6 size^3; density may be NULL for 1).  Synchronises. */
+vg_status vg_collide_tracers_device(vg_ctx* ctx, const float* bodies, int nb, float* pos_size, float* vel4,
+                                    const float* density, size_t n, float* body_out);
+
+/* RemoveEmbeddedParticles (fluidBodySim.cpp:365-417): particles inside a
+ * body (sphere: within its radius; box: contact distance below the
+ * particle's radius) are removed, for each body in turn, leaving the
+ * survivors in the order of the reference's swap-with-last walk.  The
+ * records of pos_size and, when given, b4, c4 (float4) and d1 (float) move
+ * together; *m_out receives the survivors' count.  Synchronises. */
+vg_status vg_remove_embedded_device(vg_ctx* ctx, const float* bodies, int nb, float* pos_size, float* b4, float* c4,
+                                    float* d1, size_t m, size_t* m_out);
+
 /* Isosurface of a scalar grid by marching cubes, as ExtractIsoLevel /
  * PolygoniseCellWithNormal do (Render/Resource/marchingCubes.cpp:580-866),
  * into device buffers instead of a vertex buffer: cells in z, y, x order; per

@@ -320,6 +320,50 @@ def marching_cubes_table():
     return cnt, tri
 
 
+def body(shape, position, dims, hole=False, velocity=(0, 0, 0), angular_velocity=(0, 0, 0), orientation=None,
+         temperature=300.0, conductivity=0.0):
+    """One rigid body as 32 floats (shape 0 sphere with radius dims[0], 1 box of dims)."""
+    b = np.zeros(32, np.float32)
+    b[0] = shape
+    b[1] = 1.0 if hole else 0.0
+    b[2:5], b[5:8], b[8:11] = position, velocity, angular_velocity
+    b[11:20] = np.asarray(np.eye(3) if orientation is None else orientation, np.float32).ravel()
+    d = np.atleast_1d(np.asarray(dims, np.float32))
+    b[20:20 + len(d)] = d
+    b[23], b[24] = temperature, conductivity
+    return b
+
+
+def collide_vortons(pos, vel, angvel, size, density, bodies, ambient=1.0, specific_heat=1.0):
+    """CollideVortonsSlice per body: (pos, vel, angvel, density, per-body float32[nb, 9])."""
+    p, v, w, d = f32(pos).copy(), f32(vel).copy(), f32(angvel).copy(), f32(density).copy()
+    b = f32(bodies).reshape(-1, 32)
+    out = np.zeros((len(b), 9), np.float32)
+    lib().vgo_collide_vortons(_p(p), _p(v), _p(w), _p(f32(size)), _p(d), ctypes.c_size_t(len(p)), _p(b),
+                              ctypes.c_int(len(b)), ctypes.c_float(ambient), ctypes.c_float(specific_heat), _p(out))
+    return p, v, w, d, out
+
+
+def collide_tracers(pos, vel, size, density, bodies):
+    """CollideTracersSlice per body: (pos, vel, per-body float32[nb, 6])."""
+    p, v = f32(pos).copy(), f32(vel).copy()
+    b = f32(bodies).reshape(-1, 32)
+    out = np.zeros((len(b), 6), np.float32)
+    lib().vgo_collide_tracers(_p(p), _p(v), _p(f32(size)), _p(f32(density)), ctypes.c_size_t(len(p)), _p(b),
+                              ctypes.c_int(len(b)), _p(out))
+    return p, v, out
+
+
+def remove_embedded(pos, size, bodies):
+    """RemoveEmbeddedParticles: the survivors' original indices in the order left."""
+    b = f32(bodies).reshape(-1, 32)
+    order = np.zeros(max(len(pos), 1), np.uint32)
+    m = ctypes.c_size_t()
+    lib().vgo_remove_embedded(_p(f32(pos)), _p(f32(size)), ctypes.c_size_t(len(pos)), _p(b), ctypes.c_int(len(b)),
+                              _p(order), ctypes.byref(m))
+    return order[: m.value].copy()
+
+
 def kill_age(birth, frame, age_max):
     """Survivors' original indices in the order PclOpKillAge leaves them."""
     b = np.ascontiguousarray(birth, np.int32)

@@ -22,6 +22,11 @@
 #include "Particles/Operation/pclOpKillAge.h"
 #include "Particles/Operation/pclOpWind.h"
 #include "Core/SpatialPartition/uniformGridMath.h"
+#include "FluidBodySim/fluidBodySim.h"
+#include "Impulsion/physicalObject.h"
+#include "Impulsion/rigidBody.h"
+#include "Collision/sphereShape.h"
+#include "Collision/convexPolytope.h"
 #undef private
 #undef protected
 #include <cstring>
@@ -605,6 +610,137 @@ void vgref_signed_distance(const float geom12[12], const unsigned np[3], const f
   UniformGrid<float> sdf;
   s.sim.PopulateSignedDistanceGridFromDensityGrid(sdf, s.sim.mDensityGrid, 0);
   for (size_t i = 0; i < sdf.GetGridCapacity(); ++i) out[i] = sdf[i];
+}
+
+}  // extern "C"
+
+// Rigid bodies for the fluid-body boundary conditions, 32 floats each:
+// [0] shape (0 sphere, 1 box), [1] hole (box only), [2..4] position,
+// [5..7] velocity, [8..10] angular velocity, [11..19] orientation rows
+// (x, y, z), [20..22] sphere radius (x) or box dimensions, [23] temperature,
+// [24] thermal conductivity.  The reference's own Impulsion and Collision
+// objects are built from them.
+namespace {
+struct Bodies {
+  std::vector<Impulsion::PhysicalObject*> objs;
+  std::vector<Impulsion::RigidBody*> bodies;
+  std::vector<Collision::ShapeBase*> shapes;
+  VECTOR<Impulsion::PhysicalObject*> list;
+  Bodies(const float* b, int nb) {
+    for (int k = 0; k < nb; ++k) {
+      const float* q = b + 32 * k;
+      Impulsion::RigidBody* rb = new Impulsion::RigidBody(Vec3(q[2], q[3], q[4]), Vec3(q[5], q[6], q[7]), 1.0f);
+      rb->SetOrientation(Mat33(Vec3(q[11], q[12], q[13]), Vec3(q[14], q[15], q[16]), Vec3(q[17], q[18], q[19])));
+      rb->SetAngularVelocity(Vec3(q[8], q[9], q[10]));
+      Collision::ShapeBase* sh;
+      if (q[0] == 0.0f) {
+        sh = new Collision::SphereShape(q[20]);
+      } else {
+        Collision::ConvexPolytope* cp = new Collision::ConvexPolytope(q[1] != 0.0f);
+        Collision::ConvexPolytope_MakeBox(*cp, Vec3(q[20], q[21], q[22]));
+        sh = cp;
+      }
+      Impulsion::PhysicalObject* po = new Impulsion::PhysicalObject(
+          rb, sh, Impulsion::FrictionProperties(), Impulsion::ThermalProperties(q[23], q[24], 1.0f));
+      bodies.push_back(rb);
+      shapes.push_back(sh);
+      objs.push_back(po);
+      list.PushBack(po);
+    }
+  }
+  ~Bodies() {
+    for (auto* o : objs) delete o;
+    for (auto* s : shapes) delete s;
+    for (auto* r : bodies) delete r;
+  }
+};
+
+void load_particles(VECTOR<Particle>& p, const float* pos, const float* vel, const float* angvel, const float* size,
+                    const float* density, size_t n) {
+  p.Clear();
+  p.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle q;
+    q.mPosition = Vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    q.mVelocity = Vec3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+    if (angvel) q.mAngularVelocity = Vec3(angvel[3 * i], angvel[3 * i + 1], angvel[3 * i + 2]);
+    q.mSize = size[i];
+    q.mDensity = density ? density[i] : 1.0f;
+    p.PushBack(q);
+  }
+}
+
+void store_particles(const VECTOR<Particle>& p, float* pos, float* vel, float* angvel, float* density) {
+  for (size_t i = 0; i < p.Size(); ++i) {
+    pos[3 * i] = p[i].mPosition.x, pos[3 * i + 1] = p[i].mPosition.y, pos[3 * i + 2] = p[i].mPosition.z;
+    vel[3 * i] = p[i].mVelocity.x, vel[3 * i + 1] = p[i].mVelocity.y, vel[3 * i + 2] = p[i].mVelocity.z;
+    if (angvel)
+      angvel[3 * i] = p[i].mAngularVelocity.x, angvel[3 * i + 1] = p[i].mAngularVelocity.y,
+      angvel[3 * i + 2] = p[i].mAngularVelocity.z;
+    if (density) density[i] = p[i].mDensity;
+  }
+}
+}  // namespace
+
+extern "C" {
+
+// FluidBodySim::CollideVortonsSlice (FluidBodySim/fluidBodySim.cpp:759-1180)
+// for each body in turn over all particles, as SolveBoundaryConditions runs
+// it for vortons (fluidBodySim.cpp:1651-1715); per body out9 receives the
+// linear impulse, angular impulse, heat to body, sum of particle temperatures
+// and the number of particles collided.
+void vgref_collide_vortons(float* pos, float* vel, float* angvel, const float* size, float* density, size_t n,
+                           const float* bodies, int nb, float ambient, float specific_heat, float* out9) {
+  VECTOR<Particle> p;
+  load_particles(p, pos, vel, angvel, size, density, n);
+  Bodies B(bodies, nb);
+  for (int k = 0; k < nb; ++k) {
+    Vec3 lin, ang;
+    float heat = 0.0f, sumT = 0.0f;
+    size_t cnt = 0;
+    FluidBodySim::CollideVortonsSlice(p, ambient, specific_heat, *B.objs[k], lin, ang, heat, sumT, cnt, 0, n);
+    float* o = out9 + 9 * k;
+    o[0] = lin.x, o[1] = lin.y, o[2] = lin.z, o[3] = ang.x, o[4] = ang.y, o[5] = ang.z;
+    o[6] = heat, o[7] = sumT, o[8] = (float)cnt;
+  }
+  store_particles(p, pos, vel, angvel, density);
+}
+
+// FluidBodySim::CollideTracersSlice (fluidBodySim.cpp:1300-1455) for each body
+// in turn; per body out6 receives the linear and angular impulses.
+void vgref_collide_tracers(float* pos, float* vel, const float* size, const float* density, size_t n,
+                           const float* bodies, int nb, float* out6) {
+  VECTOR<Particle> p;
+  load_particles(p, pos, vel, nullptr, size, density, n);
+  Bodies B(bodies, nb);
+  for (int k = 0; k < nb; ++k) {
+    Vec3 lin, ang;
+    FluidBodySim::CollideTracersSlice(p, *B.objs[k], lin, ang, 0, n);
+    float* o = out6 + 6 * k;
+    o[0] = lin.x, o[1] = lin.y, o[2] = lin.z, o[3] = ang.x, o[4] = ang.y, o[5] = ang.z;
+  }
+  std::vector<float> dummy(n);
+  store_particles(p, pos, vel, nullptr, nullptr);
+}
+
+// FluidBodySim::RemoveEmbeddedParticles (fluidBodySim.cpp:365-417): order_out
+// receives the surviving particles' original indices in the order the
+// operation leaves them (each particle carries its index in mDensity).
+void vgref_remove_embedded(const float* pos, const float* size, size_t n, const float* bodies, int nb,
+                           unsigned* order_out, size_t* m) {
+  VECTOR<Particle> p;
+  p.Reserve(n);
+  for (size_t i = 0; i < n; ++i) {
+    Particle q;
+    q.mPosition = Vec3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+    q.mSize = size[i];
+    q.mDensity = (float)i;
+    p.PushBack(q);
+  }
+  Bodies B(bodies, nb);
+  FluidBodySim::RemoveEmbeddedParticles(p, B.list);
+  *m = p.Size();
+  for (size_t i = 0; i < p.Size(); ++i) order_out[i] = (unsigned)p[i].mDensity;
 }
 
 }  // extern "C"

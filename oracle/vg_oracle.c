@@ -1578,3 +1578,336 @@ size_t vgo_marching_cubes(const vgo_geom* g, const float* v, float iso, float* v
 void vgo_marching_cubes_table(int* count, int* tri15) {
   for (int m = 0; m < 256; ++m) count[m] = mc_case(m, tri15 + 15 * m);
 }
+
+/* ------------------------------------------------- fluid-body boundary conditions */
+
+typedef struct {
+  float x, y, z;
+} v3_t;
+static v3_t v3(float x, float y, float z) {
+  v3_t r = {x, y, z};
+  return r;
+}
+static v3_t v3add(v3_t a, v3_t b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static v3_t v3sub(v3_t a, v3_t b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static v3_t v3mul(v3_t a, float f) { return v3(a.x * f, a.y * f, a.z * f); }
+static float v3dot(v3_t a, v3_t b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static v3_t v3cross(v3_t a, v3_t b) { return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x); }
+static float v3mag(v3_t a) { return sqrtf(v3dot(a, a)); }
+/* Vec3::GetDirFast (vec3.h:429) and GetDir (vec3.h:428). */
+static v3_t v3dirfast(v3_t a) { return v3mul(a, vgo_finvsqrtf(v3dot(a, a) + FLT_MIN)); }
+static v3_t v3dir(v3_t a) { return v3mul(v3mul(a, 1.0f), 1.0f / sqrtf(v3dot(a, a) + FLT_MIN)); }
+
+/* A rigid body of the fluid-body simulation, 32 floats: [0] shape (0 sphere,
+ * 1 box), [1] hole (box only), [2..4] position, [5..7] velocity, [8..10]
+ * angular velocity, [11..19] orientation rows, [20..22] sphere radius (x) or
+ * box dimensions, [23] temperature, [24] thermal conductivity. */
+typedef struct {
+  int box;
+  float parity, brad;
+  v3_t pos, vel, angvel, row[3];
+  v3_t pn[6];
+  float pw[6];
+  float temperature, conductivity;
+} body_t;
+
+/* PhysicalObject with SphereShape, or ConvexPolytope made by
+ * ConvexPolytope_MakeBox (Collision/convexPolytope.cpp:346-376). */
+static body_t body_load(const float* q) {
+  body_t b;
+  memset(&b, 0, sizeof(b));
+  b.box = q[0] != 0.0f;
+  b.parity = (b.box && q[1] != 0.0f) ? -1.0f : 1.0f;
+  b.pos = v3(q[2], q[3], q[4]);
+  b.vel = v3(q[5], q[6], q[7]);
+  b.angvel = v3(q[8], q[9], q[10]);
+  for (int r = 0; r < 3; ++r) b.row[r] = v3(q[11 + 3 * r], q[12 + 3 * r], q[13 + 3 * r]);
+  b.temperature = q[23];
+  b.conductivity = q[24];
+  if (!b.box) {
+    b.brad = q[20];
+  } else {
+    const float x = q[20] * 0.5f, y = q[21] * 0.5f, z = q[22] * 0.5f;
+    const float half[3] = {x, y, z};
+    for (int a = 0; a < 3; ++a) {
+      float n1[3] = {0, 0, 0}, n2[3] = {0, 0, 0};
+      n1[a] = 1.0f;
+      n2[a] = -1.0f;
+      b.pn[2 * a] = v3(n1[0], n1[1], n1[2]);
+      b.pn[2 * a + 1] = v3(n2[0], n2[1], n2[2]);
+      b.pw[2 * a] = b.pw[2 * a + 1] = half[a];
+    }
+    if (b.parity < 0.0f) {
+      const float thin = 1.0f - FLT_EPSILON;
+      b.brad = thin * minf_(minf_(x, y), z);
+    } else {
+      const float fatten = 1.0f + FLT_EPSILON;
+      b.brad = 0.5f * fatten * v3mag(v3(q[20], q[21], q[22]));
+    }
+  }
+  return b;
+}
+
+/* Mat33::TransformByTranspose (mat33.h:131-134) and Transform (mat33.h:108-113). */
+static v3_t xform_t(const body_t* b, v3_t v) { return v3(v3dot(b->row[0], v), v3dot(b->row[1], v), v3dot(b->row[2], v)); }
+static v3_t xform(const body_t* b, v3_t v) {
+  return v3(v3dot(v3(b->row[0].x, b->row[1].x, b->row[2].x), v), v3dot(v3(b->row[0].y, b->row[1].y, b->row[2].y), v),
+            v3dot(v3(b->row[0].z, b->row[1].z, b->row[2].z), v));
+}
+
+/* ConvexPolytope::ContactDistance (convexPolytope.cpp:97-144): the largest
+ * plane distance of the point in body space, times the parity. */
+static float contact_distance(const body_t* b, v3_t q, int* idx) {
+  const v3_t r = xform_t(b, v3sub(q, b->pos));
+  float largest = -FLT_MAX;
+  for (int i = 0; i < 6; ++i) {
+    const float d = v3dot(r, b->pn[i]) - b->pw[i];
+    if (d > largest) {
+      largest = d;
+      *idx = i;
+    }
+  }
+  return largest * b->parity;
+}
+
+/* ConvexPolytope::CollisionDistance with velocities (convexPolytope.cpp:151-196). */
+static float collision_distance(const body_t* b, v3_t q, v3_t qv, int* idx) {
+  const v3_t r = xform_t(b, v3sub(q, b->pos));
+  const v3_t rv = xform_t(b, v3sub(qv, b->vel));
+  float largest = -FLT_MAX;
+  for (int i = 0; i < 6; ++i) {
+    const float d = v3dot(r, b->pn[i]) - b->pw[i];
+    if (d > largest) {
+      const float speed = v3dot(rv, b->pn[i]) * b->parity;
+      if (speed <= 0.0f || d >= 0.0f || b->parity < 0.0f) {
+        largest = d;
+        *idx = i;
+      }
+    }
+  }
+  return largest * b->parity;
+}
+
+/* ConvexPolytope::ContactPoint (convexPolytope.cpp:325-339). */
+static v3_t contact_point(const body_t* b, v3_t q, int idx, float dist, v3_t* n) {
+  *n = v3mul(xform(b, b->pn[idx]), b->parity);
+  return v3sub(q, v3mul(*n, dist));
+}
+
+/* Vorton::AccumulateVelocity (vorton.h:240-243): the reference velocity law
+ * of one vorton at a query point, spreading factors 1. */
+static v3_t vorton_velocity(v3_t q, v3_t p, v3_t w, float size) {
+  float acc[3] = {0.0f, 0.0f, 0.0f};
+  const float qq[3] = {q.x, q.y, q.z}, pp[3] = {p.x, p.y, p.z}, ww[3] = {w.x, w.y, w.z};
+  accum(0, acc, qq, pp, ww, size, 1.0f, 1.0f);
+  return v3(acc[0], acc[1], acc[2]);
+}
+
+/* FluidBodySim::CollideVortonsSlice (FluidBodySim/fluidBodySim.cpp:759-1180)
+ * with the shipped switches (no-slip / no-through boundary respecting the
+ * ambient flow without the vorton's own old contribution, the vorton placed
+ * outside the body and bounced, vorticity by the Brinkman penalty blended with
+ * gain 0.1 and the body's spin, heat conducted, smoothed-particle form so no
+ * linear impulse), for each body in turn over all particles.  Per body out9
+ * receives linear impulse, angular impulse, heat to body, sum of particle
+ * temperatures and the collision count. */
+void vgo_collide_vortons(float* pos, float* vel, float* angvel, const float* size, float* density, size_t n,
+                         const float* bodies, int nb, float ambient, float specific_heat, float* out9) {
+  const float thin = 1.0f - FLT_EPSILON, fatten = 1.0f + FLT_EPSILON, nudge = 1.0f + 1.0e-4f;
+  const float impact = 1.0f + 0.01f;
+  for (int k = 0; k < nb; ++k) {
+    const body_t B = body_load(bodies + 32 * k);
+    v3_t ang_imp = v3(0.0f, 0.0f, 0.0f);
+    float heat = 0.0f, sum_t = 0.0f;
+    size_t count = 0;
+    const float one_over_cp = 1.0f / specific_heat;
+    size_t incr = 1, repeat = 0;
+    for (size_t i = 0; i < n; i += incr) {
+      repeat = (0 == incr) ? repeat + 1 : 0;
+      incr = 1;
+      v3_t p = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+      v3_t v = v3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+      v3_t w = v3(angvel[3 * i], angvel[3 * i + 1], angvel[3 * i + 2]);
+      const float r = size[i] * 0.5f, r2 = r * r;
+      const v3_t s2v = v3sub(p, B.pos);
+      const float fs2v = v3mag(s2v);
+      const float bnd = 1.5f * r;
+      int broad;
+      if (B.parity < 0.0f)
+        broad = fs2v > maxf_(B.brad - bnd, 0.0f) * thin;
+      else
+        broad = fs2v < (B.brad + bnd) * fatten;
+      if (!broad) continue;
+      v3_t cw, n3;
+      float cdist;
+      if (!B.box) {
+        const v3_t dir = v3mul(s2v, 1.0f / fs2v);
+        const v3_t crel = v3mul(dir, B.brad);
+        cw = v3add(crel, B.pos);
+        n3 = dir;
+        cdist = fs2v - B.brad;
+      } else {
+        int idx = 0;
+        cdist = contact_distance(&B, p, &idx);
+        if (!(cdist < bnd)) continue;
+        cw = contact_point(&B, p, idx, cdist, &n3);
+        if (B.parity < 0.0f && repeat < 5 && cdist < r) incr = 0;
+      }
+      ++count;
+      const v3_t vbody = B.vel;
+      v3_t vort_old = v3mul(w, 2.0f);
+      const v3_t due_old = vorton_velocity(cw, p, w, size[i]);
+      const v3_t flow = v3sub(v3sub(v, due_old), vbody);
+      (void)v3dirfast(flow);
+      const float disp = cdist < r ? r : cdist;
+      p = v3add(cw, v3mul(v3mul(n3, disp), nudge));
+      {
+        const v3_t vrel = v3sub(v, vbody);
+        const float speed_n = v3dot(vrel, n3);
+        const v3_t impulse = v3mul(n3, -speed_n);
+        v = v3add(v, v3mul(impulse, impact));
+      }
+      if (repeat >= 1) {
+        v = v3(0.0f, 0.0f, 0.0f);
+        w = v3(0.0f, 0.0f, 0.0f);
+        vort_old = w;
+      } else {
+        /* Vorton::AssignVorticityByPenalty (vorton.h:275-306) */
+        const v3_t rel = v3sub(cw, p);
+        const v3_t vd = v3sub(v, vbody);
+        const float dist = v3mag(rel) - size[i] * 0.4f;
+        const v3_t vdir = v3dir(v3cross(vd, rel));
+        const float vmag = v3mag(vd) / dist;
+        w = v3mul(v3mul(vdir, vmag), 0.5f);
+      }
+      w = v3add(w, v3sub(v3mul(B.angvel, 1.0f), v3mul(vort_old, 0.5f)));
+      {
+        const float gain = 0.1f, one_minus = 1.0f - gain;
+        w = v3mul(v3add(v3mul(v3mul(w, 2.0f), gain), v3mul(vort_old, one_minus)), 0.5f);
+      }
+      const v3_t angdiff = v3mul(v3sub(vort_old, v3mul(w, 2.0f)), 0.5f);
+      {
+        const float t_old = 300.0f * ambient / density[i];
+        const float t_diff = B.temperature - t_old;
+        const float t_gain = clampf_(B.conductivity * r * 0.03f * specific_heat, -0.5f, 0.5f);
+        const float t_change = t_diff * t_gain;
+        const float heat_ex = t_change * one_over_cp;
+        const float t_new = t_old + t_change;
+        density[i] = ambient * 300.0f / t_new;
+        heat -= heat_ex;
+        sum_t += t_old;
+      }
+      {
+        const float pi_over_6 = PI_F / 6.0f;
+        const float mass = density[i] * (pi_over_6 * size[i] * size[i] * size[i]);
+        const float moi = 0.4f * mass * r2;
+        ang_imp = v3add(ang_imp, v3mul(angdiff, moi));
+      }
+      pos[3 * i] = p.x, pos[3 * i + 1] = p.y, pos[3 * i + 2] = p.z;
+      vel[3 * i] = v.x, vel[3 * i + 1] = v.y, vel[3 * i + 2] = v.z;
+      angvel[3 * i] = w.x, angvel[3 * i + 1] = w.y, angvel[3 * i + 2] = w.z;
+    }
+    float* o = out9 + 9 * k;
+    o[0] = o[1] = o[2] = 0.0f;
+    o[3] = ang_imp.x, o[4] = ang_imp.y, o[5] = ang_imp.z;
+    o[6] = heat, o[7] = sum_t, o[8] = (float)count;
+  }
+}
+
+/* FluidBodySim::CollideTracersSlice (fluidBodySim.cpp:1300-1455) for each
+ * body in turn: a tracer in contact is placed outside the body (sphere: at
+ * bounding radius plus its radius along its direction from the centre; box:
+ * from the contact point along the face normal) and its velocity bounced
+ * with impact coefficient 1.01; per body out6 receives the linear and angular
+ * impulses on the body (tracer mass = density x volume). */
+void vgo_collide_tracers(float* pos, float* vel, const float* size, const float* density, size_t n,
+                         const float* bodies, int nb, float* out6) {
+  const float thin = 1.0f - FLT_EPSILON, fatten = 1.0f + FLT_EPSILON, nudge = 1.0f + 1.0e-4f;
+  const float impact = 1.0f + 0.01f;
+  for (int k = 0; k < nb; ++k) {
+    const body_t B = body_load(bodies + 32 * k);
+    v3_t lin = v3(0.0f, 0.0f, 0.0f), ang = v3(0.0f, 0.0f, 0.0f);
+    size_t incr = 1, repeat = 0;
+    for (size_t i = 0; i < n; i += incr) {
+      repeat = (0 == incr) ? repeat + 1 : 0;
+      incr = 1;
+      v3_t p = v3(pos[3 * i], pos[3 * i + 1], pos[3 * i + 2]);
+      v3_t v = v3(vel[3 * i], vel[3 * i + 1], vel[3 * i + 2]);
+      const float r = size[i] * 0.5f;
+      const v3_t s2t = v3sub(p, B.pos);
+      const float fs2t = v3mag(s2t);
+      int broad;
+      if (B.parity < 0.0f)
+        broad = fs2t > maxf_(B.brad - r, 0.0f) * thin;
+      else
+        broad = fs2t < (B.brad + r) * fatten;
+      if (!broad) continue;
+      v3_t cp, n3, disp_new;
+      if (!B.box) {
+        const float rescale = (B.brad + r) * (1.0f + FLT_EPSILON) / fs2t;
+        disp_new = v3mul(s2t, rescale);
+        cp = disp_new;
+        n3 = v3dirfast(s2t);
+      } else {
+        int idx = 0;
+        const float cdist = collision_distance(&B, p, v, &idx);
+        if (!(cdist < r)) continue;
+        cp = contact_point(&B, p, idx, cdist, &n3);
+        disp_new = v3sub(v3add(cp, v3mul(v3mul(n3, r), nudge)), B.pos);
+        if (B.parity < 0.0f && repeat < 5) incr = 0;
+      }
+      const v3_t vrot = v3cross(B.angvel, disp_new);
+      const v3_t vbody = v3add(B.vel, vrot);
+      const v3_t vrel = v3sub(v, vbody);
+      const float speed_n = v3dot(vrel, n3);
+      const v3_t impulse = v3mul(n3, -speed_n);
+      const v3_t vnew = v3add(v, v3mul(impulse, impact));
+      const float pi_over_6 = PI_F / 6.0f;
+      const float mass = density[i] * (pi_over_6 * size[i] * size[i] * size[i]);
+      const v3_t li = v3mul(v3sub(v, vnew), mass);
+      lin = v3add(lin, li);
+      ang = v3add(ang, v3cross(v3sub(cp, B.pos), li));
+      p = v3add(B.pos, disp_new);
+      pos[3 * i] = p.x, pos[3 * i + 1] = p.y, pos[3 * i + 2] = p.z;
+      vel[3 * i] = vnew.x, vel[3 * i + 1] = vnew.y, vel[3 * i + 2] = vnew.z;
+    }
+    float* o = out6 + 6 * k;
+    o[0] = lin.x, o[1] = lin.y, o[2] = lin.z, o[3] = ang.x, o[4] = ang.y, o[5] = ang.z;
+  }
+}
+
+/* FluidBodySim::RemoveEmbeddedParticles (fluidBodySim.cpp:365-417): for each
+ * body in turn, particles within its bounding sphere that lie inside it
+ * (sphere: inside the bounding sphere; box: contact distance below the
+ * particle's radius) are removed by moving the last particle into their slot
+ * (Particles::Kill) and testing the slot again.  order receives the
+ * survivors' original indices in the order left. */
+void vgo_remove_embedded(const float* pos, const float* size, size_t n, const float* bodies, int nb, unsigned* order,
+                         size_t* m) {
+  size_t cnt = n;
+  for (size_t i = 0; i < n; ++i) order[i] = (unsigned)i;
+  for (int k = 0; k < nb; ++k) {
+    const body_t B = body_load(bodies + 32 * k);
+    for (size_t i = 0; i < cnt;) {
+      const unsigned j = order[i];
+      const v3_t p = v3(pos[3 * j], pos[3 * j + 1], pos[3 * j + 2]);
+      const float d = v3mag(v3sub(p, B.pos));
+      int kill = 0;
+      if (d < B.brad) {
+        if (!B.box) {
+          kill = 1;
+        } else {
+          int idx = 0;
+          kill = contact_distance(&B, p, &idx) < size[j] * 0.5f;
+        }
+      }
+      if (kill) {
+        order[i] = order[cnt - 1];
+        --cnt;
+      } else {
+        ++i;
+      }
+    }
+  }
+  *m = cnt;
+}

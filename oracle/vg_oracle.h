@@ -129,6 +129,13 @@ void vgo_signed_distance(const vgo_geom* g, const float* density, float ambient,
 /* Marching cubes: up to cap triangles (9 floats of positions, 9 of normals each); returns the count. */
 size_t vgo_marching_cubes(const vgo_geom* g, const float* v, float iso, float* verts, float* normals, size_t cap);
 void vgo_marching_cubes_table(int* count, int* tri15);
+/* Fluid-body boundary conditions (bodies: 32 floats each, see vg_oracle.c). */
+void vgo_collide_vortons(float* pos, float* vel, float* angvel, const float* size, float* density, size_t n,
+                         const float* bodies, int nb, float ambient, float specific_heat, float* out9);
+void vgo_collide_tracers(float* pos, float* vel, const float* size, const float* density, size_t n,
+                         const float* bodies, int nb, float* out6);
+void vgo_remove_embedded(const float* pos, const float* size, size_t n, const float* bodies, int nb, unsigned* order,
+                         size_t* m);
 
 #ifdef __cplusplus
 }

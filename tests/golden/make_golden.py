@@ -11,6 +11,7 @@ Usage (needs the reference tree or a staged copy; run in this container):
     python tests/golden/make_golden.py lifecycle    # lifecycle.npz (PclOpKillAge, PclOpWind)
     python tests/golden/make_golden.py heat         # heat.npz (DiffuseAndDissipateHeatPSE)
     python tests/golden/make_golden.py surface      # surface.npz (density grid, gradient, baroclinic, SDF)
+    python tests/golden/make_golden.py bodies       # bodies.npz (fluid-body collisions, embedded particles)
 """
 import ctypes
 import os
@@ -27,6 +28,7 @@ OUT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "reference.npz")
 OUT_LIFE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lifecycle.npz")
 OUT_HEAT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "heat.npz")
 OUT_SURF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "surface.npz")
+OUT_BODY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bodies.npz")
 
 
 def P(a):
@@ -307,6 +309,45 @@ def surface():
     print(f"wrote {OUT_SURF} ({os.path.getsize(OUT_SURF) / 1e3:.1f} kB, {len(g)} arrays)")
 
 
+def bodies():
+    """FluidBodySim::CollideVortonsSlice, CollideTracersSlice (per body in
+    turn) and RemoveEmbeddedParticles from the reference's own code
+    (oracle/ref_build/ref_harness.cpp) on a seeded puff of 2,000 particles
+    with three bodies: a moving, spinning, hot sphere; a hollow rotated box
+    that contains the fluid; a small moving, spinning, rotated solid box."""
+    oracle.build()
+    R = oracle.ref("serial")
+    n = 2000
+    pos, w, s = workloads.puff(n, seed=9, sigma=0.5, clip=1.2)
+    rng = np.random.default_rng(2)
+    vel = rng.normal(0.0, 0.5, (n, 3)).astype(np.float32)
+    dens = (1.0 + 0.1 * rng.random(n)).astype(np.float32)
+    c, sn = np.cos(0.3), np.sin(0.3)
+    rot = np.array([[c, -sn, 0], [sn, c, 0], [0, 0, 1]], np.float32)
+    B = np.stack([oracle.body(0, [0.2, 0, 0], [0.4], velocity=[0.5, 0, 0], angular_velocity=[0, 0, 1],
+                              temperature=350, conductivity=0.5),
+                  oracle.body(1, [0, 0, 0], [2.0, 2.0, 1.6], hole=True, orientation=rot, temperature=300,
+                              conductivity=0.1),
+                  oracle.body(1, [0.0, 0.5, 0.3], [0.3, 0.4, 0.5], velocity=[0, 0.2, 0], angular_velocity=[0.3, 0, 0],
+                              orientation=rot, temperature=320, conductivity=0.2)]).astype(np.float32)
+    g = {"b_pos": pos, "b_vel": vel, "b_angvel": w, "b_size": s, "b_density": dens, "b_bodies": B}
+    p, v, a, d = pos.copy(), vel.copy(), w.copy(), dens.copy()
+    out = np.zeros((len(B), 9), np.float32)
+    R.vgref_collide_vortons(P(p), P(v), P(a), P(s), P(d), ctypes.c_size_t(n), P(B), len(B), ctypes.c_float(1.0),
+                            ctypes.c_float(1.0), P(out))
+    g.update({"b_vort_pos": p, "b_vort_vel": v, "b_vort_angvel": a, "b_vort_density": d, "b_vort_sums": out})
+    p, v = pos.copy(), vel.copy()
+    out6 = np.zeros((len(B), 6), np.float32)
+    R.vgref_collide_tracers(P(p), P(v), P(s), P(dens), ctypes.c_size_t(n), P(B), len(B), P(out6))
+    g.update({"b_tr_pos": p, "b_tr_vel": v, "b_tr_sums": out6})
+    order = np.zeros(n, np.uint32)
+    m = ctypes.c_size_t()
+    R.vgref_remove_embedded(P(pos), P(s), ctypes.c_size_t(n), P(B), len(B), P(order), ctypes.byref(m))
+    g["b_survivors"] = order[: m.value].copy()
+    np.savez_compressed(OUT_BODY, **g)
+    print(f"wrote {OUT_BODY} ({os.path.getsize(OUT_BODY) / 1e3:.1f} kB, {len(g)} arrays)")
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lifecycle":
         lifecycle()
@@ -314,5 +355,7 @@ if __name__ == "__main__":
         heat()
     elif len(sys.argv) > 1 and sys.argv[1] == "surface":
         surface()
+    elif len(sys.argv) > 1 and sys.argv[1] == "bodies":
+        bodies()
     else:
         main()

@@ -59,10 +59,14 @@ def surf():
     return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "surface.npz")))
 
 
+# Device inputs are held in named tensors until the stream is synchronised: a
+# temporary's memory goes back to torch's caching allocator when the Python
+# object dies, and the next temporary can be given the same block.
+
 def density_grid(vg, ctx, g, pos, size, dens, ambient):
     out = torch.zeros(g.capacity, dtype=torch.float32, device="cuda")
-    ctx.check(vg.lib().vg_density_grid_device(ctx.h, ctypes.byref(g), vg._ptr(dev(f4(pos, size))),
-                                              vg._ptr(dev(dens.astype(np.float32))), len(pos), ambient,
+    ps, d = dev(f4(pos, size)), dev(dens.astype(np.float32))
+    ctx.check(vg.lib().vg_density_grid_device(ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(d), len(pos), ambient,
                                               vg._ptr(out)), "density grid")
     ctx.synchronize()
     return out.cpu().numpy()
@@ -70,8 +74,9 @@ def density_grid(vg, ctx, g, pos, size, dens, ambient):
 
 def signed_distance(vg, ctx, g, dgrid, ambient, reference_stats):
     out = torch.zeros(g.capacity, dtype=torch.float32, device="cuda")
-    ctx.check(vg.lib().vg_signed_distance_device(ctx.h, ctypes.byref(g), vg._ptr(dev(dgrid)), ambient,
-                                                 reference_stats, vg._ptr(out)), "signed distance")
+    d = dev(dgrid)
+    ctx.check(vg.lib().vg_signed_distance_device(ctx.h, ctypes.byref(g), vg._ptr(d), ambient, reference_stats,
+                                                 vg._ptr(out)), "signed distance")
     ctx.synchronize()
     return out.cpu().numpy()
 
@@ -84,26 +89,28 @@ def test_density_gradient_baroclinic_bit_exact(vg, ctx, surf):
         dg = density_grid(vg, ctx, g, pos, size, dens, ambient)
         assert np.array_equal(bits(dg), bits(surf[f"s{i}_density_grid"])), i
         grad = torch.zeros((g.capacity, 3), dtype=torch.float32, device="cuda")
-        ctx.check(vg.lib().vg_gradient_device(ctx.h, ctypes.byref(g), vg._ptr(dev(dg)), vg._ptr(grad)), "gradient")
+        dgd = dev(dg)
+        ctx.check(vg.lib().vg_gradient_device(ctx.h, ctypes.byref(g), vg._ptr(dgd), vg._ptr(grad)), "gradient")
         ctx.synchronize()
         assert np.array_equal(bits(grad.cpu().numpy()), bits(surf[f"s{i}_gradient"])), i
         w = dev(f4(surf[f"s{i}_angvel"]))
+        ps, dd = dev(f4(pos, size)), dev(dens)
+        grav = np.ascontiguousarray(surf[f"s{i}_grav"], np.float32)
         applied = ctypes.c_int()
-        ctx.check(vg.lib().vg_baroclinic_device(ctx.h, ctypes.byref(g), vg._ptr(dev(f4(pos, size))),
-                                                vg._ptr(dev(dens)), vg._ptr(w), len(pos),
-                                                vg._ptr(np.ascontiguousarray(surf[f"s{i}_grav"], np.float32)),
-                                                ambient, dt, ctypes.byref(applied)), "baroclinic")
+        ctx.check(vg.lib().vg_baroclinic_device(ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(dd), vg._ptr(w),
+                                                len(pos), vg._ptr(grav), ambient, dt, ctypes.byref(applied)),
+                  "baroclinic")
         ctx.synchronize()
         assert applied.value == int(surf[f"s{i}_applied"])
         assert np.array_equal(bits(w.cpu().numpy()[:, :3]), bits(surf[f"s{i}_baroclinic"])), i
     # no gravity along the grid: nothing changes (the reference's early return)
     g = vg.GridGeom.from12(surf["s0_geom"], surf["s0_np"])
     w = dev(f4(surf["s0_angvel"]))
+    ps, dd = dev(f4(surf["s0_pos"], surf["s0_size"])), dev(surf["s0_density"])
     applied = ctypes.c_int(7)
-    ctx.check(vg.lib().vg_baroclinic_device(ctx.h, ctypes.byref(g), vg._ptr(dev(f4(surf["s0_pos"], surf["s0_size"]))),
-                                            vg._ptr(dev(surf["s0_density"])), vg._ptr(w), len(surf["s0_pos"]),
-                                            vg._ptr(np.zeros(3, np.float32)), ambient, dt, ctypes.byref(applied)),
-              "baroclinic")
+    ctx.check(vg.lib().vg_baroclinic_device(ctx.h, ctypes.byref(g), vg._ptr(ps), vg._ptr(dd), vg._ptr(w),
+                                            len(surf["s0_pos"]), vg._ptr(np.zeros(3, np.float32)), ambient, dt,
+                                            ctypes.byref(applied)), "baroclinic")
     ctx.synchronize()
     assert applied.value == 0 and np.array_equal(w.cpu().numpy()[:, :3], surf["s0_angvel"])
 

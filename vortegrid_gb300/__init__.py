@@ -120,7 +120,8 @@ EXPORTS = [
     "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
     "vg_evolve_device", "vg_direct_noalloc", "vg_wind_device", "vg_kill_age_device", "vg_heat_pse_device",
     "vg_density_grid_device", "vg_gradient_device", "vg_baroclinic_device", "vg_signed_distance_device",
-    "vg_marching_cubes_device",
+    "vg_marching_cubes_device", "vg_collide_vortons_device", "vg_collide_tracers_device",
+    "vg_remove_embedded_device",
     "vg_net_create", "vg_net_destroy", "vg_net_last_error", "vg_net_param_count", "vg_net_set_params",
     "vg_net_get_params", "vg_net_save", "vg_net_load", "vg_net_guess_device", "vg_net_backward_device",
     "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
@@ -181,6 +182,10 @@ def lib():
         L.vg_marching_cubes_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(GridGeom), ctypes.c_void_p,
                                                ctypes.c_float, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t,
                                                ctypes.POINTER(ctypes.c_size_t)]
+        _v, _i, _s, _f = ctypes.c_void_p, ctypes.c_int, ctypes.c_size_t, ctypes.c_float
+        L.vg_collide_vortons_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, _f, _f, _v, _v]
+        L.vg_collide_tracers_device.argtypes = [_v, _v, _i, _v, _v, _v, _s, _v]
+        L.vg_remove_embedded_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, ctypes.POINTER(ctypes.c_size_t)]
         L.vg_wind_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                      ctypes.c_float, ctypes.c_float]
         L.vg_kill_age_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,

@@ -235,6 +235,7 @@ enum Slot {
   S_GRAD,   // density gradient grid (baroclinic)
   S_SDF,    // signed distance: pinned flags, statistics, partial sums
   S_MC,     // marching cubes: per-cell counts and offsets
+  S_BODY,   // fluid-body collisions: per-block partial sums
   S_NUM
 };
 
