@@ -420,3 +420,60 @@ def ref(kind="serial"):
         L.vgref_step.restype = ctypes.c_int
         _ref[kind] = L
     return _ref[kind]
+
+
+def srand(seed):
+    """Seed the C library's rand(), the draws the reference's emitters consume."""
+    ctypes.CDLL(None).srand(ctypes.c_uint(seed))
+
+
+def rand_max():
+    return int(lib().vgo_rand_max())
+
+
+def jitter_hash(seed, d):
+    """Draw d of the device emitter's counter-based jitter stream."""
+    f = lib().vgo_jitter_hash
+    f.argtypes = [ctypes.c_uint, ctypes.c_uint64]
+    return int(f(seed, d))
+
+
+def emit_grid(g, multiplier, vortons=None, host_rand=True, seed=0):
+    """PclOpEmit::Emit on grid g (vortons: None or (pos, density)); host_rand
+    draws from the C library's rand() as it stands.  Returns (pos, density,
+    size) of the particles emitted."""
+    m = int(multiplier)
+    cells = int(np.prod([int(v) - 1 for v in g.np]))
+    cap = cells * m ** 3
+    pos = np.zeros((max(cap, 1), 3), np.float32)
+    dens = np.zeros(max(cap, 1), np.float32)
+    size = np.zeros(max(cap, 1), np.float32)
+    cnt = ctypes.c_size_t()
+    vp, vd, nv = (f32(vortons[0]), f32(vortons[1]), len(vortons[1])) if vortons is not None else (
+        np.zeros((1, 3), np.float32), np.zeros(1, np.float32), 0)
+    lib().vgo_emit_grid(ctypes.byref(g), ctypes.c_uint(m), _p(vp), _p(vd), ctypes.c_size_t(nv),
+                        ctypes.c_int(vortons is not None), ctypes.c_int(bool(host_rand)), ctypes.c_uint(seed),
+                        _p(pos), _p(dens), _p(size), ctypes.c_size_t(cap), ctypes.byref(cnt))
+    k = cnt.value
+    return pos[:k].copy(), dens[:k].copy(), size[:k].copy()
+
+
+def emit_operate(tmpl, spread, rate, dts, frame0=0, remainder=0.0, host_rand=True, seed=0):
+    """PclOpEmit::Operate for each time step in dts (frames frame0, frame0 + 1,
+    ...), appending to one array: (records float32[k, 18] -- 17 values and the
+    birth frame -- and the remainder after each call)."""
+    f = lib().vgo_emit_operate
+    f.restype = ctypes.c_size_t
+    t, s = f32(tmpl).ravel(), f32(spread).ravel()
+    rem = ctypes.c_float(remainder)
+    draw = ctypes.c_uint64(0)
+    recs, rems = [], []
+    for i, dt in enumerate(dts):
+        cap = int(float(dt) * float(rate) + rem.value) + 2
+        buf = np.zeros((cap, 18), np.float32)
+        k = f(_p(t), _p(s), ctypes.c_float(rate), ctypes.byref(rem), ctypes.c_float(dt),
+              ctypes.c_uint(frame0 + i), ctypes.c_int(bool(host_rand)), ctypes.c_uint(seed), ctypes.byref(draw),
+              _p(buf), ctypes.c_size_t(cap))
+        recs.append(buf[:k])
+        rems.append(rem.value)
+    return np.concatenate(recs) if recs else np.zeros((0, 18), np.float32), np.array(rems, np.float32)

@@ -21,6 +21,7 @@
 #include "Particles/Operation/pclOpFindBoundingBox.h"
 #include "Particles/Operation/pclOpKillAge.h"
 #include "Particles/Operation/pclOpWind.h"
+#include "Particles/Operation/pclOpEmit.h"
 #include "Core/SpatialPartition/uniformGridMath.h"
 #include "FluidBodySim/fluidBodySim.h"
 #include "Impulsion/physicalObject.h"
@@ -741,6 +742,74 @@ void vgref_remove_embedded(const float* pos, const float* size, size_t n, const 
   FluidBodySim::RemoveEmbeddedParticles(p, B.list);
   *m = p.Size();
   for (size_t i = 0; i < p.Size(); ++i) order_out[i] = (unsigned)p[i].mDensity;
+}
+
+}  // extern "C"
+
+extern "C" {
+
+// PclOpEmit::Emit (Particles/Operation/pclOpEmit.cpp:77-186) into an empty
+// array after srand(seed), with vortons (positions, sizes, densities) when
+// use_vortons is set.  Per emitted particle: position (3), density, size.
+void vgref_emit_grid(const float geom12[12], const unsigned np[3], unsigned multiplier, const float* vpos,
+                     const float* vsize, const float* vdens, size_t nv, int use_vortons, unsigned seed,
+                     float* pos_out, float* density_out, float* size_out, size_t max, size_t* count) {
+  UniformGridGeometry g;
+  load_geom(g, geom12, np);
+  VECTOR<Particle> vortons;
+  if (use_vortons) load_particles(vortons, vpos, vpos, nullptr, vsize, vdens, nv);
+  VECTOR<Particle> out;
+  srand(seed);
+  PclOpEmit::Emit(out, g, multiplier, use_vortons ? &vortons : nullptr);
+  *count = out.Size();
+  for (size_t i = 0; i < out.Size() && i < max; ++i) {
+    pos_out[3 * i] = out[i].mPosition.x, pos_out[3 * i + 1] = out[i].mPosition.y,
+    pos_out[3 * i + 2] = out[i].mPosition.z;
+    density_out[i] = out[i].mDensity;
+    size_out[i] = out[i].mSize;
+  }
+}
+
+// PclOpEmit::Operate (pclOpEmit.cpp:188-210) for each of `frames` calls
+// (time step dt[f], frame index frame0 + f) after one srand(seed), appending
+// to one array.  Template and spread are 17 floats (position, velocity,
+// orientation, angular velocity, density, fuel, flame and smoke fractions,
+// size); per particle rec_out receives those 17 values and the birth time (as
+// a float); remainder_out the emitter's remainder after each call.
+void vgref_emit_operate(const float tmpl[17], const float spread[17], float rate, const float* dt, int frames,
+                        unsigned frame0, unsigned seed, float* rec_out, size_t max, size_t* count,
+                        float* remainder_out) {
+  PclOpEmit op;
+  Particle* P[2] = {&op.mTemplate, &op.mSpread};
+  const float* V[2] = {tmpl, spread};
+  for (int k = 0; k < 2; ++k) {
+    const float* v = V[k];
+    P[k]->mPosition = Vec3(v[0], v[1], v[2]);
+    P[k]->mVelocity = Vec3(v[3], v[4], v[5]);
+    P[k]->mOrientation = Vec3(v[6], v[7], v[8]);
+    P[k]->mAngularVelocity = Vec3(v[9], v[10], v[11]);
+    P[k]->mDensity = v[12];
+    P[k]->mFuelFraction = v[13];
+    P[k]->mFlameFraction = v[14];
+    P[k]->mSmokeFraction = v[15];
+    P[k]->mSize = v[16];
+  }
+  op.mEmitRate = rate;
+  VECTOR<Particle> out;
+  srand(seed);
+  for (int f = 0; f < frames; ++f) {
+    op.Operate(out, dt[f], frame0 + (unsigned)f);
+    remainder_out[f] = op.mRemainder;
+  }
+  *count = out.Size();
+  for (size_t i = 0; i < out.Size() && i < max; ++i) {
+    const Particle& q = out[i];
+    const float r[18] = {q.mPosition.x, q.mPosition.y, q.mPosition.z, q.mVelocity.x, q.mVelocity.y, q.mVelocity.z,
+                         q.mOrientation.x, q.mOrientation.y, q.mOrientation.z, q.mAngularVelocity.x,
+                         q.mAngularVelocity.y, q.mAngularVelocity.z, q.mDensity, q.mFuelFraction,
+                         q.mFlameFraction, q.mSmokeFraction, q.mSize, (float)q.mBirthTime};
+    std::memcpy(rec_out + 18 * i, r, sizeof(r));
+  }
 }
 
 }  // extern "C"

@@ -1911,3 +1911,146 @@ void vgo_remove_embedded(const float* pos, const float* size, size_t n, const fl
   }
   *m = cnt;
 }
+
+/* ------------------------------------------------------------------ emitters */
+
+/* The counter-based jitter stream of the device emitter (used in place of
+ * the C library's rand() when asked): draw d of stream `seed` is the
+ * MurmurHash3 32-bit finalizer (fmix32, Austin Appleby, public domain) of the
+ * low word of d keyed by the seed and the high word, scaled to
+ * [0, RAND_MAX]. */
+static uint32_t fmix32_(uint32_t h) {
+  h ^= h >> 16;
+  h *= 0x85ebca6bu;
+  h ^= h >> 13;
+  h *= 0xc2b2ae35u;
+  h ^= h >> 16;
+  return h;
+}
+
+int vgo_jitter_hash(unsigned seed, uint64_t d) {
+  const uint32_t key = fmix32_(seed ^ ((uint32_t)(d >> 32) * 0x9e3779b9u + 0x7f4a7c15u));
+  const uint32_t h = fmix32_((uint32_t)d ^ key);
+  return (int)(((uint64_t)h * ((uint64_t)RAND_MAX + 1u)) >> 32);
+}
+
+int vgo_rand_max(void) { return RAND_MAX; }
+
+/* The next jitter draw: the C library's rand() (the reference's source) or
+ * the hash stream. */
+static int draw_(int host_rand, unsigned seed, uint64_t* d) {
+  const uint64_t k = (*d)++;
+  return host_rand ? rand() : vgo_jitter_hash(seed, k);
+}
+
+/* RandomSpread (Core/Math/math.h:183-188): spread * (r / RAND_MAX - 1/2). */
+static float spread_(float spread, int r) {
+  const float one_over_rand_max = 1.0f / (float)RAND_MAX;
+  return spread * ((float)r * one_over_rand_max - 0.5f);
+}
+
+/* RandomSpread of a Vec3 (Core/Math/vec3.h:540-545): the three calls are
+ * arguments of one constructor, which the compilers the reference targets
+ * evaluate last to first, so z draws first. */
+static void spread3_(const float s[3], int host_rand, unsigned seed, uint64_t* d, float out[3]) {
+  out[2] = spread_(s[2], draw_(host_rand, seed, d));
+  out[1] = spread_(s[1], draw_(host_rand, seed, d));
+  out[0] = spread_(s[0], draw_(host_rand, seed, d));
+}
+
+/* PclOpEmit::Emit (Particles/Operation/pclOpEmit.cpp:77-186): multiplier^3
+ * particles per cell of g, cells in z, y, x order and sub-cells likewise, at
+ * min corner + (it / m) spacing + half a sub-cell + a jitter below half a
+ * sub-cell.  With vortons, each vorton's density deviation from the ambient
+ * 1 is accumulated onto g (PopulateDensityDeviationGridFromParticles,
+ * pclOpEmit.cpp:29-57); nothing is emitted (and nothing drawn) when the
+ * deviation is zero everywhere, else a particle is kept where the
+ * interpolated deviation is at least half the largest magnitude, with
+ * density deviation + that magnitude.  Outputs: position, density, size of
+ * each particle kept, up to max; *count all kept. */
+void vgo_emit_grid(const vgo_geom* g, unsigned m, const float* vpos, const float* vdens, size_t nv, int use_vortons,
+                   int host_rand, unsigned seed, float* pos_out, float* dens_out, float* size_out, size_t max,
+                   size_t* count) {
+  const float ambient = 1.0f;
+  const float* sp = g->cell;
+  const float size = 0.5f * powf(sp[0] * sp[1] * sp[2], 1.0f / 3.0f) / (float)m;
+  const size_t pts = capacity(g);
+  float* dev = NULL;
+  float scale = 0.0f;
+  if (use_vortons) {
+    dev = (float*)calloc(pts, sizeof(float));
+    for (size_t i = 0; i < nv; ++i) accumulate1(g, dev, vpos + 3 * i, vdens[i] - ambient);
+    float lo = FLT_MAX, hi = -FLT_MAX;
+    for (size_t o = 0; o < pts; ++o) lo = minf_(dev[o], lo), hi = maxf_(dev[o], hi);
+    scale = maxf_(fabsf(hi), fabsf(lo));
+  }
+  float shift[3], jm[3];
+  const float jm_scale = 1.9999f * (1.0f - FLT_EPSILON);
+  for (int a = 0; a < 3; ++a) {
+    shift[a] = (0.5f * sp[a]) * (1.0f / (float)m);
+    jm[a] = shift[a] * jm_scale;
+  }
+  size_t kept = 0;
+  uint64_t d = 0;
+  if (!use_vortons || scale != 0.0f) {
+    const unsigned nc[3] = {g->np[0] - 1, g->np[1] - 1, g->np[2] - 1};
+    unsigned idx[3], it[3];
+    for (idx[2] = 0; idx[2] < nc[2]; ++idx[2])
+      for (idx[1] = 0; idx[1] < nc[1]; ++idx[1])
+        for (idx[0] = 0; idx[0] < nc[0]; ++idx[0]) {
+          float cmin[3];
+          for (int a = 0; a < 3; ++a) cmin[a] = g->mn[a] + (float)idx[a] * sp[a];
+          for (it[2] = 0; it[2] < m; ++it[2])
+            for (it[1] = 0; it[1] < m; ++it[1])
+              for (it[0] = 0; it[0] < m; ++it[0]) {
+                float j[3], p[3];
+                spread3_(jm, host_rand, seed, &d, j);
+                for (int a = 0; a < 3; ++a) p[a] = ((cmin[a] + ((float)it[a] / (float)m) * sp[a]) + shift[a]) + j[a];
+                float dens = ambient;
+                int emit = 1;
+                if (use_vortons) {
+                  float here;
+                  interpolate_k(g, dev, 1, p, &here);
+                  dens = (here + scale) * ambient;
+                  emit = fabsf(here / scale) >= 0.5f;
+                }
+                if (emit) {
+                  if (kept < max) {
+                    memcpy(pos_out + 3 * kept, p, sizeof(p));
+                    dens_out[kept] = dens;
+                    size_out[kept] = size;
+                  }
+                  ++kept;
+                }
+              }
+        }
+  }
+  free(dev);
+  *count = kept;
+}
+
+/* PclOpEmit::Operate (pclOpEmit.cpp:188-210): emit int(dt x rate +
+ * remainder) copies of the template, keeping the fraction in *remainder,
+ * each varied by RandomSpread of the spread in the order position,
+ * velocity, orientation, angular velocity, density, fuel, flame and smoke
+ * fractions, size.  tmpl and spread hold those 17 values; per particle rec
+ * receives them and the birth frame (as a float).  Returns the number
+ * emitted (records written up to max). */
+size_t vgo_emit_operate(const float tmpl[17], const float spread[17], float rate, float* remainder, float dt,
+                        unsigned frame, int host_rand, unsigned seed, uint64_t* draw, float* rec, size_t max) {
+  const float f = dt * rate + *remainder;
+  const int k = (int)f;
+  *remainder = f - (float)k;
+  for (int i = 0; i < k; ++i) {
+    float r[18];
+    for (int v = 0; v < 4; ++v) {
+      float s[3];
+      spread3_(spread + 3 * v, host_rand, seed, draw, s);
+      for (int a = 0; a < 3; ++a) r[3 * v + a] = tmpl[3 * v + a] + s[a];
+    }
+    for (int v = 12; v < 17; ++v) r[v] = tmpl[v] + spread_(spread[v], draw_(host_rand, seed, draw));
+    r[17] = (float)(int)frame;
+    if ((size_t)i < max) memcpy(rec + 18 * (size_t)i, r, sizeof(r));
+  }
+  return k > 0 ? (size_t)k : 0;
+}

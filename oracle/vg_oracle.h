@@ -137,6 +137,16 @@ void vgo_collide_tracers(float* pos, float* vel, const float* size, const float*
 void vgo_remove_embedded(const float* pos, const float* size, size_t n, const float* bodies, int nb, unsigned* order,
                          size_t* m);
 
+/* Emitters (PclOpEmit).  host_rand: draw from the C library's rand() (the
+ * reference's source), else from vgo_jitter_hash(seed, draw index). */
+int vgo_jitter_hash(unsigned seed, uint64_t d);
+int vgo_rand_max(void);
+void vgo_emit_grid(const vgo_geom* g, unsigned m, const float* vpos, const float* vdens, size_t nv, int use_vortons,
+                   int host_rand, unsigned seed, float* pos_out, float* dens_out, float* size_out, size_t max,
+                   size_t* count);
+size_t vgo_emit_operate(const float tmpl[17], const float spread[17], float rate, float* remainder, float dt,
+                        unsigned frame, int host_rand, unsigned seed, uint64_t* draw, float* rec, size_t max);
+
 #ifdef __cplusplus
 }
 #endif

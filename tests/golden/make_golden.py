@@ -12,6 +12,7 @@ Usage (needs the reference tree or a staged copy; run in this container):
     python tests/golden/make_golden.py heat         # heat.npz (DiffuseAndDissipateHeatPSE)
     python tests/golden/make_golden.py surface      # surface.npz (density grid, gradient, baroclinic, SDF)
     python tests/golden/make_golden.py bodies       # bodies.npz (fluid-body collisions, embedded particles)
+    python tests/golden/make_golden.py emit         # emit.npz (PclOpEmit::Emit and ::Operate)
 """
 import ctypes
 import os
@@ -29,6 +30,7 @@ OUT_LIFE = os.path.join(os.path.dirname(os.path.abspath(__file__)), "lifecycle.n
 OUT_HEAT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "heat.npz")
 OUT_SURF = os.path.join(os.path.dirname(os.path.abspath(__file__)), "surface.npz")
 OUT_BODY = os.path.join(os.path.dirname(os.path.abspath(__file__)), "bodies.npz")
+OUT_EMIT = os.path.join(os.path.dirname(os.path.abspath(__file__)), "emit.npz")
 
 
 def P(a):
@@ -348,6 +350,71 @@ def bodies():
     print(f"wrote {OUT_BODY} ({os.path.getsize(OUT_BODY) / 1e3:.1f} kB, {len(g)} arrays)")
 
 
+def emit():
+    """PclOpEmit::Emit (tracer seeding on a grid, without and with vortons)
+    and PclOpEmit::Operate (rate emission over five frames) from the
+    reference's own code after srand(seed): the jitter is the C library's
+    rand() stream, the same on every glibc host."""
+    oracle.build()
+    R = oracle.ref("serial")
+
+    def geom(mn, mx, np3):
+        go = oracle.Geom()
+        for a in range(3):
+            go.mn[a], go.ext[a], go.np[a] = mn[a], mx[a] - mn[a], np3[a]
+        oracle.lib().vgo_precompute_spacing(ctypes.byref(go))
+        return (np.array(list(go.mn) + list(go.ext) + list(go.cell) + list(go.cpe), np.float32),
+                np.array(np3, np.uint32))
+
+    rng = np.random.default_rng(31)
+    vpos, _, _ = workloads.puff(3000, seed=32, sigma=0.35, clip=0.9)
+    r2 = (vpos.astype(np.float64) ** 2).sum(1)
+    vdens = (1.0 + 0.6 * np.exp(-r2 / 0.4) - 0.4 * np.exp(-((vpos[:, 0] - 0.4) ** 2) / 0.02)
+             + 0.02 * rng.standard_normal(3000)).astype(np.float32)
+    cases = [  # grid, multiplier, seed, vortons
+        (geom([-1.0, -1.2, -0.8], [1.1, 1.0, 0.9], [7, 6, 5]), 2, 5, None),
+        (geom([-1.0, -1.2, -0.8], [1.1, 1.0, 0.9], [7, 6, 5]), 5, 11, None),
+        (geom([-1.0, -1.0, -1.0], [1.0, 1.0, 1.0], [9, 9, 9]), 3, 21, (vpos, vdens)),
+        (geom([-1.0, -1.0, -1.0], [1.0, 1.0, 1.0], [9, 9, 9]), 2, 23, (vpos, np.ones(3000, np.float32))),
+    ]
+    g = {}
+    for i, ((g12, np3), m, seed, vort) in enumerate(cases):
+        cap = int(np.prod(np3 - 1)) * m ** 3
+        pos = np.zeros((cap, 3), np.float32)
+        d = np.zeros(cap, np.float32)
+        sz = np.zeros(cap, np.float32)
+        cnt = ctypes.c_size_t()
+        vp, vd = vort if vort is not None else (np.zeros((1, 3), np.float32), np.zeros(1, np.float32))
+        vs = np.full(len(vd), 0.05, np.float32)
+        R.vgref_emit_grid(P(g12), P(np3), ctypes.c_uint(m), P(vp), P(vs), P(vd),
+                          ctypes.c_size_t(len(vd) if vort is not None else 0), ctypes.c_int(vort is not None),
+                          ctypes.c_uint(seed), P(pos), P(d), P(sz), ctypes.c_size_t(cap), ctypes.byref(cnt))
+        k = cnt.value
+        g.update({f"e{i}_geom": g12, f"e{i}_np": np3, f"e{i}_params": np.array([m, seed, vort is not None], np.int64),
+                  f"e{i}_pos": pos[:k].copy(), f"e{i}_density": d[:k].copy(), f"e{i}_size": sz[:k].copy()})
+        if vort is not None:
+            g.update({f"e{i}_vpos": vp, f"e{i}_vdens": vd})
+    g["emit_cases"] = np.array(len(cases))
+    tmpl = np.array([0.1, 0.2, 0.3, 1, 2, 3, 0.5, 0.6, 0.7, 4, 5, 6, 1.5, 0.2, 0.3, 0.4, 0.05], np.float32)
+    spread = np.array([0.5, 0.4, 0.3, 0.1, 0.2, 0.3, 0.01, 0.02, 0.03, 1, 1, 1, 0.1, 0.05, 0.05, 0.05, 0.01],
+                      np.float32)
+    dts = np.array([1 / 60, 1 / 30, 0.1, 0.013, 0.5], np.float32)
+    rate, frame0, seed = 60.0, 7, 9
+    cap = 256
+    rec = np.zeros((cap, 18), np.float32)
+    cnt = ctypes.c_size_t()
+    rem = np.zeros(len(dts), np.float32)
+    R.vgref_emit_operate(P(tmpl), P(spread), ctypes.c_float(rate), P(dts), ctypes.c_int(len(dts)),
+                         ctypes.c_uint(frame0), ctypes.c_uint(seed), P(rec), ctypes.c_size_t(cap), ctypes.byref(cnt),
+                         P(rem))
+    g.update({"op_tmpl": tmpl, "op_spread": spread, "op_dts": dts,
+              "op_params": np.array([rate, frame0, seed], np.float64), "op_records": rec[: cnt.value].copy(),
+              "op_remainders": rem})
+    np.savez_compressed(OUT_EMIT, **g)
+    print(f"wrote {OUT_EMIT} ({os.path.getsize(OUT_EMIT) / 1e3:.1f} kB, {len(g)} arrays)",
+          [len(g[f"e{i}_pos"]) for i in range(len(cases))], len(g["op_records"]))
+
+
 if __name__ == "__main__":
     if len(sys.argv) > 1 and sys.argv[1] == "lifecycle":
         lifecycle()
@@ -357,5 +424,7 @@ if __name__ == "__main__":
         surface()
     elif len(sys.argv) > 1 and sys.argv[1] == "bodies":
         bodies()
+    elif len(sys.argv) > 1 and sys.argv[1] == "emit":
+        emit()
     else:
         main()

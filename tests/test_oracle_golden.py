@@ -4,6 +4,8 @@ Every comparison here is bit-exact (integer and float bit patterns), except
 the order-independent PSE form, which is checked against the reference's
 in-place order at a stated tolerance.
 """
+import os
+
 import numpy as np
 import pytest
 
@@ -170,7 +172,6 @@ def test_full_step_bit_exact(oracle_lib, golden):
 @pytest.fixture(scope="module")
 def lifecycle():
     """PclOpKillAge / PclOpWind outputs of the reference's own code (make_golden.py lifecycle)."""
-    import os
     return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "lifecycle.npz")))
 
 
@@ -194,7 +195,6 @@ def test_heat_pse_sequential_bit_exact(oracle_lib, golden):
     """The oracle's heat PSE in the reference's in-place order reproduces the
     reference's DiffuseAndDissipateHeatPSE bit for bit (tests/golden/heat.npz),
     including a diffusivity that saturates both clamps."""
-    import os
     h = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "heat.npz")))
     g = geom_of(oracle_lib, golden)
     for i in range(int(h["heat_cases"])):
@@ -208,7 +208,6 @@ def test_heat_pse_symmetric_tolerance(oracle_lib, golden):
     in-place order at diffusivity 0.01: each pair exchanges <= 6.7e-4 of its
     difference, so the forms differ by ~(neighbours x 6.7e-4) of the change.
     Stated tolerance: 1e-4 relative on the densities, 2% on their change."""
-    import os
     h = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "heat.npz")))
     g = geom_of(oracle_lib, golden)
     kappa, ambient, dt = (np.float32(v) for v in h["heat0_params"])
@@ -284,7 +283,6 @@ def test_tree_matches_reference_at_treecode_workload_size(oracle_lib):
 
 
 def _surface():
-    import os
     return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "surface.npz")))
 
 
@@ -357,7 +355,6 @@ def test_fluid_body_collisions_bit_exact(oracle_lib):
     (tests/golden/bodies.npz): particles and body sums bit for bit, for a
     moving, spinning sphere, a hollow rotated box container and a rotated
     solid box."""
-    import os
     O = oracle_lib
     h = dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "bodies.npz")))
     p, v, w, d, out = O.collide_vortons(h["b_pos"], h["b_vel"], h["b_angvel"], h["b_size"], h["b_density"],
@@ -371,3 +368,65 @@ def test_fluid_body_collisions_bit_exact(oracle_lib):
     for got, key in ((tp, "b_tr_pos"), (tv, "b_tr_vel"), (tout, "b_tr_sums")):
         assert np.array_equal(bits(got), bits(h[key])), key
     assert np.array_equal(O.remove_embedded(h["b_pos"], h["b_size"], h["b_bodies"]), h["b_survivors"])
+
+
+def _emit_gold():
+    return dict(np.load(os.path.join(os.path.dirname(__file__), "golden", "emit.npz")))
+
+
+def _geom12(oracle_lib, g12, np3):
+    g = oracle_lib.Geom()
+    for a in range(3):
+        g.mn[a], g.ext[a], g.cell[a], g.cpe[a], g.np[a] = g12[a], g12[3 + a], g12[6 + a], g12[9 + a], int(np3[a])
+    return g
+
+
+def test_emit_grid_bit_exact(oracle_lib):
+    """PclOpEmit::Emit: the reference's tracer seeding (with and without the
+    vortons' density-deviation mask, and the empty case) after srand(seed),
+    bit for bit."""
+    e = _emit_gold()
+    for i in range(int(e["emit_cases"])):
+        m, seed, masked = (int(v) for v in e[f"e{i}_params"])
+        g = _geom12(oracle_lib, e[f"e{i}_geom"], e[f"e{i}_np"])
+        oracle_lib.srand(seed)
+        vort = (e[f"e{i}_vpos"], e[f"e{i}_vdens"]) if masked else None
+        pos, dens, size = oracle_lib.emit_grid(g, m, vort)
+        assert len(pos) == len(e[f"e{i}_pos"]), i
+        for got, key in ((pos, "pos"), (dens, "density"), (size, "size")):
+            assert np.array_equal(got.view(np.uint32), e[f"e{i}_{key}"].view(np.uint32)), (i, key)
+    assert len(e["e3_pos"]) == 0  # vortons at the ambient density: nothing emitted
+
+
+def test_emit_operate_bit_exact(oracle_lib):
+    """PclOpEmit::Operate over five frames (remainder carried), template +
+    RandomSpread of the spread in the reference's draw order, bit for bit."""
+    e = _emit_gold()
+    rate, frame0, seed = e["op_params"]
+    oracle_lib.srand(int(seed))
+    rec, rem = oracle_lib.emit_operate(e["op_tmpl"], e["op_spread"], float(rate), e["op_dts"], frame0=int(frame0))
+    assert np.array_equal(rec.view(np.uint32), e["op_records"].view(np.uint32))
+    assert np.array_equal(rem.view(np.uint32), e["op_remainders"].view(np.uint32))
+
+
+def test_emit_hash_stream_properties(oracle_lib):
+    """The device emitter's own jitter stream (no rand()): every draw in
+    [0, RAND_MAX], seeds give different streams, each particle inside its own
+    sub-cell, and the same count and sub-cell order as the rand() stream."""
+    rmax = oracle_lib.rand_max()
+    d = [oracle_lib.jitter_hash(7, k) for k in range(2000)] + [oracle_lib.jitter_hash(7, (1 << 32) + k)
+                                                               for k in range(100)]
+    assert min(d) >= 0 and max(d) <= rmax
+    assert len(set(d)) > 2000
+    assert d[:50] != [oracle_lib.jitter_hash(8, k) for k in range(50)]
+    e = _emit_gold()
+    g = _geom12(oracle_lib, e["e1_geom"], e["e1_np"])
+    m = 5
+    pos, dens, size = oracle_lib.emit_grid(g, m, None, host_rand=False, seed=3)
+    assert len(pos) == len(e["e1_pos"])
+    sub = np.array([g.cell[a] for a in range(3)], np.float64) / m
+    mn = np.array([g.mn[a] for a in range(3)], np.float64)
+    expect = np.floor((e["e1_pos"].astype(np.float64) - mn) / sub)  # sub-cell of the reference's particle
+    got = np.floor((pos.astype(np.float64) - mn) / sub)
+    assert np.array_equal(got, expect)
+    assert np.array_equal(size, e["e1_size"]) and np.all(dens == 1.0)
