@@ -376,6 +376,84 @@ vg_status vg_collide_tracers_device(vg_ctx* ctx, const float* bodies, int nb, fl
 vg_status vg_remove_embedded_device(vg_ctx* ctx, const float* bodies, int nb, float* pos_size, float* b4, float* c4,
                                     float* d1, size_t m, size_t* m_out);
 
+/* ---- Emitters: particles appended to device-resident arrays (PclOpEmit,
+ * Particles/Operation/pclOpEmit.h:16-34, pclOpEmit.cpp:77-210), for engines
+ * that keep vortons and tracers on the GPU across frames.
+ *
+ * The arrays of one particle group.  pos_size is required; any other pointer
+ * may be NULL (that attribute is not kept).  Particles [0, count) are live;
+ * an emitter writes [count, count + k) and advances count, and refuses with
+ * VG_TOO_LARGE, writing nothing, when count + k would exceed capacity. */
+typedef struct vg_particles {
+  float* pos_size; /* float4: position (mPosition), size (mSize) */
+  float* vel4;     /* float4: velocity, w = 0 */
+  float* angvel4;  /* float4: angular velocity, w = 0 */
+  float* orient4;  /* float4: orientation (axis-angle), w = 0 */
+  float* density;  /* float: mDensity */
+  float* fire4;    /* float4: fuel, flame and smoke fractions, w = 0 */
+  int* birth;      /* int: mBirthTime (frame) */
+  size_t count;
+  size_t capacity;
+} vg_particles;
+
+/* The values of one particle that PclOpEmit's template and spread hold. */
+typedef struct vg_particle_values {
+  float position[3];
+  float velocity[3];
+  float orientation[3];
+  float angular_velocity[3];
+  float density;
+  float fuel_fraction;
+  float flame_fraction;
+  float smoke_fraction;
+  float size;
+} vg_particle_values;
+
+/* PclOpEmit's state: mTemplate, mSpread, mEmitRate (60 in the reference's
+ * constructor) and mRemainder (0 there). */
+typedef struct vg_emitter {
+  vg_particle_values tmpl;
+  vg_particle_values spread;
+  float emit_rate;
+  float remainder;
+} vg_emitter;
+
+/* Where an emitter's random jitter comes from. */
+typedef enum vg_jitter {
+  VG_JITTER_HOST_RAND = 0, /* the C library's rand() on the host, drawn in the reference's order */
+  VG_JITTER_HASH = 1       /* a counter-based stream on the device (seed, draw index): no host work */
+} vg_jitter;
+
+/* Replaces PclOpEmit::Operate (pclOpEmit.cpp:188-210): emits int(time_step x
+ * emit_rate + remainder) particles, keeping the fraction in em->remainder;
+ * each is the template plus RandomSpread (Core/Math/math.h:183-188) of the
+ * spread, drawn from the C library's rand() in the reference's order
+ * (position z, y, x, then velocity, orientation, angular velocity likewise,
+ * then density, fuel, flame, smoke fractions, size), born at `frame`.  The
+ * records are made on the host, as the reference's are, and appended to the
+ * device arrays with one copy and one kernel.  On VG_TOO_LARGE nothing is
+ * drawn and em is unchanged.  Synchronises. */
+vg_status vg_emit_device(vg_ctx* ctx, vg_emitter* em, float time_step, unsigned frame, vg_particles* p);
+
+/* Replaces PclOpEmit::Emit (pclOpEmit.cpp:77-186), the tracer seeding:
+ * multiplier^3 particles per cell of grid g (cells in z, y, x order, sub-cells
+ * likewise), each at its sub-cell's centre plus a jitter below half a
+ * sub-cell, density 1 (the reference's ambient), size 1/2 cbrt(cell volume) /
+ * multiplier, smoke fraction 1, born at frame 0.  With vortons
+ * (vorton_pos_size not NULL; n_vortons may be 0), their density deviations
+ * from 1 are accumulated onto g and a particle is kept only where the
+ * interpolated deviation is at least half the largest magnitude, with
+ * density deviation + that magnitude; nothing is emitted (or drawn) when the
+ * deviation is zero everywhere.  jitter VG_JITTER_HOST_RAND consumes 3 rand()
+ * per sub-cell exactly as the reference does (bit-identical positions after
+ * the same srand); VG_JITTER_HASH draws on the device from seed.  A particle
+ * whose position rounds onto the grid's far face with vortons given is not
+ * kept and raises VG_OUT_OF_GRID (the reference reads past the grid there).
+ * Synchronises. */
+vg_status vg_emit_grid_device(vg_ctx* ctx, const vg_grid_geom* g, unsigned multiplier, const float* vorton_pos_size,
+                              const float* vorton_density, size_t n_vortons, int jitter, unsigned seed,
+                              vg_particles* p);
+
 /* Isosurface of a scalar grid by marching cubes, as ExtractIsoLevel /
  * PolygoniseCellWithNormal do (Render/Resource/marchingCubes.cpp:580-866),
  * into device buffers instead of a vertex buffer: cells in z, y, x order; per

@@ -91,6 +91,30 @@ class GridGeom(ctypes.Structure):
         return g
 
 
+class Particles(ctypes.Structure):
+    """vg_particles: one particle group's device arrays (pointers may be 0)."""
+    _fields_ = [("pos_size", ctypes.c_void_p), ("vel4", ctypes.c_void_p), ("angvel4", ctypes.c_void_p),
+                ("orient4", ctypes.c_void_p), ("density", ctypes.c_void_p), ("fire4", ctypes.c_void_p),
+                ("birth", ctypes.c_void_p), ("count", ctypes.c_size_t), ("capacity", ctypes.c_size_t)]
+
+
+class ParticleValues(ctypes.Structure):
+    """vg_particle_values: the 17 values of PclOpEmit's template and spread."""
+    _fields_ = [("position", ctypes.c_float * 3), ("velocity", ctypes.c_float * 3),
+                ("orientation", ctypes.c_float * 3), ("angular_velocity", ctypes.c_float * 3),
+                ("density", ctypes.c_float), ("fuel_fraction", ctypes.c_float), ("flame_fraction", ctypes.c_float),
+                ("smoke_fraction", ctypes.c_float), ("size", ctypes.c_float)]
+
+
+class Emitter(ctypes.Structure):
+    """vg_emitter: PclOpEmit's template, spread, rate and remainder."""
+    _fields_ = [("tmpl", ParticleValues), ("spread", ParticleValues), ("emit_rate", ctypes.c_float),
+                ("remainder", ctypes.c_float)]
+
+
+JITTER_HOST_RAND, JITTER_HASH = 0, 1
+
+
 class Config(ctypes.Structure):
     _fields_ = [("abi_version", ctypes.c_uint), ("device", ctypes.c_int), ("stream", ctypes.c_void_p),
                 ("velocity_technique", ctypes.c_int), ("numerics", ctypes.c_int), ("poisson_solver", ctypes.c_int),
@@ -121,7 +145,7 @@ EXPORTS = [
     "vg_evolve_device", "vg_direct_noalloc", "vg_wind_device", "vg_kill_age_device", "vg_heat_pse_device",
     "vg_density_grid_device", "vg_gradient_device", "vg_baroclinic_device", "vg_signed_distance_device",
     "vg_marching_cubes_device", "vg_collide_vortons_device", "vg_collide_tracers_device",
-    "vg_remove_embedded_device",
+    "vg_remove_embedded_device", "vg_emit_device", "vg_emit_grid_device",
     "vg_net_create", "vg_net_destroy", "vg_net_last_error", "vg_net_param_count", "vg_net_set_params",
     "vg_net_get_params", "vg_net_save", "vg_net_load", "vg_net_guess_device", "vg_net_backward_device",
     "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
@@ -186,6 +210,9 @@ def lib():
         L.vg_collide_vortons_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, _f, _f, _v, _v]
         L.vg_collide_tracers_device.argtypes = [_v, _v, _i, _v, _v, _v, _s, _v]
         L.vg_remove_embedded_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, ctypes.POINTER(ctypes.c_size_t)]
+        L.vg_emit_device.argtypes = [_v, ctypes.POINTER(Emitter), _f, ctypes.c_uint, ctypes.POINTER(Particles)]
+        L.vg_emit_grid_device.argtypes = [_v, ctypes.POINTER(GridGeom), ctypes.c_uint, _v, _v, _s, _i, ctypes.c_uint,
+                                          ctypes.POINTER(Particles)]
         L.vg_wind_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_void_p,
                                      ctypes.c_float, ctypes.c_float]
         L.vg_kill_age_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
@@ -437,3 +464,71 @@ def define_shape(n, vmin, vmax, pow2=True):
     if st != OK:
         raise VgError(st, "vg_define_shape")
     return g
+
+
+class ParticleGroup:
+    """Device-resident arrays of one particle group (vg_particles), sized for
+    `capacity` particles: pos_size, vel4, angvel4 (float4), density (float),
+    birth (int), and orient4 / fire4 when asked.  `count` particles are live."""
+
+    def __init__(self, capacity, device="cuda", orientation=False, fire=False):
+        import torch
+        f4 = lambda: torch.zeros((capacity, 4), dtype=torch.float32, device=device)  # noqa: E731
+        self.pos_size, self.vel4, self.angvel4 = f4(), f4(), f4()
+        self.orient4 = f4() if orientation else None
+        self.fire4 = f4() if fire else None
+        self.density = torch.zeros(capacity, dtype=torch.float32, device=device)
+        self.birth = torch.zeros(capacity, dtype=torch.int32, device=device)
+        self.capacity = capacity
+        self.count = 0
+
+    def c_struct(self):
+        return Particles(_ptr(self.pos_size), _ptr(self.vel4), _ptr(self.angvel4), _ptr(self.orient4),
+                         _ptr(self.density), _ptr(self.fire4), _ptr(self.birth), self.count, self.capacity)
+
+
+class PclOpEmit:
+    """IParticleOperation PclOpEmit (Particles/Operation/pclOpEmit.h:16-34) on a
+    device particle group: Operate(group, timeStep, uFrame) emits mEmitRate
+    particles a second from mTemplate varied by mSpread (dicts of the
+    vg_particle_values fields); Emit(ctx, group, grid, multiplier, vortons) is
+    the static tracer seeding on a grid (vortons: None or (pos_size, density)
+    device arrays)."""
+
+    def __init__(self, ctx):
+        self.ctx = ctx
+        self.mTemplate = {}
+        self.mSpread = {}
+        self.mEmitRate = 60.0
+        self.mRemainder = 0.0
+
+    @staticmethod
+    def _values(d):
+        v = ParticleValues()
+        for k, x in d.items():
+            if isinstance(getattr(v, k), float):
+                setattr(v, k, float(x))
+            else:
+                getattr(v, k)[:] = [float(c) for c in x]
+        return v
+
+    def Operate(self, group, timeStep, uFrame=0):
+        em = Emitter(self._values(self.mTemplate), self._values(self.mSpread), self.mEmitRate, self.mRemainder)
+        ps = group.c_struct()
+        self.ctx.check(lib().vg_emit_device(self.ctx.h, ctypes.byref(em), timeStep, uFrame, ctypes.byref(ps)),
+                       "PclOpEmit::Operate")
+        self.mRemainder = em.remainder
+        group.count = ps.count
+
+    @staticmethod
+    def Emit(ctx, group, grid, multiplier, vortons=None, jitter=JITTER_HOST_RAND, seed=0):
+        if vortons is not None and int(vortons[1].shape[0]) == 0:
+            return  # no vortons: no density deviation anywhere, so the reference emits nothing
+        ps = group.c_struct()
+        vp, vd, nv = (_ptr(vortons[0]), _ptr(vortons[1]), int(vortons[1].shape[0])) if vortons is not None else (
+            None, None, 0)
+        try:
+            ctx.check(lib().vg_emit_grid_device(ctx.h, ctypes.byref(grid), multiplier, vp, vd, nv, jitter, seed,
+                                                ctypes.byref(ps)), "PclOpEmit::Emit")
+        finally:
+            group.count = ps.count

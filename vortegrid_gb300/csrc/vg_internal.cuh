@@ -236,6 +236,7 @@ enum Slot {
   S_SDF,    // signed distance: pinned flags, statistics, partial sums
   S_MC,     // marching cubes: per-cell counts and offsets
   S_BODY,   // fluid-body collisions: per-block partial sums
+  S_EMIT,   // emitters: jitter draws, records, deviation grid, flags
   S_NUM
 };
 
@@ -431,6 +432,9 @@ vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
 // baroclinic generation and the signed distance grid (vg_surface.cu).
 vg_status launch_density_grid(Ctx* c, const Geom& g, const float4* ps, const float* density, size_t n,
                               float ambient, float* out);
+// Density deviation grid of the emitter's tracer mask (density - ambient, accumulated alone).
+vg_status launch_density_deviation(Ctx* c, const Geom& g, const float4* ps, const float* density, size_t n,
+                                   float ambient, float* out);
 vg_status launch_gradient(Ctx* c, const Geom& g, const float* v, float* grad3);
 vg_status launch_baroclinic(Ctx* c, const Geom& g, const float* grad3, const float4* ps, float4* w, size_t n,
                             const float grav[3], float ambient, float dt);

@@ -46,6 +46,10 @@ __device__ __forceinline__ float clamp01(float t) {
   return lo < 1.0f ? lo : 1.0f;
 }
 
+// kDeviation: the density deviation grid of PopulateDensityDeviationGridFromParticles
+// (Particles/Operation/pclOpEmit.cpp:29-57) instead -- each vorton's density minus the
+// ambient, accumulated alone, with no contribution grid and no fill.
+template <bool kDeviation>
 __global__ void __launch_bounds__(128) k_density(Geom g, const float4* __restrict__ ps,
                                                  const float* __restrict__ dens, const unsigned* __restrict__ start,
                                                  const unsigned* __restrict__ items, float ambient,
@@ -100,9 +104,13 @@ __global__ void __launch_bounds__(128) k_density(Geom g, const float4* __restric
     }
     // this point is corner `bo` of the vorton's cell
     const float wt = __fmul_rn(__fmul_rn((bo & 1) ? tw[0] : om[0], (bo & 2) ? tw[1] : om[1]), (bo & 4) ? tw[2] : om[2]);
-    const float item = __fmul_rn(dens[best], volume_ratio);
+    const float item = kDeviation ? __fsub_rn(dens[best], ambient) : __fmul_rn(dens[best], volume_ratio);
     d = __fadd_rn(d, __fmul_rn(wt, item));
     contrib = __fadd_rn(contrib, __fmul_rn(wt, 1.0f));
+  }
+  if (kDeviation) {
+    out[k] = d;
+    return;
   }
   // ambient fills what the vortons do not (vortonSim.cpp:3010-3014)
   const float pcls = __fmul_rn(contrib, volume_ratio);
@@ -615,7 +623,24 @@ vg_status launch_density_grid(Ctx* c, const Geom& g, const float4* ps, const flo
   CellLists cl;
   vg_status st = build_cell_lists(c, g, ps, n, &cl);
   if (st != VG_OK) return st;
-  pdl_launch(c->stream, blocks_for(pts, 128), 128, 0, k_density, g, ps, density, (const unsigned*)cl.start,
+  pdl_launch(c->stream, blocks_for(pts, 128), 128, 0, k_density<false>, g, ps, density, (const unsigned*)cl.start,
+             (const unsigned*)cl.items, ambient, out);
+  VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status launch_density_deviation(Ctx* c, const Geom& g, const float4* ps, const float* density, size_t n,
+                                   float ambient, float* out) {
+  const size_t pts = g.points();
+  if (n == 0) {
+    VG_CUDA(c, cudaMemsetAsync(out, 0, pts * sizeof(float), c->stream));
+    return VG_OK;
+  }
+  CellLists cl;
+  vg_status st = build_cell_lists(c, g, ps, n, &cl);
+  if (st != VG_OK) return st;
+  pdl_launch(c->stream, blocks_for(pts, 128), 128, 0, k_density<true>, g, ps, density, (const unsigned*)cl.start,
              (const unsigned*)cl.items, ambient, out);
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
