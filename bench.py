@@ -319,34 +319,51 @@ def run_ours(args, world, rank, local):
         return
     result["clocks"] = clk.summary()
 
-    # ---- roofline of the direct-sum kernel (events on the context stream)
-    q = torch.cat([vg_grid_points(grid), ps0[:, :4]]).contiguous()
-    out = torch.zeros_like(q)
+    # ---- roofline of the direct-sum kernel (events on the context stream): the step's own
+    # velocity evaluation (vg_direct_grid_device: every gridpoint and vorton), then the same
+    # kernel on arbitrary targets (vg_direct_device: 1M random points, no grid rows)
     lib = vg.lib()
-    with torch.cuda.stream(stream):
-        for _ in range(3):
-            lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), N_VORTONS, vg._ptr(q), q.shape[0], 1.0, 1.0,
-                                 vg._ptr(out))
-        reps = 20
-        a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        a.record(stream)
-        for _ in range(reps):
-            lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), N_VORTONS, vg._ptr(q), q.shape[0], 1.0, 1.0,
-                                 vg._ptr(out))
-        b.record(stream)
-        torch.cuda.synchronize()
-    kms = a.elapsed_time(b) / reps
+    vgrid = torch.zeros((grid.capacity, 3), dtype=torch.float32, device="cuda")
+    velv = torch.zeros_like(ps0)
+
+    def time_launch(fn, reps=20):
+        with torch.cuda.stream(stream):
+            for _ in range(3):
+                fn()
+            a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            for _ in range(reps):
+                fn()
+            b.record(stream)
+            torch.cuda.synchronize()
+        return a.elapsed_time(b) / reps
+
+    kms = time_launch(lambda: ctx.check(lib.vg_direct_grid_device(ctx.h, ctypes.byref(grid), vg._ptr(ps0), vg._ptr(w0),
+                                                                   N_VORTONS, vg._ptr(vgrid), vg._ptr(velv)),
+                                        "vg_direct_grid_device"))
     achieved = FLOPS_PER_INTERACTION * interactions() / (kms * 1e-3) / 1e12
     clk_mhz = result["clocks"].get("sm_mhz") or 2070.0
     sms = torch.cuda.get_device_properties(local).multi_processor_count
     peak = 2 * 128 * sms * clk_mhz * 1e6 / 1e12
-    result["roofline"] = {"bound": "fp32", "kernel": "k_direct_pair (+ k_reduce_pair)",
+    result["roofline"] = {"bound": "fp32", "kernel": "k_direct_pair (grid-row and general CTAs) + k_reduce_pair, "
+                                                     "as the step launches them (vg_direct_grid_device)",
                           "achieved": achieved, "peak": peak, "unit": "TFLOP/s", "frac": achieved / peak,
                           "traffic": profiled_traffic("direct_pair_ring4096.md"), "ms_per_launch": kms,
                           "peak_basis": f"2 flops x 128 FP32 lanes x {sms} SMs (device attribute) x {clk_mhz:.0f} MHz "
                                         "(sampled median)",
                           "flops_per_interaction": FLOPS_PER_INTERACTION,
                           "gint_per_s_kernel": interactions() / (kms * 1e-3) / 1e9}
+    m_arb = 1 << 20
+    qa = f4(np.random.default_rng(9).uniform(-1.5, 1.5, (m_arb, 3)).astype(np.float32))
+    oa = torch.zeros_like(qa)
+    kms_a = time_launch(lambda: ctx.check(lib.vg_direct_device(ctx.h, 0, vg._ptr(ps0), vg._ptr(w0), N_VORTONS,
+                                                               vg._ptr(qa), m_arb, 1.0, 1.0, vg._ptr(oa)),
+                                          "vg_direct_device"), reps=5)
+    ach_a = FLOPS_PER_INTERACTION * N_VORTONS * m_arb / (kms_a * 1e-3) / 1e12
+    result["roofline_arbitrary_targets"] = {"targets": m_arb, "sources": N_VORTONS, "ms_per_launch": kms_a,
+                                            "achieved": ach_a, "peak": peak, "unit": "TFLOP/s", "frac": ach_a / peak,
+                                            "kernel": "k_direct_pair general CTAs (+ k_reduce_pair), "
+                                                      "1M uniform random targets in [-1.5,1.5]^3"}
 
     # ---- e2e through the host-buffer ABI from pinned memory
     recs_t = torch.empty(N_VORTONS * 96, dtype=torch.uint8, pin_memory=True)

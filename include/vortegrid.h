@@ -234,6 +234,16 @@ vg_status vg_partition_device(vg_ctx* ctx, const vg_grid_geom* g, const float* p
 vg_status vg_direct_device(vg_ctx* ctx, int kind, const float* pos_size, const float* angvel, size_t n,
                            const float* q4, size_t m, float spread_range, float spread_circ, float* out4);
 
+/* The direct technique's velocity grid: ComputeVelocity_Direct
+ * (vortonSim.cpp:1113-1158) at every gridpoint of g, the gridpoint positions
+ * of ComputeVelocityGridSlice (min + i x spacing x (1 - 2 FLT_EPSILON),
+ * vortonSim.cpp:2229-2252) into velgrid3 (float[3] per point, x fastest), and
+ * when vel4 is not NULL at each of the n vortons too (float4 records, as
+ * COMPUTE_VELOCITY_AT_VORTONS does, vorton.h:63-69).  This is the velocity
+ * evaluation of vg_step_device's direct technique. */
+vg_status vg_direct_grid_device(vg_ctx* ctx, const vg_grid_geom* g, const float* pos_size, const float* angvel,
+                                size_t n, float* velgrid3, float* vel4);
+
 /* CreateInfluenceTree (vortonSim.cpp:1605-1624) on grid g; then
  * ComputeVelocity_Tree / ComputeVectorPotential_Tree from the root
  * (vortonSim.cpp:1650-1905) at m query points.  tree_out (optional): 8 floats

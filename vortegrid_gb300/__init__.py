@@ -145,7 +145,7 @@ EXPORTS = [
     "vg_evolve_device", "vg_direct_noalloc", "vg_wind_device", "vg_kill_age_device", "vg_heat_pse_device",
     "vg_density_grid_device", "vg_gradient_device", "vg_baroclinic_device", "vg_signed_distance_device",
     "vg_marching_cubes_device", "vg_collide_vortons_device", "vg_collide_tracers_device",
-    "vg_remove_embedded_device", "vg_emit_device", "vg_emit_grid_device",
+    "vg_remove_embedded_device", "vg_emit_device", "vg_emit_grid_device", "vg_direct_grid_device",
     "vg_net_create", "vg_net_destroy", "vg_net_last_error", "vg_net_param_count", "vg_net_set_params",
     "vg_net_get_params", "vg_net_save", "vg_net_load", "vg_net_guess_device", "vg_net_backward_device",
     "vg_net_adam_step", "vg_net_get_grads", "vg_net_get_output", "vg_net_get_activation", "vg_net_get_gradient",
@@ -210,6 +210,7 @@ def lib():
         L.vg_collide_vortons_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, _f, _f, _v, _v]
         L.vg_collide_tracers_device.argtypes = [_v, _v, _i, _v, _v, _v, _s, _v]
         L.vg_remove_embedded_device.argtypes = [_v, _v, _i, _v, _v, _v, _v, _s, ctypes.POINTER(ctypes.c_size_t)]
+        L.vg_direct_grid_device.argtypes = [_v, ctypes.POINTER(GridGeom), _v, _v, _s, _v, _v]
         L.vg_emit_device.argtypes = [_v, ctypes.POINTER(Emitter), _f, ctypes.c_uint, ctypes.POINTER(Particles)]
         L.vg_emit_grid_device.argtypes = [_v, ctypes.POINTER(GridGeom), ctypes.c_uint, _v, _v, _s, _i, ctypes.c_uint,
                                           ctypes.POINTER(Particles)]

@@ -397,9 +397,12 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
   if (st != VG_OK) return st;
   float4* out4 = q + nq;
   // the direct technique also evaluates every vorton, whose records follow the gridpoints
-  pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_grid_points, g, q,
-             tech == VG_VELOCITY_DIRECT ? (const float4*)ps : nullptr, nq - pts);
-  VG_LAUNCHED(c);
+  // (the FAST direct kernel forms the gridpoint positions itself and reads the vortons' records)
+  if (tech == VG_VELOCITY_TREE || ref) {
+    pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_grid_points, g, q,
+               tech == VG_VELOCITY_DIRECT ? (const float4*)ps : nullptr, nq - pts);
+    VG_LAUNCHED(c);
+  }
   float sr = 1.0f, sc = 1.0f;
   if (tech == VG_VELOCITY_TREE) {
     volatile float cv = g.cell[0] * g.cell[1];
@@ -413,7 +416,7 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
   } else {
     // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too;
     // the multi-chunk reduction writes the grid and vortons directly
-    const DirectSplit split = {s.velgrid, pts, vel};
+    const DirectSplit split = {s.velgrid, pts, vel, &g, (const float4*)ps};
     bool done = false;
     if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4, &split, &done)) != VG_OK) return st;
     if (done) return VG_OK;
@@ -906,6 +909,38 @@ vg_status vg_direct_device(vg_ctx* c, int kind, const float* pos_size, const flo
   if (!c || (kind != 0 && kind != 1)) return VG_INVALID;
   return launch_direct(c, kind, c->cfg.numerics == VG_NUMERICS_REFERENCE, (const float4*)pos_size,
                        (const float4*)angvel, n, (const float4*)q4, m, sr, sc, (float4*)out4);
+}
+
+vg_status vg_direct_grid_device(vg_ctx* c, const vg_grid_geom* gg, const float* pos_size, const float* angvel,
+                                size_t n, float* velgrid3, float* vel4) {
+  if (!c || !gg || !velgrid3 || (n && (!pos_size || !angvel))) return VG_INVALID;
+  if (n > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 vortons");
+  const Geom g = to_geom(*gg);
+  const size_t pts = g.points();
+  if (pts == 0 || pts > 0x3fffffff) return fail(c, VG_INVALID, "direct grid: empty or oversized grid");
+  const size_t nq = pts + (vel4 ? n : 0);
+  vg_status st = VG_OK;
+  float4* q = (float4*)ws(c, S_JAC, nq * sizeof(float4) * 2, &st);
+  if (st != VG_OK) return st;
+  float4* out4 = q + nq;
+  const bool ref = c->cfg.numerics == VG_NUMERICS_REFERENCE;
+  if (ref) {  // the reference-order kernel reads every target's position
+    pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_grid_points, g, q, vel4 ? (const float4*)pos_size : nullptr,
+               nq - pts);
+    VG_LAUNCHED(c);
+  }
+  const DirectSplit split = {velgrid3, pts, (float4*)vel4, &g, (const float4*)pos_size};
+  bool done = false;
+  if ((st = launch_direct(c, 0, ref, (const float4*)pos_size, (const float4*)angvel, n, q, nq, 1.0f, 1.0f, out4,
+                          &split, &done)) != VG_OK)
+    return st;
+  if (!done) {
+    pdl_launch(c->stream, blocks_for(nq, 256), 256, 0, k_f4_to_f3, (const float4*)out4, velgrid3, pts, (float4*)vel4,
+               nq - pts);
+    VG_LAUNCHED(c);
+  }
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
 }
 
 vg_status vg_tree_device(vg_ctx* c, int kind, const vg_grid_geom* gg, const float* pos_size, const float* angvel,

@@ -18,6 +18,10 @@
 //     deterministic.
 // Reference path: one thread per query, sources in index order, the
 // reference's operation order (bit-identical to the CPU).
+#include <float.h>
+#include <math.h>
+#include <string.h>
+
 #include <algorithm>
 #include <string>
 
@@ -117,68 +121,105 @@ __global__ void __launch_bounds__(kThreads) k_direct_fast(const float4* __restri
   }
 }
 
-// Velocity (KIND 0) with packed FP32x2 arithmetic (FADD2 / FMUL2 / FFMA2):
-// each thread carries its 8 targets as 4 pairs, and every source is staged in
-// shared memory already duplicated into pairs (-p, 1/R, w, -w), so each
-// operation below advances two targets in one instruction.  The per-target
-// operations and their order are those of k_direct_fast<0> (and the source
-// constants those of k_prep_sources<0>, computed here while staging), so the
-// results are bit-identical to it; only the instruction count changes (about
-// 11 issue slots per interaction instead of 19).
-// 8 targets per thread (128 registers) was the fastest of the shapes measured
-// on GB300 (4 to 16 targets; scalar accumulation FFMAs or a scalar law mixed in
-// were slower): the FFMA2s all run on the heavy half of the FMA pipe, which the
-// profile shows ~70% busy.  CTAs of 256 threads, 2 per SM, beat 4 CTAs of 128
-// by ~4%: the tile barriers keep a CTA's warps together, whereas independent
-// small CTAs on one SM finish far apart (measured 39-100 us for equal work)
-// and leave the SM short of warps at the end.
-// With more than one source chunk the partial sums go to a scratch buffer and
-// k_reduce_pair adds them in chunk order.  (Reducing them inside this kernel,
-// by the last CTA of each target block or after a grid-wide barrier, or
-// launching the reduction as a programmatic dependent, measured no faster.)
 constexpr int kPairTPT = 8;
 constexpr int kPairThreads = 256;
 
+// How a k_direct_pair launch divides its targets and sources.  Targets
+// [0, pts) may be the points of a grid: in the first `rows` grid rows (as
+// many as whole CTAs of row threads hold), the first xs = 8 floor(np0 / 8)
+// points of a row are row targets (8 consecutive points of one row per
+// thread); the last r0 = np0 - xs points of those rows (nrem in all), every
+// point of the later rows (nrest) and the targets [pts, m) (points
+// qg[0, m - pts)) form the general class (8 per thread, strided by the CTA
+// width).  Each class has its own
+// source split (ks chunks of `chunk` sources), chosen so that the CTAs of both
+// classes take about as long; CTA b < row_ctas * row_ks is a row CTA.
+struct PairPlan {
+  Geom g;                 // the grid whose points are targets [0, pts)
+  int rows, tpr;          // rows of the row class (whole CTAs of row threads), row threads per row (xs / 8)
+  int xs, r0, nrem;       // first remainder column, remainder columns, remainder points of those rows
+  int nrest;              // points of the grid rows past the row class (general targets after the remainders)
+  int row_ctas, row_ks, row_chunk;
+  int pts, m;             // targets: grid points [0, pts), then qg[0, m - pts)
+  int gen_ctas, gen_ks, gen_chunk;
+};
 
+// Position of the gridpoint (x, y, z): the velocity step's gridpoint positions,
+// min + i spacing (1 - 2 FLT_EPSILON).
+__device__ __forceinline__ float grid_coord(const Geom& g, int a, int i) {
+  return __fadd_rn(g.mn[a], __fmul_rn((float)i, __fmul_rn(g.cell[a], 1.0f - 2.0f * FLT_EPSILON)));
+}
 
-__global__ void __launch_bounds__(kPairThreads, 2)
-    k_direct_pair(const float4* __restrict__ ps, const float4* __restrict__ w, int n, int chunk, float sr, float sc,
-                  const float4* __restrict__ q, int m, float* __restrict__ partial, float4* __restrict__ out) {
-  pdl_entry();
+// Stages sources [tile, tile + cnt) as five float4 per source, each value
+// duplicated for the packed operations: (-p, 1/R, w, -w) with w scaled as in
+// k_prep_sources<0>.
+__device__ __forceinline__ void stage_pair_tile(const float4* __restrict__ ps, const float4* __restrict__ w,
+                                                int tile, int cnt, float sr, float sc, float4* sh) {
+  for (int i = threadIdx.x; i < cnt; i += kPairThreads) {
+    const float4 p = ps[tile + i], a0 = w[tile + i];
+    // k_prep_sources<0>: 1/R and the scaled angular velocity
+    const float radius = p.w * 0.5f * sr;
+    const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
+    const float invr = 1.0f / radius;
+    const float4 a = make_float4(a0.x * s, a0.y * s, a0.z * s, 0.f);
+    sh[5 * i + 0] = make_float4(-p.x, -p.x, -p.y, -p.y);
+    sh[5 * i + 1] = make_float4(-p.z, -p.z, invr, invr);
+    sh[5 * i + 2] = make_float4(a.x, a.x, a.y, a.y);
+    sh[5 * i + 3] = make_float4(a.z, a.z, -a.x, -a.x);
+    sh[5 * i + 4] = make_float4(-a.y, -a.y, -a.z, -a.z);
+  }
+}
+
+// General targets t of the class (remainder gridpoints, then qg): its
+// position, and where its sum goes (target index j).
+__device__ __forceinline__ float4 general_target(const PairPlan& P, const float4* __restrict__ qg, int t, int* j) {
+  const int np0 = (int)P.g.np[0], np1 = (int)P.g.np[1];
+  int row, x;
+  if (t < P.nrem) {
+    row = t / P.r0, x = P.xs + (t - row * P.r0);
+  } else if (t < P.nrem + P.nrest) {
+    const int u = t - P.nrem;
+    row = P.rows + u / np0, x = u % np0;
+  } else {
+    *j = P.pts + (t - P.nrem - P.nrest);
+    return qg[t - P.nrem - P.nrest];
+  }
+  *j = row * np0 + x;
+  return make_float4(grid_coord(P.g, 0, x), grid_coord(P.g, 1, row % np1), grid_coord(P.g, 2, row / np1), 0.f);
+}
+
+// Arbitrary targets: each operation advances two targets (a float2 pair) of
+// the thread's eight.  17 packed operations per pair and source: d (3), |d|^2
+// (3), the cubed law (2), b = d law (3), w x b accumulated (6).
+__device__ __forceinline__ void pair_general(const float4* __restrict__ ps, const float4* __restrict__ w, int n,
+                                             float sr, float sc, const float4* __restrict__ qg, const PairPlan& P,
+                                             int b, float4* sh, float* __restrict__ partial,
+                                             float4* __restrict__ out) {
   constexpr int kPairs = kPairTPT / 2;
-  __shared__ float4 sh[5 * kTile];
-  const int base = blockIdx.x * (kPairThreads * kPairTPT) + threadIdx.x;
+  const int tb = b / P.gen_ks, kc = b - tb * P.gen_ks;
+  const int base = tb * (kPairThreads * kPairTPT) + threadIdx.x;
+  const int count = P.nrem + P.nrest + (P.m - P.pts);
   float2 qx[kPairs], qy[kPairs], qz[kPairs], ax[kPairs], ay[kPairs], az[kPairs];
+  int jt[kPairTPT];
 #pragma unroll
   for (int pr = 0; pr < kPairs; ++pr) {
-    const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
-    const float4 v0 = (j0 < m) ? q[j0] : make_float4(0.f, 0.f, 0.f, 0.f);
-    const float4 v1 = (j1 < m) ? q[j1] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const int t0 = base + 2 * pr * kPairThreads, t1 = t0 + kPairThreads;
+    jt[2 * pr] = jt[2 * pr + 1] = -1;
+    const float4 v0 = (t0 < count) ? general_target(P, qg, t0, &jt[2 * pr]) : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 v1 = (t1 < count) ? general_target(P, qg, t1, &jt[2 * pr + 1]) : make_float4(0.f, 0.f, 0.f, 0.f);
     qx[pr] = make_float2(v0.x, v1.x);
     qy[pr] = make_float2(v0.y, v1.y);
     qz[pr] = make_float2(v0.z, v1.z);
     ax[pr] = ay[pr] = az[pr] = make_float2(0.f, 0.f);
   }
-  const int k0 = blockIdx.y * chunk;
-  const int k1 = min(n, k0 + chunk);
+  const int k0 = kc * P.gen_chunk;
+  const int k1 = min(n, k0 + P.gen_chunk);
   for (int tile = k0; tile < k1; tile += kTile) {
     const int cnt = min(kTile, k1 - tile);
     __syncthreads();
-    for (int i = threadIdx.x; i < cnt; i += kPairThreads) {
-      const float4 p = ps[tile + i], a0 = w[tile + i];
-      // k_prep_sources<0>: 1/R and the scaled angular velocity
-      const float radius = p.w * 0.5f * sr;
-      const float s = VG_TWO_THIRDS * radius * radius * radius * sc;
-      const float invr = 1.0f / radius;
-      const float4 a = make_float4(a0.x * s, a0.y * s, a0.z * s, 0.f);
-      sh[5 * i + 0] = make_float4(-p.x, -p.x, -p.y, -p.y);
-      sh[5 * i + 1] = make_float4(-p.z, -p.z, invr, invr);
-      sh[5 * i + 2] = make_float4(a.x, a.x, a.y, a.y);
-      sh[5 * i + 3] = make_float4(a.z, a.z, -a.x, -a.x);
-      sh[5 * i + 4] = make_float4(-a.y, -a.y, -a.z, -a.z);
-    }
+    stage_pair_tile(ps, w, tile, cnt, sr, sc, sh);
     __syncthreads();
-#pragma unroll 2
+#pragma unroll 4
     for (int i = 0; i < cnt; ++i) {
       const float4 e0 = sh[5 * i], e1 = sh[5 * i + 1], e2 = sh[5 * i + 2], e3 = sh[5 * i + 3], e4 = sh[5 * i + 4];
       const float2 np0 = make_float2(e0.x, e0.y), np1 = make_float2(e0.z, e0.w), np2 = make_float2(e1.x, e1.y);
@@ -198,69 +239,190 @@ __global__ void __launch_bounds__(kPairThreads, 2)
       }
     }
   }
-  if (gridDim.y == 1) {  // one chunk: the sums are final (0 + sum, as the reduction would give)
-#pragma unroll
-    for (int pr = 0; pr < kPairs; ++pr) {
-      const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
-      if (j0 < m) out[j0] = make_float4(0.f + ax[pr].x, 0.f + ay[pr].x, 0.f + az[pr].x, 0.f);
-      if (j1 < m) out[j1] = make_float4(0.f + ax[pr].y, 0.f + ay[pr].y, 0.f + az[pr].y, 0.f);
-    }
-    return;
-  }
-  float* mine = partial + (size_t)blockIdx.y * (size_t)m * 3;
+  float* mine = partial ? partial + (size_t)kc * (size_t)count * 3 : nullptr;
 #pragma unroll
   for (int pr = 0; pr < kPairs; ++pr) {
-    const int j0 = base + 2 * pr * kPairThreads, j1 = j0 + kPairThreads;
-    if (j0 < m) {
-      mine[3 * j0] = ax[pr].x;
-      mine[3 * j0 + 1] = ay[pr].x;
-      mine[3 * j0 + 2] = az[pr].x;
-    }
-    if (j1 < m) {
-      mine[3 * j1] = ax[pr].y;
-      mine[3 * j1 + 1] = ay[pr].y;
-      mine[3 * j1 + 2] = az[pr].y;
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const int t = base + (2 * pr + h) * kPairThreads, j = jt[2 * pr + h];
+      if (j < 0) continue;
+      const float vx = h ? ax[pr].y : ax[pr].x, vy = h ? ay[pr].y : ay[pr].x, vz = h ? az[pr].y : az[pr].x;
+      if (!mine) {  // one chunk: the sums are final (0 + sum, as the reduction would give)
+        out[j] = make_float4(0.f + vx, 0.f + vy, 0.f + vz, 0.f);
+      } else {
+        float* o = mine + 3 * (size_t)t;
+        o[0] = vx, o[1] = vy, o[2] = vz;
+      }
     }
   }
 }
 
-// Sums the chunks' partial sums in chunk order (as k_reduce_partials), with
-// up to 16 chunks' loads issued before the first add: the sum is bound by the
-// latency of these loads, not by their bytes.
-__global__ void __launch_bounds__(256) k_reduce_pair(const float* __restrict__ partial, int ks, int m,
+// Grid points: a thread holds 8 consecutive points of one grid row, which
+// share y and z, so per source the y and z terms are formed once -- d1, d2,
+// d1^2 + d2^2, (w x d)_x and the w d2 and w d1 products (8 packed operations)
+// -- and each target pair needs 9: d0, |d|^2 = d0^2 + (d1^2 + d2^2) (the
+// general path's rounding order, so the same bits), the cubed law (2), the
+// (w x d)_y and _z components that depend on d0 (2), and law (w x d)
+// accumulated (3).
+__device__ __forceinline__ void pair_rows(const float4* __restrict__ ps, const float4* __restrict__ w, int n,
+                                          float sr, float sc, const PairPlan& P, int b, float4* sh,
+                                          float* __restrict__ partial, float4* __restrict__ out) {
+  constexpr int kPairs = kPairTPT / 2;
+  const int tb = b / P.row_ks, kc = b - tb * P.row_ks;
+  const int t = tb * kPairThreads + threadIdx.x;
+  const int r = t / P.tpr, seg = t - r * P.tpr;
+  const bool live = r < P.rows;
+  const int rr = live ? r : P.rows - 1;
+  const int np0 = (int)P.g.np[0], np1 = (int)P.g.np[1];
+  const int iy = rr % np1, iz = rr / np1;
+  const int x0 = seg * kPairTPT;
+  float2 qx[kPairs], ax[kPairs], ay[kPairs], az[kPairs];
+#pragma unroll
+  for (int pr = 0; pr < kPairs; ++pr) {
+    qx[pr] = make_float2(grid_coord(P.g, 0, x0 + 2 * pr), grid_coord(P.g, 0, x0 + 2 * pr + 1));
+    ax[pr] = ay[pr] = az[pr] = make_float2(0.f, 0.f);
+  }
+  const float qyv = grid_coord(P.g, 1, iy), qzv = grid_coord(P.g, 2, iz);
+  const float2 qy = make_float2(qyv, qyv), qz = make_float2(qzv, qzv);
+  const int k0 = kc * P.row_chunk;
+  const int k1 = min(n, k0 + P.row_chunk);
+  for (int tile = k0; tile < k1; tile += kTile) {
+    const int cnt = min(kTile, k1 - tile);
+    __syncthreads();
+    stage_pair_tile(ps, w, tile, cnt, sr, sc, sh);
+    __syncthreads();
+#pragma unroll 4
+    for (int i = 0; i < cnt; ++i) {
+      const float4 e0 = sh[5 * i], e1 = sh[5 * i + 1], e2 = sh[5 * i + 2], e3 = sh[5 * i + 3], e4 = sh[5 * i + 4];
+      const float2 np0d = make_float2(e0.x, e0.y), np1d = make_float2(e0.z, e0.w), np2d = make_float2(e1.x, e1.y);
+      const float invr = e1.z;
+      const float2 wx = make_float2(e2.x, e2.y), wy = make_float2(e2.z, e2.w), wz = make_float2(e3.x, e3.y);
+      const float2 nwx = make_float2(e3.z, e3.w), nwy = make_float2(e4.x, e4.y), nwz = make_float2(e4.z, e4.w);
+      const float2 d1 = __fadd2_rn(qy, np1d), d2 = __fadd2_rn(qz, np2d);
+      const float2 yz2 = __ffma2_rn(d1, d1, __fmul2_rn(d2, d2));
+      const float2 cx = __ffma2_rn(nwz, d1, __fmul2_rn(wy, d2));  // wy d2 - wz d1
+      const float2 nwxd2 = __fmul2_rn(nwx, d2), wxd1 = __fmul2_rn(wx, d1);
+#pragma unroll
+      for (int pr = 0; pr < kPairs; ++pr) {
+        const float2 d0 = __fadd2_rn(qx[pr], np0d);
+        const float2 r2 = __ffma2_rn(d0, d0, yz2);
+        const float2 inv = make_float2(fminf(rsqrt_ftz(r2.x), invr), fminf(rsqrt_ftz(r2.y), invr));
+        const float2 law = __fmul2_rn(__fmul2_rn(inv, inv), inv);
+        const float2 cy = __ffma2_rn(wz, d0, nwxd2);  // wz d0 - wx d2
+        const float2 cz = __ffma2_rn(nwy, d0, wxd1);  // wx d1 - wy d0
+        ax[pr] = __ffma2_rn(law, cx, ax[pr]);
+        ay[pr] = __ffma2_rn(law, cy, ay[pr]);
+        az[pr] = __ffma2_rn(law, cz, az[pr]);
+      }
+    }
+  }
+  if (!live) return;
+  float4* mine = partial ? reinterpret_cast<float4*>(partial) + (size_t)kc * (size_t)P.pts : nullptr;
+  const size_t jrow = (size_t)rr * np0 + x0;
+#pragma unroll
+  for (int pr = 0; pr < kPairs; ++pr) {
+#pragma unroll
+    for (int h = 0; h < 2; ++h) {
+      const size_t j = jrow + 2 * pr + h;
+      const float vx = h ? ax[pr].y : ax[pr].x, vy = h ? ay[pr].y : ay[pr].x, vz = h ? az[pr].y : az[pr].x;
+      if (!mine)
+        out[j] = make_float4(0.f + vx, 0.f + vy, 0.f + vz, 0.f);
+      else
+        mine[j] = make_float4(vx, vy, vz, 0.f);
+    }
+  }
+}
+
+// Velocity (KIND 0) with packed FP32x2 arithmetic (FADD2 / FMUL2 / FFMA2):
+// every source is staged in shared memory already duplicated into pairs, so
+// each operation advances two targets in one instruction.  Row CTAs (grid
+// points) and general CTAs (arbitrary points) run in the same launch, each
+// class with its own source split.  With one chunk per class the sums are
+// written to out; otherwise the partial sums go to a scratch buffer per class
+// ([chunk][target][3]) and k_reduce_pair adds them in chunk order, so results
+// are run-to-run deterministic.
+// 8 targets per thread (126 registers) was the fastest of the shapes measured
+// on GB300 for the general path (4 to 16 targets); CTAs of 256 threads, 2 per
+// SM, beat 4 CTAs of 128 by ~4%: the tile barriers keep a CTA's warps
+// together, whereas independent small CTAs on one SM finish far apart and
+// leave the SM short of warps at the end.
+__global__ void __launch_bounds__(kPairThreads, 2)
+    k_direct_pair(const float4* __restrict__ ps, const float4* __restrict__ w, int n, float sr, float sc,
+                  const float4* __restrict__ qg, PairPlan P, float* __restrict__ partial_rows,
+                  float* __restrict__ partial_gen, float4* __restrict__ out) {
+  pdl_entry();
+  __shared__ float4 sh[5 * kTile];
+  const int row_total = P.row_ctas * P.row_ks;
+  if ((int)blockIdx.x < row_total)
+    pair_rows(ps, w, n, sr, sc, P, (int)blockIdx.x, sh, partial_rows, out);
+  else
+    pair_general(ps, w, n, sr, sc, qg, P, (int)blockIdx.x - row_total, sh, partial_gen, out);
+}
+
+// Sums each target's partial sums in chunk order -- row targets from the
+// row partials (float4, indexed by target), general targets (remainder and
+// later-row gridpoints, targets past the grid) from the general partials
+// (float[3], indexed by class position) -- with up to 16 chunks' loads issued
+// before the first add: the sum is bound by the latency of these loads, not
+// by their bytes.
+__global__ void __launch_bounds__(128) k_reduce_pair(const float4* __restrict__ partial_rows,
+                                                     const float* __restrict__ partial_gen, PairPlan P,
                                                      float4* __restrict__ out, float* __restrict__ grid3, int pts,
                                                      float4* __restrict__ vel) {
   pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
-  if (j >= m) return;
+  if (j >= P.m) return;
   constexpr int kBatch = 16;
-  float x = 0.f, y = 0.f, z = 0.f;
-  for (int k0 = 0; k0 < ks; k0 += kBatch) {
-    float v[kBatch][3];
+  float sx = 0.f, sy = 0.f, sz = 0.f;
+  const int np0 = (int)P.g.np[0];
+  const int row = j < P.pts ? j / np0 : 0, x = j < P.pts ? j - row * np0 : 0;
+  if (j < P.pts && row < P.rows && x < P.xs) {  // row partials: float4 per target
+    const float4* src = partial_rows + j;
+    for (int k0 = 0; k0 < P.row_ks; k0 += kBatch) {
+      float4 v[kBatch];
 #pragma unroll
-    for (int k = 0; k < kBatch; ++k)
-      if (k0 + k < ks) {
-        const float* p = partial + ((size_t)(k0 + k) * m + j) * 3;
-        v[k][0] = p[0];
-        v[k][1] = p[1];
-        v[k][2] = p[2];
-      }
+      for (int k = 0; k < kBatch; ++k)
+        if (k0 + k < P.row_ks) v[k] = src[(size_t)(k0 + k) * P.pts];
 #pragma unroll
-    for (int k = 0; k < kBatch; ++k)
-      if (k0 + k < ks) {
-        x += v[k][0];
-        y += v[k][1];
-        z += v[k][2];
-      }
+      for (int k = 0; k < kBatch; ++k)
+        if (k0 + k < P.row_ks) {
+          sx += v[k].x;
+          sy += v[k].y;
+          sz += v[k].z;
+        }
+    }
+  } else {  // general partials: float[3] per target
+    const int t = j >= P.pts ? P.nrem + P.nrest + (j - P.pts)
+                             : (row < P.rows ? row * P.r0 + (x - P.xs) : P.nrem + (row - P.rows) * np0 + x);
+    const float* src = partial_gen + 3 * (size_t)t;
+    const size_t stride = 3 * (size_t)(P.nrem + P.nrest + (P.m - P.pts));
+    for (int k0 = 0; k0 < P.gen_ks; k0 += kBatch) {
+      float v[kBatch][3];
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k)
+        if (k0 + k < P.gen_ks) {
+          const float* p = src + (size_t)(k0 + k) * stride;
+          v[k][0] = p[0];
+          v[k][1] = p[1];
+          v[k][2] = p[2];
+        }
+#pragma unroll
+      for (int k = 0; k < kBatch; ++k)
+        if (k0 + k < P.gen_ks) {
+          sx += v[k][0];
+          sy += v[k][1];
+          sz += v[k][2];
+        }
+    }
   }
   if (!grid3) {
-    out[j] = make_float4(x, y, z, 0.f);
+    out[j] = make_float4(sx, sy, sz, 0.f);
   } else if (j < pts) {  // the velocity step's split: gridpoints as float[3], vortons as records
-    grid3[3 * j] = x;
-    grid3[3 * j + 1] = y;
-    grid3[3 * j + 2] = z;
+    grid3[3 * j] = sx;
+    grid3[3 * j + 1] = sy;
+    grid3[3 * j + 2] = sz;
   } else {
-    vel[j - pts] = make_float4(x, y, z, 0.f);
+    vel[j - pts] = make_float4(sx, sy, sz, 0.f);
   }
 }
 
@@ -333,6 +495,88 @@ int direct_split(int kind, size_t n, size_t m, unsigned* tblocks_out, unsigned* 
   return chunk;
 }
 
+// The source split of a k_direct_pair launch.  Each class of targets (grid
+// rows, general points) gets its own number of source chunks, chosen to
+// minimise the estimated time: the CTAs of both classes run in one wave
+// where possible (SMs x CTAs per SM), and the slowest CTA sets the time.  A
+// CTA's time is its chunk length times the class's packed operations per
+// source and thread (row CTAs 8 + 4 x 9 = 44, general CTAs 4 x 17 = 68), plus
+// a fixed set-up; more chunks cost more partial sums to reduce.
+PairPlan plan_pair(size_t n, size_t m, const Geom* grid) {
+  PairPlan P = {};
+  if (grid) {
+    P.g = *grid;
+    const int all_rows = (int)(grid->np[1] * grid->np[2]);
+    P.xs = (int)(grid->np[0] / kPairTPT) * kPairTPT;
+    P.r0 = (int)grid->np[0] - P.xs;
+    P.tpr = P.xs / kPairTPT;
+    // whole CTAs of row threads only: the rows they cannot hold go to the general class
+    P.row_ctas = P.tpr ? (int)(((size_t)all_rows * P.tpr) / kPairThreads) : 0;
+    P.rows = P.row_ctas ? std::min(all_rows, P.row_ctas * kPairThreads / P.tpr) : 0;
+    if (!P.rows) P.row_ctas = 0;
+    P.nrem = P.rows * P.r0;
+    P.nrest = (all_rows - P.rows) * (int)grid->np[0];
+    P.pts = (int)grid->points();
+  }
+  P.m = (int)m;
+  const size_t gcount = (size_t)P.nrem + (size_t)P.nrest + (m - (size_t)P.pts);
+  P.gen_ctas = (int)blocks_for(gcount, kPairThreads * kPairTPT);
+  struct Key {
+    size_t n, m;
+    int pts, rows, tpr, nrem, nrest, pad;
+  };
+  thread_local Key cached_key = {0, 0, 0, 0, 0, 0, 0, 0};
+  thread_local int cached_ks[2] = {0, 0};
+  const Key key = {n, m, P.pts, P.rows, P.tpr, P.nrem, P.nrest, 0};
+  int kr = 1, kg = 1;
+  if (cached_ks[0] && memcmp(&key, &cached_key, sizeof(Key)) == 0) {
+    kr = cached_ks[0], kg = cached_ks[1];
+  } else {
+    const double slots = direct_slots(0), c_row = 44.0, c_gen = 68.0, setup = 24.0, reduce = 0.002;
+    const int kmax = (int)std::max<size_t>(1, std::min<size_t>(256, n / 64));
+    double best = 1e300;
+    for (int a = 1; a <= (P.row_ctas ? kmax : 1); ++a)
+      for (int b = 1; b <= (P.gen_ctas ? kmax : 1); ++b) {
+        const size_t cr = (n + a - 1) / a, cg = (n + b - 1) / b;
+        const double ctas = (double)P.row_ctas * a + (double)P.gen_ctas * b;
+        const double waves = std::ceil(ctas / slots);
+        const double slow = std::max(P.row_ctas ? c_row * (cr + setup) : 0.0, P.gen_ctas ? c_gen * (cg + setup) : 0.0);
+        const double t =
+            waves * slow + ((a > 1 || b > 1) ? reduce * ((double)a * P.pts + (double)b * (double)gcount) : 0.0);
+        if (t < best) best = t, kr = a, kg = b;
+      }
+    cached_key = key;
+    cached_ks[0] = kr, cached_ks[1] = kg;
+  }
+  P.row_chunk = (int)((n + kr - 1) / kr);
+  P.row_ks = P.row_ctas ? (int)((n + P.row_chunk - 1) / P.row_chunk) : 1;
+  P.gen_chunk = (int)((n + kg - 1) / kg);
+  P.gen_ks = P.gen_ctas ? (int)((n + P.gen_chunk - 1) / P.gen_chunk) : 1;
+  return P;
+}
+
+// Launches k_direct_pair (and, with more than one chunk in either class,
+// k_reduce_pair) for plan P; partial has room for the plan's partial sums.
+template <typename Launch>
+cudaError_t launch_pair_plan(Launch launch, const PairPlan& P, const float4* ps, const float4* w, int n, float sr,
+                             float sc, const float4* qg, float* partial, float4* out, const DirectSplit* split) {
+  const bool reduce = P.row_ks > 1 || P.gen_ks > 1;
+  float* pr = reduce ? partial : nullptr;
+  float* pg = reduce ? partial + (P.row_ctas ? (size_t)P.row_ks * P.pts * 4 : 0) : nullptr;
+  const unsigned ctas = (unsigned)(P.row_ctas * P.row_ks + P.gen_ctas * P.gen_ks);
+  cudaError_t e = launch(dim3(ctas), dim3(kPairThreads), k_direct_pair, ps, w, n, sr, sc, qg, P, pr, pg, out);
+  if (e != cudaSuccess || !reduce) return e;
+  return launch(dim3(blocks_for((size_t)P.m, 128)), dim3(128), k_reduce_pair, (const float4*)pr, (const float*)pg,
+                P, out, split ? split->grid3 : (float*)nullptr, split ? (int)split->pts : 0,
+                split ? split->vel : (float4*)nullptr);
+}
+
+// Partial sums of a plan: per chunk, float4 per gridpoint (row class), float[3] per general target.
+size_t pair_partial_floats(const PairPlan& P) {
+  const size_t rows = P.row_ctas ? (size_t)P.row_ks * (size_t)P.pts * 4 : 0;
+  return rows + 3 * (size_t)P.gen_ks * ((size_t)P.nrem + (size_t)P.nrest + (size_t)(P.m - P.pts));
+}
+
 }  // namespace
 
 vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const float4* w, size_t n, const float4* q,
@@ -353,30 +597,31 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
     VG_CUDA(c, cudaGetLastError());
     return VG_OK;
   }
-  unsigned tblocks = 0, ksplit = 0;
-  const int chunk = direct_split(kind, n, m, &tblocks, &ksplit);
   vg_status st = VG_OK;
   if (kind == 0) {
+    // grid rows for the step's gridpoint targets, when they are the grid's points
+    const Geom* grid = (split && split->grid && split->grid->points() == split->pts && split->pts <= m &&
+                        split->grid->np[0] >= 1)
+                           ? split->grid
+                           : nullptr;
+    const PairPlan P = plan_pair(n, m, grid);
+    const bool reduce = P.row_ks > 1 || P.gen_ks > 1;
     float* partial = nullptr;
-    if (ksplit > 1) {
-      partial = (float*)ws(c, S_DIRECT, (size_t)ksplit * m * 3 * sizeof(float), &st);
+    if (reduce) {
+      partial = (float*)ws(c, S_DIRECT, pair_partial_floats(P) * sizeof(float), &st);
       if (st != VG_OK) return st;
     }
-    dim3 grid(tblocks, ksplit);
-    pdl_launch(c->stream, grid, dim3(kPairThreads), 0, k_direct_pair, ps, w, (int)n, chunk, sr, sc, q, (int)m, partial,
-               out);
-    VG_LAUNCHED(c);
-    if (ksplit > 1) {
-      const bool to_split = split != nullptr;
-      pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_reduce_pair, (const float*)partial, (int)ksplit, (int)m, out,
-                 to_split ? split->grid3 : (float*)nullptr, to_split ? (int)split->pts : 0,
-                 to_split ? split->vel : (float4*)nullptr);
-      if (split_done) *split_done = to_split;
-      VG_LAUNCHED(c);
-    }
+    cudaStream_t s = c->stream;
+    auto launch = [s](dim3 g, dim3 b, auto kernel, auto... args) { return pdl_launch(s, g, b, 0, kernel, args...); };
+    const float4* qg = (grid && split->after_grid) ? split->after_grid : q + P.pts;
+    VG_CUDA(c, launch_pair_plan(launch, P, ps, w, (int)n, sr, sc, qg, partial, out, split));
+    c->launches += reduce ? 2 : 1;
+    if (split_done) *split_done = reduce && split != nullptr;
     VG_CUDA(c, cudaGetLastError());
     return VG_OK;
   }
+  unsigned tblocks = 0, ksplit = 0;
+  const int chunk = direct_split(kind, n, m, &tblocks, &ksplit);
   const size_t srcb = ((n * sizeof(float4) + 255) / 256) * 256;
   char* scratch = (char*)ws(c, S_DIRECT, 2 * srcb + (size_t)ksplit * m * 3 * sizeof(float), &st);
   if (st != VG_OK) return st;
@@ -470,11 +715,22 @@ extern "C" vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_
   // the partial sums fit the array: wherever the cap does not bind, the
   // results are bit-identical to vg_direct_device's.
   unsigned tblocks = 0, ksplit = 0;
-  int chunk = direct_split(kind, n, m, &tblocks, &ksplit);
-  while (ksplit > 1 && (size_t)ksplit * m * 3 * sizeof(float) > room) {
-    const unsigned k = ksplit - 1;
-    chunk = (int)((n + k - 1) / k);
-    ksplit = (unsigned)((n + chunk - 1) / chunk);
+  int chunk = 0;
+  PairPlan P = {};
+  if (kind == 0) {
+    P = plan_pair(n, m, nullptr);
+    while (P.gen_ks > 1 && (size_t)P.gen_ks * m * 3 * sizeof(float) > room) {
+      const int k = P.gen_ks - 1;
+      P.gen_chunk = (int)((n + k - 1) / k);
+      P.gen_ks = (int)((n + P.gen_chunk - 1) / P.gen_chunk);
+    }
+  } else {
+    chunk = direct_split(kind, n, m, &tblocks, &ksplit);
+    while (ksplit > 1 && (size_t)ksplit * m * 3 * sizeof(float) > room) {
+      const unsigned k = ksplit - 1;
+      chunk = (int)((n + k - 1) / k);
+      ksplit = (unsigned)((n + chunk - 1) / chunk);
+    }
   }
   float4* s0 = (float4*)base;
   float4* s1 = (float4*)((char*)base + src_bytes);
@@ -486,14 +742,9 @@ extern "C" vg_status vg_direct_noalloc(void* stream, int kind, const float* pos_
   const float4* q = (const float4*)q4;
   float4* out = (float4*)out4;
   if (kind == 0) {
-    e = launch_plain(st, dim3(tblocks, ksplit), dim3(kPairThreads), k_direct_pair, ps, w, (int)n, chunk, spread_range,
-                     spread_circ, q, (int)m, ksplit > 1 ? partial : (float*)nullptr, out);
-    if (e != cudaSuccess) return noalloc_fail(e, "k_direct_pair launch");
-    if (ksplit > 1) {
-      e = launch_plain(st, dim3(blocks_for(m, 256)), dim3(256), k_reduce_pair, (const float*)partial, (int)ksplit,
-                       (int)m, out, (float*)nullptr, 0, (float4*)nullptr);
-      if (e != cudaSuccess) return noalloc_fail(e, "k_reduce_pair launch");
-    }
+    auto launch = [st](dim3 g, dim3 b, auto kernel, auto... args) { return launch_plain(st, g, b, kernel, args...); };
+    e = launch_pair_plan(launch, P, ps, w, (int)n, spread_range, spread_circ, q, partial, out, nullptr);
+    if (e != cudaSuccess) return noalloc_fail(e, "k_direct_pair / k_reduce_pair launch");
     return VG_OK;
   }
   e = launch_plain(st, dim3(blocks_for(n, 256)), dim3(256), k_prep_sources<1>, ps, w, (int)n, spread_range,

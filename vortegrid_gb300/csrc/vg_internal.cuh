@@ -345,10 +345,16 @@ inline cudaError_t pdl_launch(cudaStream_t s, dim3 grid, dim3 block, size_t smem
 
 // Where the velocity step wants the direct sum's results: targets [0, pts)
 // as float[3] into grid3, the rest as float4 records into vel.
+// When grid is given, targets [0, pts) are that grid's points (the step's
+// gridpoint positions), which the packed kernel evaluates row by row without
+// reading them from q; after_grid, when given, holds targets [pts, m) (the
+// vortons' records) for it in place of q + pts.
 struct DirectSplit {
   float* grid3;
   size_t pts;
   float4* vel;
+  const Geom* grid;
+  const float4* after_grid;
 };
 // With split, *split_done says whether the results went there (the
 // multi-chunk packed path writes them from its reduction) or to out.
