@@ -790,8 +790,19 @@ def poisson_section(vg, torch, stream, local, steps=3):
     k1, k2 = zero_ctx.poisson_schedule()
     zero_ctx.set_poisson_schedule(k1, k2)
     fixed = summary(run(zero_ctx, True))
-    zero_ctx.set_poisson_schedule(0, 0)
     st_fixed = zero_ctx.stats()
+    v32 = velocity(zero_ctx)
+    # the same schedule with the coarsest level (33^3, sine transforms) solved in FP64
+    zero_ctx.set_coarsest_fp64(True)
+    c64 = summary(run(zero_ctx, True))
+    st64 = zero_ctx.stats()
+    v64 = velocity(zero_ctx)
+    zero_ctx.set_coarsest_fp64(False)
+    zero_ctx.set_poisson_schedule(0, 0)
+    out["coarsest_fp64"] = {"ms": c64["ms"], "relres": st64.poisson_relres,
+                            "velocity_rel_diff_vs_fp32_coarsest": float((v64 - v32).norm() / v32.norm()),
+                            "note": "the fixed schedule with the coarsest solve's tables and arithmetic in FP64; "
+                                    "the default solve keeps them in FP32"}
     out["fixed_schedule"] = {"ms": fixed["ms"], "fp32_cycles": k1, "refinement_cycles": k2,
                              "relres": st_fixed.poisson_relres}
     out["plain_mg_ms"] = fixed["ms"]

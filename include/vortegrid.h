@@ -171,6 +171,14 @@ vg_status vg_get_stats(vg_ctx* ctx, vg_step_stats* stats);
  * (vortonSim.cpp:2539-2571). */
 vg_status vg_set_poisson_schedule(vg_ctx* ctx, int fp32_cycles, int refinement_cycles);
 vg_status vg_get_poisson_schedule(const vg_ctx* ctx, int* fp32_cycles, int* refinement_cycles);
+
+/* Precision of the multigrid's coarsest solve (sine transforms over the whole
+ * GPU, used when the coarsest level has more than 512 interior points): FP32
+ * (on = 0, the default) or FP64 tables and arithmetic (on = 1).  No
+ * counterpart in the reference, whose cascade has no coarsest solve.  Cycles
+ * captured earlier are recaptured; a step captured by the caller in a CUDA
+ * graph must be captured again.  The batched persistent solve needs FP32. */
+vg_status vg_set_coarsest_fp64(vg_ctx* ctx, int on);
 /* Wait for the context's stream and report any error a device stage flagged
  * since the last synchronising call (VG_OUT_OF_GRID, VG_NONFINITE).  The
  * *_device entry points do not synchronise; host-buffer calls do this

@@ -138,7 +138,7 @@ EXPORTS = [
     "vg_status_string", "vg_last_error", "vg_abi_version", "vg_config_default", "vg_create", "vg_destroy",
     "vg_set_config", "vg_step", "vg_step_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
     "vg_get_vector_potential", "vg_get_stats", "vg_advect", "vg_advect_device", "vg_define_shape",
-    "vg_set_poisson_schedule", "vg_get_poisson_schedule",
+    "vg_set_poisson_schedule", "vg_get_poisson_schedule", "vg_set_coarsest_fp64",
     "vg_bin_device", "vg_partition_device", "vg_direct_device", "vg_tree_device", "vg_splat_device", "vg_boundary_vecpot_device",
     "vg_sor_device", "vg_cascade_device", "vg_multigrid_device", "vg_downsample_device", "vg_upsample_device",
     "vg_jacobian_curl_device", "vg_stretch_device", "vg_pse_device", "vg_gather_advect_device", "vg_synchronize",
@@ -228,6 +228,7 @@ def lib():
         L.vg_bin_device.argtypes = [vp, G, vp, sz, vp, vp]
         L.vg_partition_device.argtypes = [vp, G, vp, sz, vp, vp]
         L.vg_set_poisson_schedule.argtypes = [vp, i, i]
+        L.vg_set_coarsest_fp64.argtypes = [vp, i]
         L.vg_get_poisson_schedule.argtypes = [vp, ctypes.POINTER(ctypes.c_int), ctypes.POINTER(ctypes.c_int)]
         L.vg_direct_device.argtypes = [vp, i, vp, vp, sz, vp, sz, fl, fl, vp]
         L.vg_tree_device.argtypes = [vp, i, G, vp, vp, sz, vp, sz, fl, fl, vp, vp, sz, ctypes.POINTER(ctypes.c_size_t)]
@@ -344,6 +345,10 @@ class Context:
     def set_poisson_schedule(self, fp32_cycles=0, refinement_cycles=0):
         """Fixed multigrid schedule (no host round trip); (0, 0) = adaptive."""
         self.check(lib().vg_set_poisson_schedule(self.h, fp32_cycles, refinement_cycles), "vg_set_poisson_schedule")
+
+    def set_coarsest_fp64(self, on=True):
+        """Solve the multigrid's coarsest level in FP64 (True) or FP32 (False, the default)."""
+        self.check(lib().vg_set_coarsest_fp64(self.h, int(bool(on))), "vg_set_coarsest_fp64")
 
     def poisson_schedule(self):
         """(FP32 cycles, refinement cycles) the last adaptive solve used."""

@@ -884,6 +884,20 @@ vg_status vg_set_poisson_schedule(vg_ctx* c, int k1, int k2) {
   return VG_OK;
 }
 
+vg_status vg_set_coarsest_fp64(vg_ctx* c, int on) {
+  if (!c) return VG_INVALID;
+  const bool v = on != 0;
+  if (c->mg_coarse_fp64 != v) {
+    c->mg_coarse_fp64 = v;
+    for (MgGraphCache& G : c->mg_graph)  // the captured cycles hold the other precision's kernels
+      if (G.exec) {
+        cudaGraphExecDestroy(G.exec);
+        G.exec = nullptr;
+      }
+  }
+  return VG_OK;
+}
+
 vg_status vg_get_poisson_schedule(const vg_ctx* c, int* k1, int* k2) {
   if (!c || !k1 || !k2) return VG_INVALID;
   *k1 = c->mg_last_k1;

@@ -282,6 +282,10 @@ struct Ctx {
   // the multigrid coarsest-level inverse held in buf[S_MGINV]: its level's shape and 1 / spacing^2
   unsigned mginv_np[3] = {0, 0, 0};
   double mginv_r2[3] = {0.0, 0.0, 0.0};
+  bool mginv_fp64 = false;  // the tables in buf[S_MGINV] are double
+  // The coarsest multigrid level (sine transforms over the whole GPU) solved
+  // in FP64 instead of FP32 (vg_set_coarsest_fp64).
+  bool mg_coarse_fp64 = false;
   // A step split at the Poisson solve, for batched frames that solve every
   // simulation's problem in one persistent launch between the two halves:
   // 0 the whole step; 1 up to the solve (its state kept in *split); 2 from

@@ -35,6 +35,7 @@
 #include <algorithm>
 #include <cmath>
 #include <cstring>
+#include <type_traits>
 #include <vector>
 
 #include "vg_internal.cuh"
@@ -828,34 +829,42 @@ static void add_f32(Ctx* c, float* a, const float* e, size_t n) {
 // for a coarsest level of up to kDirectGlobalMax interior points: gather r
 // into compact order (3 (x + nx' (y + ny' z)) + c), five sine-transform passes
 // (the third scaled by 1 / eigenvalue), and the last x pass writing e in
-// full layout (zero on the boundary).  Same operations as the CTA form.
-__global__ void __launch_bounds__(256) k_dst_gather(Geom g, const float* __restrict__ rfull, float* __restrict__ X) {
+// full layout (zero on the boundary).  Same operations as the CTA form.  T is
+// the arithmetic of the transform (float, or double for the FP64 coarsest
+// solve, whose tables and intermediate fields are double).
+__device__ __forceinline__ float fma_t(float a, float b, float c) { return fmaf(a, b, c); }
+__device__ __forceinline__ double fma_t(double a, double b, double c) { return fma(a, b, c); }
+
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_gather(Geom g, const float* __restrict__ rfull, T* __restrict__ X) {
   pdl_entry();
   const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * N) return;
   const unsigned c = i % 3u, p = i / 3u;
   const unsigned x = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
-  X[i] = rfull[3 * ((x + 1) + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c];
+  X[i] = (T)rfull[3 * ((x + 1) + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c];
 }
 
-__global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const float* __restrict__ in, float* __restrict__ out,
-                                                  const float* __restrict__ T, unsigned n, unsigned st,
-                                                  const float* __restrict__ Dinv) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const T* __restrict__ in, T* __restrict__ out,
+                                                  const T* __restrict__ Tab, unsigned n, unsigned st,
+                                                  const T* __restrict__ Dinv) {
   pdl_entry();
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
   if (i >= 3 * N) return;
   const unsigned c = i % 3u, p = i / 3u;
   const unsigned k = (p / st) % n, p0 = p - k * st;
-  float acc = 0.f;
-  for (unsigned m = 0; m < n; ++m) acc = fmaf(__ldg(T + k * n + m), in[3 * (p0 + m * st) + c], acc);
+  T acc = 0;
+  for (unsigned m = 0; m < n; ++m) acc = fma_t(__ldg(Tab + k * n + m), in[3 * (p0 + m * st) + c], acc);
   out[i] = Dinv ? acc * __ldg(Dinv + p) : acc;
 }
 
 // The first x pass reading r in full layout (the gather folded in): the same
 // sums as k_dst_gather followed by k_dst_pass along x.
-__global__ void __launch_bounds__(256) k_dst_first(Geom g, const float* __restrict__ rfull, float* __restrict__ out,
-                                                   const float* __restrict__ Sx) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_first(Geom g, const float* __restrict__ rfull, T* __restrict__ out,
+                                                   const T* __restrict__ Sx) {
   pdl_entry();
   const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -863,41 +872,44 @@ __global__ void __launch_bounds__(256) k_dst_first(Geom g, const float* __restri
   const unsigned c = i % 3u, p = i / 3u;
   const unsigned k = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
   const unsigned row = 3 * (1 + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c;  // r at (1, y + 1, z + 1)
-  float acc = 0.f;
-  for (unsigned m = 0; m < nxi; ++m) acc = fmaf(__ldg(Sx + k * nxi + m), rfull[row + 3 * m], acc);
+  T acc = 0;
+  for (unsigned m = 0; m < nxi; ++m) acc = fma_t(__ldg(Sx + k * nxi + m), (T)rfull[row + 3 * m], acc);
   out[i] = acc;
 }
 
 // The two z passes around the eigenvalue scaling, fused: a CTA owns whole z
 // columns (32 x's, one y, one component), keeps the first pass's results in
 // shared memory and runs the second from there -- the same sums as two
-// k_dst_pass launches.  Dynamic shared memory: nzi x 32 floats.
+// k_dst_pass launches.  Dynamic shared memory: nzi x 32 values.
 constexpr unsigned kZZMaxN = 384;
-__global__ void __launch_bounds__(256) k_dst_zz(unsigned nxi, unsigned nyi, unsigned nzi, const float* __restrict__ in,
-                                                float* __restrict__ out, const float* __restrict__ Sz,
-                                                const float* __restrict__ Dinv) {
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_zz(unsigned nxi, unsigned nyi, unsigned nzi, const T* __restrict__ in,
+                                                T* __restrict__ out, const T* __restrict__ Sz,
+                                                const T* __restrict__ Dinv) {
   pdl_entry();
-  extern __shared__ float col[];  // [z][x - x0]
+  extern __shared__ __align__(8) unsigned char col_raw[];
+  T* col = reinterpret_cast<T*>(col_raw);  // [z][x - x0]
   const unsigned x0 = blockIdx.x * 32, y = blockIdx.y, c = blockIdx.z, st = nxi * nyi;
   for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
     const unsigned xl = it % 32, z = it / 32, x = x0 + xl;
     if (x >= nxi) continue;
     const unsigned p0 = x + nxi * y;
-    float acc = 0.f;
-    for (unsigned m = 0; m < nzi; ++m) acc = fmaf(__ldg(Sz + z * nzi + m), in[3 * (p0 + m * st) + c], acc);
+    T acc = 0;
+    for (unsigned m = 0; m < nzi; ++m) acc = fma_t(__ldg(Sz + z * nzi + m), in[3 * (p0 + m * st) + c], acc);
     col[z * 32 + xl] = acc * __ldg(Dinv + p0 + z * st);
   }
   __syncthreads();
   for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
     const unsigned xl = it % 32, z = it / 32, x = x0 + xl;
     if (x >= nxi) continue;
-    float acc = 0.f;
-    for (unsigned m = 0; m < nzi; ++m) acc = fmaf(__ldg(Sz + z * nzi + m), col[m * 32 + xl], acc);
+    T acc = 0;
+    for (unsigned m = 0; m < nzi; ++m) acc = fma_t(__ldg(Sz + z * nzi + m), col[m * 32 + xl], acc);
     out[3 * (x + nxi * y + z * st) + c] = acc;
   }
 }
 
-__global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const float* __restrict__ Y, const float* __restrict__ Sx,
+template <typename T>
+__global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const T* __restrict__ Y, const T* __restrict__ Sx,
                                                      float* __restrict__ efull) {
   pdl_entry();
   const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -905,12 +917,12 @@ __global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const float* __rest
   const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2;
   const unsigned c = i % 3u, k = i / 3u;
   const unsigned x = k % g.np[0], q = k / g.np[0], y = q % g.np[1], z = q / g.np[1];
-  float v = 0.f;
+  T v = 0;
   if (x > 0 && y > 0 && z > 0 && x + 1 < g.np[0] && y + 1 < g.np[1] && z + 1 < g.np[2]) {
     const unsigned kx = x - 1, p0 = nxi * ((y - 1) + nyi * (z - 1));
-    for (unsigned m = 0; m < nxi; ++m) v = fmaf(__ldg(Sx + kx * nxi + m), Y[3 * (p0 + m) + c], v);
+    for (unsigned m = 0; m < nxi; ++m) v = fma_t(__ldg(Sx + kx * nxi + m), Y[3 * (p0 + m) + c], v);
   }
-  efull[i] = v;
+  efull[i] = (float)v;
 }
 
 struct MgPlan {
@@ -983,7 +995,10 @@ struct MgBufs {
   double* part;
   double* sums;
   double* cwork;
-  const float* dst;  // the coarsest level's sine-transform tables when P.direct
+  const void* dst;  // the coarsest level's sine-transform tables when P.direct (float, or double with dst64)
+  bool dst64;       // FP64 coarsest solve: double tables, and double ping-pong fields d64a, d64b (3 N each)
+  double* d64a;
+  double* d64b;
   unsigned nb0;  // residual blocks (partial sums)
   ResLaunch rl;   // the residual kernels' launch over level 0
 };
@@ -1018,30 +1033,37 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
     const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, nzi = g.np[2] - 2, N = nxi * nyi * nzi;
     float* E = B.E + 3 * L.base;  // ping-pong buffers in compact layout (3 N <= 3 points)
     float* R = B.R + 3 * L.base;
-    const float* Sx = B.dst;
-    const float* Sy = Sx + nxi * nxi;
-    const float* Sz = Sy + nyi * nyi;
-    const float* Dinv = Sz + nzi * nzi;
     const unsigned nb = blocks_for(3 * N, 256);
-    if (nzi <= kZZMaxN) {
-      // x pass from r (full layout) -> E, y -> R, z (scaled) z -> E, y -> R, x -> e (full)
-      pdl_launch(c->stream, nb, 256, 0, k_dst_first, g, (const float*)R, E, Sx);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, (const float*)E, R, Sy, nyi, nxi, (const float*)nullptr);
-      pdl_launch(c->stream, dim3((nxi + 31) / 32, nyi, 3), 256, (size_t)nzi * 32 * sizeof(float), k_dst_zz, nxi, nyi,
-                 nzi, (const float*)R, E, Sz, Dinv);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, (const float*)E, R, Sy, nyi, nxi, (const float*)nullptr);
-      *nl += 4;
-    } else {
-      pdl_launch(c->stream, nb, 256, 0, k_dst_gather, g, R, E);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sx, nxi, 1, nullptr);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sy, nyi, nxi, nullptr);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sz, nzi, nxi * nyi, Dinv);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, R, E, Sz, nzi, nxi * nyi, nullptr);
-      pdl_launch(c->stream, nb, 256, 0, k_dst_pass, N, E, R, Sy, nyi, nxi, nullptr);
-      *nl += 6;
-    }
-    pdl_launch(c->stream, blocks_for(3 * g.points(), 256), 256, 0, k_dst_scatter, g, R, Sx, E);
-    ++*nl;
+    auto transform = [&](auto* X, auto* Y, auto* tab) {
+      using T = typename std::remove_const<typename std::remove_pointer<decltype(tab)>::type>::type;
+      const T* Sx = tab;
+      const T* Sy = Sx + nxi * nxi;
+      const T* Sz = Sy + nyi * nyi;
+      const T* Dinv = Sz + nzi * nzi;
+      if (nzi <= kZZMaxN) {
+        // x pass from r (full layout) -> X, y -> Y, z (scaled) z -> X, y -> Y, x -> e (full)
+        pdl_launch(c->stream, nb, 256, 0, k_dst_first<T>, g, (const float*)R, X, Sx);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sy, nyi, nxi, (const T*)nullptr);
+        pdl_launch(c->stream, dim3((nxi + 31) / 32, nyi, 3), 256, (size_t)nzi * 32 * sizeof(T), k_dst_zz<T>, nxi, nyi,
+                   nzi, (const T*)Y, X, Sz, Dinv);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sy, nyi, nxi, (const T*)nullptr);
+        *nl += 4;
+      } else {
+        pdl_launch(c->stream, nb, 256, 0, k_dst_gather<T>, g, (const float*)R, X);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sx, nxi, 1u, (const T*)nullptr);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)Y, X, Sy, nyi, nxi, (const T*)nullptr);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sz, nzi, nxi * nyi, Dinv);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)Y, X, Sz, nzi, nxi * nyi, (const T*)nullptr);
+        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sy, nyi, nxi, (const T*)nullptr);
+        *nl += 6;
+      }
+      pdl_launch(c->stream, blocks_for(3 * g.points(), 256), 256, 0, k_dst_scatter<T>, g, (const T*)Y, Sx, E);
+      ++*nl;
+    };
+    if (B.dst64)
+      transform(B.d64a, B.d64b, (const double*)B.dst);
+    else
+      transform(E, R, (const float*)B.dst);
   } else {
     SmallLevels S;
     S.n = P.nlev - fs;
@@ -1062,7 +1084,7 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
       S.inv_nyi[i] = 1.0f / (float)(L.g.np[1] - 2);
       off += (unsigned)(6 * L.g.points());
     }
-    S.dst = P.direct ? B.dst : nullptr;
+    S.dst = P.direct ? (const float*)B.dst : nullptr;
     S.r_in = B.R + 3 * P.lev[fs].base;
     S.e_out = B.E + 3 * P.lev[fs].base;
     S.pre = pre;
@@ -1194,42 +1216,60 @@ static vg_status read_norm(Ctx* c, const MgBufs& B, double* rr, double* bb) {
 // (FP64 on the host, stored as FP32).  Uploaded when the level's shape or
 // spacing changes; never during stream capture, which the calibrated
 // schedules guarantee by running the same grid uncaptured first.
-static vg_status direct_tables(Ctx* c, const Geom& lg, const float** out) {
+static vg_status direct_tables(Ctx* c, const Geom& lg, bool fp64, const void** out, double** d64a, double** d64b) {
   const double r2[3] = {1.0 / ((double)lg.cell[0] * lg.cell[0]), 1.0 / ((double)lg.cell[1] * lg.cell[1]),
                         1.0 / ((double)lg.cell[2] * lg.cell[2])};
+  const unsigned n[3] = {lg.np[0] - 2, lg.np[1] - 2, lg.np[2] - 2};
+  const size_t N = (size_t)n[0] * n[1] * n[2];
+  const size_t count = (size_t)n[0] * n[0] + (size_t)n[1] * n[1] + (size_t)n[2] * n[2] + N;
+  const size_t tab_bytes = ((count * (fp64 ? sizeof(double) : sizeof(float)) + 255) / 256) * 256;
+  auto fields = [&](void* base) {
+    if (!fp64) return;
+    *d64a = (double*)((char*)base + tab_bytes);
+    *d64b = *d64a + 3 * N;
+  };
   if (c->mginv_np[0] == lg.np[0] && c->mginv_np[1] == lg.np[1] && c->mginv_np[2] == lg.np[2] &&
-      c->mginv_r2[0] == r2[0] && c->mginv_r2[1] == r2[1] && c->mginv_r2[2] == r2[2] && c->buf[S_MGINV].p) {
-    *out = (const float*)c->buf[S_MGINV].p;
+      c->mginv_r2[0] == r2[0] && c->mginv_r2[1] == r2[1] && c->mginv_r2[2] == r2[2] && c->mginv_fp64 == fp64 &&
+      c->buf[S_MGINV].p) {
+    *out = c->buf[S_MGINV].p;
+    fields(c->buf[S_MGINV].p);
     return VG_OK;
   }
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
   if (cap != cudaStreamCaptureStatusNone)
     return fail(c, VG_INVALID, "multigrid: the coarsest-level tables are not ready (run this grid uncaptured first)");
-  const unsigned n[3] = {lg.np[0] - 2, lg.np[1] - 2, lg.np[2] - 2};
   const double pi = 3.14159265358979323846;
-  std::vector<float> h;
+  std::vector<double> h;
   std::vector<double> lam[3];
   for (int a = 0; a < 3; ++a) {
     const double f = std::sqrt(2.0 / (n[a] + 1));
     for (unsigned k = 0; k < n[a]; ++k)
-      for (unsigned m = 0; m < n[a]; ++m) h.push_back((float)(f * std::sin(pi * (m + 1) * (k + 1) / (n[a] + 1))));
+      for (unsigned m = 0; m < n[a]; ++m) h.push_back(f * std::sin(pi * (m + 1) * (k + 1) / (n[a] + 1)));
     for (unsigned k = 0; k < n[a]; ++k) lam[a].push_back(2.0 - 2.0 * std::cos(pi * (k + 1) / (n[a] + 1)));
   }
   for (unsigned z = 0; z < n[2]; ++z)
     for (unsigned y = 0; y < n[1]; ++y)
       for (unsigned x = 0; x < n[0]; ++x)
-        h.push_back((float)(-1.0 / (r2[0] * lam[0][x] + r2[1] * lam[1][y] + r2[2] * lam[2][z])));
+        h.push_back(-1.0 / (r2[0] * lam[0][x] + r2[1] * lam[1][y] + r2[2] * lam[2][z]));
   vg_status st = VG_OK;
-  float* d = (float*)ws(c, S_MGINV, h.size() * sizeof(float), &st);
+  void* d = ws(c, S_MGINV, tab_bytes + (fp64 ? 2 * 3 * N * sizeof(double) : 0), &st);
   if (st != VG_OK) return st;
-  VG_CUDA(c, cudaMemcpyAsync(d, h.data(), h.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));  // h is released on return
+  if (fp64) {
+    VG_CUDA(c, cudaMemcpyAsync(d, h.data(), h.size() * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));  // h is released on return
+  } else {
+    std::vector<float> hf(h.begin(), h.end());
+    VG_CUDA(c, cudaMemcpyAsync(d, hf.data(), hf.size() * sizeof(float), cudaMemcpyHostToDevice, c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+  }
   for (int a = 0; a < 3; ++a) {
     c->mginv_np[a] = lg.np[a];
     c->mginv_r2[a] = r2[a];
   }
+  c->mginv_fp64 = fp64;
   *out = d;
+  fields(d);
   return VG_OK;
 }
 
@@ -1254,7 +1294,10 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
   B.nb0 = nb0;
   B.rl = rl;
   B.dst = nullptr;
-  if (P.direct && (st = direct_tables(c, P.lev[P.nlev - 1].g, &B.dst)) != VG_OK) return st;
+  B.dst64 = P.direct_global && c->mg_coarse_fp64;
+  B.d64a = B.d64b = nullptr;
+  if (P.direct && (st = direct_tables(c, P.lev[P.nlev - 1].g, B.dst64, &B.dst, &B.d64a, &B.d64b)) != VG_OK)
+    return st;
   *etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
   *rir = *etot + 3 * n0;                                                                 // IR right-hand side
   static bool smem_set = false;
@@ -2127,7 +2170,11 @@ vg_status mg_batch_build(const std::vector<MgBatchItem>& items, int device, int 
     S.etot = etot;
     S.rir = rir;
     S.rhs = it.rhs;
-    S.dst = B.dst;
+    if (B.dst64) {
+      *err = "persistent solve: the coarsest level must be solved in FP32 (vg_set_coarsest_fp64 off)";
+      return VG_INVALID;
+    }
+    S.dst = (const float*)B.dst;
     S.relres = c->mg_relres_dev;
     S.n0 = (unsigned)it.g.points();
     S.total = (unsigned)P.total;
