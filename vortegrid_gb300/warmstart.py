@@ -300,6 +300,22 @@ class Solver:
             c.check(st, "vg_multigrid_device")
         return cyc.value, r0.value, r1.value
 
+    def down(self, fine3, coarse, coarse3):
+        """Full-weighting restriction of a field on this grid to `coarse` (DownSampleInto)."""
+        c = self.ctx
+        with _Ordered(self.stream):
+            c.check(lib().vg_downsample_device(c.h, ctypes.byref(self.grid), ctypes.c_void_p(fine3.data_ptr()),
+                                               ctypes.byref(coarse), 0, ctypes.c_void_p(coarse3.data_ptr())),
+                    "vg_downsample_device")
+
+    def up(self, coarse, coarse3, fine3):
+        """Trilinear prolongation of a field on `coarse` to this grid's interior points (UpSampleFrom)."""
+        c = self.ctx
+        with _Ordered(self.stream):
+            c.check(lib().vg_upsample_device(c.h, ctypes.byref(coarse), ctypes.c_void_p(coarse3.data_ptr()),
+                                             ctypes.byref(self.grid), 1, ctypes.c_void_p(fine3.data_ptr())),
+                    "vg_upsample_device")
+
     def direct(self, ps, w, q, out):
         """Direct-sum velocity of the vortons at q (float4 rows) into out."""
         c = self.ctx
@@ -424,6 +440,13 @@ def _evaluate(torch, stream, weights, fields, seed, device, log, dt):
     vp0 = torch.empty_like(rhs)
     vp = torch.empty_like(rhs)
     prev = torch.empty_like(rhs)
+    sol_full, solz, diff = torch.empty_like(rhs), torch.empty_like(rhs), torch.empty_like(rhs)
+    g = solver.grid
+    coarse = []
+    for name, div in (("coarse65", 2), ("coarse33", 4)):
+        pts_c = (int(g.num_points[0]) - 1) // div + 1
+        cg = GridGeom.make(list(g.min_corner), list(g.extent), [pts_c] * 3)
+        coarse.append((name, cg, torch.zeros(cg.capacity * 3, dtype=torch.float32, device="cuda")))
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     rows = []
 
@@ -453,6 +476,7 @@ def _evaluate(torch, stream, weights, fields, seed, device, log, dt):
             lambda: solver.multigrid(rhs, vp))
         sol = vp[interior].double()
         sol_norm = float(sol.norm())
+        sol_full.copy_(vp)
 
         def start_error(start):
             return float((start[interior].double() - sol).norm()) / sol_norm
@@ -462,6 +486,27 @@ def _evaluate(torch, stream, weights, fields, seed, device, log, dt):
         vp[bmask] = vp0[bmask]
         row["prev_err0"] = start_error(vp)
         (row["prev_cycles"], row["prev_relres0"], row["prev_relres"]), row["prev_ms"] = timed(
+            lambda: solver.multigrid(rhs, vp))
+        # ceilings of a warm start that predicts only the smooth part: the converged
+        # solution restricted to a coarse grid and prolonged back (what an exact coarse
+        # network could give), alone and on top of the previous frame
+        solz.copy_(sol_full)
+        for name, cg, cbuf in coarse:
+            vp.copy_(vp0)
+            solver.down(solz, cg, cbuf)
+            solver.up(cg, cbuf, vp)
+            row[name + "_err0"] = start_error(vp)
+            (row[name + "_cycles"], row[name + "_relres0"], _), row[name + "_ms"] = timed(
+                lambda: solver.multigrid(rhs, vp))
+        name, cg, cbuf = coarse[0]
+        diff.copy_(solz - prev)
+        solver.down(diff, cg, cbuf)
+        vp.zero_()
+        solver.up(cg, cbuf, vp)
+        vp += prev
+        vp[bmask] = vp0[bmask]
+        row["prev_coarse65_err0"] = start_error(vp)
+        (row["prev_coarse65_cycles"], row["prev_coarse65_relres0"], _), row["prev_coarse65_ms"] = timed(
             lambda: solver.multigrid(rhs, vp))
         vp.copy_(vp0)
         _, row["nn_guess_ms"] = timed(lambda: net.guess(solver.grid, rhs, vp))
@@ -494,7 +539,12 @@ def boundary_mask(torch, pts_axis):
 def summarise(rows):
     out = {"fields": len(rows)}
     for k in ("zero_cycles", "prev_cycles", "nn_cycles", "zero_ms", "prev_ms", "nn_guess_ms", "nn_mg_ms", "nn_ms",
-              "zero_relres0", "prev_relres0", "nn_relres0", "prev_err0", "nn_err0", "nn_vs_zero_solution"):
+              "zero_relres0", "prev_relres0", "nn_relres0", "prev_err0", "nn_err0", "nn_vs_zero_solution",
+              "coarse65_cycles", "coarse65_ms", "coarse65_relres0", "coarse65_err0",
+              "coarse33_cycles", "coarse33_ms", "coarse33_relres0", "coarse33_err0",
+              "prev_coarse65_cycles", "prev_coarse65_ms", "prev_coarse65_relres0", "prev_coarse65_err0"):
+        if not rows or k not in rows[0]:
+            continue
         v = [r[k] for r in rows]
         out[k] = float(np.median(v))
         out[k + "_mean"] = float(np.mean(v))
