@@ -636,6 +636,22 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
     graphs, max_nodes, total_nodes = B.graph_info()
     p_sims, p_teams, p_ctas, p_graph = B.solver_info()
     left = sum(B.outside(i) for i in range(len(B)))
+    # the alternative the autotuner weighed: the Poisson solves in one persistent
+    # cooperative launch per frame (teams of 16 CTAs), the rest in the branch graphs
+    persistent = None
+    if p_sims == 0:
+        B.set_solver(True, 16)
+        B.step(dt)
+        B.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(frames):
+            B.step(dt)
+        B.synchronize()
+        pers_ms = (time.perf_counter() - t0) / frames * 1e3
+        n_in, teams, ctas, _ = B.solver_info()
+        persistent = {"ms_per_frame": pers_ms, "simulations_in_launch": n_in, "teams": teams, "ctas_per_team": ctas,
+                      "vs_branch_graphs": pers_ms / graph_ms}
+        B.set_solver(False)
     cells = [int(e.grid.num_points[0]) - 1 for e in effects]
     nv = sum(e.n for e in effects)
     B.close()
@@ -648,6 +664,7 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
                           "persistent_solve": {"simulations": p_sims, "teams": p_teams, "ctas_per_team": p_ctas,
                                                "captured_as_graph": p_graph}},
             "graph_ms_per_frame": graph_ms, "sequential_ms_per_frame": seq_ms,
+            "persistent_solve_alternative": persistent,
             "speedup_vs_sequential": seq_ms / graph_ms,
             "graphs_per_frame": graphs, "graph_nodes_max": max_nodes, "graph_nodes_total": total_nodes,
             "effect_steps_per_s": n_sims / (graph_ms * 1e-3), "vorton_steps_per_s": nv / (graph_ms * 1e-3),
