@@ -402,6 +402,7 @@ def run_ours(args, world, rank, local):
         result["poisson"] = poisson_section(vg, torch, stream, local)
         result["treecode"] = treecode_section(vg, torch, stream, local)
         result["batched"] = batched_section(torch, local)
+        result["rows"] = rows_section(vg, torch, stream, local)
     print(json.dumps(result), flush=True)
 
 
@@ -674,6 +675,191 @@ def batched_section(torch, local, n_sims=256, frames=6, seq_frames=2, dt=1.0 / 6
             "timing": "host wall clock over the frames plus one synchronisation (graph launches are asynchronous)"}
 
 
+def body_record(shape, position, dims, hole=False, velocity=(0, 0, 0), angular_velocity=(0, 0, 0), rot=None,
+                temperature=300.0, conductivity=0.0):
+    """One rigid body in the library's 32-float layout (shape 0 sphere, 1 box)."""
+    b = np.zeros(32, np.float32)
+    b[0], b[1] = shape, 1.0 if hole else 0.0
+    b[2:5], b[5:8], b[8:11] = position, velocity, angular_velocity
+    b[11:20] = np.asarray(np.eye(3) if rot is None else rot, np.float32).ravel()
+    d = np.atleast_1d(np.asarray(dims, np.float32))
+    b[20:20 + len(d)] = d
+    b[23], b[24] = temperature, conductivity
+    return b
+
+
+def rows_cpu_baseline(L, pos, s, dens, w, g12, np3, bodies, amb, grav, dt):
+    """The reference's own code for the same operations on the host (single-threaded: these
+    functions are serial loops in the reference), each on the full workload or a stated sample."""
+    P = lambda a: a.ctypes.data_as(ctypes.c_void_p)  # noqa: E731
+    out = {}
+
+    def timed(fn):
+        t0 = time.perf_counter()
+        fn()
+        return (time.perf_counter() - t0) * 1e3
+    n = len(pos)
+    wc = w.copy()
+    out["baroclinic_ms"] = timed(lambda: L.vgref_baroclinic(P(pos), P(wc), P(s), P(dens), ctypes.c_size_t(n), P(g12),
+                                                            P(np3), P(grav), ctypes.c_float(amb), ctypes.c_float(dt)))
+    dg = np.zeros(int(np.prod(np3)), np.float32)
+    out["density_grid_ms"] = timed(lambda: L.vgref_density_grid(P(pos), P(s), P(dens), ctypes.c_size_t(n), P(g12),
+                                                                P(np3), ctypes.c_float(amb), P(dg)))
+    sdf = np.zeros_like(dg)
+    out["signed_distance_ms"] = timed(lambda: L.vgref_signed_distance(P(g12), P(np3), P(dg), ctypes.c_float(amb),
+                                                                      P(sdf)))
+    pp, vv, ww, dd = pos.copy(), np.zeros_like(pos), w.copy(), dens.copy()
+    o9 = np.zeros((len(bodies), 9), np.float32)
+    out["collide_vortons_ms"] = timed(lambda: L.vgref_collide_vortons(P(pp), P(vv), P(ww), P(s), P(dd),
+                                                                      ctypes.c_size_t(n), P(bodies), len(bodies),
+                                                                      ctypes.c_float(amb), ctypes.c_float(1.0), P(o9)))
+    hd = dens.copy()
+    out["heat_pse_ms"] = timed(lambda: L.vgref_heat_pse(P(pos), P(hd), P(s), ctypes.c_size_t(n), P(g12), P(np3),
+                                                        ctypes.c_float(1e-3), ctypes.c_float(amb),
+                                                        ctypes.c_float(dt)))
+    # tracer seeding on a 16^3-cell sample of the tracer grid (512,000 particles), scaled per particle
+    cells = 16
+    sg = np.array([-2.0, -2.0, -2.0, 2.0, 2.0, 2.0, 0.25, 0.25, 0.25, 4.0, 4.0, 4.0], np.float32)
+    snp = np.array([cells + 1] * 3, np.uint32)
+    cap = cells ** 3 * 125
+    ep, ed, es = np.zeros((cap, 3), np.float32), np.zeros(cap, np.float32), np.zeros(cap, np.float32)
+    cnt = ctypes.c_size_t()
+    t = timed(lambda: L.vgref_emit_grid(P(sg), P(snp), ctypes.c_uint(5), P(pos), P(s), P(dens), ctypes.c_size_t(0), 0,
+                                        ctypes.c_uint(1), P(ep), P(ed), P(es), ctypes.c_size_t(cap),
+                                        ctypes.byref(cnt)))
+    out["emit_ns_per_particle"] = t * 1e6 / cap
+    out["cores"] = int(os.environ.get("NUMBER_OF_PROCESSORS", "1"))
+    out["kind"] = "reference"
+    out["sample"] = ("the full workload per operation (262,144 vortons on 129^3, 3 bodies), the tracer seeding on "
+                     "512,000 particles; the reference's code with its own threading where it has any (the "
+                     "std::thread stand-in for TBB); particle records converted to the reference's Particle "
+                     "vectors inside the timed call")
+    return out
+
+
+def rows_section(vg, torch, stream, local):
+    """The operations around the step, at the multigrid workload's sizes (262,144 puff vortons on the
+    129^3 grid of [-2, 2]^3, 4,194,304 tracers): emitters, wind and age kill, heat PSE, the density
+    grid / gradient / baroclinic generation, signed distance and marching cubes, fluid-body
+    collisions with three bodies.  GPU time per call (CUDA events on the context's stream, median of
+    5 after 2 warm-ups), the bytes each call must move against the measured HBM peak, and the
+    reference's own code on the host cores beside them."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.puff(262144, seed=3)
+    n = len(pos)
+    dens = (1.0 + 0.2 * np.exp(-(pos.astype(np.float64) ** 2).sum(1) / 0.2)).astype(np.float32)
+    grid = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [129] * 3)
+    pts = grid.capacity
+    amb, dt = 1.0, 1.0 / 30.0
+    grav = np.array([0.0, -9.8, 0.0], np.float32)
+    c, sn = np.cos(0.3), np.sin(0.3)
+    rot = np.array([[c, -sn, 0], [sn, c, 0], [0, 0, 1]], np.float32)
+    bodies = np.stack([body_record(0, [0.2, 0, 0], [0.4], velocity=[0.5, 0, 0], angular_velocity=[0, 0, 1],
+                                   temperature=350, conductivity=0.5),
+                       body_record(1, [0, 0, 0], [3.6, 3.6, 3.2], hole=True, rot=rot, conductivity=0.1),
+                       body_record(1, [0.0, 0.5, 0.3], [0.3, 0.4, 0.5], velocity=[0, 0.2, 0],
+                                   angular_velocity=[0.3, 0, 0], rot=rot, temperature=320, conductivity=0.2)])
+    cfg = vg.default_config(device=local)
+    cfg.stream = stream.cuda_stream
+    ctx = vg.Context(cfg)
+    lib = vg.lib()
+    P = vg._ptr
+
+    def f4(a, wv=None):
+        o = np.zeros((len(a), 4), np.float32)
+        o[:, :3] = a
+        if wv is not None:
+            o[:, 3] = wv
+        return torch.from_numpy(o).cuda()
+    ps0, w0, d0 = f4(pos, s), f4(w), torch.from_numpy(dens).cuda()
+    ps, ww, dd, vel = ps0.clone(), w0.clone(), d0.clone(), torch.zeros_like(ps0)
+    dg = torch.zeros(pts, dtype=torch.float32, device="cuda")
+    gr = torch.zeros(pts * 3, dtype=torch.float32, device="cuda")
+    sdf = torch.zeros(pts, dtype=torch.float32, device="cuda")
+    m_tr = N_TRACERS_POISSON
+    tr0 = f4(np.random.default_rng(6).uniform(-1.9, 1.9, (m_tr, 3)).astype(np.float32), 0.01)
+    trp, trv = tr0.clone(), torch.zeros_like(tr0)
+    birth0 = torch.randint(0, 100, (m_tr,), dtype=torch.int32, device="cuda")
+    birth = birth0.clone()
+    applied = ctypes.c_int()
+    out9 = np.zeros((len(bodies), 9), np.float32)
+    hits = np.zeros(len(bodies), np.uint64)
+    out6 = np.zeros((len(bodies), 6), np.float32)
+    tris = ctypes.c_size_t()
+    cap_tris = 4 * pts
+    verts = torch.empty(cap_tris * 9, dtype=torch.float32, device="cuda")
+
+    def timed(fn, reset=None, reps=5):
+        ms = []
+        with torch.cuda.stream(stream):
+            for k in range(reps + 2):
+                if reset:
+                    reset()
+                a, b = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+                a.record(stream)
+                fn()
+                b.record(stream)
+                torch.cuda.synchronize()
+                if k >= 2:
+                    ms.append(a.elapsed_time(b))
+        return statistics.median(ms)
+    peaks = measured_peaks()
+    res = {}
+
+    def row(name, ms, nbytes, note):
+        gbs = nbytes / (ms * 1e-3) / 1e9
+        res[name] = {"ms": ms, "algorithmic_bytes": nbytes, "achieved_gbs": gbs, "frac_of_hbm": gbs / peaks["hbm_gbs"],
+                     "bytes_basis": note}
+    g = ctypes.byref(grid)
+    # tracer seeding: 32^3 cells x 5^3 = 4,096,000 tracers, counter-based jitter
+    tg = vg.GridGeom.make([-2.0] * 3, [4.0] * 3, [33] * 3)
+    grp = vg.ParticleGroup(32 ** 3 * 125)
+    row("emit_grid_4096000", timed(lambda: vg.PclOpEmit.Emit(ctx, grp, tg, 5, None, vg.JITTER_HASH, 1),
+                                   reset=lambda: setattr(grp, "count", 0)),
+        4096000 * 56, "pos_size, vel4, angvel4 (16 B each), density, birth (4 B each) written per tracer")
+    del grp
+    row("wind_4194304", timed(lambda: ctx.check(lib.vg_wind_device(ctx.h, P(trv), m_tr, P(np.array([1.0, 0, 0],
+        np.float32)), 0.125, 0.875), "wind")), m_tr * 32, "vel4 read and written")
+    alive = ctypes.c_size_t()
+    row("kill_age_4194304", timed(lambda: ctx.check(lib.vg_kill_age_device(ctx.h, P(trp), P(trv), None, P(birth), m_tr,
+        120, 60, ctypes.byref(alive)), "kill"), reset=lambda: (trp.copy_(tr0), birth.copy_(birth0))),
+        m_tr * 4 * 2, "birth read for the flags and the scan (the moves of removed slots not counted)")
+    row("heat_pse_262144", timed(lambda: ctx.check(lib.vg_heat_pse_device(ctx.h, g, P(ps0), P(dd), n, 1e-3, amb, dt),
+                                                   "heat"), reset=lambda: dd.copy_(d0)),
+        n * (16 + 4 + 4), "pos_size and density read, density written per vorton")
+    row("density_grid_129", timed(lambda: ctx.check(lib.vg_density_grid_device(ctx.h, g, P(ps0), P(d0), n, amb, P(dg)),
+                                                    "density")), n * 20 + pts * 4,
+        "pos_size and density read per vorton, one float written per point")
+    row("gradient_129", timed(lambda: ctx.check(lib.vg_gradient_device(ctx.h, g, P(dg), P(gr)), "gradient")),
+        pts * 16, "4 B read and 12 B written per point")
+    row("baroclinic_262144", timed(lambda: ctx.check(lib.vg_baroclinic_device(ctx.h, g, P(ps0), P(d0), P(ww), n,
+        P(grav), amb, dt, ctypes.byref(applied)), "baroclinic"), reset=lambda: ww.copy_(w0)),
+        n * 20 + pts * 20 + n * 32, "density grid, its gradient, then pos_size + angvel read and angvel written")
+    row("signed_distance_129", timed(lambda: ctx.check(lib.vg_signed_distance_device(ctx.h, g, P(dg), amb, 0, P(sdf)),
+                                                       "sdf")), pts * 8, "density read, distance written per point")
+    row("marching_cubes_129", timed(lambda: ctx.check(lib.vg_marching_cubes_device(ctx.h, g, P(sdf), 0.0, P(verts),
+        None, cap_tris, ctypes.byref(tris)), "mc")), pts * 4 * 2,
+        "the field read twice (count, emit); triangles written not counted")
+    res["marching_cubes_129"]["triangles"] = tris.value
+    bods = np.ascontiguousarray(bodies, np.float32)
+    row("collide_vortons_262144_3_bodies", timed(lambda: ctx.check(lib.vg_collide_vortons_device(ctx.h, P(bods),
+        len(bods), P(ps), P(vel), P(ww), P(dd), n, amb, 1.0, P(out9), P(hits)), "collide"),
+        reset=lambda: (ps.copy_(ps0), vel.zero_(), ww.copy_(w0), dd.copy_(d0))),
+        n * 3 * 2 * 52, "pos_size, vel4, angvel4, density read and written per vorton and body")
+    row("collide_tracers_4194304_3_bodies", timed(lambda: ctx.check(lib.vg_collide_tracers_device(ctx.h, P(bods),
+        len(bods), P(trp), P(trv), None, m_tr, P(out6)), "collide tracers"), reset=lambda: trp.copy_(tr0)),
+        m_tr * 3 * 2 * 32, "pos_size and vel4 read and written per tracer and body")
+    res["workload"] = ("262,144 puff vortons (density 1 + 0.2 exp(-r^2/0.2)) on 129^3 over [-2,2]^3; 4,194,304 "
+                       "tracers; three bodies (a moving, spinning, hot sphere, a rotated hole box holding the "
+                       "fluid, a rotated solid box); emitted tracers 32^3 cells x 5^3")
+    res["hbm_peak_gbs"] = peaks["hbm_gbs"]
+    L = reference_lib()
+    if L is not None:
+        g12, np3 = grid.as12(), np.array(grid.points, np.uint32)
+        res["cpu_baseline"] = rows_cpu_baseline(L, pos, s, dens, w, g12, np3, bods, amb, grav, dt)
+    return res
+
+
 MG_BYTES_PER_POINT_CYCLE = 250  # V(2,2) over the levels: smoothing, residual + restriction, prolongation + correction
 ADVECT_BYTES_PER_TRACER = 48     # float4 position read and written, float4 velocity written
 N_TRACERS_POISSON = 1 << 22
@@ -890,6 +1076,8 @@ def run_section(name):
         out = poisson_section(vg, torch, stream, 0)
     elif name == "treecode":
         out = treecode_section(vg, torch, stream, 0)
+    elif name == "rows":
+        out = rows_section(vg, torch, stream, 0)
     else:
         out = batched_section(torch, 0)
     print(json.dumps({"section": name, name: out}), flush=True)
@@ -903,7 +1091,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--cpu-seconds", type=float, default=3.0)
     ap.add_argument("--skip-poisson", action="store_true")
-    ap.add_argument("--section", choices=["poisson", "treecode", "batched"],
+    ap.add_argument("--section", choices=["poisson", "treecode", "batched", "rows"],
                     help="run one workload section alone and print its JSON (for profiling)")
     args = ap.parse_args()
     if args.section:

@@ -164,6 +164,14 @@ __device__ __forceinline__ V3 contact_point(const Body& b, V3 q, int idx, float 
 template <int K>
 __device__ void block_sums(double (&v)[K], double* __restrict__ out) {
   __shared__ double sh[kBodyThreads / 32][K];
+  // most blocks hold no particle in contact with the body: their sums are zero
+  bool any = false;
+#pragma unroll
+  for (int k = 0; k < K; ++k) any = any || v[k] != 0.0;
+  if (!__syncthreads_or(any)) {
+    if (threadIdx.x < K) out[K * blockIdx.x + threadIdx.x] = 0.0;
+    return;
+  }
   for (int o = 16; o > 0; o >>= 1)
 #pragma unroll
     for (int k = 0; k < K; ++k) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
@@ -182,13 +190,35 @@ __device__ void block_sums(double (&v)[K], double* __restrict__ out) {
   }
 }
 
+// The blocks' partial sums added in a fixed order by one CTA: thread t sums
+// the contiguous run of blocks [t c, (t + 1) c), then a tree over the threads
+// (halving strides) -- deterministic, and with enough loads in flight that a
+// launch over millions of particles is not held up by a serial chain.
+constexpr int kSumThreads = 256;
 template <int K>
-__global__ void k_sum_blocks(const double* __restrict__ part, int nb, double* __restrict__ out) {
-  const int k = threadIdx.x;
-  if (k >= K) return;
-  double s = 0.0;
-  for (int b = 0; b < nb; ++b) s += part[K * b + k];
-  out[k] = s;
+__global__ void __launch_bounds__(kSumThreads) k_sum_blocks(const double* __restrict__ part, int nb,
+                                                            double* __restrict__ out) {
+  __shared__ double sh[K][kSumThreads];
+  const int t = threadIdx.x;
+  const int per = (nb + kSumThreads - 1) / kSumThreads;
+  const int b0 = min(nb, t * per), b1 = min(nb, b0 + per);
+  double s[K];
+#pragma unroll
+  for (int k = 0; k < K; ++k) s[k] = 0.0;
+#pragma unroll 4
+  for (int b = b0; b < b1; ++b)
+#pragma unroll
+    for (int k = 0; k < K; ++k) s[k] += part[K * (size_t)b + k];
+#pragma unroll
+  for (int k = 0; k < K; ++k) sh[k][t] = s[k];
+  __syncthreads();
+  for (int h = kSumThreads / 2; h > 0; h >>= 1) {
+    if (t < h)
+#pragma unroll
+      for (int k = 0; k < K; ++k) sh[k][t] += sh[k][t + h];
+    __syncthreads();
+  }
+  if (t < K) out[t] = sh[t][0];
 }
 
 // One body's CollideVortonsSlice for one vorton per thread.  Partial sums per
@@ -440,7 +470,7 @@ vg_status vg_collide_vortons_device(vg_ctx* c, const float* bodies, int nb, floa
     k_collide_vortons<<<blocks, kBodyThreads, 0, c->stream>>>(B[k], (float4*)pos_size, (float4*)vel4,
                                                              (float4*)angvel4, density, (int)n, ambient_density,
                                                              specific_heat, part);
-    k_sum_blocks<6><<<1, 32, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
+    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
     c->launches += 2;
   }
   VG_CUDA(c, cudaGetLastError());
@@ -485,7 +515,7 @@ vg_status vg_collide_tracers_device(vg_ctx* c, const float* bodies, int nb, floa
   for (int k = 0; k < nb; ++k) {
     k_collide_tracers<<<blocks, kBodyThreads, 0, c->stream>>>(B[k], (float4*)pos_size, (float4*)vel4, density,
                                                              (int)n, part);
-    k_sum_blocks<6><<<1, 32, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
+    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
     c->launches += 2;
   }
   VG_CUDA(c, cudaGetLastError());

@@ -346,56 +346,100 @@ __global__ void k_sdf_immediate(Geom g, const float* __restrict__ dens, float am
 
 // One sweep of ComputeRemainingSDFFromImmediateSDF_Nearest over the tiles on
 // tile diagonal `diag` (forward: inc +1 on every axis; backward: -1).  A CTA
-// owns one kSdfTile^3 tile and walks its local diagonal planes in order.
-constexpr int kSdfTile = 8;
-constexpr int kSdfThreads = 128;
+// owns one kSdfTile^3 tile: it stages the tile and its three backward faces
+// (tiles of earlier diagonals, final for this sweep) in shared memory, walks
+// the tile's local diagonal planes there in order, and writes the tile back.
+// The points, their neighbours and the updates are those of the serial sweep,
+// in an order that respects every dependence, so the result is its own bit
+// for bit.
+constexpr int kSdfTile = 16;
+constexpr int kSdfThreads = kSdfTile * kSdfTile;  // one thread per (j, k) of a local diagonal plane
 __global__ void __launch_bounds__(kSdfThreads) k_sdf_sweep(Geom g, int diag, int backward, unsigned tiles_x,
                                                            float* __restrict__ sdf,
                                                            const unsigned char* __restrict__ pinned) {
   pdl_entry();
+  constexpr int T = kSdfTile, E = kSdfTile + 1;  // staged extent: the tile plus one backward layer
+  __shared__ float S[E * E * E];                 // S[(w + 1) E^2 + (v + 1) E + (u + 1)], u, v, w in [-1, T)
+  __shared__ unsigned char pin[T * T * T];
   const int ty = blockIdx.x, tz = blockIdx.y;
   const int tx = diag - ty - tz;
   if (tx < 0 || tx >= (int)tiles_x) return;
   const int nx = g.np[0], ny = g.np[1], nz = g.np[2];
   const long long sy = nx, sz = (long long)nx * ny;
-  const int inc = backward ? -1 : 1;
   // tile origin in sweep coordinates (distance from the sweep's first point)
-  const int ox = tx * kSdfTile, oy = ty * kSdfTile, oz = tz * kSdfTile;
-  for (int s = 0; s <= 3 * (kSdfTile - 1); ++s) {
+  const int ox = tx * T, oy = ty * T, oz = tz * T;
+  auto gidx = [&](int u, int v, int w) -> long long {
+    const int x = backward ? nx - 1 - u : u, y = backward ? ny - 1 - v : v, z = backward ? nz - 1 - w : w;
+    return x + sy * y + sz * z;
+  };
+  // stage: the tile (u, v, w in [0, T)) and the backward faces (one of u, v, w = -1, the others in
+  // [0, T)); a neighbour before the grid's first point reads FLT_MAX, as in the serial sweep
+  // all of a thread's loads are issued before any is stored, so the staging
+  // costs one memory latency rather than one per element
+  constexpr int kStage = (E * E * E + kSdfThreads - 1) / kSdfThreads;
+  float val[kStage];
+  unsigned char pv[kStage];
+#pragma unroll
+  for (int q = 0; q < kStage; ++q) {
+    const int t = threadIdx.x + q * kSdfThreads;
+    val[q] = FLT_MAX;
+    pv[q] = 0;
+    if (t >= E * E * E) continue;
+    const int lu = t % E - 1, lv = (t / E) % E - 1, lw = t / (E * E) - 1;
+    if ((lu < 0) + (lv < 0) + (lw < 0) > 1) continue;  // edges and corners of the backward layer are never read
+    const int u = ox + lu, v = oy + lv, w = oz + lw;
+    if (u >= 0 && v >= 0 && w >= 0 && u < nx && v < ny && w < nz) {
+      const long long o = gidx(u, v, w);
+      val[q] = sdf[o];
+      pv[q] = pinned[o];
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < kStage; ++q) {
+    const int t = threadIdx.x + q * kSdfThreads;
+    if (t >= E * E * E) continue;
+    S[t] = val[q];
+    const int lu = t % E - 1, lv = (t / E) % E - 1, lw = t / (E * E) - 1;
+    if (lu >= 0 && lv >= 0 && lw >= 0) pin[lu + T * (lv + T * lw)] = pv[q];
+  }
+  __syncthreads();
+  const int j = threadIdx.x % T, kk = threadIdx.x / T;
+  for (int s = 0; s <= 3 * (T - 1); ++s) {
     // points (i, j, k) of the tile with i + j + k = s
-    for (int t = threadIdx.x; t < kSdfTile * kSdfTile; t += kSdfThreads) {
-      const int j = t % kSdfTile, kk = t / kSdfTile, i = s - j - kk;
-      if (i < 0 || i >= kSdfTile) continue;
-      const int u = ox + i, v = oy + j, w = oz + kk;  // sweep coordinates
-      if (u >= nx || v >= ny || w >= nz) continue;
-      const int x = backward ? nx - 1 - u : u, y = backward ? ny - 1 - v : v, z = backward ? nz - 1 - w : w;
-      const long long o = x + sy * y + sz * z;
-      if (pinned[o]) continue;
-      const float sx = (u != 0) ? sdf[o - inc] : FLT_MAX;
-      const float syv = (v != 0) ? sdf[o - inc * sy] : FLT_MAX;
-      const float szv = (w != 0) ? sdf[o - inc * sz] : FLT_MAX;
-      const float ax = fabsf(sx), ay = fabsf(syv), az = fabsf(szv);
-      float nb, sp;
-      if (ax <= ay) {
-        if (ax <= az) {
-          nb = sx;
-          sp = g.cell[0];
+    const int i = s - j - kk;
+    if (i >= 0 && i < T) {
+      const int u = ox + i, v = oy + j, w = oz + kk;
+      if (u < nx && v < ny && w < nz && !pin[i + T * (j + T * kk)]) {
+        const int c = (kk + 1) * E * E + (j + 1) * E + (i + 1);
+        const float sx = S[c - 1], syv = S[c - E], szv = S[c - E * E];
+        const float ax = fabsf(sx), ay = fabsf(syv), az = fabsf(szv);
+        float nb, sp;
+        if (ax <= ay) {
+          if (ax <= az) {
+            nb = sx;
+            sp = g.cell[0];
+          } else {
+            nb = szv;
+            sp = g.cell[2];
+          }
+        } else if (ay <= az) {
+          nb = syv;
+          sp = g.cell[1];
         } else {
           nb = szv;
           sp = g.cell[2];
         }
-      } else if (ay <= az) {
-        nb = syv;
-        sp = g.cell[1];
-      } else {
-        nb = szv;
-        sp = g.cell[2];
+        float here = S[c];
+        update_sdf(here, __fadd_rn(nb, copysignf(sp, nb)));
+        S[c] = here;
       }
-      float here = sdf[o];
-      update_sdf(here, __fadd_rn(nb, copysignf(sp, nb)));
-      sdf[o] = here;
     }
     __syncthreads();
+  }
+  for (int t = threadIdx.x; t < T * T * T; t += kSdfThreads) {
+    const int li = t % T, lj = (t / T) % T, lk = t / (T * T);
+    const int u = ox + li, v = oy + lj, w = oz + lk;
+    if (u < nx && v < ny && w < nz && !pin[t]) sdf[gidx(u, v, w)] = S[(lk + 1) * E * E + (lj + 1) * E + (li + 1)];
   }
 }
 
