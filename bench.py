@@ -373,13 +373,15 @@ def run_ours(args, world, rank, local):
     trr = trr_t.numpy().view(vg.PARTICLE_DTYPE)
     trr0 = vg.make_particles(tr)
     host = vg.VortonSim(cfg=cfg)
+    rf = recs.view(np.float32).reshape(-1, 24)  # the records' float words (position 0-2, velocity 3-5)
     e2e_ms = []
     for k in range(args.warmup + args.steps):
         recs[...] = recs0
         trr[...] = trr0
         t0 = time.perf_counter()
         host.Update(recs, float(DT), k)
-        recs["position"] += recs["velocity"] * DT  # PclOpEvolve on the host records (vortons)
+        for j in range(3):  # PclOpEvolve on the host records (vortons): position += velocity dt, per axis
+            rf[:, j] += rf[:, 3 + j] * DT
         host.Advect(trr, float(DT))
         t1 = time.perf_counter()
         if k >= args.warmup:

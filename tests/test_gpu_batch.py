@@ -93,10 +93,11 @@ def test_solver_settings_give_identical_frames(mod, persistent, team):
 
 
 def test_long_branch_splits_into_bounded_graphs(mod):
-    """Twenty-four simulations on one branch (~6,500 graph nodes a frame) are
-    captured as more than one graph, each of bounded size, and still replay
-    exactly the sequential frames."""
-    ef = effects(mod, range(31, 55))
+    """Forty simulations on one branch (~5,300 graph nodes a frame, over
+    the 3,072 kernels at which a graph ends) are captured as more than one
+    graph, each of bounded size, and still replay exactly the sequential
+    frames."""
+    ef = effects(mod, range(31, 71))
     A, B = mod.Batch(ef, streams=1), mod.Batch(ef, streams=1)
     A.calibrate(DT)
     B.calibrate(DT)

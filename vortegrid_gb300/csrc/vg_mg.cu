@@ -860,42 +860,69 @@ __global__ void __launch_bounds__(256) k_dst_pass(unsigned N, const T* __restric
   out[i] = Dinv ? acc * __ldg(Dinv + p) : acc;
 }
 
-// The first x pass reading r in full layout (the gather folded in): the same
-// sums as k_dst_gather followed by k_dst_pass along x.
+constexpr unsigned kDstThreads = 1024;  // threads of the plane and column kernels
+
+// The x and y passes of one (z, component) plane of the interior in shared
+// memory, reading r in full layout: the same sums in the same order as
+// k_dst_gather followed by k_dst_pass along x and along y.  A CTA per plane;
+// dynamic shared memory: two planes of nxi x nyi values and the x table
+// transposed (so that a warp's threads, on consecutive k, read consecutive
+// words).
 template <typename T>
-__global__ void __launch_bounds__(256) k_dst_first(Geom g, const float* __restrict__ rfull, T* __restrict__ out,
-                                                   const T* __restrict__ Sx) {
+__global__ void __launch_bounds__(kDstThreads) k_dst_xy(Geom g, const float* __restrict__ rfull, T* __restrict__ out,
+                                                        const T* __restrict__ Sx, const T* __restrict__ Sy) {
   pdl_entry();
-  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, N = nxi * nyi * (g.np[2] - 2);
-  const unsigned i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= 3 * N) return;
-  const unsigned c = i % 3u, p = i / 3u;
-  const unsigned k = p % nxi, q = p / nxi, y = q % nyi, z = q / nyi;
-  const unsigned row = 3 * (1 + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c;  // r at (1, y + 1, z + 1)
-  T acc = 0;
-  for (unsigned m = 0; m < nxi; ++m) acc = fma_t(__ldg(Sx + k * nxi + m), (T)rfull[row + 3 * m], acc);
-  out[i] = acc;
+  extern __shared__ __align__(16) unsigned char plane_raw[];
+  const unsigned nxi = g.np[0] - 2, nyi = g.np[1] - 2, np = nxi * nyi;
+  T* a = reinterpret_cast<T*>(plane_raw);  // [y][m]: r
+  T* b = a + np;                            // [y][k]: after the x pass
+  T* sxt = b + np;                          // [m][k]: Sx transposed
+  const unsigned z = blockIdx.x, c = blockIdx.y;
+  for (unsigned it = threadIdx.x; it < np; it += blockDim.x) {
+    const unsigned x = it % nxi, y = it / nxi;
+    a[it] = (T)rfull[3 * ((x + 1) + g.np[0] * ((y + 1) + g.np[1] * (z + 1))) + c];
+  }
+  for (unsigned it = threadIdx.x; it < nxi * nxi; it += blockDim.x) sxt[(it % nxi) * nxi + it / nxi] = __ldg(Sx + it);
+  __syncthreads();
+  for (unsigned it = threadIdx.x; it < np; it += blockDim.x) {
+    const unsigned k = it % nxi, y = it / nxi;
+    T acc = 0;
+    for (unsigned m = 0; m < nxi; ++m) acc = fma_t(sxt[m * nxi + k], a[y * nxi + m], acc);
+    b[it] = acc;
+  }
+  __syncthreads();
+  for (unsigned it = threadIdx.x; it < np; it += blockDim.x) {
+    const unsigned x = it % nxi, k = it / nxi;
+    T acc = 0;
+    for (unsigned m = 0; m < nyi; ++m) acc = fma_t(__ldg(Sy + k * nyi + m), b[m * nxi + x], acc);
+    out[3 * (it + np * z) + c] = acc;
+  }
 }
 
 // The two z passes around the eigenvalue scaling, fused: a CTA owns whole z
-// columns (32 x's, one y, one component), keeps the first pass's results in
-// shared memory and runs the second from there -- the same sums as two
-// k_dst_pass launches.  Dynamic shared memory: nzi x 32 values.
-constexpr unsigned kZZMaxN = 384;
+// columns (32 x's, one y, one component), stages them in shared memory, keeps
+// the first pass's results there and runs the second from them -- the same
+// sums as two k_dst_pass launches.  Dynamic shared memory: 2 nzi x 32 values.
 template <typename T>
-__global__ void __launch_bounds__(256) k_dst_zz(unsigned nxi, unsigned nyi, unsigned nzi, const T* __restrict__ in,
+__global__ void __launch_bounds__(kDstThreads) k_dst_zz(unsigned nxi, unsigned nyi, unsigned nzi, const T* __restrict__ in,
                                                 T* __restrict__ out, const T* __restrict__ Sz,
                                                 const T* __restrict__ Dinv) {
   pdl_entry();
-  extern __shared__ __align__(8) unsigned char col_raw[];
-  T* col = reinterpret_cast<T*>(col_raw);  // [z][x - x0]
+  extern __shared__ __align__(16) unsigned char col_raw[];
+  T* src = reinterpret_cast<T*>(col_raw);  // [m][x - x0]: the input columns
+  T* col = src + nzi * 32;                  // [z][x - x0]: after the scaled first pass
   const unsigned x0 = blockIdx.x * 32, y = blockIdx.y, c = blockIdx.z, st = nxi * nyi;
+  for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
+    const unsigned xl = it % 32, m = it / 32, x = x0 + xl;
+    if (x < nxi) src[it] = in[3 * (x + nxi * y + m * st) + c];
+  }
+  __syncthreads();
   for (unsigned it = threadIdx.x; it < nzi * 32; it += blockDim.x) {
     const unsigned xl = it % 32, z = it / 32, x = x0 + xl;
     if (x >= nxi) continue;
     const unsigned p0 = x + nxi * y;
     T acc = 0;
-    for (unsigned m = 0; m < nzi; ++m) acc = fma_t(__ldg(Sz + z * nzi + m), in[3 * (p0 + m * st) + c], acc);
+    for (unsigned m = 0; m < nzi; ++m) acc = fma_t(__ldg(Sz + z * nzi + m), src[m * 32 + xl], acc);
     col[z * 32 + xl] = acc * __ldg(Dinv + p0 + z * st);
   }
   __syncthreads();
@@ -905,6 +932,48 @@ __global__ void __launch_bounds__(256) k_dst_zz(unsigned nxi, unsigned nyi, unsi
     T acc = 0;
     for (unsigned m = 0; m < nzi; ++m) acc = fma_t(__ldg(Sz + z * nzi + m), col[m * 32 + xl], acc);
     out[3 * (x + nxi * y + z * st) + c] = acc;
+  }
+}
+
+// The inverse y and x passes of one (z, component) plane, writing e in full
+// layout (zero on the boundary, whole boundary planes included): the same
+// sums as k_dst_pass along y followed by k_dst_scatter.  A CTA per plane of
+// the full grid; dynamic shared memory: two planes of nxi x nyi values and
+// the x table transposed.
+template <typename T>
+__global__ void __launch_bounds__(kDstThreads) k_dst_yx(Geom g, const T* __restrict__ in, const T* __restrict__ Sx,
+                                                        const T* __restrict__ Sy, float* __restrict__ efull) {
+  pdl_entry();
+  extern __shared__ __align__(16) unsigned char plane_raw[];
+  const unsigned nx = g.np[0], ny = g.np[1], nxi = nx - 2, nyi = ny - 2, np = nxi * nyi;
+  const unsigned z = blockIdx.x, c = blockIdx.y;
+  float* ep = efull + 3 * (size_t)nx * ny * z + c;
+  if (z == 0 || z + 1 >= g.np[2]) {
+    for (unsigned it = threadIdx.x; it < nx * ny; it += blockDim.x) ep[3 * it] = 0.f;
+    return;
+  }
+  T* a = reinterpret_cast<T*>(plane_raw);  // [m][x]: the plane
+  T* b = a + np;                            // [y][x]: after the y pass
+  T* sxt = b + np;                          // [m][k]: Sx transposed
+  const unsigned zi = z - 1;
+  for (unsigned it = threadIdx.x; it < np; it += blockDim.x) a[it] = in[3 * (it + np * zi) + c];
+  for (unsigned it = threadIdx.x; it < nxi * nxi; it += blockDim.x) sxt[(it % nxi) * nxi + it / nxi] = __ldg(Sx + it);
+  __syncthreads();
+  for (unsigned it = threadIdx.x; it < np; it += blockDim.x) {
+    const unsigned x = it % nxi, k = it / nxi;
+    T acc = 0;
+    for (unsigned m = 0; m < nyi; ++m) acc = fma_t(__ldg(Sy + k * nyi + m), a[m * nxi + x], acc);
+    b[it] = acc;
+  }
+  __syncthreads();
+  for (unsigned it = threadIdx.x; it < nx * ny; it += blockDim.x) {
+    const unsigned x = it % nx, y = it / nx;
+    T v = 0;
+    if (x > 0 && y > 0 && x + 1 < nx && y + 1 < ny) {
+      const unsigned kx = x - 1, row = nxi * (y - 1);
+      for (unsigned m = 0; m < nxi; ++m) v = fma_t(sxt[m * nxi + kx], b[row + m], v);
+    }
+    ep[3 * it] = (float)v;
   }
 }
 
@@ -924,6 +993,10 @@ __global__ void __launch_bounds__(256) k_dst_scatter(Geom g, const T* __restrict
   }
   efull[i] = (float)v;
 }
+
+// Shared memory of the plane and column kernels above (their attribute is
+// raised to this once); larger coarsest levels take the pass-per-axis form.
+constexpr size_t kDstSmemMax = 96 * 1024;
 
 struct MgPlan {
   int nlev;
@@ -1040,14 +1113,16 @@ static vg_status enqueue_vcycle(Ctx* c, const MgPlan& P, const MgBufs& B, unsign
       const T* Sy = Sx + nxi * nxi;
       const T* Sz = Sy + nyi * nyi;
       const T* Dinv = Sz + nzi * nzi;
-      if (nzi <= kZZMaxN) {
-        // x pass from r (full layout) -> X, y -> Y, z (scaled) z -> X, y -> Y, x -> e (full)
-        pdl_launch(c->stream, nb, 256, 0, k_dst_first<T>, g, (const float*)R, X, Sx);
-        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sy, nyi, nxi, (const T*)nullptr);
-        pdl_launch(c->stream, dim3((nxi + 31) / 32, nyi, 3), 256, (size_t)nzi * 32 * sizeof(T), k_dst_zz<T>, nxi, nyi,
-                   nzi, (const T*)Y, X, Sz, Dinv);
-        pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sy, nyi, nxi, (const T*)nullptr);
-        *nl += 4;
+      const size_t plane_smem = (2 * (size_t)nxi * nyi + (size_t)nxi * nxi) * sizeof(T);
+      const size_t col_smem = 2 * (size_t)nzi * 32 * sizeof(T);
+      if (plane_smem <= kDstSmemMax && col_smem <= kDstSmemMax) {
+        // x and y passes per plane from r (full layout) -> X, z (scaled) z -> Y, y and x per plane -> e (full)
+        pdl_launch(c->stream, dim3(nzi, 3), kDstThreads, plane_smem, k_dst_xy<T>, g, (const float*)R, X, Sx, Sy);
+        pdl_launch(c->stream, dim3((nxi + 31) / 32, nyi, 3), kDstThreads, col_smem, k_dst_zz<T>, nxi, nyi, nzi,
+                   (const T*)X, Y, Sz, Dinv);
+        pdl_launch(c->stream, dim3(g.np[2], 3), kDstThreads, plane_smem, k_dst_yx<T>, g, (const T*)Y, Sx, Sy, E);
+        *nl += 3;
+        return;
       } else {
         pdl_launch(c->stream, nb, 256, 0, k_dst_gather<T>, g, (const float*)R, X);
         pdl_launch(c->stream, nb, 256, 0, k_dst_pass<T>, N, (const T*)X, Y, Sx, nxi, 1u, (const T*)nullptr);
@@ -1303,6 +1378,12 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
   static bool smem_set = false;
   if (!smem_set) {
     cudaFuncSetAttribute(k_vcycle_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
+    cudaFuncSetAttribute(k_dst_xy<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
+    cudaFuncSetAttribute(k_dst_xy<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
+    cudaFuncSetAttribute(k_dst_zz<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
+    cudaFuncSetAttribute(k_dst_zz<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
+    cudaFuncSetAttribute(k_dst_yx<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
+    cudaFuncSetAttribute(k_dst_yx<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
     smem_set = true;
   }
   return VG_OK;
