@@ -281,14 +281,38 @@ __device__ float3 tree_walk_fast(const TreeParams& T, const float4* __restrict__
       }
     }
     const bool any = on[0] && on[1] && on[2];
-    for (unsigned iz = 0; iz < cn[2]; ++iz)
-      for (unsigned iy = 0; iy < cn[1]; ++iy)
-        for (unsigned ix = 0; ix < cn[0]; ++ix) {
-          const unsigned chx = c0[0] + ix, chy = c0[1] + iy, chz = c0[2] + iz;
-          if (any && chx - o0[0] < on[0] && chy - o0[1] < on[1] && chz - o0[2] < on[2]) continue;  // opened
-          const size_t o = T.base[L - 1] + chx + (size_t)C.np[0] * (chy + (size_t)C.np[1] * chz);
-          prep_accum<KIND>(acc, qx, qy, qz, tp[o], tw[o]);
+    // the layer's cells (fewer than 2^32 in a layer); a row's cells are
+    // consecutive, visited up to 4 at a time with their loads issued
+    // together; an opened cell's term is computed and dropped (acc kept)
+    const float4* __restrict__ lp = tp + T.base[L - 1];
+    const float4* __restrict__ lw = tw + T.base[L - 1];
+    const unsigned sy = C.np[0], sz = C.np[0] * C.np[1];
+    for (unsigned iz = 0; iz < cn[2]; ++iz) {
+      const unsigned chz = c0[2] + iz;
+      const bool oz = any && chz - o0[2] < on[2];
+      for (unsigned iy = 0; iy < cn[1]; ++iy) {
+        const unsigned chy = c0[1] + iy;
+        const bool oyz = oz && chy - o0[1] < on[1];
+        const unsigned row = c0[0] + sy * chy + sz * chz;
+        for (unsigned ix0 = 0; ix0 < cn[0]; ix0 += 4) {
+          float4 cp[4], cw[4];
+#pragma unroll
+          for (unsigned u = 0; u < 4; ++u)
+            if (ix0 + u < cn[0]) {
+              cp[u] = lp[row + ix0 + u];
+              cw[u] = lw[row + ix0 + u];
+            }
+#pragma unroll
+          for (unsigned u = 0; u < 4; ++u) {
+            const unsigned ix = ix0 + u;
+            if (ix >= cn[0]) break;
+            float3 next = acc;
+            prep_accum<KIND>(next, qx, qy, qz, cp[u], cw[u]);
+            if (!(oyz && c0[0] + ix - o0[0] < on[0])) acc = next;
+          }
         }
+      }
+    }
     if (!any) break;
 #pragma unroll
     for (int a = 0; a < 3; ++a) {
