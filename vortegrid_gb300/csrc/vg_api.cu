@@ -473,14 +473,14 @@ static vg_status step_back(Ctx* c, StepState& s) {
     float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), (pts + n) * 2 * sizeof(float4)), &st);
     if (st != VG_OK) return st;
     if ((st = launch_jacobian(c, g, s.velgrid, jac)) != VG_OK) return st;
-    if ((st = launch_stretch(c, g, jac, s.ps, s.w, n, s.dt)) != VG_OK) return st;
+    if ((st = launch_stretch(c, g, jac, s.ps, s.w, n, s.dt, s.cl.items)) != VG_OK) return st;
   }
   if (c->cfg.enable_diffusion) {
     if ((st = launch_pse(c, g, s.cl, s.ps, s.w, n, c->cfg.viscosity, s.dt)) != VG_OK) return st;
   }
   if (tech != VG_VELOCITY_DIRECT) {
     // AssignVelocityFromField(vortons, mVelGrid, 1) (vortonSim.cpp:4251-4255)
-    if ((st = launch_gather_advect(c, g, s.velgrid, s.ps, s.vel, n, 0.0f, false)) != VG_OK) return st;
+    if ((st = launch_gather_advect(c, g, s.velgrid, s.ps, s.vel, n, 0.0f, false, s.cl.items)) != VG_OK) return st;
   }
   VG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   c->stats_pending = true;

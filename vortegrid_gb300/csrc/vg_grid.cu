@@ -177,11 +177,16 @@ __global__ void k_curl(Geom g, float rsx, float rsy, float rsz, const float* __r
   curl[3 * c + 2] = __fsub_rn(J[0][1], J[1][0]);
 }
 
+// order (optional): the vortons grouped by cell, so that a warp's vortons
+// interpolate from the same few cells' corners (each vorton's update is the
+// same whichever thread runs it).
 __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* __restrict__ ps,
-                          float4* __restrict__ w, int n, float dt, int* __restrict__ flag) {
+                          float4* __restrict__ w, int n, float dt, const unsigned* __restrict__ order,
+                          int* __restrict__ flag) {
   pdl_entry();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = order ? (int)order[t] : t;
   const float4 p = ps[i];
   if (!inside_cells(g, p.x, p.y, p.z)) {
     atomicOr(flag, (int)DF_OUT_OF_GRID);
@@ -343,11 +348,14 @@ __global__ void __launch_bounds__(128) k_heat_pse(Geom g, const float4* __restri
   d[i] = v;
 }
 
+// order (optional): the particles grouped by cell, as in k_stretch.
 __global__ void k_gather_advect(Geom g, const float* __restrict__ vel3, float4* __restrict__ pos,
-                                float4* __restrict__ vel, int m, float dt, int evolve, int* __restrict__ flag) {
+                                float4* __restrict__ vel, int m, float dt, int evolve,
+                                const unsigned* __restrict__ order, int* __restrict__ flag) {
   pdl_entry();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= m) return;
+  const int i = order ? (int)order[t] : t;
   float4 p = pos[i];
   if (!inside_cells(g, p.x, p.y, p.z)) {
     atomicOr(flag, (int)DF_OUT_OF_GRID);
@@ -514,10 +522,11 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3) {
   return VG_OK;
 }
 
-vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt) {
+vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt,
+                         const unsigned* order) {
   if (0.0f == g.ext[0] || 0.0f == g.ext[1] || 0.0f == g.ext[2]) return VG_OK;  // 2D: no stretching
   if (n == 0) return VG_OK;
-  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_stretch, g, jac9, ps, w, (int)n, dt, outside_flag(c));
+  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_stretch, g, jac9, ps, w, (int)n, dt, order, outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;
@@ -553,10 +562,10 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
 }
 
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m, float dt,
-                               bool evolve) {
+                               bool evolve, const unsigned* order) {
   if (m == 0) return VG_OK;
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "advect: more than 2^31 particles");
-  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect, g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0,
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect, g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0, order,
                                                               outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());

@@ -430,13 +430,15 @@ void mg_batch_destroy(MgBatch* mb);
 
 vg_status launch_jacobian(Ctx* c, const Geom& g, const float* v3, float* jac9);
 vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);
-vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt);
+// order: NULL, or the vortons' indices grouped by cell (the cell lists' items)
+vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt,
+                         const unsigned* order = nullptr);
 vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float4* w, size_t n, float nu,
                      float dt);
 vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float* density, size_t n,
                           float kappa, float ambient, float dt);
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
-                               float dt, bool evolve);
+                               float dt, bool evolve, const unsigned* order = nullptr);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
 // Density grid (PopulateDensityAndMassFractionGrids), gradient (ComputeGradient),
 // baroclinic generation and the signed distance grid (vg_surface.cu).
