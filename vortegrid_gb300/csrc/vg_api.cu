@@ -470,10 +470,7 @@ static vg_status step_back(Ctx* c, StepState& s) {
     if ((st = launch_curl(c, g, s.vecpot, s.velgrid)) != VG_OK) return st;
   }
   if (c->cfg.enable_stretch) {
-    float* jac = (float*)ws(c, S_JAC, std::max(pts * 9 * sizeof(float), (pts + n) * 2 * sizeof(float4)), &st);
-    if (st != VG_OK) return st;
-    if ((st = launch_jacobian(c, g, s.velgrid, jac)) != VG_OK) return st;
-    if ((st = launch_stretch(c, g, jac, s.ps, s.w, n, s.dt, s.cl.items)) != VG_OK) return st;
+    if ((st = launch_stretch_vel(c, g, s.velgrid, s.ps, s.w, n, s.dt, s.cl.items)) != VG_OK) return st;
   }
   if (c->cfg.enable_diffusion) {
     if ((st = launch_pse(c, g, s.cl, s.ps, s.w, n, c->cfg.viscosity, s.dt)) != VG_OK) return st;

@@ -204,6 +204,69 @@ __global__ void k_stretch(Geom g, const float* __restrict__ jac, const float4* _
   w[i] = a;
 }
 
+// k_jacobian and k_stretch fused: the velocity Jacobian is formed at the 8
+// corners of each vorton's cell from the velocity grid (the differences of
+// k_jacobian at those grid points) and interpolated as interp<9> would from
+// the Jacobian grid, so the 9-float-per-point grid is never written.  Same
+// float operations on the same values as the two kernels; order as k_stretch.
+__global__ void k_stretch_vel(Geom g, float rsx, float rsy, float rsz, const float* __restrict__ v,
+                              const float4* __restrict__ ps, float4* __restrict__ w, int n, float dt,
+                              const unsigned* __restrict__ order, int* __restrict__ flag) {
+  pdl_entry();
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= n) return;
+  const int i = order ? (int)order[t] : t;
+  const float4 p = ps[i];
+  if (!inside_cells(g, p.x, p.y, p.z)) {
+    atomicOr(flag, (int)DF_OUT_OF_GRID);
+    return;
+  }
+  const float pp[3] = {p.x, p.y, p.z};
+  unsigned idx[3];
+  float tw[3], om[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    idx[a] = bin_axis(pp[a], g.mn[a], g.cpe[a]);
+    const float cmin = __fadd_rn(g.mn[a], __fmul_rn((float)idx[a], g.cell[a]));
+    tw[a] = __fmul_rn(__fsub_rn(pp[a], cmin), g.cpe[a]);
+    om[a] = __fsub_rn(1.0f, tw[a]);
+  }
+  const unsigned nx = g.np[0], ny = g.np[1];
+  const size_t stride[3] = {1, nx, (size_t)nx * ny};
+  const float rs[3] = {rsx, rsy, rsz};
+  float J[9];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    const float hrs = __fmul_rn(0.5f, rs[a]);
+#pragma unroll
+    for (int b = 0; b < 3; ++b) {
+      float cv[8];  // corners (dx, dy, dz), x fastest: v000, v100, v010, v110, v001, v101, v011, v111
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const unsigned ci[3] = {idx[0] + (q & 1), idx[1] + ((q >> 1) & 1), idx[2] + (q >> 2)};
+        const size_t c = ci[0] + (size_t)nx * (ci[1] + (size_t)ny * ci[2]);
+        size_t hi, lo;
+        float f;
+        diff_axis(c, ci[a], g.np[a], stride[a], rs[a], hrs, hi, lo, f);
+        cv[q] = __fmul_rn(__fsub_rn(v[3 * hi + b], v[3 * lo + b]), f);
+      }
+      const float y0 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], cv[0]), __fmul_rn(tw[0], cv[1])), om[1]),
+                                 __fmul_rn(__fadd_rn(__fmul_rn(om[0], cv[2]), __fmul_rn(tw[0], cv[3])), tw[1]));
+      const float y1 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], cv[4]), __fmul_rn(tw[0], cv[5])), om[1]),
+                                 __fmul_rn(__fadd_rn(__fmul_rn(om[0], cv[6]), __fmul_rn(tw[0], cv[7])), tw[1]));
+      J[3 * a + b] = __fadd_rn(__fmul_rn(y0, om[2]), __fmul_rn(y1, tw[2]));
+    }
+  }
+  float4 wa = w[i];
+  const float s0 = __fadd_rn(__fadd_rn(__fmul_rn(J[0], wa.x), __fmul_rn(J[1], wa.y)), __fmul_rn(J[2], wa.z));
+  const float s1 = __fadd_rn(__fadd_rn(__fmul_rn(J[3], wa.x), __fmul_rn(J[4], wa.y)), __fmul_rn(J[5], wa.z));
+  const float s2 = __fadd_rn(__fadd_rn(__fmul_rn(J[6], wa.x), __fmul_rn(J[7], wa.y)), __fmul_rn(J[8], wa.z));
+  wa.x = __fadd_rn(wa.x, __fmul_rn(__fmul_rn(0.5f, s0), dt));
+  wa.y = __fadd_rn(wa.y, __fmul_rn(__fmul_rn(0.5f, s1), dt));
+  wa.z = __fadd_rn(wa.z, __fmul_rn(__fmul_rn(0.5f, s2), dt));
+  w[i] = wa;
+}
+
 // Order-independent PSE: vorton i exchanges with every vorton of the pair set
 // the reference visits (same cell, or cells offset by {0,1}^3 either way with
 // the lower cell strictly inside the point range), using pre-step values.
@@ -517,6 +580,19 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3) {
   float rs[3];
   recip_spacing(g, rs);
   pdl_launch(c->stream, blocks_for(g.points(), 128), 128, 0, k_curl, g, rs[0], rs[1], rs[2], v3, curl3);
+  VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
+vg_status launch_stretch_vel(Ctx* c, const Geom& g, const float* v3, const float4* ps, float4* w, size_t n, float dt,
+                             const unsigned* order) {
+  if (0.0f == g.ext[0] || 0.0f == g.ext[1] || 0.0f == g.ext[2]) return VG_OK;  // 2D: no stretching
+  if (n == 0) return VG_OK;
+  float rs[3];
+  recip_spacing(g, rs);
+  pdl_launch(c->stream, blocks_for(n, 128), 128, 0, k_stretch_vel, g, rs[0], rs[1], rs[2], v3, ps, w, (int)n, dt, order,
+             outside_flag(c));
   VG_LAUNCHED(c);
   VG_CUDA(c, cudaGetLastError());
   return VG_OK;

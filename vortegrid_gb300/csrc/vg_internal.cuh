@@ -433,6 +433,9 @@ vg_status launch_curl(Ctx* c, const Geom& g, const float* v3, float* curl3);
 // order: NULL, or the vortons' indices grouped by cell (the cell lists' items)
 vg_status launch_stretch(Ctx* c, const Geom& g, const float* jac9, const float4* ps, float4* w, size_t n, float dt,
                          const unsigned* order = nullptr);
+// The same stretch from the velocity grid (the Jacobian formed at each vorton's cell corners).
+vg_status launch_stretch_vel(Ctx* c, const Geom& g, const float* v3, const float4* ps, float4* w, size_t n, float dt,
+                             const unsigned* order = nullptr);
 vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float4* w, size_t n, float nu,
                      float dt);
 vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float* density, size_t n,
