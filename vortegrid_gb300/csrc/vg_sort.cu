@@ -8,8 +8,8 @@
 //   1. k_bin: one thread per vorton computes the leaf offset with the
 //      reference's FP32 binning (bit-exact) and counts vortons per cell;
 //   2. an exclusive scan of the counts gives each cell's first slot;
-//   3. a stable LSD radix sort of (offset, index) pairs by offset (8-bit
-//      digits, as many passes as the cell count needs) produces each cell's
+//   3. a stable LSD radix sort of (offset, index) pairs by offset (digits
+//      of up to 11 bits, as few passes as the cell count needs) produces each cell's
 //      vorton indices in ascending order -- the order in which the
 //      reference accumulates them -- independent of thread timing.
 #include "vg_internal.cuh"
@@ -107,64 +107,71 @@ __global__ void k_scan_add(unsigned* __restrict__ out, size_t n, const unsigned*
   if (i < n) out[i] += sums[blockIdx.x];
 }
 
-// ---- stable LSD radix sort, 8-bit digits -------------------------------------
+// ---- stable LSD radix sort, digits of up to 11 bits ----------------------------
 constexpr int kSortThreads = 256;
 constexpr int kSortItems = 8;  // keys per thread per tile
 constexpr int kTileKeys = kSortThreads * kSortItems;
+constexpr int kMaxDigitBits = 11;  // as few passes as the cell count needs (2 up to 2^22 cells)
 
 __global__ void __launch_bounds__(kSortThreads) k_digit_hist(const unsigned* __restrict__ key, int n, int shift,
-                                                             int ntiles, unsigned* __restrict__ hist) {
+                                                             unsigned mask, int ntiles, unsigned* __restrict__ hist) {
   pdl_entry();
-  __shared__ unsigned h[256];
-  h[threadIdx.x] = 0;
+  __shared__ unsigned h[1u << kMaxDigitBits];
+  for (unsigned d = threadIdx.x; d <= mask; d += kSortThreads) h[d] = 0;
   __syncthreads();
   const int base = blockIdx.x * kTileKeys;
   for (int k = 0; k < kSortItems; ++k) {
     const int i = base + k * kSortThreads + threadIdx.x;
-    if (i < n) atomicAdd(&h[(key[i] >> shift) & 255u], 1u);
+    if (i < n) atomicAdd(&h[(key[i] >> shift) & mask], 1u);
   }
   __syncthreads();
-  hist[(size_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];  // digit-major
+  for (unsigned d = threadIdx.x; d <= mask; d += kSortThreads) hist[(size_t)d * ntiles + blockIdx.x] = h[d];  // digit-major
 }
 
 // Scatter one tile: keys are taken in rounds of kSortThreads consecutive
 // elements; within a round, a key's rank among equal digits comes from warp
-// match masks and per-warp digit counts, so the output is stable.
+// match masks and per-warp digit counts, so the output is stable.  Only the
+// digits present in a round are touched: each (warp, digit) leader posts its
+// count, and after the round adds it to the digit's running slot and clears
+// its post.  Dynamic shared memory: (1 + warps) x (mask + 1) counters.
 __global__ void __launch_bounds__(kSortThreads) k_digit_scatter(const unsigned* __restrict__ key_in,
                                                                 const unsigned* __restrict__ val_in, int n, int shift,
-                                                                int ntiles, const unsigned* __restrict__ offsets,
+                                                                unsigned mask, int ntiles,
+                                                                const unsigned* __restrict__ offsets,
                                                                 unsigned* __restrict__ key_out,
                                                                 unsigned* __restrict__ val_out) {
   pdl_entry();
   constexpr int kWarps = kSortThreads / 32;
-  __shared__ unsigned running[256];
-  __shared__ unsigned warp_cnt[kWarps][256];
+  extern __shared__ unsigned sort_smem[];
+  const unsigned nd = mask + 1;
+  unsigned* running = sort_smem;     // [digit]
+  unsigned* warp_cnt = running + nd;  // [warp][digit]
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-  running[threadIdx.x] = offsets[(size_t)threadIdx.x * ntiles + blockIdx.x];
+  for (unsigned d = threadIdx.x; d < nd; d += kSortThreads) running[d] = offsets[(size_t)d * ntiles + blockIdx.x];
+  for (unsigned d = threadIdx.x; d < kWarps * nd; d += kSortThreads) warp_cnt[d] = 0;
+  __syncthreads();
   const int base = blockIdx.x * kTileKeys;
   for (int k = 0; k < kSortItems; ++k) {
-    for (int d = threadIdx.x; d < kWarps * 256; d += kSortThreads) (&warp_cnt[0][0])[d] = 0;
-    __syncthreads();
     const int i = base + k * kSortThreads + threadIdx.x;
     const bool valid = i < n;
     const unsigned kv = valid ? key_in[i] : 0u;
-    const unsigned digit = valid ? ((kv >> shift) & 255u) : 256u;
+    const unsigned digit = valid ? ((kv >> shift) & mask) : nd;
     const unsigned peers = __match_any_sync(0xffffffffu, digit);
     const unsigned lower = __popc(peers & ((1u << lane) - 1u));
-    if (valid && lower == 0) warp_cnt[wid][digit] = __popc(peers);
+    const bool leader = valid && lower == 0;
+    if (leader) warp_cnt[wid * nd + digit] = __popc(peers);
     __syncthreads();
     if (valid) {
       unsigned before = 0;
-      for (int ww = 0; ww < wid; ++ww) before += warp_cnt[ww][digit];
+      for (int ww = 0; ww < wid; ++ww) before += warp_cnt[ww * nd + digit];
       const unsigned dst = running[digit] + before + lower;
       key_out[dst] = kv;
       val_out[dst] = val_in[i];
     }
     __syncthreads();
-    {
-      unsigned add = 0;
-      for (int ww = 0; ww < kWarps; ++ww) add += warp_cnt[ww][threadIdx.x];
-      running[threadIdx.x] += add;
+    if (leader) {
+      atomicAdd(&running[digit], (unsigned)__popc(peers));
+      warp_cnt[wid * nd + digit] = 0;
     }
     __syncthreads();
   }
@@ -207,21 +214,32 @@ vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, Ce
   }
   st = exclusive_scan(c, count, slots, start, true);
   if (st != VG_OK) return st;
-  // Stable radix sort by key: only as many 8-bit passes as the largest key (ncells) needs.
+  // Stable radix sort by key: as few passes of at most kMaxDigitBits-bit
+  // digits as the largest key (ncells) needs, the bits split evenly.
   int bits = 0;
   while (bits < 32 && ncells >> bits) ++bits;
-  const int passes = (bits + 7) / 8;
+  const int passes = (bits + kMaxDigitBits - 1) / kMaxDigitBits;
+  const int dbits = passes > 0 ? (bits + passes - 1) / passes : 0;
+  const unsigned mask = (1u << dbits) - 1u, nd = mask + 1;
   const int ntiles = (int)((n + kTileKeys - 1) / kTileKeys);
   if (n > 0 && passes > 0) {
-    unsigned* hist = (unsigned*)ws(c, S_FILL, (size_t)256 * ntiles * sizeof(unsigned) * 2 + 16, &st);
+    unsigned* hist = (unsigned*)ws(c, S_FILL, (size_t)nd * ntiles * sizeof(unsigned) * 2 + 16, &st);
     if (st != VG_OK) return st;
-    unsigned* offs = hist + (size_t)256 * ntiles;
+    unsigned* offs = hist + (size_t)nd * ntiles;
+    const size_t scatter_smem = (size_t)(1 + kSortThreads / 32) * nd * sizeof(unsigned);
+    static bool smem_set = false;
+    if (!smem_set) {
+      cudaFuncSetAttribute(k_digit_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)((1 + kSortThreads / 32) * (1u << kMaxDigitBits) * sizeof(unsigned)));
+      smem_set = true;
+    }
     for (int p = 0; p < passes; ++p) {
-      pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_hist, key, (int)n, 8 * p, ntiles, hist);
+      pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_hist, key, (int)n, dbits * p, mask, ntiles, hist);
       VG_LAUNCHED(c);
-      st = exclusive_scan(c, hist, (size_t)256 * ntiles, offs, false);
+      st = exclusive_scan(c, hist, (size_t)nd * ntiles, offs, false);
       if (st != VG_OK) return st;
-      pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_scatter, key, val, (int)n, 8 * p, ntiles, offs, key2, val2);
+      pdl_launch(c->stream, ntiles, kSortThreads, scatter_smem, k_digit_scatter, key, val, (int)n, dbits * p, mask,
+                 ntiles, offs, key2, val2);
       VG_LAUNCHED(c);
       unsigned* t = key; key = key2; key2 = t;
       t = val; val = val2; val2 = t;
