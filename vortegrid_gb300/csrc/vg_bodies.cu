@@ -159,15 +159,18 @@ __device__ __forceinline__ V3 contact_point(const Body& b, V3 q, int idx, float 
   return sub(q, mul(*n, dist));
 }
 
-// Block sum of K doubles in a fixed order (warps in order, lanes by tree);
-// thread 0 writes the block's partial sums.
+// Block sum of K values in a fixed order: lanes by a tree in FP32 (a warp
+// holds a few contacts; FP64 arithmetic is a small fraction of FP32's rate on
+// this part, and a tree of FP64 shuffles over every warp of every block
+// dominated the launch), then the 8 warps in order in FP64; thread 0 writes
+// the block's partial sums.
 template <int K>
-__device__ void block_sums(double (&v)[K], double* __restrict__ out) {
+__device__ void block_sums(float (&v)[K], double* __restrict__ out) {
   __shared__ double sh[kBodyThreads / 32][K];
   // most blocks hold no particle in contact with the body: their sums are zero
   bool any = false;
 #pragma unroll
-  for (int k = 0; k < K; ++k) any = any || v[k] != 0.0;
+  for (int k = 0; k < K; ++k) any = any || v[k] != 0.0f;
   if (!__syncthreads_or(any)) {
     if (threadIdx.x < K) out[K * blockIdx.x + threadIdx.x] = 0.0;
     return;
@@ -178,7 +181,7 @@ __device__ void block_sums(double (&v)[K], double* __restrict__ out) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < K; ++k) sh[warp][k] = v[k];
+    for (int k = 0; k < K; ++k) sh[warp][k] = (double)v[k];
   __syncthreads();
   if (threadIdx.x == 0) {
 #pragma unroll
@@ -221,16 +224,19 @@ __global__ void __launch_bounds__(kSumThreads) k_sum_blocks(const double* __rest
   if (t < K) out[t] = sh[t][0];
 }
 
-// One body's CollideVortonsSlice for one vorton per thread.  Partial sums per
-// block: angular impulse (3), heat to body, sum of particle temperatures,
-// particles collided.
-__global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_constant__ Body B, float4* __restrict__ ps,
-                                                                  float4* __restrict__ vel, float4* __restrict__ w4,
-                                                                  float* __restrict__ dens, int n, float ambient,
-                                                                  float cp, double* __restrict__ part) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
-  if (i < n) {
+// The bodies of one call, in order (a kernel parameter).
+struct Bodies {
+  Body b[kMaxBodies];
+};
+
+// One body's CollideVortonsSlice for one vorton, on the vorton's state in
+// registers (position + size, velocity, angular velocity, density); the sums
+// of its contacts go to acc: angular impulse (3), heat to body, sum of
+// particle temperatures, particles collided.  Returns whether it changed.
+__device__ bool collide_vorton(const Body& B, float4& p4s, float4& v4s, float4& a4s, float& dens_s, float ambient,
+                               float cp, float (&acc)[6]) {
+  bool changed = false;
+  {
     const float thin = __fsub_rn(1.0f, FLT_EPSILON), fatten = __fadd_rn(1.0f, FLT_EPSILON);
     const float nudge = __fadd_rn(1.0f, 1.0e-4f), impact = __fadd_rn(1.0f, 0.01f);
     const float one_over_cp = __fdiv_rn(1.0f, cp);
@@ -240,7 +246,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_c
       repeat = (0 == incr) ? repeat + 1 : 0;
       if (pass > 0 && incr != 0) break;
       incr = 1;
-      const float4 p4 = ps[i], v4 = vel[i], a4 = w4[i];
+      const float4 p4 = p4s, v4 = v4s, a4 = a4s;
       V3 p = mk(p4.x, p4.y, p4.z), v = mk(v4.x, v4.y, v4.z), w = mk(a4.x, a4.y, a4.z);
       const float size = p4.w, r = __fmul_rn(size, 0.5f), r2 = __fmul_rn(r, r);
       const V3 s2v = sub(p, bpos);
@@ -268,7 +274,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_c
         cw = contact_point(B, p, idx, cdist, &nrm);
         if (B.parity < 0.0f && repeat < 5 && cdist < r) incr = 0;
       }
-      acc[5] += 1.0;
+      acc[5] += 1.0f;
       V3 vort_old = mul(w, 2.0f);
       // (the flow relative to the body at the contact point, and the bend
       // direction formed from it, feed only the reference's disabled
@@ -301,7 +307,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_c
       const V3 angdiff = mul(sub(vort_old, mul(w, 2.0f)), 0.5f);
       float d_new;
       {
-        const float d_old = dens[i];
+        const float d_old = dens_s;
         const float t_old = __fdiv_rn(__fmul_rn(300.0f, ambient), d_old);
         const float t_diff = __fsub_rn(B.temperature, t_old);
         const float g0 = __fmul_rn(__fmul_rn(__fmul_rn(B.conductivity, r), 0.03f), cp);
@@ -311,36 +317,68 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_c
         const float heat_ex = __fmul_rn(t_change, one_over_cp);
         const float t_new = __fadd_rn(t_old, t_change);
         d_new = __fdiv_rn(__fmul_rn(ambient, 300.0f), t_new);
-        acc[3] -= (double)heat_ex;
-        acc[4] += (double)t_old;
+        acc[3] -= heat_ex;
+        acc[4] += t_old;
       }
       {
         const float pi_over_6 = __fdiv_rn(3.1415926535897932384626433832795f, 6.0f);
         const float volume = __fmul_rn(__fmul_rn(__fmul_rn(pi_over_6, size), size), size);
         const float moi = __fmul_rn(__fmul_rn(0.4f, __fmul_rn(d_new, volume)), r2);
         const V3 ai = mul(angdiff, moi);
-        acc[0] += (double)ai.x;
-        acc[1] += (double)ai.y;
-        acc[2] += (double)ai.z;
+        acc[0] += ai.x;
+        acc[1] += ai.y;
+        acc[2] += ai.z;
       }
-      ps[i] = make_float4(p.x, p.y, p.z, p4.w);
-      vel[i] = make_float4(v.x, v.y, v.z, v4.w);
-      w4[i] = make_float4(w.x, w.y, w.z, a4.w);
-      dens[i] = d_new;
+      p4s = make_float4(p.x, p.y, p.z, p4.w);
+      v4s = make_float4(v.x, v.y, v.z, v4.w);
+      a4s = make_float4(w.x, w.y, w.z, a4.w);
+      dens_s = d_new;
+      changed = true;
     }
   }
-  block_sums<6>(acc, part);
+  return changed;
 }
 
-// One body's CollideTracersSlice for one tracer per thread.  Partial sums per
-// block: linear impulse (3), angular impulse (3).
-__global__ void __launch_bounds__(kBodyThreads) k_collide_tracers(const __grid_constant__ Body B, float4* __restrict__ ps,
-                                                                  float4* __restrict__ vel,
-                                                                  const float* __restrict__ dens, int n,
+// CollideVortonsSlice for every body in order, one vorton per thread: its
+// state stays in registers from body to body (each body sees the vorton as
+// the bodies before left it, as with one launch per body) and is written
+// once.  Per body, block partial sums at part + 6 blocks k.
+__global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_constant__ Bodies BB, int nb,
+                                                                  float4* __restrict__ ps, float4* __restrict__ vel,
+                                                                  float4* __restrict__ w4, float* __restrict__ dens,
+                                                                  int n, float ambient, float cp,
                                                                   double* __restrict__ part) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double acc[6] = {0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  float4 p4, v4, a4;
+  float d = 0.f;
   if (i < n) {
+    p4 = ps[i];
+    v4 = vel[i];
+    a4 = w4[i];
+    d = dens[i];
+  }
+  bool changed = false;
+  for (int k = 0; k < nb; ++k) {
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < n) changed |= collide_vorton(BB.b[k], p4, v4, a4, d, ambient, cp, acc);
+    block_sums<6>(acc, part + (size_t)6 * gridDim.x * k);
+  }
+  if (i < n && changed) {
+    ps[i] = p4;
+    vel[i] = v4;
+    w4[i] = a4;
+    dens[i] = d;
+  }
+}
+
+// One body's CollideTracersSlice for one tracer, on its state in registers;
+// the sums of its contacts go to acc: linear impulse (3), angular impulse (3).
+// dens: NULL, or the tracers' densities (tracer i's read when it collides).
+// Returns whether it changed.
+__device__ bool collide_tracer(const Body& B, float4& p4s, float4& v4s, const float* __restrict__ dens, int i,
+                               float (&acc)[6]) {
+  bool changed = false;
+  {
     const float thin = __fsub_rn(1.0f, FLT_EPSILON), fatten = __fadd_rn(1.0f, FLT_EPSILON);
     const float nudge = __fadd_rn(1.0f, 1.0e-4f), impact = __fadd_rn(1.0f, 0.01f);
     const V3 bpos = from(B.pos), bvel = from(B.vel), bspin = from(B.angvel);
@@ -349,7 +387,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_tracers(const __grid_c
       repeat = (0 == incr) ? repeat + 1 : 0;
       if (pass > 0 && incr != 0) break;
       incr = 1;
-      const float4 p4 = ps[i], v4 = vel[i];
+      const float4 p4 = p4s, v4 = v4s;
       const V3 p = mk(p4.x, p4.y, p4.z), v = mk(v4.x, v4.y, v4.z);
       const float size = p4.w, r = __fmul_rn(size, 0.5f);
       const V3 s2t = sub(p, bpos);
@@ -384,18 +422,43 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_tracers(const __grid_c
       const float mass = __fmul_rn(d0, __fmul_rn(__fmul_rn(__fmul_rn(pi_over_6, size), size), size));
       const V3 li = mul(sub(v, vnew), mass);
       const V3 ai = cross(sub(cpt, bpos), li);
-      acc[0] += (double)li.x;
-      acc[1] += (double)li.y;
-      acc[2] += (double)li.z;
-      acc[3] += (double)ai.x;
-      acc[4] += (double)ai.y;
-      acc[5] += (double)ai.z;
+      acc[0] += li.x;
+      acc[1] += li.y;
+      acc[2] += li.z;
+      acc[3] += ai.x;
+      acc[4] += ai.y;
+      acc[5] += ai.z;
       const V3 pn = add(bpos, disp_new);
-      ps[i] = make_float4(pn.x, pn.y, pn.z, p4.w);
-      vel[i] = make_float4(vnew.x, vnew.y, vnew.z, v4.w);
+      p4s = make_float4(pn.x, pn.y, pn.z, p4.w);
+      v4s = make_float4(vnew.x, vnew.y, vnew.z, v4.w);
+      changed = true;
     }
   }
-  block_sums<6>(acc, part);
+  return changed;
+}
+
+// CollideTracersSlice for every body in order, one tracer per thread, its
+// state in registers from body to body and written once (as k_collide_vortons).
+__global__ void __launch_bounds__(kBodyThreads) k_collide_tracers(const __grid_constant__ Bodies BB, int nb,
+                                                                  float4* __restrict__ ps, float4* __restrict__ vel,
+                                                                  const float* __restrict__ dens, int n,
+                                                                  double* __restrict__ part) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  float4 p4, v4;
+  if (i < n) {
+    p4 = ps[i];
+    v4 = vel[i];
+  }
+  bool changed = false;
+  for (int k = 0; k < nb; ++k) {
+    float acc[6] = {0.f, 0.f, 0.f, 0.f, 0.f, 0.f};
+    if (i < n) changed |= collide_tracer(BB.b[k], p4, v4, dens, i, acc);
+    block_sums<6>(acc, part + (size_t)6 * gridDim.x * k);
+  }
+  if (i < n && changed) {
+    ps[i] = p4;
+    vel[i] = v4;
+  }
 }
 
 // RemoveEmbeddedParticles' test for one body: survives unless inside it.
@@ -463,15 +526,20 @@ vg_status vg_collide_vortons_device(vg_ctx* c, const float* bodies, int nb, floa
   vg_status st = load_bodies(c, bodies, nb, B);
   if (st != VG_OK) return st;
   const unsigned blocks = n ? blocks_for(n, kBodyThreads) : 1;
-  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 + 6 * kMaxBodies) * sizeof(double), &st);
+  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 * kMaxBodies + 6 * kMaxBodies) * sizeof(double), &st);
   if (st != VG_OK) return st;
-  double* sums = part + (size_t)blocks * 6;
-  for (int k = 0; k < nb; ++k) {
-    k_collide_vortons<<<blocks, kBodyThreads, 0, c->stream>>>(B[k], (float4*)pos_size, (float4*)vel4,
+  double* sums = part + (size_t)blocks * 6 * kMaxBodies;
+  if (nb) {
+    Bodies BB;
+    memcpy(BB.b, B, sizeof(BB.b));
+    k_collide_vortons<<<blocks, kBodyThreads, 0, c->stream>>>(BB, nb, (float4*)pos_size, (float4*)vel4,
                                                              (float4*)angvel4, density, (int)n, ambient_density,
                                                              specific_heat, part);
-    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
-    c->launches += 2;
+    ++c->launches;
+  }
+  for (int k = 0; k < nb; ++k) {
+    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
+    ++c->launches;
   }
   VG_CUDA(c, cudaGetLastError());
   double h[6 * kMaxBodies];
@@ -509,14 +577,19 @@ vg_status vg_collide_tracers_device(vg_ctx* c, const float* bodies, int nb, floa
   vg_status st = load_bodies(c, bodies, nb, B);
   if (st != VG_OK) return st;
   const unsigned blocks = n ? blocks_for(n, kBodyThreads) : 1;
-  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 + 6 * kMaxBodies) * sizeof(double), &st);
+  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 * kMaxBodies + 6 * kMaxBodies) * sizeof(double), &st);
   if (st != VG_OK) return st;
-  double* sums = part + (size_t)blocks * 6;
-  for (int k = 0; k < nb; ++k) {
-    k_collide_tracers<<<blocks, kBodyThreads, 0, c->stream>>>(B[k], (float4*)pos_size, (float4*)vel4, density,
+  double* sums = part + (size_t)blocks * 6 * kMaxBodies;
+  if (nb) {
+    Bodies BB;
+    memcpy(BB.b, B, sizeof(BB.b));
+    k_collide_tracers<<<blocks, kBodyThreads, 0, c->stream>>>(BB, nb, (float4*)pos_size, (float4*)vel4, density,
                                                              (int)n, part);
-    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part, (int)blocks, sums + 6 * k);
-    c->launches += 2;
+    ++c->launches;
+  }
+  for (int k = 0; k < nb; ++k) {
+    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
+    ++c->launches;
   }
   VG_CUDA(c, cudaGetLastError());
   double h[6 * kMaxBodies];
