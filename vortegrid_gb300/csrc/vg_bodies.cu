@@ -159,20 +159,19 @@ __device__ __forceinline__ V3 contact_point(const Body& b, V3 q, int idx, float 
   return sub(q, mul(*n, dist));
 }
 
-// Block sum of K values in a fixed order: lanes by a tree in FP32 (a warp
-// holds a few contacts; FP64 arithmetic is a small fraction of FP32's rate on
-// this part, and a tree of FP64 shuffles over every warp of every block
-// dominated the launch), then the 8 warps in order in FP64; thread 0 writes
-// the block's partial sums.
+// Block sum of K values in a fixed order: lanes by a tree, then the 8 warps
+// in order (threads 0..K-1), in FP32 -- FP64 arithmetic runs at a small
+// fraction of FP32's rate on this part, and FP64 sums over every block
+// dominated the launch; thread k writes the block's partial sum k.
 template <int K>
-__device__ void block_sums(float (&v)[K], double* __restrict__ out) {
-  __shared__ double sh[kBodyThreads / 32][K];
+__device__ void block_sums(float (&v)[K], float* __restrict__ out) {
+  __shared__ float sh[kBodyThreads / 32][K];
   // most blocks hold no particle in contact with the body: their sums are zero
   bool any = false;
 #pragma unroll
   for (int k = 0; k < K; ++k) any = any || v[k] != 0.0f;
   if (!__syncthreads_or(any)) {
-    if (threadIdx.x < K) out[K * blockIdx.x + threadIdx.x] = 0.0;
+    if (threadIdx.x < K) out[K * blockIdx.x + threadIdx.x] = 0.0f;
     return;
   }
   for (int o = 16; o > 0; o >>= 1)
@@ -181,39 +180,46 @@ __device__ void block_sums(float (&v)[K], double* __restrict__ out) {
   const int warp = threadIdx.x / 32, lane = threadIdx.x % 32;
   if (lane == 0)
 #pragma unroll
-    for (int k = 0; k < K; ++k) sh[warp][k] = (double)v[k];
+    for (int k = 0; k < K; ++k) sh[warp][k] = v[k];
   __syncthreads();
-  if (threadIdx.x == 0) {
-#pragma unroll
-    for (int k = 0; k < K; ++k) {
-      double s = 0.0;
-      for (int w = 0; w < kBodyThreads / 32; ++w) s += sh[w][k];
-      out[K * blockIdx.x + k] = s;
-    }
+  if (threadIdx.x < K) {
+    float s = 0.0f;
+    for (int w = 0; w < kBodyThreads / 32; ++w) s += sh[w][threadIdx.x];
+    out[K * blockIdx.x + threadIdx.x] = s;
   }
 }
 
 // The blocks' partial sums added in a fixed order by one CTA: thread t sums
-// the contiguous run of blocks [t c, (t + 1) c), then a tree over the threads
-// (halving strides) -- deterministic, and with enough loads in flight that a
-// launch over millions of particles is not held up by a serial chain.
+// the contiguous run of blocks [t c, (t + 1) c) with compensated (Kahan) FP32
+// additions -- or, for a count (the last value when kCount), exactly in
+// integers -- then a tree over the threads in FP64 (halving strides):
+// deterministic, within a few FP32 rounding units of the exact sum.
 constexpr int kSumThreads = 256;
-template <int K>
-__global__ void __launch_bounds__(kSumThreads) k_sum_blocks(const double* __restrict__ part, int nb,
+template <int K, bool kCount>
+__global__ void __launch_bounds__(kSumThreads) k_sum_blocks(const float* __restrict__ part, int nb,
                                                             double* __restrict__ out) {
   __shared__ double sh[K][kSumThreads];
   const int t = threadIdx.x;
   const int per = (nb + kSumThreads - 1) / kSumThreads;
   const int b0 = min(nb, t * per), b1 = min(nb, b0 + per);
-  double s[K];
+  constexpr int KF = kCount ? K - 1 : K;
+  float s[K], comp[K];
+  unsigned long long cnt = 0;
 #pragma unroll
-  for (int k = 0; k < K; ++k) s[k] = 0.0;
-#pragma unroll 4
-  for (int b = b0; b < b1; ++b)
+  for (int k = 0; k < K; ++k) s[k] = comp[k] = 0.0f;
+  for (int b = b0; b < b1; ++b) {
 #pragma unroll
-    for (int k = 0; k < K; ++k) s[k] += part[K * (size_t)b + k];
+    for (int k = 0; k < KF; ++k) {
+      const float y = __fsub_rn(part[K * (size_t)b + k], comp[k]);
+      const float tt = __fadd_rn(s[k], y);
+      comp[k] = __fsub_rn(__fsub_rn(tt, s[k]), y);
+      s[k] = tt;
+    }
+    if (kCount) cnt += (unsigned long long)part[K * (size_t)b + K - 1];
+  }
 #pragma unroll
-  for (int k = 0; k < K; ++k) sh[k][t] = s[k];
+  for (int k = 0; k < KF; ++k) sh[k][t] = (double)s[k];
+  if (kCount) sh[K - 1][t] = (double)cnt;
   __syncthreads();
   for (int h = kSumThreads / 2; h > 0; h >>= 1) {
     if (t < h)
@@ -347,7 +353,7 @@ __global__ void __launch_bounds__(kBodyThreads) k_collide_vortons(const __grid_c
                                                                   float4* __restrict__ ps, float4* __restrict__ vel,
                                                                   float4* __restrict__ w4, float* __restrict__ dens,
                                                                   int n, float ambient, float cp,
-                                                                  double* __restrict__ part) {
+                                                                  float* __restrict__ part) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float4 p4, v4, a4;
   float d = 0.f;
@@ -442,7 +448,7 @@ __device__ bool collide_tracer(const Body& B, float4& p4s, float4& v4s, const fl
 __global__ void __launch_bounds__(kBodyThreads) k_collide_tracers(const __grid_constant__ Bodies BB, int nb,
                                                                   float4* __restrict__ ps, float4* __restrict__ vel,
                                                                   const float* __restrict__ dens, int n,
-                                                                  double* __restrict__ part) {
+                                                                  float* __restrict__ part) {
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   float4 p4, v4;
   if (i < n) {
@@ -526,9 +532,10 @@ vg_status vg_collide_vortons_device(vg_ctx* c, const float* bodies, int nb, floa
   vg_status st = load_bodies(c, bodies, nb, B);
   if (st != VG_OK) return st;
   const unsigned blocks = n ? blocks_for(n, kBodyThreads) : 1;
-  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 * kMaxBodies + 6 * kMaxBodies) * sizeof(double), &st);
+  double* sums = (double*)ws(c, S_BODY, 6 * kMaxBodies * sizeof(double) + (size_t)blocks * 6 * kMaxBodies * sizeof(float),
+                             &st);
   if (st != VG_OK) return st;
-  double* sums = part + (size_t)blocks * 6 * kMaxBodies;
+  float* part = (float*)(sums + 6 * kMaxBodies);
   if (nb) {
     Bodies BB;
     memcpy(BB.b, B, sizeof(BB.b));
@@ -538,7 +545,7 @@ vg_status vg_collide_vortons_device(vg_ctx* c, const float* bodies, int nb, floa
     ++c->launches;
   }
   for (int k = 0; k < nb; ++k) {
-    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
+    k_sum_blocks<6, true><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
     ++c->launches;
   }
   VG_CUDA(c, cudaGetLastError());
@@ -577,9 +584,10 @@ vg_status vg_collide_tracers_device(vg_ctx* c, const float* bodies, int nb, floa
   vg_status st = load_bodies(c, bodies, nb, B);
   if (st != VG_OK) return st;
   const unsigned blocks = n ? blocks_for(n, kBodyThreads) : 1;
-  double* part = (double*)ws(c, S_BODY, ((size_t)blocks * 6 * kMaxBodies + 6 * kMaxBodies) * sizeof(double), &st);
+  double* sums = (double*)ws(c, S_BODY, 6 * kMaxBodies * sizeof(double) + (size_t)blocks * 6 * kMaxBodies * sizeof(float),
+                             &st);
   if (st != VG_OK) return st;
-  double* sums = part + (size_t)blocks * 6 * kMaxBodies;
+  float* part = (float*)(sums + 6 * kMaxBodies);
   if (nb) {
     Bodies BB;
     memcpy(BB.b, B, sizeof(BB.b));
@@ -588,7 +596,7 @@ vg_status vg_collide_tracers_device(vg_ctx* c, const float* bodies, int nb, floa
     ++c->launches;
   }
   for (int k = 0; k < nb; ++k) {
-    k_sum_blocks<6><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
+    k_sum_blocks<6, false><<<1, kSumThreads, 0, c->stream>>>(part + (size_t)6 * blocks * k, (int)blocks, sums + 6 * k);
     ++c->launches;
   }
   VG_CUDA(c, cudaGetLastError());
