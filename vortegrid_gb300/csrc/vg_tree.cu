@@ -76,11 +76,12 @@ __global__ void k_leaf(Geom g, const float4* __restrict__ ps, const float4* __re
   out_w[c] = make_float4(wx, wy, wz, 0.f);
 }
 
-__global__ void k_aggregate(Geom P, Geom C, uint3 d, const float4* __restrict__ cpos, const float4* __restrict__ cw,
-                            float4* __restrict__ ppos, float4* __restrict__ pw) {
-  pdl_entry();
-  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (k >= P.points()) return;
+// AggregateClusters for parent point k of layer P from its children in C
+// (decimation d): vorticity-weighted centroid, summed angular velocity, the
+// last child's nonzero size.
+__device__ __forceinline__ void aggregate_point(const Geom& P, const Geom& C, uint3 d, const float4* __restrict__ cpos,
+                                                const float4* __restrict__ cw, float4* __restrict__ ppos,
+                                                float4* __restrict__ pw, size_t k) {
   const unsigned px = (unsigned)(k % P.np[0]);
   const unsigned py = (unsigned)((k / P.np[0]) % P.np[1]);
   const unsigned pz = (unsigned)(k / ((size_t)P.np[0] * P.np[1]));
@@ -110,6 +111,32 @@ __global__ void k_aggregate(Geom P, Geom C, uint3 d, const float4* __restrict__ 
   }
   ppos[k] = make_float4(x, y, z, size);
   pw[k] = make_float4(wx, wy, wz, 0.f);
+}
+
+__global__ void k_aggregate(Geom P, Geom C, uint3 d, const float4* __restrict__ cpos, const float4* __restrict__ cw,
+                            float4* __restrict__ ppos, float4* __restrict__ pw) {
+  pdl_entry();
+  const size_t k = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= P.points()) return;
+  aggregate_point(P, C, d, cpos, cw, ppos, pw, k);
+}
+
+// The small top layers l0 .. depth-1 in one CTA, layer after layer (a barrier
+// between them makes each layer's writes visible to the next): the same cells
+// as one k_aggregate launch per layer, without a launch per few hundred points.
+constexpr size_t kTopLayerPoints = 4096;  // layers of at most this many points go to k_aggregate_top
+constexpr int kTopThreads = 1024;
+__global__ void __launch_bounds__(kTopThreads) k_aggregate_top(const __grid_constant__ TreeParams T, int l0,
+                                                               float4* __restrict__ sv_pos, float4* __restrict__ sv_w) {
+  pdl_entry();
+  for (int l = l0; l < T.depth; ++l) {
+    const Geom& P = T.layer[l];
+    const Geom& C = T.layer[l - 1];
+    const uint3 d = make_uint3(T.decim[l][0], T.decim[l][1], T.decim[l][2]);
+    for (size_t k = threadIdx.x; k < P.points(); k += blockDim.x)
+      aggregate_point(P, C, d, sv_pos + T.base[l - 1], sv_w + T.base[l - 1], sv_pos + T.base[l], sv_w + T.base[l], k);
+    __syncthreads();
+  }
 }
 
 template <int KIND, bool REF>
@@ -524,12 +551,19 @@ vg_status build_tree(Ctx* c, const Geom& g, const float4* ps, const float4* w, s
   pdl_launch(c->stream, blocks_for(leaf.points(), 256), 256, 0, k_leaf, leaf, ps, w, cl.start, cl.items, t->sv_pos,
                                                                   t->sv_w);
   VG_LAUNCHED(c);
-  for (int l = 1; l < t->depth; ++l) {
+  // the first layer from which every layer is small: those run in one CTA
+  int l0 = t->depth;
+  while (l0 > 1 && t->layer[l0 - 1].points() <= kTopLayerPoints) --l0;
+  for (int l = 1; l < l0; ++l) {
     const Geom& P = t->layer[l];
     const uint3 d = make_uint3(t->decim[l][0], t->decim[l][1], t->decim[l][2]);
     pdl_launch(c->stream, blocks_for(P.points(), 128), 128, 0, k_aggregate, P, t->layer[l - 1], d, t->sv_pos + t->base[l - 1],
                                                                      t->sv_w + t->base[l - 1], t->sv_pos + t->base[l],
                                                                      t->sv_w + t->base[l]);
+    VG_LAUNCHED(c);
+  }
+  if (l0 < t->depth) {
+    pdl_launch(c->stream, 1, kTopThreads, 0, k_aggregate_top, make_params(*t), l0, t->sv_pos, t->sv_w);
     VG_LAUNCHED(c);
   }
   VG_CUDA(c, cudaGetLastError());
