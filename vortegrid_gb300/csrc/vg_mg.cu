@@ -1375,8 +1375,10 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
     return st;
   *etot = (float*)(((uintptr_t)(B.cwork + 3 * coarse_pts) + 255) & ~(uintptr_t)255);  // IR correction
   *rir = *etot + 3 * n0;                                                                 // IR right-hand side
-  static bool smem_set = false;
-  if (!smem_set) {
+  // kernel attributes are per device: set once for each device used
+  static unsigned long long smem_set = 0;
+  const unsigned long long dev_bit = 1ull << (c->cfg.device & 63);
+  if (!(smem_set & dev_bit)) {
     cudaFuncSetAttribute(k_vcycle_small, cudaFuncAttributeMaxDynamicSharedMemorySize, 200 * 1024);
     cudaFuncSetAttribute(k_dst_xy<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
     cudaFuncSetAttribute(k_dst_xy<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
@@ -1384,7 +1386,7 @@ static vg_status setup_bufs(Ctx* c, const Geom& g, const MgPlan& P, MgBufs& B, f
     cudaFuncSetAttribute(k_dst_zz<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
     cudaFuncSetAttribute(k_dst_yx<float>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
     cudaFuncSetAttribute(k_dst_yx<double>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kDstSmemMax);
-    smem_set = true;
+    smem_set |= dev_bit;
   }
   return VG_OK;
 }

@@ -227,11 +227,13 @@ vg_status build_cell_lists(Ctx* c, const Geom& g, const float4* ps, size_t n, Ce
     if (st != VG_OK) return st;
     unsigned* offs = hist + (size_t)nd * ntiles;
     const size_t scatter_smem = (size_t)(1 + kSortThreads / 32) * nd * sizeof(unsigned);
-    static bool smem_set = false;
-    if (!smem_set) {
+    // kernel attributes are per device: set once for each device used
+    static unsigned long long smem_set = 0;
+    const unsigned long long dev_bit = 1ull << (c->cfg.device & 63);
+    if (!(smem_set & dev_bit)) {
       cudaFuncSetAttribute(k_digit_scatter, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)((1 + kSortThreads / 32) * (1u << kMaxDigitBits) * sizeof(unsigned)));
-      smem_set = true;
+      smem_set |= dev_bit;
     }
     for (int p = 0; p < passes; ++p) {
       pdl_launch(c->stream, ntiles, kSortThreads, 0, k_digit_hist, key, (int)n, dbits * p, mask, ntiles, hist);
