@@ -11,9 +11,9 @@ advected through the velocity grid.  A step is that whole pass; interactions
 per step = 4,096 x (4,096 + 35,937).
 
 Keys beyond the base contract:
-  * "e2e": the same metric through the host-buffer C ABI (vg_step on the
-    reference's 96-byte Particle records + vg_advect on tracer records, from
-    pinned host memory, copies included);
+  * "e2e": the same metric through the host-buffer C ABI (vg_step_evolve --
+    the step and PclOpEvolve -- on the reference's 96-byte Particle records +
+    vg_advect on tracer records, from pinned host memory, copies included);
   * "roofline": the direct-sum kernel against the FP32 pipe (2 flops x 128
     lanes x the device's SM count x the SM clock sampled during the run), 26 algorithmic
     flops per interaction;
@@ -373,15 +373,12 @@ def run_ours(args, world, rank, local):
     trr = trr_t.numpy().view(vg.PARTICLE_DTYPE)
     trr0 = vg.make_particles(tr)
     host = vg.VortonSim(cfg=cfg)
-    rf = recs.view(np.float32).reshape(-1, 24)  # the records' float words (position 0-2, velocity 3-5)
     e2e_ms = []
     for k in range(args.warmup + args.steps):
         recs[...] = recs0
         trr[...] = trr0
         t0 = time.perf_counter()
-        host.Update(recs, float(DT), k)
-        for j in range(3):  # PclOpEvolve on the host records (vortons): position += velocity dt, per axis
-            rf[:, j] += rf[:, 3 + j] * DT
+        host.UpdateAndEvolve(recs, float(DT), k)  # PclOpVortonSim + PclOpEvolve on the vorton records
         host.Advect(trr, float(DT))
         t1 = time.perf_counter()
         if k >= args.warmup:
@@ -391,7 +388,8 @@ def run_ours(args, world, rank, local):
                      # 96-byte records travel whole, one contiguous copy each way
                      "h2d_bytes_per_step": (N_VORTONS + N_TRACERS) * 96,
                      "d2h_bytes_per_step": (N_VORTONS + N_TRACERS) * 96, "ms_per_step": e2e_step,
-                     "path": "vg_step (Particle records) + host Evolve + vg_advect (tracer records), pinned"}
+                     "path": "vg_step_evolve (Particle records: the step and PclOpEvolve) + vg_advect (tracer "
+                             "records: AssignVelocityFromField + Evolve), pinned"}
 
     # ---- CPU baseline (reference code, all host threads)
     from vortegrid_gb300 import workloads

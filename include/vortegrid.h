@@ -142,6 +142,14 @@ vg_status vg_set_config(vg_ctx* ctx, const vg_config* cfg);
 vg_status vg_step(vg_ctx* ctx, void* particles, size_t n, size_t stride, const float* extra_min,
                   const float* extra_max, float dt, unsigned frame);
 
+/* vg_step followed by PclOpEvolve::Operate (Particles/Operation/
+ * pclOpEvolve.cpp:36-58) on the same vorton records, fused: each record also
+ * gets position += velocity x dt before the records go back to the host --
+ * the plugin pair a scene runs on its vorton group, in one call and one copy
+ * each way.  Positions bit-identical to vg_step then the Euler step in FP32. */
+vg_status vg_step_evolve(vg_ctx* ctx, void* particles, size_t n, size_t stride, const float* extra_min,
+                         const float* extra_max, float dt, unsigned frame);
+
 /* Device-resident form of vg_step.  pos_size: float4 per vorton (x, y, z,
  * size); angvel: float4 (x, y, z, unused), updated in place; vel: float4
  * written.  extra_minmax: 6 host floats (min xyz, max xyz) or NULL. */

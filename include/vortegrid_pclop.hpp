@@ -62,6 +62,16 @@ class VortonSimGpu {
           "vg_step");
   }
 
+  // Update followed by PclOpEvolve on the same vorton records (vg_step_evolve).
+  template <class ParticleVector, class Vec3Like>
+  void UpdateAndEvolve(ParticleVector& particles, float timeStep, unsigned uFrame, const Vec3Like* minCorner,
+                       const Vec3Like* maxCorner) {
+    check(vg_step_evolve(ctx_, particles.data(), particles.size(), sizeof(particles.data()[0]),
+                         minCorner ? reinterpret_cast<const float*>(minCorner) : nullptr,
+                         maxCorner ? reinterpret_cast<const float*>(maxCorner) : nullptr, timeStep, uFrame),
+          "vg_step_evolve");
+  }
+
   // GetVelocityGrid (vortonSim.h:334-335): copies the grid into `xyz`.
   vg_grid_geom GetVelocityGrid(float* xyz, size_t cap_points) {
     vg_grid_geom g;
@@ -97,14 +107,19 @@ class PclOpVortonSimGpu : public Base {
   explicit PclOpVortonSimGpu(float viscosity = 0.01f) : mVortonSim(viscosity) {}
   Base* Create() { return new PclOpVortonSimGpu(); }
   Base* Clone() { return new PclOpVortonSimGpu(); }
-  // PclOpVortonSim::Operate (pclOpVortonSim.cpp:51-71).
+  // PclOpVortonSim::Operate (pclOpVortonSim.cpp:51-71); with mEvolve, also
+  // the PclOpEvolve that follows it on the vorton group, in the same call.
   void Operate(ParticleVector& particles, float timeStep, unsigned uFrame) {
     if (particles.size() == 0) return;  // the reference returns early on no vortons
-    mVortonSim.Update(particles, timeStep, uFrame, mMinCorner, mMaxCorner);
+    if (mEvolve)
+      mVortonSim.UpdateAndEvolve(particles, timeStep, uFrame, mMinCorner, mMaxCorner);
+    else
+      mVortonSim.Update(particles, timeStep, uFrame, mMinCorner, mMaxCorner);
   }
   VortonSimGpu mVortonSim;
   const Vec3Like* mMinCorner = nullptr;
   const Vec3Like* mMaxCorner = nullptr;
+  bool mEvolve = false;  // true: drop the vorton group's PclOpEvolve, this op moves the vortons
 };
 
 // Drop-in for the tracer group's PclOpAssignVelocityFromField (gain 1) +

@@ -516,6 +516,37 @@ def test_pinned_records_match_pageable(vg):
             assert np.array_equal(np.ascontiguousarray(a[f]).view(np.uint8), np.ascontiguousarray(b[f]).view(np.uint8)), f
 
 
+def test_step_evolve_matches_step_then_evolve(vg):
+    """vg_step_evolve (the step and PclOpEvolve on the same vorton records,
+    fused) gives every field bit for bit what vg_step followed by the FP32
+    Euler step on the host records gives (pclOpEvolve.cpp:36-58), over three
+    frames, for 96-byte records (copied whole) and for wider ones (copied as
+    their first 48 bytes)."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(3000, seed=9)
+    dt = np.float32(DT)
+    wide = np.dtype({"names": list(vg.PARTICLE_DTYPE.names) + ["extra"],
+                     "formats": [vg.PARTICLE_DTYPE.fields[f][0] for f in vg.PARTICLE_DTYPE.names] + [(np.float32, 40)],
+                     "offsets": [vg.PARTICLE_DTYPE.fields[f][1] for f in vg.PARTICLE_DTYPE.names] + [96],
+                     "itemsize": 256})
+    for dtype in (vg.PARTICLE_DTYPE, wide):
+        recs0 = np.zeros(len(pos), dtype)
+        base = vg.make_particles(pos, w, s)
+        for f in vg.PARTICLE_DTYPE.names:
+            recs0[f] = base[f]
+        a, b = recs0.copy(), recs0.copy()
+        sa, sb = vg.VortonSim(0.01), vg.VortonSim(0.01)
+        for k in range(3):
+            sa.Update(a, DT, k)
+            for j in range(3):  # position += velocity dt, FP32
+                a["position"][:, j] = (a["position"][:, j] + a["velocity"][:, j] * dt).astype(np.float32)
+            sb.UpdateAndEvolve(b, DT, k)
+        for f in vg.PARTICLE_DTYPE.names:
+            assert np.array_equal(np.ascontiguousarray(a[f]).view(np.uint8),
+                                  np.ascontiguousarray(b[f]).view(np.uint8)), (dtype.itemsize, f)
+        assert np.abs(b["position"] - recs0["position"]).max() > 0  # the vortons moved
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)

@@ -183,6 +183,28 @@ __global__ void k_unpack_records(const unsigned char* __restrict__ rec, size_t p
   w[i] = make_float4(r[9], r[10], r[11], 0.f);   // angular velocity @36
 }
 
+// k_pack_records followed by PclOpEvolve's Euler step (pclOpEvolve.cpp:36-58)
+// on the same records: record bytes [0, 48) -- position + velocity dt, then
+// velocity, (unchanged) orientation, angular velocity.
+__global__ void k_pack_records_evolve(unsigned char* __restrict__ rec, size_t pitch, int n,
+                                      const float4* __restrict__ ps, const float4* __restrict__ v,
+                                      const float4* __restrict__ w, float dt) {
+  pdl_entry();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  float* r = (float*)(rec + (size_t)i * pitch);
+  const float4 p = ps[i], u = v[i], a = w[i];
+  r[0] = __fadd_rn(p.x, __fmul_rn(u.x, dt));
+  r[1] = __fadd_rn(p.y, __fmul_rn(u.y, dt));
+  r[2] = __fadd_rn(p.z, __fmul_rn(u.z, dt));
+  r[3] = u.x;
+  r[4] = u.y;
+  r[5] = u.z;
+  r[9] = a.x;
+  r[10] = a.y;
+  r[11] = a.z;
+}
+
 __global__ void k_pack_records(unsigned char* __restrict__ rec, size_t pitch, int n, const float4* __restrict__ v,
                                const float4* __restrict__ w) {
   pdl_entry();
@@ -643,9 +665,10 @@ vg_status vg_set_config(vg_ctx* c, const vg_config* cfg) {
   return VG_OK;
 }
 
-vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
-                  const float* extra_max, float dt, unsigned frame) {
-  (void)frame;
+// vg_step and vg_step_evolve on host records (evolve: the vortons move by
+// velocity x dt before the records go back).
+static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                              const float* extra_max, float dt, bool evolve) {
   if (!c) return VG_INVALID;
   if (n == 0) return fail(c, VG_EMPTY, "no vortons");
   if (!particles || stride < 56 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 56 / unaligned");
@@ -677,15 +700,33 @@ vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const flo
   st = run_step(c, ps, w, vel, n, rec0, radius, extra_min, extra_max, dt);
   if (st != VG_OK) return st;
   // write back record bytes [12, 48): velocity, (unchanged) orientation,
-  // angular velocity (whole records carry their other bytes back unchanged)
-  pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records, stage + 12, pitch, (int)n, vel, w);
+  // angular velocity (whole records carry their other bytes back unchanged);
+  // evolving, bytes [0, 48) with the moved position
+  if (evolve)
+    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records_evolve, stage, pitch, (int)n, (const float4*)ps,
+               (const float4*)vel, (const float4*)w, dt);
+  else
+    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records, stage + 12, pitch, (int)n, vel, w);
   VG_CUDA(c, cudaGetLastError());
+  const size_t from = evolve ? 0 : 12;
   if (whole)
     VG_CUDA(c, cudaMemcpyAsync(particles, stage, n * stride, cudaMemcpyDeviceToHost, c->stream));
   else
-    VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + 12, stride, stage + 12, 56, 36, n,
+    VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + from, stride, stage + from, 56, 48 - from, n,
                                  cudaMemcpyDeviceToHost, c->stream));
-  return sync_and_check(c, "vg_step");
+  return sync_and_check(c, evolve ? "vg_step_evolve" : "vg_step");
+}
+
+vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                  const float* extra_max, float dt, unsigned frame) {
+  (void)frame;
+  return step_records(c, particles, n, stride, extra_min, extra_max, dt, false);
+}
+
+vg_status vg_step_evolve(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                         const float* extra_max, float dt, unsigned frame) {
+  (void)frame;
+  return step_records(c, particles, n, stride, extra_min, extra_max, dt, true);
 }
 
 vg_status vg_step_device(vg_ctx* c, const float* pos_size, float* angvel, float* vel, size_t n,
