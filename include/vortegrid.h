@@ -150,6 +150,19 @@ vg_status vg_step(vg_ctx* ctx, void* particles, size_t n, size_t stride, const f
 vg_status vg_step_evolve(vg_ctx* ctx, void* particles, size_t n, size_t stride, const float* extra_min,
                          const float* extra_max, float dt, unsigned frame);
 
+/* One frame of a scene's two particle groups in one call: vg_step (or, with
+ * evolve_vortons, vg_step_evolve) on the n vorton records, then vg_advect on
+ * the m tracer records through that step's velocity grid -- the vorton
+ * group's PclOpVortonSim (+ PclOpEvolve) and the tracer group's
+ * PclOpAssignVelocityFromField (gain 1) + PclOpEvolve
+ * (Particles/Operation/pclOpAdvect.cpp:132-152, pclOpEvolve.cpp:36-58).  The
+ * tracer records' upload runs on a second stream while the vortons step.
+ * Results bit-identical to the two calls; m = 0 is vg_step / vg_step_evolve
+ * alone. */
+vg_status vg_step_advect(vg_ctx* ctx, void* vortons, size_t n, size_t stride, const float* extra_min,
+                         const float* extra_max, float dt, unsigned frame, int evolve_vortons, void* tracers,
+                         size_t m, size_t tracer_stride);
+
 /* Device-resident form of vg_step.  pos_size: float4 per vorton (x, y, z,
  * size); angvel: float4 (x, y, z, unused), updated in place; vel: float4
  * written.  extra_minmax: 6 host floats (min xyz, max xyz) or NULL. */

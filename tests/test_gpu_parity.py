@@ -547,6 +547,35 @@ def test_step_evolve_matches_step_then_evolve(vg):
         assert np.abs(b["position"] - recs0["position"]).max() > 0  # the vortons moved
 
 
+def test_step_advect_matches_the_separate_calls(vg):
+    """vg_step_advect (both groups of a frame in one call, the tracer upload on
+    a second stream during the step) gives every field of the vorton and
+    tracer records bit for bit what vg_step_evolve (or vg_step) then vg_advect
+    give, over three frames, with whole and wide tracer records."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(3000, seed=11)
+    tr = (pos[::3] * np.float32(0.8)).astype(np.float32)
+    wide = np.dtype({"names": ["position", "velocity", "extra"], "formats": [(np.float32, 3), (np.float32, 3),
+                                                                           (np.float32, 30)],
+                     "offsets": [0, 12, 24], "itemsize": 144})
+    for evolve in (True, False):
+        for tdtype in (vg.PARTICLE_DTYPE, wide):
+            t0 = np.zeros(len(tr), tdtype)
+            t0["position"] = tr
+            v0 = vg.make_particles(pos, w, s)
+            va, ta, vb, tb = v0.copy(), t0.copy(), v0.copy(), t0.copy()
+            sa, sb = vg.VortonSim(0.01), vg.VortonSim(0.01)
+            for k in range(3):
+                (sa.UpdateAndEvolve if evolve else sa.Update)(va, DT, k)
+                sa.Advect(ta, DT)
+                sb.UpdateAndAdvect(vb, tb, DT, k, evolve=evolve)
+            for a, b, names in ((va, vb, vg.PARTICLE_DTYPE.names), (ta, tb, tdtype.names)):
+                for f in names:
+                    assert np.array_equal(np.ascontiguousarray(a[f]).view(np.uint8),
+                                          np.ascontiguousarray(b[f]).view(np.uint8)), (evolve, tdtype.itemsize, f)
+            assert np.abs(tb["position"] - t0["position"]).max() > 0
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)

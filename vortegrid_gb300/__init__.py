@@ -136,7 +136,7 @@ _lib = None
 
 EXPORTS = [
     "vg_status_string", "vg_last_error", "vg_abi_version", "vg_config_default", "vg_create", "vg_destroy",
-    "vg_set_config", "vg_step", "vg_step_evolve", "vg_step_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
+    "vg_set_config", "vg_step", "vg_step_evolve", "vg_step_advect", "vg_step_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
     "vg_get_vector_potential", "vg_get_stats", "vg_advect", "vg_advect_device", "vg_define_shape",
     "vg_set_poisson_schedule", "vg_get_poisson_schedule", "vg_set_coarsest_fp64",
     "vg_bin_device", "vg_partition_device", "vg_direct_device", "vg_tree_device", "vg_splat_device", "vg_boundary_vecpot_device",
@@ -181,6 +181,9 @@ def lib():
                               ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
         L.vg_step_evolve.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
                                      ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
+        L.vg_step_advect.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t,
+                                     ctypes.c_void_p, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint, ctypes.c_int,
+                                     ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
         L.vg_step_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
         L.vg_get_velocity_grid.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GridGeom)]
@@ -399,6 +402,20 @@ class VortonSim(Context):
         emax = np.ascontiguousarray(extra_max, np.float32) if extra_max is not None else None
         self.check(lib().vg_step_evolve(self.h, _ptr(particles), len(particles), particles.dtype.itemsize,
                                         _ptr(emin), _ptr(emax), timeStep, uFrame), "vg_step_evolve")
+
+    def UpdateAndAdvect(self, particles, tracers, timeStep, uFrame=0, evolve=True, extra_min=None, extra_max=None):
+        """One frame of both groups (vg_step_advect): Update (+ Evolve) on the vorton records, then
+        AssignVelocityFromField (gain 1) + Evolve on the tracer records through the new velocity grid."""
+        for a in (particles, tracers):
+            if not a.flags.c_contiguous:
+                raise ValueError("particle records must be C-contiguous")
+        if particles.dtype.itemsize < 56 or tracers.dtype.itemsize < 24:
+            raise ValueError("vorton records of at least 56 bytes and tracer records of at least 24 bytes")
+        emin = np.ascontiguousarray(extra_min, np.float32) if extra_min is not None else None
+        emax = np.ascontiguousarray(extra_max, np.float32) if extra_max is not None else None
+        self.check(lib().vg_step_advect(self.h, _ptr(particles), len(particles), particles.dtype.itemsize,
+                                        _ptr(emin), _ptr(emax), timeStep, uFrame, int(bool(evolve)), _ptr(tracers),
+                                        len(tracers), tracers.dtype.itemsize), "vg_step_advect")
 
     def UpdateDevice(self, pos_size, angvel, vel, timeStep, uFrame=0, extra_minmax=None):
         e = np.ascontiguousarray(extra_minmax, np.float32) if extra_minmax is not None else None

@@ -641,6 +641,12 @@ vg_status vg_destroy(vg_ctx* c) {
   if (c->ev1) cudaEventDestroy(c->ev1);
   if (c->ev2) cudaEventDestroy(c->ev2);
   if (c->ev3) cudaEventDestroy(c->ev3);
+  if (c->aux) {
+    cudaStreamSynchronize(c->aux);
+    cudaStreamDestroy(c->aux);
+  }
+  if (c->aux_ev0) cudaEventDestroy(c->aux_ev0);
+  if (c->aux_ev1) cudaEventDestroy(c->aux_ev1);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c->split;
   delete c;
@@ -665,10 +671,68 @@ vg_status vg_set_config(vg_ctx* c, const vg_config* cfg) {
   return VG_OK;
 }
 
-// vg_step and vg_step_evolve on host records (evolve: the vortons move by
-// velocity x dt before the records go back).
+// Tracer records on their way through the advection (vg_advect,
+// vg_step_advect): the records (whole when at most 4x the 24 bytes used, as
+// one contiguous copy each way; else their bytes [0, 24): position, velocity)
+// staged on the device, then float4 position and velocity.
+struct TracerJob {
+  void* recs = nullptr;
+  size_t m = 0, stride = 0, pitch = 0;
+  bool whole = true;
+  unsigned char* stage = nullptr;
+  float4* p = nullptr;
+  float4* v = nullptr;
+};
+
+static vg_status tracer_prepare(vg_ctx* c, void* particles, size_t m, size_t stride, TracerJob* t) {
+  if (!particles || stride < 24 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 24 / unaligned");
+  if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
+  vg_status st = VG_OK;
+  t->recs = particles;
+  t->m = m;
+  t->stride = stride;
+  t->whole = stride <= 4 * 24;
+  t->pitch = t->whole ? stride : 24;
+  const size_t rec_bytes = ((m * t->pitch + 255) / 256) * 256;
+  t->stage = (unsigned char*)ws(c, S_TRACERS, rec_bytes + 2 * m * sizeof(float4), &st);
+  if (st != VG_OK) return st;
+  t->p = (float4*)(t->stage + rec_bytes);
+  t->v = t->p + m;
+  return VG_OK;
+}
+
+static cudaError_t tracer_upload(const TracerJob& t, cudaStream_t s) {
+  if (t.whole) return cudaMemcpyAsync(t.stage, t.recs, t.m * t.stride, cudaMemcpyHostToDevice, s);
+  return cudaMemcpy2DAsync(t.stage, 24, t.recs, t.stride, 12, t.m, cudaMemcpyHostToDevice, s);
+}
+
+// The gather + Euler step on the staged records and their copy back, on the
+// context's stream, through the last step's velocity grid.
+static vg_status tracer_advect_enqueue(vg_ctx* c, const TracerJob& t, float dt) {
+  vg_status st = VG_OK;
+  const size_t m = t.m;
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, t.stage, t.pitch, (int)m, t.p);
+  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, t.p, t.v, m, dt, true)) != VG_OK)
+    return st;
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, t.stage, t.pitch, (int)m, t.p, t.v);
+  VG_CUDA(c, cudaGetLastError());
+  if (t.whole)
+    VG_CUDA(c, cudaMemcpyAsync(t.recs, t.stage, m * t.stride, cudaMemcpyDeviceToHost, c->stream));
+  else
+    VG_CUDA(c, cudaMemcpy2DAsync(t.recs, t.stride, t.stage, 24, 24, m, cudaMemcpyDeviceToHost, c->stream));
+  return VG_OK;
+}
+
+static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                                   const float* extra_max, float dt, bool evolve, bool whole, size_t pitch,
+                                   unsigned char* stage, float4* ps, float4* w, float4* vel);
+
+// vg_step, vg_step_evolve and vg_step_advect on host records (evolve: the
+// vortons move by velocity x dt before the records go back; tj: tracer
+// records uploaded on a second stream during the step, then advected through
+// its velocity grid).
 static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
-                              const float* extra_max, float dt, bool evolve) {
+                              const float* extra_max, float dt, bool evolve, TracerJob* tj = nullptr) {
   if (!c) return VG_INVALID;
   if (n == 0) return fail(c, VG_EMPTY, "no vortons");
   if (!particles || stride < 56 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 56 / unaligned");
@@ -688,6 +752,34 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
   if (st != VG_OK) return st;
   float4* vel = (float4*)ws(c, S_VVEL, n * sizeof(float4), &st);
   if (st != VG_OK) return st;
+  if (tj) {
+    // the tracer records go up on the second stream while the vortons step
+    // (after whatever the context's stream already holds)
+    if (!c->aux) VG_CUDA(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
+    if (!c->aux_ev0) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev0, cudaEventDisableTiming));
+    if (!c->aux_ev1) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev1, cudaEventDisableTiming));
+    VG_CUDA(c, cudaEventRecord(c->aux_ev0, c->stream));
+    VG_CUDA(c, cudaStreamWaitEvent(c->aux, c->aux_ev0, 0));
+    VG_CUDA(c, tracer_upload(*tj, c->aux));
+    VG_CUDA(c, cudaEventRecord(c->aux_ev1, c->aux));
+  }
+  st = step_records_body(c, particles, n, stride, extra_min, extra_max, dt, evolve, whole, pitch, stage, ps, w, vel);
+  if (st == VG_OK && tj) {
+    VG_CUDA(c, cudaStreamWaitEvent(c->stream, c->aux_ev1, 0));
+    st = tracer_advect_enqueue(c, *tj, dt);
+  }
+  if (st != VG_OK) {
+    if (tj) cudaStreamSynchronize(c->aux);  // no copy of the caller's records left in flight
+    return st;
+  }
+  return sync_and_check(c, tj ? "vg_step_advect" : evolve ? "vg_step_evolve" : "vg_step");
+}
+
+// The vortons' part of step_records, enqueued on the context's stream.
+static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
+                                   const float* extra_max, float dt, bool evolve, bool whole, size_t pitch,
+                                   unsigned char* stage, float4* ps, float4* w, float4* vel) {
+  vg_status st = VG_OK;
   // record bytes [0, 56): position, velocity, orientation, angular velocity, density, size
   if (whole)
     VG_CUDA(c, cudaMemcpyAsync(stage, particles, n * stride, cudaMemcpyHostToDevice, c->stream));
@@ -714,7 +806,7 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
   else
     VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + from, stride, stage + from, 56, 48 - from, n,
                                  cudaMemcpyDeviceToHost, c->stream));
-  return sync_and_check(c, evolve ? "vg_step_evolve" : "vg_step");
+  return VG_OK;
 }
 
 vg_status vg_step(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
@@ -727,6 +819,19 @@ vg_status vg_step_evolve(vg_ctx* c, void* particles, size_t n, size_t stride, co
                          const float* extra_max, float dt, unsigned frame) {
   (void)frame;
   return step_records(c, particles, n, stride, extra_min, extra_max, dt, true);
+}
+
+vg_status vg_step_advect(vg_ctx* c, void* vortons, size_t n, size_t stride, const float* extra_min,
+                         const float* extra_max, float dt, unsigned frame, int evolve_vortons, void* tracers,
+                         size_t m, size_t tracer_stride) {
+  (void)frame;
+  if (!c) return VG_INVALID;
+  if (m == 0) return step_records(c, vortons, n, stride, extra_min, extra_max, dt, evolve_vortons != 0);
+  // the tracers' staging first: an allocation may synchronise the stream
+  TracerJob tj;
+  vg_status st = tracer_prepare(c, tracers, m, tracer_stride, &tj);
+  if (st != VG_OK) return st;
+  return step_records(c, vortons, n, stride, extra_min, extra_max, dt, evolve_vortons != 0, &tj);
 }
 
 vg_status vg_step_device(vg_ctx* c, const float* pos_size, float* angvel, float* vel, size_t n,
@@ -821,31 +926,11 @@ vg_status vg_advect(vg_ctx* c, void* particles, size_t m, size_t stride, float d
   if (!c) return VG_INVALID;
   if (!c->have_grid) return fail(c, VG_EMPTY, "no velocity grid yet: run a step first");
   if (m == 0) return VG_OK;
-  if (!particles || stride < 24 || stride % 4) return fail(c, VG_INVALID, "particles NULL or stride < 24 / unaligned");
-  if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "more than 2^31 particles");
-  vg_status st = VG_OK;
-  // staging: the records (whole when at most 4x the 24 bytes used, as one
-  // contiguous copy each way; else their bytes [0, 24): position, velocity),
-  // then float4 position and velocity
-  const bool whole = stride <= 4 * 24;
-  const size_t pitch = whole ? stride : 24;
-  const size_t rec_bytes = ((m * pitch + 255) / 256) * 256;
-  unsigned char* stage = (unsigned char*)ws(c, S_TRACERS, rec_bytes + 2 * m * sizeof(float4), &st);
+  TracerJob t;
+  vg_status st = tracer_prepare(c, particles, m, stride, &t);
   if (st != VG_OK) return st;
-  float4* p = (float4*)(stage + rec_bytes);
-  float4* v = p + m;
-  if (whole)
-    VG_CUDA(c, cudaMemcpyAsync(stage, particles, m * stride, cudaMemcpyHostToDevice, c->stream));
-  else
-    VG_CUDA(c, cudaMemcpy2DAsync(stage, 24, particles, stride, 12, m, cudaMemcpyHostToDevice, c->stream));
-  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, stage, pitch, (int)m, p);
-  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, p, v, m, dt, true)) != VG_OK) return st;
-  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, stage, pitch, (int)m, p, v);
-  VG_CUDA(c, cudaGetLastError());
-  if (whole)
-    VG_CUDA(c, cudaMemcpyAsync(particles, stage, m * stride, cudaMemcpyDeviceToHost, c->stream));
-  else
-    VG_CUDA(c, cudaMemcpy2DAsync(particles, stride, stage, 24, 24, m, cudaMemcpyDeviceToHost, c->stream));
+  VG_CUDA(c, tracer_upload(t, c->stream));
+  if ((st = tracer_advect_enqueue(c, t, dt)) != VG_OK) return st;
   return sync_and_check(c, "vg_advect");
 }
 

@@ -264,6 +264,10 @@ struct Ctx {
   bool have_grid = false;
   vg_step_stats stats;
   cudaEvent_t ev0 = nullptr, ev1 = nullptr, ev2 = nullptr, ev3 = nullptr;
+  // second stream of vg_step_advect (the tracer records' upload beside the
+  // vortons' step) and its two ordering events, created on first use
+  cudaStream_t aux = nullptr;
+  cudaEvent_t aux_ev0 = nullptr, aux_ev1 = nullptr;
   unsigned launches = 0;    // kernel launches since the counter was reset
   Geom prev_grid;           // grid of the stored previous solution
   bool have_prev = false;
