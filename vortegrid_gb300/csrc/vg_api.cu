@@ -121,9 +121,16 @@ vg_status cuda_check(Ctx* c, cudaError_t e, const char* what) {
 }
 
 vg_status sync_and_check(Ctx* c, const char* what) {
-  VG_CUDA(c, cudaStreamSynchronize(c->stream));
   int h = 0;
-  VG_CUDA(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
+  if (c->hflag) {
+    // the error word comes back behind the stream's work: one wait, no second round trip
+    VG_CUDA(c, cudaMemcpyAsync(c->hflag, c->dflag, sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+    h = *c->hflag;
+  } else {
+    VG_CUDA(c, cudaStreamSynchronize(c->stream));
+    VG_CUDA(c, cudaMemcpy(&h, c->dflag, sizeof(int), cudaMemcpyDeviceToHost));
+  }
   if (h) {
     VG_CUDA(c, cudaMemset(c->dflag, 0, sizeof(int)));
     if (h & DF_TIMEOUT) return fail(c, VG_TIMEOUT, std::string(what) + ": a bounded device wait gave up");
@@ -616,6 +623,7 @@ vg_status vg_create(const vg_config* cfg, vg_ctx** out) {
   if (e == cudaSuccess) e = cudaEventCreate(&c->ev3);
   if (e == cudaSuccess) e = cudaMalloc(&c->dflag, 256);
   if (e == cudaSuccess) e = cudaMemset(c->dflag, 0, 256);
+  if (e == cudaSuccess) e = cudaHostAlloc(&c->hflag, 64, cudaHostAllocDefault);
   if (e == cudaSuccess) e = cudaMalloc(&c->mg_relres_dev, 2 * sizeof(double));
   if (e != cudaSuccess) {
     g_err_noctx = std::string("vg_create: ") + cudaGetErrorString(e);
@@ -636,6 +644,7 @@ vg_status vg_destroy(vg_ctx* c) {
   for (MgGraphCache& G : c->mg_graph)
     if (G.exec) cudaGraphExecDestroy(G.exec);
   if (c->dflag) cudaFree(c->dflag);
+  if (c->hflag) cudaFreeHost(c->hflag);
   if (c->mg_relres_dev) cudaFree(c->mg_relres_dev);
   if (c->ev0) cudaEventDestroy(c->ev0);
   if (c->ev1) cudaEventDestroy(c->ev1);

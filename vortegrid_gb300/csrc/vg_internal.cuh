@@ -272,6 +272,7 @@ struct Ctx {
   Geom prev_grid;           // grid of the stored previous solution
   bool have_prev = false;
   int* dflag = nullptr;     // device error word: bit 0 = a sample left the grid
+  int* hflag = nullptr;     // pinned host copy of dflag[0], read back with the stream's work
   bool stats_pending = false;
   // Multigrid schedule.  mg_fixed_k1 > 0 runs a fixed schedule with no host
   // round trip (k1 FP32 cycles, then k2 refinement cycles), so that a step can
