@@ -282,9 +282,8 @@ def run_ours(args, world, rank, local):
         ww.copy_(w0, non_blocking=True)
         trp.copy_(tr0, non_blocking=True)
 
-    def step():
-        ctx.UpdateDevice(ps, ww, vel, float(DT))
-        ctx.EvolveDevice(ps, vel, float(DT))
+    def step():  # the step with the vortons' Euler step, then the tracers' gather + Euler step
+        ctx.UpdateAndEvolveDevice(ps, ww, vel, float(DT))
         ctx.AdvectDevice(trp, trv, float(DT))
 
     with torch.cuda.stream(stream):
@@ -293,7 +292,7 @@ def run_ours(args, world, rank, local):
             step()
         ctx.synchronize()
         stats = ctx.stats()
-        launches_per_step = stats.kernels_launched + 2
+        launches_per_step = stats.kernels_launched + 1  # the step's kernels + the tracer advection
         barrier(world)
         torch.cuda.synchronize()
         ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(args.steps)]

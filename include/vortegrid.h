@@ -168,6 +168,12 @@ vg_status vg_step_advect(vg_ctx* ctx, void* vortons, size_t n, size_t stride, co
  * written.  extra_minmax: 6 host floats (min xyz, max xyz) or NULL. */
 vg_status vg_step_device(vg_ctx* ctx, const float* pos_size, float* angvel, float* vel, size_t n,
                          const float* extra_minmax, float dt, unsigned frame);
+/* vg_step_device followed by PclOpEvolve on the same vortons: pos_size's
+ * x, y, z also move by velocity x dt (written in place), folded into the
+ * kernel that writes the velocities when no later stage of the step reads the
+ * positions.  Bit-identical to vg_step_device then vg_evolve_device. */
+vg_status vg_step_evolve_device(vg_ctx* ctx, float* pos_size, float* angvel, float* vel, size_t n,
+                                const float* extra_minmax, float dt, unsigned frame);
 
 /* Replaces VortonSim::GetVelocityGrid (vortonSim.h:334-335).  Copies the last
  * step's velocity grid (float[3] per point) into host memory when xyz is not

@@ -576,6 +576,45 @@ def test_step_advect_matches_the_separate_calls(vg):
             assert np.abs(tb["position"] - t0["position"]).max() > 0
 
 
+def test_step_evolve_device_matches_step_then_evolve(vg):
+    """vg_step_evolve_device gives positions, velocities and angular
+    velocities bit for bit equal to vg_step_device then vg_evolve_device: the
+    direct technique on a fixed grid (the Euler step folded into the
+    reduction), the direct technique with stretch and diffusion (a separate
+    Euler kernel after them), the treecode and the Poisson technique (the
+    Euler step in the vortons' gather)."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(4096, seed=1)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+    cases = [dict(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid, enable_stretch=0, enable_diffusion=0),
+             dict(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid),
+             dict(velocity_technique=vg.VELOCITY_TREE, enable_stretch=0, enable_diffusion=0),
+             dict(velocity_technique=vg.VELOCITY_POISSON)]
+
+    def f4(a, wv=None):
+        o = np.zeros((len(a), 4), np.float32)
+        o[:, :3] = a
+        if wv is not None:
+            o[:, 3] = wv
+        return torch.from_numpy(o).cuda()
+    for kw in cases:
+        out = []
+        for fused in (False, True):
+            sim = vg.VortonSim(cfg=vg.default_config(device=0, **kw))
+            ps, ww, vel = f4(pos, s), f4(w), torch.zeros((len(pos), 4), device="cuda")
+            for k in range(2):
+                if fused:
+                    sim.UpdateAndEvolveDevice(ps, ww, vel, DT, k)
+                else:
+                    sim.UpdateDevice(ps, ww, vel, DT, k)
+                    sim.EvolveDevice(ps, vel, DT)
+            sim.synchronize()
+            out.append([t.cpu().numpy() for t in (ps, ww, vel)])
+        for a, b in zip(*out):
+            assert np.array_equal(a.view(np.uint32), b.view(np.uint32)), kw
+        assert np.abs(out[1][0][:, :3] - pos).max() > 0
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)

@@ -136,7 +136,7 @@ _lib = None
 
 EXPORTS = [
     "vg_status_string", "vg_last_error", "vg_abi_version", "vg_config_default", "vg_create", "vg_destroy",
-    "vg_set_config", "vg_step", "vg_step_evolve", "vg_step_advect", "vg_step_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
+    "vg_set_config", "vg_step", "vg_step_evolve", "vg_step_advect", "vg_step_device", "vg_step_evolve_device", "vg_get_velocity_grid", "vg_get_velocity_grid_device",
     "vg_get_vector_potential", "vg_get_stats", "vg_advect", "vg_advect_device", "vg_define_shape",
     "vg_set_poisson_schedule", "vg_get_poisson_schedule", "vg_set_coarsest_fp64",
     "vg_bin_device", "vg_partition_device", "vg_direct_device", "vg_tree_device", "vg_splat_device", "vg_boundary_vecpot_device",
@@ -186,6 +186,8 @@ def lib():
                                      ctypes.c_void_p, ctypes.c_size_t, ctypes.c_size_t]
         L.vg_step_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
                                      ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
+        L.vg_step_evolve_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p,
+                                            ctypes.c_size_t, ctypes.c_void_p, ctypes.c_float, ctypes.c_uint]
         L.vg_get_velocity_grid.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_size_t, ctypes.POINTER(GridGeom)]
         L.vg_get_velocity_grid_device.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_void_p),
                                                   ctypes.POINTER(GridGeom)]
@@ -416,6 +418,12 @@ class VortonSim(Context):
         self.check(lib().vg_step_advect(self.h, _ptr(particles), len(particles), particles.dtype.itemsize,
                                         _ptr(emin), _ptr(emax), timeStep, uFrame, int(bool(evolve)), _ptr(tracers),
                                         len(tracers), tracers.dtype.itemsize), "vg_step_advect")
+
+    def UpdateAndEvolveDevice(self, pos_size, angvel, vel, timeStep, uFrame=0, extra_minmax=None):
+        """UpdateDevice followed by EvolveDevice on the same vortons (vg_step_evolve_device)."""
+        e = np.ascontiguousarray(extra_minmax, np.float32) if extra_minmax is not None else None
+        self.check(lib().vg_step_evolve_device(self.h, _ptr(pos_size), _ptr(angvel), _ptr(vel), pos_size.shape[0],
+                                               _ptr(e), timeStep, uFrame), "vg_step_evolve_device")
 
     def UpdateDevice(self, pos_size, angvel, vel, timeStep, uFrame=0, extra_minmax=None):
         e = np.ascontiguousarray(extra_minmax, np.float32) if extra_minmax is not None else None

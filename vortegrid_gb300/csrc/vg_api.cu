@@ -445,7 +445,13 @@ static vg_status step_front(Ctx* c, StepState& s, const float* first_pos, const 
   } else {
     // COMPUTE_VELOCITY_AT_VORTONS (vorton.h:63-69): direct velocity at every vorton too;
     // the multi-chunk reduction writes the grid and vortons directly
-    const DirectSplit split = {s.velgrid, pts, vel, &g, (const float4*)ps};
+    DirectSplit split = {s.velgrid, pts, vel, &g, (const float4*)ps};
+    // the vortons' Euler step folded into the reduction when no later stage
+    // of the step reads their positions (stretch and PSE do)
+    if (c->step_evolve && !c->cfg.enable_stretch && !c->cfg.enable_diffusion) {
+      split.evolve_pos = ps;
+      split.evolve_dt = s.dt;
+    }
     bool done = false;
     if ((st = launch_direct(c, 0, ref, ps, w, n, q, nq, 1.0f, 1.0f, out4, &split, &done)) != VG_OK) return st;
     if (done) return VG_OK;
@@ -480,6 +486,18 @@ static vg_status step_solve(Ctx* c, StepState& s) {
   return VG_OK;
 }
 
+__global__ void k_evolve(float4* __restrict__ pos, const float4* __restrict__ vel, int m, float dt) {
+  pdl_entry();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float4 p = pos[i];
+  const float4 v = vel[i];
+  p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));  // pcl.mPosition += pcl.mVelocity * timeStep
+  p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
+  p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
+  pos[i] = p;
+}
+
 // The step after the solve: curl of the vector potential, stretching, PSE,
 // and the vortons' velocity from the grid.
 static vg_status step_back(Ctx* c, StepState& s) {
@@ -505,8 +523,17 @@ static vg_status step_back(Ctx* c, StepState& s) {
     if ((st = launch_pse(c, g, s.cl, s.ps, s.w, n, c->cfg.viscosity, s.dt)) != VG_OK) return st;
   }
   if (tech != VG_VELOCITY_DIRECT) {
-    // AssignVelocityFromField(vortons, mVelGrid, 1) (vortonSim.cpp:4251-4255)
-    if ((st = launch_gather_advect(c, g, s.velgrid, s.ps, s.vel, n, 0.0f, false, s.cl.items)) != VG_OK) return st;
+    // AssignVelocityFromField(vortons, mVelGrid, 1) (vortonSim.cpp:4251-4255);
+    // for vg_step_evolve_device with the Euler step of the same kernel
+    if ((st = launch_gather_advect(c, g, s.velgrid, s.ps, s.vel, n, c->step_evolve ? s.dt : 0.0f, c->step_evolve,
+                                   s.cl.items)) != VG_OK)
+      return st;
+    if (c->step_evolve) c->step_evolved = true;
+  }
+  if (c->step_evolve && !c->step_evolved) {  // PclOpEvolve on the vortons
+    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_evolve, s.ps, (const float4*)s.vel, (int)n, s.dt);
+    VG_LAUNCHED(c);
+    c->step_evolved = true;
   }
   VG_CUDA(c, cudaEventRecord(c->ev1, c->stream));
   c->stats_pending = true;
@@ -843,6 +870,16 @@ vg_status vg_step_advect(vg_ctx* c, void* vortons, size_t n, size_t stride, cons
   return step_records(c, vortons, n, stride, extra_min, extra_max, dt, evolve_vortons != 0, &tj);
 }
 
+vg_status vg_step_evolve_device(vg_ctx* c, float* pos_size, float* angvel, float* vel, size_t n,
+                                const float* extra_minmax, float dt, unsigned frame) {
+  if (!c) return VG_INVALID;
+  c->step_evolve = true;
+  c->step_evolved = false;
+  const vg_status st = vg_step_device(c, pos_size, angvel, vel, n, extra_minmax, dt, frame);
+  c->step_evolve = false;
+  return st;
+}
+
 vg_status vg_step_device(vg_ctx* c, const float* pos_size, float* angvel, float* vel, size_t n,
                          const float* extra_minmax, float dt, unsigned frame) {
   (void)frame;
@@ -951,17 +988,6 @@ vg_status vg_advect_device(vg_ctx* c, float* pos, float* vel, size_t m, float dt
 }
 
 namespace {
-__global__ void k_evolve(float4* __restrict__ pos, const float4* __restrict__ vel, int m, float dt) {
-  pdl_entry();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= m) return;
-  float4 p = pos[i];
-  const float4 v = vel[i];
-  p.x = __fadd_rn(p.x, __fmul_rn(v.x, dt));  // pcl.mPosition += pcl.mVelocity * timeStep
-  p.y = __fadd_rn(p.y, __fmul_rn(v.y, dt));
-  p.z = __fadd_rn(p.z, __fmul_rn(v.z, dt));
-  pos[i] = p;
-}
 }  // namespace
 
 vg_status vg_evolve_device(vg_ctx* c, float* pos4, const float* vel4, size_t m, float dt) {

@@ -365,10 +365,13 @@ __global__ void __launch_bounds__(kPairThreads, 2)
 // (float[3], indexed by class position) -- with up to 16 chunks' loads issued
 // before the first add: the sum is bound by the latency of these loads, not
 // by their bytes.
+// With evolve_pos, the vortons' positions also move by their velocity x dt
+// (PclOpEvolve's Euler step, as k_evolve would do next).
 __global__ void __launch_bounds__(128) k_reduce_pair(const float4* __restrict__ partial_rows,
                                                      const float* __restrict__ partial_gen, PairPlan P,
                                                      float4* __restrict__ out, float* __restrict__ grid3, int pts,
-                                                     float4* __restrict__ vel) {
+                                                     float4* __restrict__ vel, float4* __restrict__ evolve_pos,
+                                                     float dt) {
   pdl_entry();
   const int j = blockIdx.x * blockDim.x + threadIdx.x;
   if (j >= P.m) return;
@@ -423,6 +426,13 @@ __global__ void __launch_bounds__(128) k_reduce_pair(const float4* __restrict__ 
     grid3[3 * j + 2] = sz;
   } else {
     vel[j - pts] = make_float4(sx, sy, sz, 0.f);
+    if (evolve_pos) {
+      float4 p = evolve_pos[j - pts];
+      p.x = __fadd_rn(p.x, __fmul_rn(sx, dt));
+      p.y = __fadd_rn(p.y, __fmul_rn(sy, dt));
+      p.z = __fadd_rn(p.z, __fmul_rn(sz, dt));
+      evolve_pos[j - pts] = p;
+    }
   }
 }
 
@@ -568,7 +578,8 @@ cudaError_t launch_pair_plan(Launch launch, const PairPlan& P, const float4* ps,
   if (e != cudaSuccess || !reduce) return e;
   return launch(dim3(blocks_for((size_t)P.m, 128)), dim3(128), k_reduce_pair, (const float4*)pr, (const float*)pg,
                 P, out, split ? split->grid3 : (float*)nullptr, split ? (int)split->pts : 0,
-                split ? split->vel : (float4*)nullptr);
+                split ? split->vel : (float4*)nullptr, split ? split->evolve_pos : (float4*)nullptr,
+                split ? split->evolve_dt : 0.f);
 }
 
 // Partial sums of a plan: per chunk, float4 per gridpoint (row class), float[3] per general target.
@@ -617,6 +628,7 @@ vg_status launch_direct(Ctx* c, int kind, bool ref, const float4* ps, const floa
     VG_CUDA(c, launch_pair_plan(launch, P, ps, w, (int)n, sr, sc, qg, partial, out, split));
     c->launches += reduce ? 2 : 1;
     if (split_done) *split_done = reduce && split != nullptr;
+    if (reduce && split && split->evolve_pos) c->step_evolved = true;
     VG_CUDA(c, cudaGetLastError());
     return VG_OK;
   }

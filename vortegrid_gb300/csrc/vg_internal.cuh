@@ -273,6 +273,9 @@ struct Ctx {
   bool have_prev = false;
   int* dflag = nullptr;     // device error word: bit 0 = a sample left the grid
   int* hflag = nullptr;     // pinned host copy of dflag[0], read back with the stream's work
+  // vg_step_evolve_device: the step also moves the vortons by velocity x dt
+  // (step_evolved: a kernel of the step has done it)
+  bool step_evolve = false, step_evolved = false;
   bool stats_pending = false;
   // Multigrid schedule.  mg_fixed_k1 > 0 runs a fixed schedule with no host
   // round trip (k1 FP32 cycles, then k2 refinement cycles), so that a step can
@@ -364,6 +367,8 @@ struct DirectSplit {
   float4* vel;
   const Geom* grid;
   const float4* after_grid;
+  float4* evolve_pos = nullptr;  // not NULL: the reduction also moves these vortons by velocity x evolve_dt
+  float evolve_dt = 0.f;
 };
 // With split, *split_done says whether the results went there (the
 // multi-chunk packed path writes them from its reduction) or to out.
