@@ -615,6 +615,53 @@ def test_step_evolve_device_matches_step_then_evolve(vg):
         assert np.abs(out[1][0][:, :3] - pos).max() > 0
 
 
+def test_host_record_graph_replay_matches_direct_runs(vg):
+    """On a fixed grid with pinned records, repeated host-record calls run
+    from a captured CUDA graph (second call captures, later ones replay):
+    six frames of vg_step_advect and of vg_step_evolve + vg_advect give every
+    record field bit for bit what the same calls give on pageable records
+    (always run directly); a change of the vortons' size between frames is
+    picked up (a new capture); direct and treecode techniques."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(2048, seed=5)
+    tr = np.random.default_rng(3).uniform(-1.2, 1.2, (8192, 3)).astype(np.float32)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+
+    def pinned_copy(a):
+        t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
+        b = t.numpy().view(a.dtype)
+        b[...] = a
+        return b, t
+    for tech in (vg.VELOCITY_DIRECT, vg.VELOCITY_TREE):
+        for one_call in (True, False):
+            results = []
+            for pinned in (False, True):
+                sim = vg.VortonSim(cfg=vg.default_config(velocity_technique=tech, fixed_grid=grid, enable_stretch=0,
+                                                         enable_diffusion=0, device=0))
+                v0, t0 = vg.make_particles(pos, w, s), vg.make_particles(tr)
+                keep = []
+                if pinned:
+                    (v, tv), (t, tt) = pinned_copy(v0), pinned_copy(t0)
+                    keep = [tv, tt]
+                else:
+                    v, t = v0.copy(), t0.copy()
+                for k in range(6):
+                    if k == 4:
+                        v["size"] *= np.float32(1.1)  # the vortons grow: the graph's key changes
+                    if one_call:
+                        sim.UpdateAndAdvect(v, t, DT, k, evolve=True)
+                    else:
+                        sim.UpdateAndEvolve(v, DT, k)
+                        sim.Advect(t, DT)
+                results.append((v.copy(), t.copy()))
+                del keep
+            (va, ta), (vb, tb) = results
+            for a, b in ((va, vb), (ta, tb)):
+                for f in vg.PARTICLE_DTYPE.names:
+                    assert np.array_equal(np.ascontiguousarray(a[f]).view(np.uint8),
+                                          np.ascontiguousarray(b[f]).view(np.uint8)), (tech, one_call, f)
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)

@@ -663,6 +663,8 @@ vg_status vg_create(const vg_config* cfg, vg_ctx** out) {
   return VG_OK;
 }
 
+static void destroy_host_graph(Ctx* c);
+
 vg_status vg_destroy(vg_ctx* c) {
   if (!c) return VG_OK;
   if (c->stream) cudaStreamSynchronize(c->stream);
@@ -685,6 +687,7 @@ vg_status vg_destroy(vg_ctx* c) {
   if (c->aux_ev1) cudaEventDestroy(c->aux_ev1);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c->split;
+  destroy_host_graph(c);
   delete c;
   return VG_OK;
 }
@@ -759,6 +762,95 @@ static vg_status tracer_advect_enqueue(vg_ctx* c, const TracerJob& t, float dt) 
   return VG_OK;
 }
 
+
+// The host-record step as one CUDA graph.  A frame's call (vg_step,
+// vg_step_evolve, vg_step_advect) enqueues some twenty copies, kernels and
+// event operations; while the same call repeats -- same records, sizes, dt,
+// configuration and workspace -- its work is captured once and replayed with
+// one launch.  Only where the step needs no host round trip (a fixed grid; for
+// the Poisson technique, a fixed multigrid schedule) and the records are in
+// pinned host memory.  The first call of a new key runs directly (and sizes
+// the workspace), the second is captured.
+struct vg::HostStepGraph {
+  cudaGraphExec_t exec = nullptr;
+  bool valid = false, nocapture = false;
+  int seen = 0;
+  const void* vortons = nullptr;
+  const void* tracers = nullptr;
+  size_t n = 0, stride = 0, m = 0, tstride = 0;
+  float dt = 0.f, extra[6] = {0, 0, 0, 0, 0, 0};
+  float size0 = 0.f;  // the first vorton's size, read on the host (its radius sets the mollification)
+  bool evolve = false, has_extra = false;
+  vg_config cfg;
+  const void* net = nullptr;
+  int k1 = 0, k2 = 0;
+  bool coarse64 = false;
+  void* bufs[S_NUM];
+  size_t bytes[S_NUM];
+};
+
+static void destroy_host_graph(Ctx* c) {
+  if (!c->host_graph) return;
+  if (c->host_graph->exec) cudaGraphExecDestroy(c->host_graph->exec);
+  delete c->host_graph;
+  c->host_graph = nullptr;
+}
+
+static bool pinned_host(const void* p) {
+  cudaPointerAttributes a;
+  if (cudaPointerGetAttributes(&a, p) != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return a.type == cudaMemoryTypeHost;
+}
+
+static void fill_key(Ctx* c, HostStepGraph* k, const void* vortons, size_t n, size_t stride, const void* tracers,
+                     size_t m, size_t tstride, float dt, bool evolve, const float* emin, const float* emax) {
+  k->vortons = vortons;
+  k->n = n;
+  k->stride = stride;
+  k->tracers = tracers;
+  k->m = m;
+  k->tstride = tstride;
+  k->dt = dt;
+  k->size0 = ((const float*)vortons)[13];
+  k->evolve = evolve;
+  k->has_extra = emin && emax;
+  for (int a = 0; a < 3; ++a) {
+    k->extra[a] = k->has_extra ? emin[a] : 0.f;
+    k->extra[3 + a] = k->has_extra ? emax[a] : 0.f;
+  }
+  memcpy(&k->cfg, &c->cfg, sizeof(vg_config));
+  k->net = c->net;
+  k->k1 = c->mg_fixed_k1;
+  k->k2 = c->mg_fixed_k2;
+  k->coarse64 = c->mg_coarse_fp64;
+  for (int i = 0; i < S_NUM; ++i) {
+    k->bufs[i] = c->buf[i].p;
+    k->bytes[i] = c->buf[i].bytes;
+  }
+}
+
+static bool same_key(const HostStepGraph& a, const HostStepGraph& b) {
+  return a.vortons == b.vortons && a.n == b.n && a.stride == b.stride && a.tracers == b.tracers && a.m == b.m &&
+         a.tstride == b.tstride && memcmp(&a.dt, &b.dt, sizeof(float)) == 0 &&
+         memcmp(&a.size0, &b.size0, sizeof(float)) == 0 && a.evolve == b.evolve &&
+         a.has_extra == b.has_extra && memcmp(a.extra, b.extra, sizeof(a.extra)) == 0 &&
+         memcmp(&a.cfg, &b.cfg, sizeof(vg_config)) == 0 && a.net == b.net && a.k1 == b.k1 && a.k2 == b.k2 &&
+         a.coarse64 == b.coarse64 && memcmp(a.bufs, b.bufs, sizeof(a.bufs)) == 0 &&
+         memcmp(a.bytes, b.bytes, sizeof(a.bytes)) == 0;
+}
+
+// Whether this context's step can run from a graph (no host round trip inside).
+static bool graph_step_possible(Ctx* c) {
+  if (!c->cfg.use_fixed_grid) return false;
+  if (c->cfg.velocity_technique == VG_VELOCITY_POISSON && c->cfg.poisson_solver != VG_POISSON_REFERENCE_CASCADE &&
+      c->mg_fixed_k1 <= 0)
+    return false;
+  return true;
+}
+
 static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
                                    const float* extra_max, float dt, bool evolve, bool whole, size_t pitch,
                                    unsigned char* stage, float4* ps, float4* w, float4* vel);
@@ -789,26 +881,79 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
   float4* vel = (float4*)ws(c, S_VVEL, n * sizeof(float4), &st);
   if (st != VG_OK) return st;
   if (tj) {
-    // the tracer records go up on the second stream while the vortons step
-    // (after whatever the context's stream already holds)
     if (!c->aux) VG_CUDA(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
     if (!c->aux_ev0) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev0, cudaEventDisableTiming));
     if (!c->aux_ev1) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev1, cudaEventDisableTiming));
-    VG_CUDA(c, cudaEventRecord(c->aux_ev0, c->stream));
-    VG_CUDA(c, cudaStreamWaitEvent(c->aux, c->aux_ev0, 0));
-    VG_CUDA(c, tracer_upload(*tj, c->aux));
-    VG_CUDA(c, cudaEventRecord(c->aux_ev1, c->aux));
   }
-  st = step_records_body(c, particles, n, stride, extra_min, extra_max, dt, evolve, whole, pitch, stage, ps, w, vel);
-  if (st == VG_OK && tj) {
-    VG_CUDA(c, cudaStreamWaitEvent(c->stream, c->aux_ev1, 0));
-    st = tracer_advect_enqueue(c, *tj, dt);
+  const char* what = tj ? "vg_step_advect" : evolve ? "vg_step_evolve" : "vg_step";
+  auto enqueue = [&]() -> vg_status {
+    if (tj) {
+      // the tracer records go up on the second stream while the vortons step
+      // (after whatever the context's stream already holds)
+      VG_CUDA(c, cudaEventRecord(c->aux_ev0, c->stream));
+      VG_CUDA(c, cudaStreamWaitEvent(c->aux, c->aux_ev0, 0));
+      VG_CUDA(c, tracer_upload(*tj, c->aux));
+      VG_CUDA(c, cudaEventRecord(c->aux_ev1, c->aux));
+    }
+    vg_status est =
+        step_records_body(c, particles, n, stride, extra_min, extra_max, dt, evolve, whole, pitch, stage, ps, w, vel);
+    if (est == VG_OK && tj) {
+      VG_CUDA(c, cudaStreamWaitEvent(c->stream, c->aux_ev1, 0));
+      est = tracer_advect_enqueue(c, *tj, dt);
+    }
+    return est;
+  };
+  // replay, capture, or run directly
+  if (graph_step_possible(c) && pinned_host(particles) && (!tj || pinned_host(tj->recs))) {
+    if (!c->host_graph) c->host_graph = new (std::nothrow) HostStepGraph();
+    HostStepGraph* G = c->host_graph;
+    if (G) {
+      HostStepGraph key;
+      fill_key(c, &key, particles, n, stride, tj ? tj->recs : nullptr, tj ? tj->m : 0, tj ? tj->stride : 0, dt,
+               evolve, extra_min, extra_max);
+      const bool same = G->valid && same_key(*G, key);
+      if (same && G->exec) {
+        VG_CUDA(c, cudaGraphLaunch(G->exec, c->stream));
+        return sync_and_check(c, what);
+      }
+      if (same && !G->nocapture && G->seen >= 1) {
+        cudaGraph_t graph = nullptr;
+        cudaGraphExec_t exec = nullptr;
+        if (cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+          const vg_status cst = enqueue();
+          const cudaError_t ce = cudaStreamEndCapture(c->stream, &graph);
+          if (cst == VG_OK && ce == cudaSuccess && graph && cudaGraphInstantiate(&exec, graph, 0) == cudaSuccess) {
+            cudaGraphDestroy(graph);
+            // the same call with the workspace as it stands after the capture
+            fill_key(c, G, particles, n, stride, tj ? tj->recs : nullptr, tj ? tj->m : 0, tj ? tj->stride : 0, dt,
+                     evolve, extra_min, extra_max);
+            G->exec = exec;
+            G->valid = true;
+            VG_CUDA(c, cudaGraphLaunch(G->exec, c->stream));
+            return sync_and_check(c, what);
+          }
+          if (graph) cudaGraphDestroy(graph);
+        }
+        cudaGetLastError();  // capture refused: run directly from now on for this call
+        if (tj) cudaStreamSynchronize(c->aux);
+        G->nocapture = true;
+      } else if (!same) {
+        if (G->exec) cudaGraphExecDestroy(G->exec);
+        *G = key;
+        G->exec = nullptr;
+        G->valid = true;
+        G->nocapture = false;
+        G->seen = 0;
+      }
+      ++G->seen;
+    }
   }
+  st = enqueue();
   if (st != VG_OK) {
     if (tj) cudaStreamSynchronize(c->aux);  // no copy of the caller's records left in flight
     return st;
   }
-  return sync_and_check(c, tj ? "vg_step_advect" : evolve ? "vg_step_evolve" : "vg_step");
+  return sync_and_check(c, what);
 }
 
 // The vortons' part of step_records, enqueued on the context's stream.

@@ -300,6 +300,9 @@ struct Ctx {
   // the solve on, resuming *split.
   int step_split = 0;
   struct StepState* split = nullptr;
+  // the host-record step's CUDA graph (vg_api.cu), replayed while the same
+  // call repeats
+  struct HostStepGraph* host_graph = nullptr;
 };
 
 // The word a kernel marks when a sample lies outside the grid's cells.
