@@ -158,7 +158,12 @@ vg_status vg_step_evolve(vg_ctx* ctx, void* particles, size_t n, size_t stride, 
  * (Particles/Operation/pclOpAdvect.cpp:132-152, pclOpEvolve.cpp:36-58).  The
  * tracer records' upload runs on a second stream while the vortons step.
  * Results bit-identical to the two calls; m = 0 is vg_step / vg_step_evolve
- * alone. */
+ * alone.
+ * vg_step, vg_step_evolve and vg_step_advect on a fixed grid (and, for the
+ * Poisson technique, a fixed multigrid schedule) with records in pinned host
+ * memory capture their work as a CUDA graph on the second identical call and
+ * replay it on later ones (identical: the same record pointers, counts,
+ * strides, dt, extra box, first vorton's size, configuration and workspace). */
 vg_status vg_step_advect(vg_ctx* ctx, void* vortons, size_t n, size_t stride, const float* extra_min,
                          const float* extra_max, float dt, unsigned frame, int evolve_vortons, void* tracers,
                          size_t m, size_t tracer_stride);
