@@ -624,7 +624,8 @@ def test_host_record_graph_replay_matches_direct_runs(vg):
     picked up (a new capture); direct and treecode techniques."""
     from vortegrid_gb300 import workloads
     pos, w, s = workloads.ring(2048, seed=5)
-    tr = np.random.default_rng(3).uniform(-1.2, 1.2, (8192, 3)).astype(np.float32)
+    # 80,000 tracers: over two per cell of the 33^3 grid, so vg_advect gathers from the grid arranged by cell
+    tr = np.random.default_rng(3).uniform(-1.2, 1.2, (80000, 3)).astype(np.float32)
     grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
 
     def pinned_copy(a):
@@ -660,6 +661,41 @@ def test_host_record_graph_replay_matches_direct_runs(vg):
                 for f in vg.PARTICLE_DTYPE.names:
                     assert np.array_equal(np.ascontiguousarray(a[f]).view(np.uint8),
                                           np.ascontiguousarray(b[f]).view(np.uint8)), (tech, one_call, f)
+
+
+def test_tracer_gather_by_cell_matches_grid_gather(vg):
+    """A tracer group of at least two per cell (here 200,000 on 33^3) is
+    gathered from the step's velocity grid arranged by cell: positions and
+    velocities bit for bit those of the same tracers gathered from the grid
+    itself (vg_gather_advect_device), over three steps with the grid changing
+    in between (the by-cell copy is remade for every step)."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(2048, seed=6)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+    sim = vg.VortonSim(cfg=vg.default_config(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid, enable_stretch=0,
+                                             enable_diffusion=0, device=0))
+
+    def f4(a, wv=None):
+        o = np.zeros((len(a), 4), np.float32)
+        o[:, :3] = a
+        if wv is not None:
+            o[:, 3] = wv
+        return torch.from_numpy(o).cuda()
+    ps, ww, vel = f4(pos, s), f4(w), torch.zeros((len(pos), 4), device="cuda")
+    trp = f4(np.random.default_rng(8).uniform(-1.2, 1.2, (200000, 3)).astype(np.float32))
+    trv = torch.zeros_like(trp)
+    for k in range(3):
+        sim.UpdateDevice(ps, ww, vel, DT, k)
+        ref_p, ref_v = trp.clone(), torch.zeros_like(trv)
+        vg3 = ctypes.c_void_p()
+        geom = vg.GridGeom()
+        sim.check(vg.lib().vg_get_velocity_grid_device(sim.h, ctypes.byref(vg3), ctypes.byref(geom)), "grid")
+        sim.check(vg.lib().vg_gather_advect_device(sim.h, ctypes.byref(geom), vg3, vg._ptr(ref_p), vg._ptr(ref_v),
+                                                   ref_p.shape[0], DT), "gather")
+        sim.AdvectDevice(trp, trv, DT)
+        sim.synchronize()
+        assert torch.equal(trp, ref_p) and torch.equal(trv[:, :3], ref_v[:, :3]), k
+        ps[:, 0] += 0.01  # the vortons move: the next step's grid differs
 
 
 def test_status_paths(vg):

@@ -542,6 +542,7 @@ static vg_status step_back(Ctx* c, StepState& s) {
   c->stats.kernels_launched = c->launches;
   c->grid = g;
   c->have_grid = true;
+  ++c->vel_gen;  // a new velocity grid (any by-cell copy is stale)
   return VG_OK;
 }
 
@@ -751,7 +752,8 @@ static vg_status tracer_advect_enqueue(vg_ctx* c, const TracerJob& t, float dt) 
   vg_status st = VG_OK;
   const size_t m = t.m;
   pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, t.stage, t.pitch, (int)m, t.p);
-  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, t.p, t.v, m, dt, true)) != VG_OK)
+  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, t.p, t.v, m, dt, true, nullptr,
+                                 true)) != VG_OK)
     return st;
   pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, t.stage, t.pitch, (int)m, t.p, t.v);
   VG_CUDA(c, cudaGetLastError());
@@ -914,6 +916,7 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
       const bool same = G->valid && same_key(*G, key);
       if (same && G->exec) {
         VG_CUDA(c, cudaGraphLaunch(G->exec, c->stream));
+        ++c->vel_gen;  // the replayed step wrote a new velocity grid
         return sync_and_check(c, what);
       }
       if (same && !G->nocapture && G->seen >= 1) {
@@ -930,6 +933,7 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
             G->exec = exec;
             G->valid = true;
             VG_CUDA(c, cudaGraphLaunch(G->exec, c->stream));
+            ++c->vel_gen;
             return sync_and_check(c, what);
           }
           if (graph) cudaGraphDestroy(graph);
@@ -1129,7 +1133,8 @@ vg_status vg_advect_device(vg_ctx* c, float* pos, float* vel, size_t m, float dt
   if (!c) return VG_INVALID;
   if (!c->have_grid) return fail(c, VG_EMPTY, "no velocity grid yet: run a step first");
   if (!pos) return fail(c, VG_INVALID, "NULL position pointer");
-  return launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, (float4*)pos, (float4*)vel, m, dt, true);
+  return launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, (float4*)pos, (float4*)vel, m, dt, true,
+                              nullptr, true);
 }
 
 namespace {

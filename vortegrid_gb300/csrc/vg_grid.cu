@@ -436,6 +436,69 @@ __global__ void k_gather_advect(Geom g, const float* __restrict__ vel3, float4* 
   }
 }
 
+// The velocity grid arranged by cell: the 8 corners of cell (x, y, z) as
+// float4 (u, v, w, 0), corners in interp's order (x fastest), so that a
+// tracer's gather is one 128-byte line instead of four scattered row pairs.
+__global__ void k_vel_cells(Geom g, const float* __restrict__ v3, float4* __restrict__ vc) {
+  pdl_entry();
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const size_t cx = g.np[0] - 1, cy = g.np[1] - 1;
+  const size_t cells = cx * cy * (size_t)(g.np[2] - 1);
+  if (t >= 8 * cells) return;
+  const size_t cell = t >> 3;
+  const unsigned q = (unsigned)(t & 7);
+  const size_t x = cell % cx, y = (cell / cx) % cy, z = cell / (cx * cy);
+  const size_t k = (x + (q & 1)) + (size_t)g.np[0] * ((y + ((q >> 1) & 1)) + (size_t)g.np[1] * (z + (q >> 2)));
+  vc[t] = make_float4(v3[3 * k], v3[3 * k + 1], v3[3 * k + 2], 0.f);
+}
+
+// k_gather_advect reading the by-cell copy: the same cell, weights and
+// trilinear sums as interp<3> on the grid (bit-identical).
+__global__ void k_gather_advect_cells(Geom g, const float4* __restrict__ vc, float4* __restrict__ pos,
+                                      float4* __restrict__ vel, int m, float dt, int evolve,
+                                      int* __restrict__ flag) {
+  pdl_entry();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float4 p = pos[i];
+  if (!inside_cells(g, p.x, p.y, p.z)) {
+    atomicOr(flag, (int)DF_OUT_OF_GRID);
+    if (vel) vel[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  const float pp[3] = {p.x, p.y, p.z};
+  unsigned idx[3];
+  float tw[3], om[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    idx[a] = bin_axis(pp[a], g.mn[a], g.cpe[a]);
+    const float cmin = __fadd_rn(g.mn[a], __fmul_rn((float)idx[a], g.cell[a]));
+    tw[a] = __fmul_rn(__fsub_rn(pp[a], cmin), g.cpe[a]);
+    om[a] = __fsub_rn(1.0f, tw[a]);
+  }
+  const size_t cell = idx[0] + (size_t)(g.np[0] - 1) * (idx[1] + (size_t)(g.np[1] - 1) * idx[2]);
+  float4 c[8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q) c[q] = vc[8 * cell + q];
+  float u[3];
+#pragma unroll
+  for (int a = 0; a < 3; ++a) {
+    auto comp = [&](const float4& v) { return a == 0 ? v.x : (a == 1 ? v.y : v.z); };
+    const float y0 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], comp(c[0])), __fmul_rn(tw[0], comp(c[1]))), om[1]),
+                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], comp(c[2])), __fmul_rn(tw[0], comp(c[3]))), tw[1]));
+    const float y1 = __fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(om[0], comp(c[4])), __fmul_rn(tw[0], comp(c[5]))), om[1]),
+                               __fmul_rn(__fadd_rn(__fmul_rn(om[0], comp(c[6])), __fmul_rn(tw[0], comp(c[7]))), tw[1]));
+    u[a] = __fadd_rn(__fmul_rn(y0, om[2]), __fmul_rn(y1, tw[2]));
+  }
+  if (vel) vel[i] = make_float4(u[0], u[1], u[2], 0.f);
+  if (evolve) {
+    p.x = __fadd_rn(p.x, __fmul_rn(u[0], dt));
+    p.y = __fadd_rn(p.y, __fmul_rn(u[1], dt));
+    p.z = __fadd_rn(p.z, __fmul_rn(u[2], dt));
+    pos[i] = p;
+  }
+}
+
 // Order-preserving float <-> uint map for atomic min/max.
 __device__ __forceinline__ unsigned f2key(float f) {
   const unsigned u = __float_as_uint(f);
@@ -638,9 +701,32 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
 }
 
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m, float dt,
-                               bool evolve, const unsigned* order) {
+                               bool evolve, const unsigned* order, bool by_cell) {
   if (m == 0) return VG_OK;
   if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "advect: more than 2^31 particles");
+  const size_t cells = g.np[0] >= 2 && g.np[1] >= 2 && g.np[2] >= 2
+                           ? (size_t)(g.np[0] - 1) * (g.np[1] - 1) * (size_t)(g.np[2] - 1)
+                           : 0;
+  // Tracer groups of at least two per cell gather from the grid arranged by
+  // cell (made once per step; inside a graph capture always, so that every
+  // replay remakes it from that replay's grid).
+  if (by_cell && cells && m >= 2 * cells && !order) {
+    vg_status st = VG_OK;
+    float4* vc = (float4*)ws(c, S_VELCELL, 8 * cells * sizeof(float4), &st);
+    if (st != VG_OK) return st;
+    cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+    VG_CUDA(c, cudaStreamIsCapturing(c->stream, &cap));
+    if (cap != cudaStreamCaptureStatusNone || c->velcell_gen != c->vel_gen) {
+      pdl_launch(c->stream, blocks_for(8 * cells, 256), 256, 0, k_vel_cells, g, vel3, vc);
+      VG_LAUNCHED(c);
+      c->velcell_gen = cap != cudaStreamCaptureStatusNone ? ~0ull : c->vel_gen;
+    }
+    pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect_cells, g, (const float4*)vc, pos, vel, (int)m,
+               dt, evolve ? 1 : 0, outside_flag(c));
+    VG_LAUNCHED(c);
+    VG_CUDA(c, cudaGetLastError());
+    return VG_OK;
+  }
   pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect, g, vel3, pos, vel, (int)m, dt, evolve ? 1 : 0, order,
                                                               outside_flag(c));
   VG_LAUNCHED(c);

@@ -237,6 +237,7 @@ enum Slot {
   S_MC,     // marching cubes: per-cell counts and offsets
   S_BODY,   // fluid-body collisions: per-block partial sums
   S_EMIT,   // emitters: jitter draws, records, deviation grid, flags
+  S_VELCELL,  // the velocity grid by cell (8 corners x float4) for large tracer groups
   S_NUM
 };
 
@@ -276,6 +277,9 @@ struct Ctx {
   // vg_step_evolve_device: the step also moves the vortons by velocity x dt
   // (step_evolved: a kernel of the step has done it)
   bool step_evolve = false, step_evolved = false;
+  // generation of the step's velocity grid (counted on the host at each step)
+  // and the one the by-cell copy in buf[S_VELCELL] was made from
+  unsigned long long vel_gen = 0, velcell_gen = ~0ull;
   bool stats_pending = false;
   // Multigrid schedule.  mg_fixed_k1 > 0 runs a fixed schedule with no host
   // round trip (k1 FP32 cycles, then k2 refinement cycles), so that a step can
@@ -453,8 +457,10 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
                      float dt);
 vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* ps, float* density, size_t n,
                           float kappa, float ambient, float dt);
+// by_cell: a tracer group of the step's own velocity grid (vel3 = buf[S_VEL]),
+// which may be gathered from a copy of the grid arranged by cell.
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
-                               float dt, bool evolve, const unsigned* order = nullptr);
+                               float dt, bool evolve, const unsigned* order = nullptr, bool by_cell = false);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
 // Density grid (PopulateDensityAndMassFractionGrids), gradient (ComputeGradient),
 // baroclinic generation and the signed distance grid (vg_surface.cu).
