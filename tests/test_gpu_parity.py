@@ -624,9 +624,9 @@ def test_host_record_graph_replay_matches_direct_runs(vg):
     picked up (a new capture); direct and treecode techniques."""
     from vortegrid_gb300 import workloads
     pos, w, s = workloads.ring(2048, seed=5)
-    # 80,000 tracers: over two per cell of the 33^3 grid, so vg_advect gathers from the grid arranged by cell
-    tr = np.random.default_rng(3).uniform(-1.2, 1.2, (80000, 3)).astype(np.float32)
-    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+    # 600,000 tracers: over two per cell of the 65^3 grid, so vg_advect gathers from the grid arranged by cell
+    tr = np.random.default_rng(3).uniform(-1.2, 1.2, (600000, 3)).astype(np.float32)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [65] * 3)
 
     def pinned_copy(a):
         t = torch.empty(a.nbytes, dtype=torch.uint8, pin_memory=True)
@@ -664,14 +664,15 @@ def test_host_record_graph_replay_matches_direct_runs(vg):
 
 
 def test_tracer_gather_by_cell_matches_grid_gather(vg):
-    """A tracer group of at least two per cell (here 200,000 on 33^3) is
-    gathered from the step's velocity grid arranged by cell: positions and
-    velocities bit for bit those of the same tracers gathered from the grid
-    itself (vg_gather_advect_device), over three steps with the grid changing
-    in between (the by-cell copy is remade for every step)."""
+    """A tracer group of at least two per cell on a grid of at least 2^17
+    cells (here 600,000 tracers on 65^3 points) is gathered from the step's
+    velocity grid arranged by cell: positions and velocities bit for bit those
+    of the same tracers gathered from the grid itself
+    (vg_gather_advect_device), over three steps with the grid changing in
+    between (the by-cell copy is remade for every step)."""
     from vortegrid_gb300 import workloads
     pos, w, s = workloads.ring(2048, seed=6)
-    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [33] * 3)
+    grid = vg.GridGeom.make([-1.5] * 3, [3.0] * 3, [65] * 3)
     sim = vg.VortonSim(cfg=vg.default_config(velocity_technique=vg.VELOCITY_DIRECT, fixed_grid=grid, enable_stretch=0,
                                              enable_diffusion=0, device=0))
 
@@ -682,7 +683,7 @@ def test_tracer_gather_by_cell_matches_grid_gather(vg):
             o[:, 3] = wv
         return torch.from_numpy(o).cuda()
     ps, ww, vel = f4(pos, s), f4(w), torch.zeros((len(pos), 4), device="cuda")
-    trp = f4(np.random.default_rng(8).uniform(-1.2, 1.2, (200000, 3)).astype(np.float32))
+    trp = f4(np.random.default_rng(8).uniform(-1.2, 1.2, (600000, 3)).astype(np.float32))
     trv = torch.zeros_like(trp)
     for k in range(3):
         sim.UpdateDevice(ps, ww, vel, DT, k)

@@ -709,8 +709,10 @@ vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4*
                            : 0;
   // Tracer groups of at least two per cell gather from the grid arranged by
   // cell (made once per step; inside a graph capture always, so that every
-  // replay remakes it from that replay's grid).
-  if (by_cell && cells && m >= 2 * cells && !order) {
+  // replay remakes it from that replay's grid) -- on grids of at least 2^17
+  // cells: a smaller grid stays in L1/L2 and the copy costs more than it saves
+  // (65,536 tracers on 32^3 cells: the step 1.6% slower with it).
+  if (by_cell && cells >= ((size_t)1 << 17) && m >= 2 * cells && !order) {
     vg_status st = VG_OK;
     float4* vc = (float4*)ws(c, S_VELCELL, 8 * cells * sizeof(float4), &st);
     if (st != VG_OK) return st;
