@@ -686,6 +686,8 @@ vg_status vg_destroy(vg_ctx* c) {
   }
   if (c->aux_ev0) cudaEventDestroy(c->aux_ev0);
   if (c->aux_ev1) cudaEventDestroy(c->aux_ev1);
+  if (c->aux_ev2) cudaEventDestroy(c->aux_ev2);
+  if (c->aux_ev3) cudaEventDestroy(c->aux_ev3);
   if (c->own_stream) cudaStreamDestroy(c->stream);
   delete c->split;
   destroy_host_graph(c);
@@ -855,7 +857,7 @@ static bool graph_step_possible(Ctx* c) {
 
 static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
                                    const float* extra_max, float dt, bool evolve, bool whole, size_t pitch,
-                                   unsigned char* stage, float4* ps, float4* w, float4* vel);
+                                   unsigned char* stage, float4* ps, float4* w, float4* vel, bool pack_on_aux);
 
 // vg_step, vg_step_evolve and vg_step_advect on host records (evolve: the
 // vortons move by velocity x dt before the records go back; tj: tracer
@@ -886,6 +888,8 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
     if (!c->aux) VG_CUDA(c, cudaStreamCreateWithFlags(&c->aux, cudaStreamNonBlocking));
     if (!c->aux_ev0) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev0, cudaEventDisableTiming));
     if (!c->aux_ev1) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev1, cudaEventDisableTiming));
+    if (!c->aux_ev2) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev2, cudaEventDisableTiming));
+    if (!c->aux_ev3) VG_CUDA(c, cudaEventCreateWithFlags(&c->aux_ev3, cudaEventDisableTiming));
   }
   const char* what = tj ? "vg_step_advect" : evolve ? "vg_step_evolve" : "vg_step";
   auto enqueue = [&]() -> vg_status {
@@ -897,11 +901,13 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
       VG_CUDA(c, tracer_upload(*tj, c->aux));
       VG_CUDA(c, cudaEventRecord(c->aux_ev1, c->aux));
     }
-    vg_status est =
-        step_records_body(c, particles, n, stride, extra_min, extra_max, dt, evolve, whole, pitch, stage, ps, w, vel);
+    vg_status est = step_records_body(c, particles, n, stride, extra_min, extra_max, dt, evolve, whole, pitch, stage,
+                                      ps, w, vel, tj != nullptr);
     if (est == VG_OK && tj) {
       VG_CUDA(c, cudaStreamWaitEvent(c->stream, c->aux_ev1, 0));
       est = tracer_advect_enqueue(c, *tj, dt);
+      // the vortons' records are back too before the call returns
+      if (est == VG_OK) VG_CUDA(c, cudaStreamWaitEvent(c->stream, c->aux_ev3, 0));
     }
     return est;
   };
@@ -963,7 +969,7 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
 // The vortons' part of step_records, enqueued on the context's stream.
 static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t stride, const float* extra_min,
                                    const float* extra_max, float dt, bool evolve, bool whole, size_t pitch,
-                                   unsigned char* stage, float4* ps, float4* w, float4* vel) {
+                                   unsigned char* stage, float4* ps, float4* w, float4* vel, bool pack_on_aux) {
   vg_status st = VG_OK;
   // record bytes [0, 56): position, velocity, orientation, angular velocity, density, size
   if (whole)
@@ -976,21 +982,30 @@ static vg_status step_records_body(vg_ctx* c, void* particles, size_t n, size_t 
   const float radius = rec0[13] * 0.5f;  // Particle::GetRadius of the first vorton
   st = run_step(c, ps, w, vel, n, rec0, radius, extra_min, extra_max, dt);
   if (st != VG_OK) return st;
+  // pack_on_aux: the vortons' records go back on the second stream while the
+  // tracers are advected on the first (aux_ev3 marks their return)
+  cudaStream_t ps_stream = c->stream;
+  if (pack_on_aux) {
+    VG_CUDA(c, cudaEventRecord(c->aux_ev2, c->stream));
+    VG_CUDA(c, cudaStreamWaitEvent(c->aux, c->aux_ev2, 0));
+    ps_stream = c->aux;
+  }
   // write back record bytes [12, 48): velocity, (unchanged) orientation,
   // angular velocity (whole records carry their other bytes back unchanged);
   // evolving, bytes [0, 48) with the moved position
   if (evolve)
-    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records_evolve, stage, pitch, (int)n, (const float4*)ps,
+    pdl_launch(ps_stream, blocks_for(n, 256), 256, 0, k_pack_records_evolve, stage, pitch, (int)n, (const float4*)ps,
                (const float4*)vel, (const float4*)w, dt);
   else
-    pdl_launch(c->stream, blocks_for(n, 256), 256, 0, k_pack_records, stage + 12, pitch, (int)n, vel, w);
+    pdl_launch(ps_stream, blocks_for(n, 256), 256, 0, k_pack_records, stage + 12, pitch, (int)n, vel, w);
   VG_CUDA(c, cudaGetLastError());
   const size_t from = evolve ? 0 : 12;
   if (whole)
-    VG_CUDA(c, cudaMemcpyAsync(particles, stage, n * stride, cudaMemcpyDeviceToHost, c->stream));
+    VG_CUDA(c, cudaMemcpyAsync(particles, stage, n * stride, cudaMemcpyDeviceToHost, ps_stream));
   else
     VG_CUDA(c, cudaMemcpy2DAsync((unsigned char*)particles + from, stride, stage + from, 56, 48 - from, n,
-                                 cudaMemcpyDeviceToHost, c->stream));
+                                 cudaMemcpyDeviceToHost, ps_stream));
+  if (pack_on_aux) VG_CUDA(c, cudaEventRecord(c->aux_ev3, c->aux));
   return VG_OK;
 }
 

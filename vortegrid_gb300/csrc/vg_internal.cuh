@@ -268,7 +268,7 @@ struct Ctx {
   // second stream of vg_step_advect (the tracer records' upload beside the
   // vortons' step) and its two ordering events, created on first use
   cudaStream_t aux = nullptr;
-  cudaEvent_t aux_ev0 = nullptr, aux_ev1 = nullptr;
+  cudaEvent_t aux_ev0 = nullptr, aux_ev1 = nullptr, aux_ev2 = nullptr, aux_ev3 = nullptr;
   unsigned launches = 0;    // kernel launches since the counter was reset
   Geom prev_grid;           // grid of the stored previous solution
   bool have_prev = false;
