@@ -156,7 +156,8 @@ vg_status vg_step_evolve(vg_ctx* ctx, void* particles, size_t n, size_t stride, 
  * group's PclOpVortonSim (+ PclOpEvolve) and the tracer group's
  * PclOpAssignVelocityFromField (gain 1) + PclOpEvolve
  * (Particles/Operation/pclOpAdvect.cpp:132-152, pclOpEvolve.cpp:36-58).  The
- * tracer records' upload runs on a second stream while the vortons step.
+ * tracer records' upload runs on a second stream while the vortons step,
+ * and the vortons' records return on it while the tracers are advected.
  * Results bit-identical to the two calls; m = 0 is vg_step / vg_step_evolve
  * alone.
  * vg_step, vg_step_evolve and vg_step_advect on a fixed grid (and, for the
