@@ -911,14 +911,19 @@ static vg_status step_records(vg_ctx* c, void* particles, size_t n, size_t strid
     }
     return est;
   };
-  // replay, capture, or run directly
-  if (graph_step_possible(c) && pinned_host(particles) && (!tj || pinned_host(tj->recs))) {
+  // replay, capture, or run directly (the records' pinned check is made when
+  // a key is new: a replayed key passed it)
+  if (graph_step_possible(c)) {
     if (!c->host_graph) c->host_graph = new (std::nothrow) HostStepGraph();
     HostStepGraph* G = c->host_graph;
+    HostStepGraph key;
     if (G) {
-      HostStepGraph key;
       fill_key(c, &key, particles, n, stride, tj ? tj->recs : nullptr, tj ? tj->m : 0, tj ? tj->stride : 0, dt,
                evolve, extra_min, extra_max);
+      if (!(G->valid && same_key(*G, key)) && !(pinned_host(particles) && (!tj || pinned_host(tj->recs))))
+        G = nullptr;  // pageable records: run directly
+    }
+    if (G) {
       const bool same = G->valid && same_key(*G, key);
       if (same && G->exec) {
         VG_CUDA(c, cudaGraphLaunch(G->exec, c->stream));
