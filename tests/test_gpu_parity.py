@@ -699,6 +699,32 @@ def test_tracer_gather_by_cell_matches_grid_gather(vg):
         ps[:, 0] += 0.01  # the vortons move: the next step's grid differs
 
 
+def test_advect_records_match_the_float4_path(vg):
+    """vg_advect on host records (gathering in place on the staged records)
+    moves and assigns every tracer bit for bit as vg_advect_device does on
+    float4 arrays, for whole (96-byte) and wide records."""
+    from vortegrid_gb300 import workloads
+    pos, w, s = workloads.ring(2000, seed=12)
+    tr = (pos[::2] * np.float32(0.85)).astype(np.float32)
+    wide = np.dtype({"names": ["position", "velocity", "extra"], "formats": [(np.float32, 3), (np.float32, 3),
+                                                                           (np.float32, 30)],
+                     "offsets": [0, 12, 24], "itemsize": 144})
+    for tdtype in (vg.PARTICLE_DTYPE, wide):
+        sim = vg.VortonSim(0.01)
+        v = vg.make_particles(pos, w, s)
+        sim.Update(v, DT, 0)
+        recs = np.zeros(len(tr), tdtype)
+        recs["position"] = tr
+        p4 = np.zeros((len(tr), 4), np.float32)
+        p4[:, :3] = tr
+        dp, dv = torch.from_numpy(p4).cuda(), torch.zeros((len(tr), 4), device="cuda")
+        sim.Advect(recs, DT)
+        sim.AdvectDevice(dp, dv, DT)
+        sim.synchronize()
+        assert np.array_equal(recs["position"].view(np.uint32), dp.cpu().numpy()[:, :3].copy().view(np.uint32))
+        assert np.array_equal(recs["velocity"].view(np.uint32), dv.cpu().numpy()[:, :3].copy().view(np.uint32))
+
+
 def test_status_paths(vg):
     sim = vg.VortonSim(0.01)
     empty = np.zeros(0, vg.PARTICLE_DTYPE)

@@ -753,12 +753,16 @@ static cudaError_t tracer_upload(const TracerJob& t, cudaStream_t s) {
 static vg_status tracer_advect_enqueue(vg_ctx* c, const TracerJob& t, float dt) {
   vg_status st = VG_OK;
   const size_t m = t.m;
-  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, t.stage, t.pitch, (int)m, t.p);
-  if ((st = launch_gather_advect(c, c->grid, (const float*)c->buf[S_VEL].p, t.p, t.v, m, dt, true, nullptr,
-                                 true)) != VG_OK)
+  const float* vel3 = (const float*)c->buf[S_VEL].p;
+  if (gather_by_cell(c->grid, m)) {
+    // float4 positions and velocities out of the records, the by-cell gather, and back
+    pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_copy_pos3, t.stage, t.pitch, (int)m, t.p);
+    if ((st = launch_gather_advect(c, c->grid, vel3, t.p, t.v, m, dt, true, nullptr, true)) != VG_OK) return st;
+    pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, t.stage, t.pitch, (int)m, t.p, t.v);
+    VG_CUDA(c, cudaGetLastError());
+  } else if ((st = launch_gather_advect_records(c, c->grid, vel3, t.stage, t.pitch, m, dt)) != VG_OK) {
     return st;
-  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_store_posvel, t.stage, t.pitch, (int)m, t.p, t.v);
-  VG_CUDA(c, cudaGetLastError());
+  }
   if (t.whole)
     VG_CUDA(c, cudaMemcpyAsync(t.recs, t.stage, m * t.stride, cudaMemcpyDeviceToHost, c->stream));
   else

@@ -436,6 +436,35 @@ __global__ void k_gather_advect(Geom g, const float* __restrict__ vel3, float4* 
   }
 }
 
+// AssignParticleVelocityFromField (gain 1) + EvolveParticlesSlice on staged
+// particle records (position at bytes 0-11, velocity at 12-23, pitch bytes
+// apart), in place: k_gather_advect without copying positions and velocities
+// out of and back into the records.  A record outside the grid's cells keeps
+// its position and gets zero velocity, as on the copy path.
+__global__ void k_gather_advect_records(Geom g, const float* __restrict__ vel3, unsigned char* __restrict__ rec,
+                                        size_t pitch, int m, float dt, int* __restrict__ flag) {
+  pdl_entry();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= m) return;
+  float* r = (float*)(rec + (size_t)i * pitch);
+  const float px = r[0], py = r[1], pz = r[2];
+  if (!inside_cells(g, px, py, pz)) {
+    atomicOr(flag, (int)DF_OUT_OF_GRID);
+    r[3] = 0.f;
+    r[4] = 0.f;
+    r[5] = 0.f;
+    return;
+  }
+  float u[3];
+  interp<3>(g, vel3, px, py, pz, u);
+  r[0] = __fadd_rn(px, __fmul_rn(u[0], dt));
+  r[1] = __fadd_rn(py, __fmul_rn(u[1], dt));
+  r[2] = __fadd_rn(pz, __fmul_rn(u[2], dt));
+  r[3] = u[0];
+  r[4] = u[1];
+  r[5] = u[2];
+}
+
 // The velocity grid arranged by cell: the 8 corners of cell (x, y, z) as
 // float4 (u, v, w, 0), corners in interp's order (x fastest), so that a
 // tracer's gather is one 128-byte line instead of four scattered row pairs.
@@ -700,6 +729,23 @@ vg_status launch_pse(Ctx* c, const Geom& g, const CellLists& cl, const float4* p
   return VG_OK;
 }
 
+bool gather_by_cell(const Geom& g, size_t m) {
+  if (g.np[0] < 2 || g.np[1] < 2 || g.np[2] < 2) return false;
+  const size_t cells = (size_t)(g.np[0] - 1) * (g.np[1] - 1) * (size_t)(g.np[2] - 1);
+  return cells >= ((size_t)1 << 17) && m >= 2 * cells;
+}
+
+vg_status launch_gather_advect_records(Ctx* c, const Geom& g, const float* vel3, unsigned char* rec, size_t pitch,
+                                       size_t m, float dt) {
+  if (m == 0) return VG_OK;
+  if (m > 0x7fffffff) return fail(c, VG_TOO_LARGE, "advect: more than 2^31 particles");
+  pdl_launch(c->stream, blocks_for(m, 256), 256, 0, k_gather_advect_records, g, vel3, rec, pitch, (int)m, dt,
+             outside_flag(c));
+  VG_LAUNCHED(c);
+  VG_CUDA(c, cudaGetLastError());
+  return VG_OK;
+}
+
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m, float dt,
                                bool evolve, const unsigned* order, bool by_cell) {
   if (m == 0) return VG_OK;
@@ -712,7 +758,7 @@ vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4*
   // replay remakes it from that replay's grid) -- on grids of at least 2^17
   // cells: a smaller grid stays in L1/L2 and the copy costs more than it saves
   // (65,536 tracers on 32^3 cells: the step 1.6% slower with it).
-  if (by_cell && cells >= ((size_t)1 << 17) && m >= 2 * cells && !order) {
+  if (by_cell && !order && gather_by_cell(g, m)) {
     vg_status st = VG_OK;
     float4* vc = (float4*)ws(c, S_VELCELL, 8 * cells * sizeof(float4), &st);
     if (st != VG_OK) return st;

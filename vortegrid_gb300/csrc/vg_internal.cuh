@@ -461,6 +461,12 @@ vg_status launch_heat_pse(Ctx* c, const Geom& g, const CellLists& cl, const floa
 // which may be gathered from a copy of the grid arranged by cell.
 vg_status launch_gather_advect(Ctx* c, const Geom& g, const float* vel3, float4* pos, float4* vel, size_t m,
                                float dt, bool evolve, const unsigned* order = nullptr, bool by_cell = false);
+// Whether m tracers on grid g gather from the grid arranged by cell.
+bool gather_by_cell(const Geom& g, size_t m);
+// The gather + Euler step in place on m staged particle records (position at
+// bytes 0-11, velocity at 12-23, pitch bytes apart).
+vg_status launch_gather_advect_records(Ctx* c, const Geom& g, const float* vel3, unsigned char* rec, size_t pitch,
+                                       size_t m, float dt);
 vg_status launch_bbox(Ctx* c, const float4* pos, size_t n, float* out6_dev);
 // Density grid (PopulateDensityAndMassFractionGrids), gradient (ComputeGradient),
 // baroclinic generation and the signed distance grid (vg_surface.cu).
